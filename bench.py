@@ -1,0 +1,345 @@
+"""Benchmark of the SIS force/integration hot path on GB300.
+
+Metric: bead*steps/s of the mixed-precision path (FP32 pair/bonded terms,
+FP64 accumulation and integration) next to the plain FP64 GPU path, at the
+stated force error against FP64.
+
+Workload (default, single GPU): the crowded single-system run -- 200 chains
+x 500 nt (100,000 beads), seeded random sequences and random-coil starts
+placed without overlap in a cubic PBC box at 10 mM nucleotide, 150 mM salt,
+300 K, sis.ff parameters, base-pair model 1.  Inputs are synthetic (no
+dataset is involved).
+
+A bench "step" is one block of MD steps (``--md-steps``, default 100) of all
+instances; L2 is flushed (512 MiB write) between timed blocks.  Positions,
+velocities and the noise state stay resident in HBM for ``value``; ``e2e``
+runs the same blocks through the public C ABI with host buffers: every block
+uploads x, v and the GJF-2GJ noise term from pinned host memory and reads the
+positions back.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "bead·steps/s batched-FP32 vs plain-FP64 on 1 GB300 at stated force err; p99 job ms"
+UNIT = "bead*steps/s"
+WORKLOADS = {
+    "crowded": "200 chains x 500 nt (100,000 beads), cubic PBC box at 10 mM nucleotide, 150 mM salt, 300 K",
+    "uneven": "256 independent chains, lengths U[20,500], salt U[20,500] mM, T U[280,340] K",
+    "remd": "64 replicas x 120 nt, T geometric 280-360 K",
+    "chain64": "one 64-nt chain, 300 K, 150 mM, no PBC",
+}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_system(name, seed_offset=0):
+    from sis_gb300.coil import crowded_box, remd_batch, single_chain, uneven_batch
+    from sis_gb300.inputs import read_ff
+
+    ff = read_ff(ROOT / "sis_gb300" / "data" / "sis.ff")
+    if name == "crowded":
+        return crowded_box(ff, 200, 500, 0.01, seed=1002 + seed_offset)
+    if name == "uneven":
+        return uneven_batch(ff, 256, seed=1004 + seed_offset)
+    if name == "remd":
+        return remd_batch(ff, 64, 120, seed=1003 + seed_offset)
+    return single_chain(ff, 64, seed=1001 + seed_offset)
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def list_stats(eng):
+    """List entries per bead in the reference's convention (WCA + DH + bp half lists)."""
+    tot = {0: 0, 1: 0, 2: 0}
+    for k in range(eng.n_inst):
+        for kind in (0, 1, 2):
+            tot[kind] += len(eng.get_list(k, kind))
+    return tot
+
+
+def run_gpu(args):
+    from sis_gb300 import FP64, MIXED
+    from sis_gb300.engine import Engine
+
+    rank, world, local = dist_env()
+    sysm = make_system(args.workload, seed_offset=rank)
+    S = args.md_steps
+    N = sysm.nmp
+    eng = Engine(sysm, precision=MIXED, seed=2024 + rank)
+    eng.init_velocities()
+    # relax the random-coil starts (4 A contacts) before timing
+    eng.step(args.relax)
+    for _ in range(args.warmup):
+        eng.flush_l2()
+        eng.step(S)
+    launches0 = eng.kernel_launches()
+    st0 = eng.stats()
+    times = []
+    barrier(world)
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            eng.flush_l2()
+            eng.event(0)
+            eng.step(S)
+            eng.event(1)
+            times.append(eng.elapsed_ms(0, 1))
+    launches = eng.kernel_launches() - launches0
+    st1 = eng.stats()
+    total_ms = max_over_ranks(sum(times), world)
+    value = world * N * S * args.steps / (total_ms * 1e-3)
+
+    # roofline of the dominant kernel (k_step), per-kernel events on the same stream
+    prof_steps = min(200, S * args.steps)
+    ms3 = eng.step_profiled(prof_steps)
+    lst = list_stats(eng)
+    L = (lst[0] + lst[1] + lst[2]) / N
+    bytes_per_bead = 144 + 32 + 4 * L
+    step_ms = ms3[1] / prof_steps
+    achieved = N * bytes_per_bead / (step_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    rebuilds = st1["rebuilds"] - st0["rebuilds"]
+    k_rebuild = (S * args.steps * len(sysm.instances)) / rebuilds if rebuilds else None
+    traffic = None
+    tf = ROOT / "profiles" / f"k_step_{args.workload}_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("bytes_per_launch")
+
+    # plain FP64 GPU path on the same state, and the force error against it
+    x, v, a = eng.get_state(-1)
+    e64 = Engine(sysm, precision=FP64, seed=2024 + rank)
+    e64.set_state(-1, x, v, a)
+    f64 = np.concatenate([e64.force(k) for k in range(e64.n_inst)])
+    eng.set_state(-1, x, v, a)
+    f32 = np.concatenate([eng.force(k) for k in range(eng.n_inst)])
+    err = float(np.sqrt(np.mean(np.sum((f32 - f64) ** 2, axis=1)) / np.mean(np.sum(f64 ** 2, axis=1))))
+    e64.step(S)
+    t64 = []
+    for _ in range(max(2, args.steps // 3)):
+        e64.flush_l2()
+        e64.event(0)
+        e64.step(S)
+        e64.event(1)
+        t64.append(e64.elapsed_ms(0, 1))
+    fp64_value = world * N * S * len(t64) / (max_over_ranks(sum(t64), world) * 1e-3)
+    e64.close()
+
+    # end to end through the C ABI with host buffers
+    x, v, a = eng.get_state(-1)
+    e2e_t = []
+    for _ in range(args.steps):
+        eng.flush_l2()
+        eng.synchronize()
+        t0 = time.perf_counter()
+        eng.set_state(-1, x, v, a)
+        eng.step(S)
+        x, v, a = eng.get_state(-1)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(sum(e2e_t), world)
+    e2e_value = world * N * S * args.steps / e2e_s
+    cfg = {"workload": args.workload, "description": WORKLOADS[args.workload], "n_beads": N,
+           "n_instances": len(sysm.instances), "md_steps_per_step": S, "precision": "FP32 terms / FP64 accumulate+integrate",
+           "list_entries_per_bead": round(L, 3), "steps_per_rebuild": k_rebuild, "lanes_per_bead": st1["lanes_per_bead"],
+           "l2": "flushed between timed steps (512 MiB write)", "fp64_value": fp64_value,
+           "speedup_vs_fp64": value / fp64_value, "force_rms_rel_err_vs_fp64": err, "relax_steps": args.relax,
+           "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "fp32+fp64", "data": "synthetic (seeded sequences and random-coil starts)", "config": cfg,
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * 32 * N, "d2h_bytes_per_step": 3 * 32 * N},
+           "gpu_launches": int(launches),
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_step", "kernel_ms": step_ms,
+                        "bytes_per_bead_step": bytes_per_bead},
+           "clocks": clk.summary()}
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(args, sysm, eng)
+    eng.close()
+    return out, rank
+
+
+def cpu_baseline(args, sysm, eng=None, sample_steps=None):
+    """The FP64 oracle (C++ restatement of the reference, OpenMP over all host
+    threads) on a bounded sample of the same workload."""
+    from oracle.oracle import Oracle
+
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    N = sysm.nmp
+    # about 20 s of CPU work: scale the step count to the system size
+    if sample_steps is None:
+        sample_steps = max(2, int(2e7 / max(N, 1) / 4))
+        sample_steps = min(sample_steps, 200)
+    x = None
+    if eng is not None:
+        x, v, a = eng.get_state(-1)
+    t_total, beads_steps = 0.0, 0
+    insts = range(len(sysm.instances))
+    if len(sysm.instances) > 8:
+        insts = range(0, len(sysm.instances), max(1, len(sysm.instances) // 8))
+    off = sysm.offsets()
+    for k in insts:
+        o = Oracle.from_instance(sysm, k)
+        if x is not None:
+            o.set_xyz(0, x[off[k]:off[k + 1]])
+            o.set_velos(0, v[off[k]:off[k + 1]])
+            o.set_accels(0, a[off[k]:off[k + 1]])
+        o.seed(1234 + k)
+        o.md_init()
+        t0 = time.perf_counter()
+        o.run(sample_steps)
+        t_total += time.perf_counter() - t0
+        beads_steps += o.nmp * sample_steps
+    return {"value": beads_steps / t_total, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{sample_steps} MD steps of {len(list(insts))} instance(s) ({beads_steps // sample_steps} beads) after "
+                      f"the initial list build; FP64 C++ restatement of the reference with OpenMP"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None, rank
+    sysm = make_system(args.workload)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(args, sysm, sample_steps=2)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(args, sysm, sample_steps=max(2, args.ref_sample)))
+    value = statistics.median(v["value"] for v in vals)
+    cb = dict(vals[-1])
+    cb["value"] = value
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+           "data": "synthetic (seeded sequences and random-coil starts)", "impl": "reference",
+           "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "n_beads": sysm.nmp,
+                      "note": "Fortran reference unavailable on this box (no Fortran compiler, toml-f not vendored); "
+                              "timed arm is the FP64 C++ restatement of its algorithms"},
+           "cpu_baseline": cb, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return out, rank
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="crowded", choices=list(WORKLOADS))
+    ap.add_argument("--md-steps", type=int, default=100)
+    ap.add_argument("--relax", type=int, default=200)
+    ap.add_argument("--ref-sample", type=int, default=10)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        out, rank = run_reference(args)
+    else:
+        out, rank = run_gpu(args)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

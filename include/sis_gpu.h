@@ -1,0 +1,205 @@
+/*
+ * sis_gpu.h -- C ABI of libsisgpu.so, the GB300 (sm_103a) engine for the SIS
+ * coarse-grained RNA model's force and integration hot path.
+ *
+ * The reference (Hori-Lab/SIS, Fortran) exposes this path as subroutines on
+ * module-global state:
+ *     subroutine force(irep, forces)                     src/force.F90:1,14-15
+ *     subroutine energy_sumup(irep, tempK_in, energies)  src/energy_sumup.F90:1,11-13
+ *     subroutine neighbor_list(irep)                     src/neighbor_list.F90:1
+ *     the GJF-2GJ / Ermak-McCammon update                src/job_md.F90:360-460
+ * Here the state lives on the device inside an opaque context; every entry
+ * point takes the replica (instance) index explicitly, copies caller-owned
+ * host buffers in or out, and returns an int status instead of aborting.
+ *
+ * Units and layouts follow the reference: Angstrom, kcal/mol, K, mol/L;
+ * coordinates of one instance are xyz(3,nmp) column-major (bead-major xyz
+ * triples); pair lists use 1-based bead indices local to the instance.
+ *
+ * Instances generalise the reference's replicas: the reference runs nrep
+ * copies of one topology; a context holds n_inst instances which may each
+ * have their own chains, temperature, salt and box.  One host thread per
+ * context; calls are stream-ordered on the context's own CUDA stream.
+ */
+#ifndef SIS_GPU_H
+#define SIS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference has none: it calls sis_abort, src/sis_abort.F90) */
+#define SIS_OK 0
+#define SIS_ERR_ARG -1          /* invalid argument */
+#define SIS_ERR_CUDA -2         /* CUDA runtime error; see sis_gpu_last_error */
+#define SIS_ERR_LIST_OVERFLOW -3/* a neighbour list exceeded its capacity */
+#define SIS_ERR_NONFINITE -4    /* NaN/Inf detected in coordinates or forces */
+#define SIS_ERR_NOMEM -5        /* device allocation failed */
+#define SIS_ERR_STATE -6        /* call out of order (e.g. force before set_state) */
+
+/* arithmetic of the force terms */
+#define SIS_PREC_FP64 0  /* all terms and the integration in FP64 (plain path) */
+#define SIS_PREC_MIXED 1 /* FP32 pair/bonded terms accumulated per bead into FP64, FP64 integration */
+
+/* integrators, const_idx.F90 INTGRT */
+#define SIS_INTGRT_GJF2GJ 1
+#define SIS_INTGRT_BD_EM 2
+
+/* energies(0:10) slots, const_idx.F90:7-21 ENE */
+#define SIS_ENE_TOTAL 0
+#define SIS_ENE_BOND 1
+#define SIS_ENE_ANGL 2
+#define SIS_ENE_DIHE 3
+#define SIS_ENE_BP 4
+#define SIS_ENE_EXV 5
+#define SIS_ENE_ELE 6
+#define SIS_ENE_MAX 10
+
+/* list kinds for sis_gpu_get_list */
+#define SIS_LIST_WCA 0 /* wca_mp(2,n)  src/var_potential.F90 */
+#define SIS_LIST_ELE 1 /* ele_mp(2,n) */
+#define SIS_LIST_BP 2  /* bp_mp(7,n)  */
+
+/* Model parameters: the .ff file (src/read_force_field.F90) and the input
+ * TOML sections [Basepair] [Electrostatic] [MD] (src/read_input.F90). */
+typedef struct sis_params {
+    double bond_k, bond_r0;          /* [potential.bond] k, r0 */
+    int32_t angl_reb;                /* 1: [potential.angle_ReB] instead of [potential.angle] */
+    double angl_k, angl_t0;          /* k, a0 */
+    int32_t dih_type;                /* 0 none, 1 [potential.dihedral], 2 [potential.dihedral_exp] */
+    double dih_k, dih_w, dih_p0;
+    double wca_sigma, wca_eps;       /* [potential.wca] */
+    int32_t bp_model;                /* [Basepair] model: 1, 3, 4 or 5 */
+    int32_t bp_min_loop;             /* [Basepair] min_loop */
+    int32_t bp_jnext_compat;         /* 1: reproduce src/neighbor_list.F90:212 (jmp+1 of the pair
+                                        tested against the length of imp's chain) */
+    double bp_cutoff_energy;         /* [potential.basepair] cutoff_energy */
+    /* [potential.basepair.GC|AU|GU]: U0 bond_k bond_r angl_k1..4 angl_theta1..4
+       dihd_k1 dihd_k2 dihd_phi1 dihd_phi2 */
+    double bp_ff[3][15];
+    double nn_dH[21], nn_dS[21];     /* [NN.dH] [NN.dS] in NNT order (src/const_idx.F90) */
+    double dH0, dS0;
+    int32_t nnend;
+    double nnend_dH[6], nnend_dS[6], dHend0, dSend0;
+    int32_t flg_ele;                 /* [Electrostatic] present */
+    int32_t ele_cutoff_type;         /* 1: cutoff in Angstrom, 2: in units of the Debye length */
+    double ele_cutoff_inp, length_per_charge;
+    int32_t ele_excl_bond, ele_excl_angle;
+    int32_t temp_independent;
+    double tempK_ref;
+    int32_t integrator;              /* SIS_INTGRT_* */
+    double dt, viscosity_Pas, nl_margin;
+    /* engine options (no counterpart in the reference) */
+    int32_t precision;               /* SIS_PREC_* */
+    uint64_t seed;                   /* Philox key for the Langevin noise */
+    int32_t nbr_cap;                 /* per-bead pair-list capacity (0: automatic) */
+    int32_t bp_cap;                  /* per-bead base-pair candidate capacity (0: automatic) */
+} sis_params;
+
+/* Topology and conditions of all instances. */
+typedef struct sis_topology {
+    int32_t n_inst;
+    const int32_t *inst_chain_off;   /* [n_inst+1]: chains of instance k are [off[k], off[k+1]) */
+    const int32_t *chain_len;        /* [n_chains] nmp_chain */
+    const int32_t *chain_moltype;    /* [n_chains] 1 linearRNA, 2 circRNA (MOLT) */
+    const int32_t *seq;              /* [n_beads] SEQT: A=0 U=1 G=2 C=3 D=4 */
+    const uint8_t *has_charge;       /* [n_beads] */
+    const double *tempK;             /* [n_inst] */
+    const double *ionic_strength;    /* [n_inst] mol/L */
+    const double *box;               /* [3*n_inst] PBC box, or NULL / zeros for no PBC */
+    const uint32_t *stream;          /* [n_inst] Philox noise stream per instance, or NULL (= index) */
+} sis_topology;
+
+typedef struct sis_ctx sis_ctx;
+
+typedef struct sis_stats {
+    int64_t steps;          /* MD steps taken */
+    int64_t rebuilds;       /* instance neighbour-list rebuilds (sum over instances) */
+    int64_t pair_entries;   /* current full pair-list entries (both directions) */
+    int64_t wca_pairs;      /* current half-list WCA pairs */
+    int64_t ele_pairs;      /* current half-list ele pairs */
+    int64_t bp_pairs;       /* current base-pair candidates */
+    int32_t error_flags;    /* bit 0 pair overflow, bit 1 bp overflow, bit 2 nonfinite */
+    int32_t n_beads;
+    int32_t n_inst;
+    int32_t lanes_per_bead; /* autotuned group width of the step kernel */
+} sis_stats;
+
+/* Creates a context and uploads topology and parameters.  Replaces the
+ * set-up the reference does in init_bp, init_ele/set_ele, list_local and
+ * set_md_coef (src/init_bp.F90, src/set_ele.F90, src/list_local.F90,
+ * src/job_md.F90:94-133,700-767). */
+int sis_gpu_create(const sis_topology *top, const sis_params *par, sis_ctx **out);
+void sis_gpu_destroy(sis_ctx *ctx);
+/* number of beads of instance inst (nmp), or of all instances for inst = -1 */
+int sis_gpu_nmp(const sis_ctx *ctx, int32_t inst);
+
+/* State of instance inst: xyz/velos/accels (3,nmp); NULL leaves a field
+ * unchanged.  inst = -1 addresses all beads of all instances at once.
+ * (src/var_state.F90 xyz, velos, accels) */
+int sis_gpu_set_state(sis_ctx *ctx, int32_t inst, const double *xyz, const double *velos, const double *accels);
+int sis_gpu_get_state(sis_ctx *ctx, int32_t inst, double *xyz, double *velos, double *accels);
+/* Maxwell-Boltzmann velocities and initial GJF-2GJ accels from the Philox
+ * stream (src/job_md.F90:214-238). */
+int sis_gpu_init_velocities(sis_ctx *ctx);
+
+/* neighbor_list(irep): pbc_wrap + list rebuild of instance inst (-1: all);
+ * replaces src/neighbor_list.F90:1 and src/pbc.F90:196-226. */
+int sis_gpu_neighbor_list(sis_ctx *ctx, int32_t inst);
+/* Copies a list of instance inst (kind SIS_LIST_*, 1-based local indices,
+ * records (2,n) or (7,n) in unspecified order).  *n_out = number of records. */
+int sis_gpu_get_list(sis_ctx *ctx, int32_t inst, int32_t kind, int32_t *out, int32_t cap, int32_t *n_out);
+/* bp_coef(2,n) (dH, dS) aligned with the SIS_LIST_BP records of the last get_list call order */
+int sis_gpu_get_bp_coef(sis_ctx *ctx, int32_t inst, double *out, int32_t cap, int32_t *n_out);
+
+/* force(irep, forces): forces(3,nmp) of instance inst at the current
+ * coordinates (src/force.F90:1).  Also caches the base-pair energies as the
+ * reference's flg_bp_energy does. */
+int sis_gpu_force(sis_ctx *ctx, int32_t inst, double *forces);
+/* forces of one term: 1 bond, 2 angle, 3 dihedral, 4 base pair, 5 WCA, 6 DH */
+int sis_gpu_force_term(sis_ctx *ctx, int32_t inst, int32_t term, double *forces);
+/* energy_sumup(irep, tempK_in, energies(0:10)) (src/energy_sumup.F90:1).
+ * The base-pair slot uses the energies cached by the last force evaluation
+ * while that cache is valid, as src/energy_bp.F90 does. */
+int sis_gpu_energy_sumup(sis_ctx *ctx, int32_t inst, double tempK, double *energies11);
+/* energy_kinetic (src/energy_kinetic.F90) */
+int sis_gpu_energy_kinetic(sis_ctx *ctx, int32_t inst, double *ekin);
+/* invalidates the base-pair energy cache (flg_bp_energy = .False.) */
+int sis_gpu_invalidate_bp_cache(sis_ctx *ctx);
+
+/* Advances all instances by nsteps MD steps (src/job_md.F90:360-460): per
+ * step and instance the displacement-triggered list rebuild, forces, noise
+ * and the GJF-2GJ (or Ermak-McCammon) update.  noise == NULL draws Gaussian
+ * noise from a counter-based Philox4x32-10 stream; otherwise noise holds
+ * [nsteps][n_beads_total][3] doubles in the reference's rnd_bm order. */
+int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise);
+
+/* set_ele + set_md_coef for one instance at a new temperature / salt
+ * (src/set_ele.F90, src/job_md.F90:700-767). */
+int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic_strength);
+/* derived per-instance electrostatic values [ele_coef, lambdaD, ele_cutoff, diele] */
+int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *out4);
+
+int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *st);
+/* Human-readable description of the last error on this context. */
+const char *sis_gpu_last_error(const sis_ctx *ctx);
+
+/* Timing on the context's stream (CUDA events), for benchmarks. */
+int sis_gpu_event_record(sis_ctx *ctx, int32_t slot);
+int sis_gpu_event_elapsed(sis_ctx *ctx, int32_t slot_a, int32_t slot_b, float *ms);
+int sis_gpu_synchronize(sis_ctx *ctx);
+/* Writes a device buffer larger than L2 on the context's stream. */
+int sis_gpu_flush_l2(sis_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+int64_t sis_gpu_kernel_launches(const sis_ctx *ctx);
+/* Like sis_gpu_step (Philox noise) with CUDA events around every kernel
+ * group on the context's stream; ms[0..2] receive the summed durations of the
+ * base-pair, step and rebuild kernels.  For roofline measurements. */
+int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

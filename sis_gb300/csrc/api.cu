@@ -1,0 +1,908 @@
+// libsisgpu host side: context, set-up derivations and the C ABI of
+// include/sis_gpu.h.
+//
+// Set-up restates, for the device tables, the reference's init_bp
+// (cutoff_ddist, bp_cutoff_dist, the NN triplet table), set_ele (dielectric
+// constant, Bjerrum length, ele_coef, Debye length), list_local (the bonded
+// topology, here implicit in the per-bead chain information) and the
+// friction / mass / GJF-2GJ coefficients of job_md.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/sis_gpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace sisg;
+
+namespace {
+
+// const_phys.F90:5-13
+const double PI = 4.0 * atan(1.0);
+const double EPS0 = 8.8541878128e-12;
+const double ELE = 1.602176634e-19;
+const double BOLTZ_J = 1.380649e-23;
+const double N_AVO = 6.02214076e23;
+const double KCAL2JOUL = 4184.0;
+const double JOUL2KCAL_MOL = (1.0 / KCAL2JOUL) * N_AVO;
+const double BOLTZ_KCAL_MOL = BOLTZ_J * JOUL2KCAL_MOL;
+
+constexpr int kAllPairsMax = 4096;
+constexpr int kEvents = 16;
+
+bool is_comp(int a, int b) {
+    return (a == 0 && b == 1) || (a == 1 && (b == 0 || b == 2)) || (a == 2 && (b == 3 || b == 1)) || (a == 3 && b == 2);
+}
+
+// NNT index (1..21) of the stack 5'-ij-3'/3'-kl-5' (const_idx.F90 char2nnt, with its aliases)
+int nnt_index(int i, int j, int k, int l) {
+    static const char C[4] = {'A', 'U', 'G', 'C'};
+    static const char *canon[21] = {"GC_CG", "CC_GG", "GA_CU", "CG_GC", "AC_UG", "CA_GU", "AG_UC", "UA_AU", "AU_UA", "AA_UU", "GC_UG",
+                                    "CU_GG", "GG_CU", "CG_GU", "AU_UG", "GA_UU", "UG_GU", "UA_GU", "GG_UU", "GU_UG", "AG_UU"};
+    static const char *alias[21] = {"",      "GG_CC", "UC_AG", "",      "GU_CA", "UG_AC", "CU_GA", "",      "",      "UU_AA", "GU_CG",
+                                    "GG_UC", "UC_GG", "UG_GC", "GU_UA", "UU_AG", "",      "UG_AU", "UU_GG", "",      "UU_GA"};
+    char s[6] = {C[i], C[j], '_', C[k], C[l], 0};
+    for (int n = 0; n < 21; ++n)
+        if (!strcmp(s, canon[n]) || (alias[n][0] && !strcmp(s, alias[n]))) return n + 1;
+    return 0;
+}
+
+} // namespace
+
+struct sis_ctx {
+    Dev D{};
+    GlobP g{};
+    sis_params p{};
+    int n = 0, n_inst = 0, cur = 0, G = 8;
+    std::vector<InstP> ip;
+    std::vector<int4> binfo;
+    std::vector<int> seq;
+    std::vector<double> mass;
+    std::vector<double> fric;
+    std::vector<double> ionic;
+    InstP *ip_d = nullptr;
+    BPP bpp[MAX_BP_TYPES]{};
+    double bp_cutoff_dist = 0.0;
+    RebuildPlan plan{};
+    int2 *items_d = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[kEvents]{};
+    bool lists_valid = false, state_set = false, bp_cache = false;
+    long long launches = 0, steps = 0;
+    std::string err;
+    double *noise_d = nullptr;
+    size_t noise_cap = 0;
+    double *fout_d = nullptr;
+    void *flush_d = nullptr;
+    size_t flush_bytes = 0;
+    std::vector<void *> allocs;
+    double4 *pin = nullptr; // pinned staging buffer for state transfers (n double4)
+    cudaGraphExec_t gexec = nullptr;
+    int graph_steps = 0;
+    int n_vel_init = 0;
+};
+
+namespace {
+
+int fail(sis_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+#define CK(call)                                                                                                               \
+    do {                                                                                                                       \
+        cudaError_t e_ = (call);                                                                                               \
+        if (e_ != cudaSuccess) return fail(ctx, SIS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));             \
+    } while (0)
+
+template <typename T> int dalloc(sis_ctx *ctx, T **p, size_t count) {
+    void *q = nullptr;
+    const size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+    if (cudaMalloc(&q, bytes) != cudaSuccess) return fail(ctx, SIS_ERR_NOMEM, "device allocation failed");
+    if (cudaMemset(q, 0, bytes) != cudaSuccess) return fail(ctx, SIS_ERR_CUDA, "memset failed");
+    ctx->allocs.push_back(q);
+    *p = (T *)q;
+    return SIS_OK;
+}
+
+// set_ele.F90:45-99 (default constants) for instance k
+void set_ele(sis_ctx *ctx, int k) {
+    InstP &I = ctx->ip[k];
+    const sis_params &p = ctx->p;
+    const double MM_A = 87.740, MM_B = -0.40008, MM_C = 9.398e-4, MM_D = -1.410e-6;
+    const double T = I.tempK;
+    double Tc, diele;
+    I.diele_dTcoef = 0.0;
+    if (p.temp_independent == 0) {
+        Tc = T - 273.15;
+        diele = MM_A + MM_B * Tc + MM_C * Tc * Tc + MM_D * Tc * Tc * Tc;
+    } else {
+        Tc = p.tempK_ref - 273.15;
+        diele = MM_A + MM_B * Tc + MM_C * Tc * Tc + MM_D * Tc * Tc * Tc;
+        I.diele_dTcoef = 1.0 + p.tempK_ref / diele * (MM_B + 2.0 * MM_C * Tc + 3.0 * MM_D * Tc * Tc);
+    }
+    const double lb = ELE * ELE / (4.0 * PI * EPS0 * diele * BOLTZ_J * T) * 1.0e10;
+    const double Zp = p.length_per_charge / lb;
+    double coef = JOUL2KCAL_MOL * 1.0e10 * (ELE * ELE) / (4.0 * PI * EPS0 * diele);
+    coef = coef * (Zp * Zp);
+    const double lambdaD = 1.0e10 * sqrt((1.0e-3 * EPS0 * diele * BOLTZ_J) / (2.0 * N_AVO * (ELE * ELE))) * sqrt(T / ctx->ionic[k]);
+    I.ele_coef = coef;
+    I.rcdist = 1.0 / lambdaD;
+    I.ele_cut = (p.ele_cutoff_type == 2) ? p.ele_cutoff_inp * lambdaD : p.ele_cutoff_inp;
+    I.ele_cut2 = I.ele_cut * I.ele_cut;
+    I.ele_coef_f = (float)I.ele_coef;
+    I.rcdist_f = (float)I.rcdist;
+    I.ele_cut2_f = (float)I.ele_cut2;
+    const double m = p.nl_margin;
+    I.ele_nl_cut2 = p.flg_ele ? (I.ele_cut + m) * (I.ele_cut + m) : -1.0;
+}
+
+double diele_of(const sis_ctx *ctx, int k) {
+    const double MM_A = 87.740, MM_B = -0.40008, MM_C = 9.398e-4, MM_D = -1.410e-6;
+    const double Tc = (ctx->p.temp_independent == 0 ? ctx->ip[k].tempK : ctx->p.tempK_ref) - 273.15;
+    return MM_A + MM_B * Tc + MM_C * Tc * Tc + MM_D * Tc * Tc * Tc;
+}
+
+// job_md.F90:94-133 friction and masses, set_md_coef job_md.F90:700-767
+void md_coefs(sis_ctx *ctx, std::vector<double4> &mdc) {
+    const sis_params &p = ctx->p;
+    const double radius = 10.0;
+    const double v = (p.integrator == SIS_INTGRT_GJF2GJ) ? p.viscosity_Pas * sqrt(1.0e3 / KCAL2JOUL) * N_AVO * 1.0e-20
+                                                          : (JOUL2KCAL_MOL * 1.0e-18) * p.viscosity_Pas;
+    const double fric = 6.0 * PI * v * radius;
+    mdc.resize(ctx->n);
+    ctx->mass.resize(ctx->n);
+    for (int i = 0; i < ctx->n; ++i) {
+        double m;
+        switch (ctx->seq[i]) {
+        case 0: m = 328.212; break; // A
+        case 2: m = 344.212; break; // G
+        case 3: m = 304.182; break; // C
+        case 1: m = 305.164; break; // U
+        default: m = 320.443; break; // D
+        }
+        ctx->mass[i] = m;
+        const double T = ctx->ip[ctx->binfo[i].x].tempK;
+        const double dt = p.dt;
+        if (p.integrator == SIS_INTGRT_GJF2GJ) {
+            const double c1 = 0.5 * dt * fric / m;
+            const double c2 = sqrt(1.0 / (1.0 + c1));
+            mdc[i] = make_double4((1.0 - c1) / (1.0 + c1), c2 * dt / m, c2 * dt,
+                                  0.5 * c2 / m * sqrt(2.0 * fric * BOLTZ_KCAL_MOL * T * dt));
+        } else {
+            mdc[i] = make_double4(dt / fric, 0.0, 0.0, sqrt(2.0 * BOLTZ_KCAL_MOL * T * dt / fric));
+        }
+    }
+}
+
+// init_bp.F90:39-172 NN triplet tables (model 5)
+void bp3_tables(const sis_params &p, std::vector<short> &hash, std::vector<double> &dH, std::vector<double> &dS) {
+    hash.assign(4097, 0);
+    dH.assign(469, 0.0);
+    dS.assign(469, 0.0);
+    if (p.bp_model != 5) return;
+    auto key = [](int w, int x, int u, int z, int y, int v) {
+        if (x < y) return 1 + w + x * 4 + u * 16 + z * 64 + y * 256 + v * 1024;
+        return 1 + v + y * 4 + z * 16 + u * 64 + x * 256 + w * 1024;
+    };
+    auto isAU = [](int a, int b) { return (a == 0 && b == 1) || (a == 1 && b == 0); };
+    auto isGC = [](int a, int b) { return (a == 2 && b == 3) || (a == 3 && b == 2); };
+    auto isGU = [](int a, int b) { return (a == 2 && b == 1) || (a == 1 && b == 2); };
+    int h = 0;
+    for (int x = 0; x <= 2; ++x)
+        for (int y = x + 1; y <= 3; ++y) {
+            if (!is_comp(x, y)) continue;
+            for (int w = 0; w <= 3; ++w)
+                for (int z = 0; z <= 3; ++z) {
+                    const bool cwz = is_comp(w, z);
+                    const double h1 = cwz ? 0.5 * (p.nn_dH[nnt_index(w, x, z, y) - 1] - p.dH0) : 0.0;
+                    const double s1 = cwz ? 0.5 * (p.nn_dS[nnt_index(w, x, z, y) - 1] - p.dS0) : 0.0;
+                    for (int u = 0; u <= 3; ++u)
+                        for (int v = 0; v <= 3; ++v) {
+                            const bool cuv = is_comp(u, v);
+                            if (!cwz && !cuv) continue;
+                            ++h;
+                            hash[key(w, x, u, z, y, v)] = (short)h;
+                            if (cuv) {
+                                dH[h] = h1 + 0.5 * (p.nn_dH[nnt_index(x, u, y, v) - 1] - p.dH0);
+                                dS[h] = (s1 + 0.5 * (p.nn_dS[nnt_index(x, u, y, v) - 1] - p.dS0)) * 1.0e-3;
+                            } else {
+                                dH[h] = h1;
+                                dS[h] = s1 * 1.0e-3;
+                            }
+                            if (p.nnend && cwz != cuv) {
+                                const int o1 = cwz ? w : u, o2 = cwz ? z : v;
+                                int k = 0;
+                                if (isAU(x, y)) k = isAU(o1, o2) ? 1 : isGC(o1, o2) ? 2 : isGU(o1, o2) ? 3 : 0;
+                                else if (isGU(x, y)) k = isAU(o1, o2) ? 5 : isGC(o1, o2) ? 4 : isGU(o1, o2) ? 6 : 0;
+                                if (k) {
+                                    dH[h] = dH[h] + p.nnend_dH[k - 1] - p.dHend0;
+                                    dS[h] = dS[h] + (p.nnend_dS[k - 1] - p.dSend0) * 1.0e-3;
+                                }
+                            }
+                        }
+                }
+        }
+}
+
+int upload_ip(sis_ctx *ctx) {
+    CK(cudaMemcpyAsync(ctx->ip_d, ctx->ip.data(), sizeof(InstP) * ctx->n_inst, cudaMemcpyHostToDevice, ctx->st));
+    return SIS_OK;
+}
+
+int ensure_lists(sis_ctx *ctx);
+
+int run_rebuild(sis_ctx *ctx) {
+    ctx->launches += 2 + (ctx->plan.n_small_items > 0) + 5 * (ctx->plan.n_large_items > 0);
+    CK(launch_rebuild(ctx->D, ctx->g, ctx->cur, ctx->plan, ctx->st));
+    return SIS_OK;
+}
+
+int flag_all(sis_ctx *ctx, int inst) {
+    std::vector<int> f(ctx->n_inst, 0);
+    for (int k = 0; k < ctx->n_inst; ++k) f[k] = (inst < 0 || inst == k) ? 1 : 0;
+    CK(cudaMemcpyAsync(ctx->D.flag, f.data(), sizeof(int) * ctx->n_inst, cudaMemcpyHostToDevice, ctx->st));
+    const int one = 1;
+    CK(cudaMemcpyAsync(ctx->D.any, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
+int ensure_lists(sis_ctx *ctx) {
+    if (!ctx->state_set) return fail(ctx, SIS_ERR_STATE, "coordinates have not been set");
+    if (ctx->lists_valid) return SIS_OK;
+    int rc = flag_all(ctx, -1);
+    if (rc) return rc;
+    rc = run_rebuild(ctx);
+    if (rc) return rc;
+    ctx->lists_valid = true;
+    return SIS_OK;
+}
+
+int check_err(sis_ctx *ctx) {
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, ctx->D.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (e & ERR_PAIR_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "pair list capacity exceeded");
+    if (e & ERR_BP_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "base-pair list capacity exceeded");
+    if (e & ERR_NONFINITE) return fail(ctx, SIS_ERR_NONFINITE, "non-finite displacement");
+    return SIS_OK;
+}
+
+int inst_range(const sis_ctx *ctx, int inst, int &off, int &cnt) {
+    if (inst < -1 || inst >= ctx->n_inst) return SIS_ERR_ARG;
+    off = inst < 0 ? 0 : ctx->ip[inst].bead_off;
+    cnt = inst < 0 ? ctx->n : ctx->ip[inst].n;
+    return SIS_OK;
+}
+
+int bp_blocks(const sis_ctx *ctx) { return 2 * 152; }
+
+int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
+    if (ctx->g.bp_model > 0) {
+        CK(launch_bp(ctx->D, ctx->g, ctx->cur, 0, -1.0, bp_blocks(ctx), ctx->st));
+        ctx->launches++;
+    }
+    CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, noise, ns, ctx->st));
+    ctx->launches++;
+    ctx->cur ^= 1;
+    return run_rebuild(ctx);
+}
+
+} // namespace
+
+// ====================================================================== API
+extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, sis_ctx **out) {
+    if (!top || !par || !out || top->n_inst <= 0) return SIS_ERR_ARG;
+    sis_ctx *ctx = new sis_ctx();
+    *out = nullptr;
+    ctx->p = *par;
+    const sis_params &p = ctx->p;
+    ctx->n_inst = top->n_inst;
+    // ------------------------------------------------ topology and instances
+    ctx->ip.resize(ctx->n_inst);
+    ctx->ionic.resize(ctx->n_inst);
+    int nb = 0;
+    for (int k = 0; k < ctx->n_inst; ++k) {
+        InstP &I = ctx->ip[k];
+        memset(&I, 0, sizeof(InstP));
+        I.bead_off = nb;
+        for (int c = top->inst_chain_off[k]; c < top->inst_chain_off[k + 1]; ++c) {
+            const int len = top->chain_len[c];
+            if (len < 1) {
+                delete ctx;
+                return SIS_ERR_ARG;
+            }
+            const bool circ = top->chain_moltype[c] == 2;
+            for (int l = 0; l < len; ++l) {
+                const int i = nb + l;
+                const int s = top->seq[i];
+                const int q = top->has_charge ? (top->has_charge[i] ? 1 : 0) : 1;
+                ctx->binfo.push_back(make_int4(k, nb, len | (circ ? (int)0x80000000u : 0), l | (s << 24) | (q << 28)));
+                ctx->seq.push_back(s);
+            }
+            nb += len;
+        }
+        I.n = nb - I.bead_off;
+        I.stream = top->stream ? top->stream[k] : (unsigned)k;
+        I.step0 = 0ull;
+        I.tempK = top->tempK[k];
+        ctx->ionic[k] = top->ionic_strength[k];
+        const double *bx = top->box ? top->box + 3 * k : nullptr;
+        I.pbc = bx && bx[0] > 0.0 && bx[1] > 0.0 && bx[2] > 0.0;
+        for (int d = 0; d < 3; ++d) {
+            I.box[d] = I.pbc ? bx[d] : 0.0;
+            I.half[d] = 0.5 * I.box[d];
+            I.fsc[d] = I.pbc ? 4294967296.0 / I.box[d] : 1048576.0;
+            I.finv[d] = (float)(1.0 / I.fsc[d]);
+        }
+    }
+    ctx->n = nb;
+    if (nb <= 0 || nb >= (1 << 30)) {
+        delete ctx;
+        return SIS_ERR_ARG;
+    }
+    // ------------------------------------------------------ base pairs
+    for (int t = 0; t < 3; ++t) {
+        const double *f = p.bp_ff[t];
+        BPP b{};
+        b.U0 = f[0]; b.bond_k = f[1]; b.bond_r = f[2];
+        for (int a = 0; a < 4; ++a) {
+            b.angl_k[a] = f[3 + a];
+            b.angl_theta[a] = f[7 + a];
+        }
+        b.dihd_k[0] = f[11]; b.dihd_k[1] = f[12]; b.dihd_phi[0] = f[13]; b.dihd_phi[1] = f[14];
+        ctx->bpp[1 + t] = b;
+        // read_force_field.F90:203-258: CG/UA/UG swap k1<->k2, k3<->k4, not the angles
+        BPP r = b;
+        r.angl_k[0] = b.angl_k[1]; r.angl_k[1] = b.angl_k[0];
+        r.angl_k[2] = b.angl_k[3]; r.angl_k[3] = b.angl_k[2];
+        ctx->bpp[4 + t] = r;
+    }
+    // init_bp.F90:315-346
+    if (fabs(p.bp_cutoff_energy) <= 2.220446049250313e-16) {
+        ctx->bp_cutoff_dist = 18.0;
+        for (int t = 1; t <= 6; ++t) ctx->bpp[t].cutoff_ddist = ctx->bp_cutoff_dist - 13.8;
+    } else {
+        ctx->bp_cutoff_dist = 0.0;
+        for (int t = 1; t <= 6; ++t) {
+            ctx->bpp[t].cutoff_ddist = sqrt(log(fabs(10.0 / p.bp_cutoff_energy)) / ctx->bpp[t].bond_k);
+            const double cut = ctx->bpp[t].bond_r + ctx->bpp[t].cutoff_ddist;
+            if (cut > ctx->bp_cutoff_dist) ctx->bp_cutoff_dist = cut;
+        }
+    }
+    std::vector<short> hash;
+    std::vector<double> dH, dS;
+    bp3_tables(p, hash, dH, dS);
+    // ---------------------------------------------- per-instance cutoffs
+    const double m = p.nl_margin;
+    int cap = 32, bp_total_cap = 0, ncells = 0;
+    for (int k = 0; k < ctx->n_inst; ++k) {
+        InstP &I = ctx->ip[k];
+        set_ele(ctx, k);
+        I.wca_nl_cut2 = (p.wca_sigma + m) * (p.wca_sigma + m);
+        I.bp_nl_cut2 = p.bp_model > 0 ? (ctx->bp_cutoff_dist + m) * (ctx->bp_cutoff_dist + m) : -1.0;
+        const int bpc = p.bp_cap > 0 ? p.bp_cap : 12;
+        I.bp_off = bp_total_cap;
+        I.bp_cap = bpc * I.n + 64;
+        bp_total_cap += I.bp_cap;
+        I.large = 0;
+        if (I.pbc && I.n > kAllPairsMax) {
+            double mc2 = std::max(std::max(I.wca_nl_cut2, I.ele_nl_cut2), I.bp_nl_cut2);
+            // type-2 cutoffs move with lambdaD; leave room for the largest
+            const double lc = sqrt(mc2) * 1.0005;
+            int nc[3];
+            for (int d = 0; d < 3; ++d) nc[d] = (int)floor(I.box[d] / lc);
+            if (nc[0] >= 3 && nc[1] >= 3 && nc[2] >= 3) {
+                I.large = 1;
+                I.cell_base = ncells;
+                for (int d = 0; d < 3; ++d) {
+                    I.nc[d] = nc[d];
+                    I.cell_len[d] = I.box[d] / nc[d];
+                }
+                ncells += nc[0] * nc[1] * nc[2];
+            }
+        }
+        const int need = I.large ? 512 : std::min(I.n - 1, 512);
+        cap = std::max(cap, need);
+    }
+    cap = (cap + 31) / 32 * 32;
+    if (p.nbr_cap > 0) cap = p.nbr_cap;
+    // ------------------------------------------------------ global params
+    GlobP &g = ctx->g;
+    g.n = ctx->n;
+    g.n_inst = ctx->n_inst;
+    g.cap = cap;
+    g.prec = p.precision;
+    g.integrator = p.integrator;
+    g.angl_reb = p.angl_reb;
+    g.dih_type = p.dih_type;
+    g.bp_model = p.bp_model;
+    g.flg_ele = p.flg_ele;
+    g.temp_indep = p.temp_independent;
+    g.bp_min_loop = p.bp_min_loop;
+    g.bp_jnext_compat = p.bp_jnext_compat;
+    g.ele_excl_bond = p.ele_excl_bond;
+    g.ele_excl_angle = p.ele_excl_angle;
+    g.bond_k = p.bond_k; g.bond_r0 = p.bond_r0;
+    g.angl_k = p.angl_k; g.angl_t0 = p.angl_t0; g.cos_t0 = cos(p.angl_t0);
+    g.dih_k = p.dih_k; g.dih_w = p.dih_w; g.dih_p0 = p.dih_p0;
+    g.wca_sigma = p.wca_sigma; g.wca_eps = p.wca_eps;
+    g.wca_sig2 = p.wca_sigma * p.wca_sigma;
+    g.wca_coef = 12.0 * p.wca_eps / g.wca_sig2;
+    g.bp_cutoff_energy = p.bp_cutoff_energy;
+    g.nl_margin = p.nl_margin;
+    g.f_bond_k = (float)g.bond_k; g.f_bond_r0 = (float)g.bond_r0;
+    g.f_angl_k = (float)g.angl_k; g.f_angl_t0 = (float)g.angl_t0; g.f_cos_t0 = (float)g.cos_t0;
+    g.f_dih_k = (float)g.dih_k; g.f_dih_w = (float)g.dih_w; g.f_dih_p0 = (float)g.dih_p0;
+    g.f_wca_sig2 = (float)g.wca_sig2; g.f_wca_coef = (float)g.wca_coef;
+    g.f_wca_sigma = (float)g.wca_sigma; g.f_wca_eps = (float)g.wca_eps;
+    g.seed = p.seed;
+    // ----------------------------------------------------------- device
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return SIS_ERR_CUDA;
+    }
+    for (int e = 0; e < kEvents; ++e) cudaEventCreate(&ctx->ev[e]);
+    Dev &D = ctx->D;
+    const int n = ctx->n, ni = ctx->n_inst;
+    int rc = 0;
+    rc |= dalloc(ctx, &D.x[0], n);
+    rc |= dalloc(ctx, &D.x[1], n);
+    rc |= dalloc(ctx, &D.mir[0], n);
+    rc |= dalloc(ctx, &D.mir[1], n);
+    rc |= dalloc(ctx, &D.v, n);
+    rc |= dalloc(ctx, &D.beta, n);
+    rc |= dalloc(ctx, &D.move, n);
+    rc |= dalloc(ctx, &D.mdc, n);
+    rc |= dalloc(ctx, &D.fbp, n);
+    rc |= dalloc(ctx, &D.binfo, n);
+    rc |= dalloc(ctx, &D.mass, n);
+    rc |= dalloc(ctx, &D.nbr, (size_t)n * cap);
+    rc |= dalloc(ctx, &D.nnbr, n);
+    rc |= dalloc(ctx, &D.bps, bp_total_cap);
+    rc |= dalloc(ctx, &D.bps_n, bp_total_cap);
+    rc |= dalloc(ctx, &D.bp_cnt, 2 * ni);
+    rc |= dalloc(ctx, &D.bp_total, 1);
+    rc |= dalloc(ctx, &D.ene_bp, bp_total_cap);
+    rc |= dalloc(ctx, &D.bp_status, bp_total_cap);
+    BPP *bpp_d;
+    short *hash_d;
+    double *dH_d, *dS_d;
+    rc |= dalloc(ctx, &bpp_d, MAX_BP_TYPES);
+    rc |= dalloc(ctx, &hash_d, 4097);
+    rc |= dalloc(ctx, &dH_d, 469);
+    rc |= dalloc(ctx, &dS_d, 469);
+    rc |= dalloc(ctx, &ctx->ip_d, ni);
+    rc |= dalloc(ctx, &D.m1, ni);
+    rc |= dalloc(ctx, &D.m2, ni);
+    rc |= dalloc(ctx, &D.flag, ni);
+    rc |= dalloc(ctx, &D.any, 1);
+    rc |= dalloc(ctx, &D.ticket, 2);
+    rc |= dalloc(ctx, &D.step_ctr, 1);
+    rc |= dalloc(ctx, &D.err, 1);
+    rc |= dalloc(ctx, &D.max_need, 2);
+    rc |= dalloc(ctx, &D.rebuilds, 1);
+    rc |= dalloc(ctx, &D.bead_cell, n);
+    rc |= dalloc(ctx, &D.cell_cnt, ncells);
+    rc |= dalloc(ctx, &D.cell_start, ncells + 1);
+    rc |= dalloc(ctx, &D.cell_beads, n);
+    rc |= dalloc(ctx, &D.ene, (size_t)12 * ni);
+    rc |= dalloc(ctx, &ctx->fout_d, (size_t)3 * n);
+    if (rc) {
+        sis_gpu_destroy(ctx);
+        return SIS_ERR_NOMEM;
+    }
+    D.n_cells = ncells;
+    D.bpp = bpp_d;
+    D.bp3_hash = hash_d;
+    D.bp3_dH = dH_d;
+    D.bp3_dS = dS_d;
+    D.ip = ctx->ip_d;
+    std::vector<double4> mdc;
+    md_coefs(ctx, mdc);
+    // rebuild work items
+    std::vector<int2> small, large;
+    for (int k = 0; k < ni; ++k) {
+        const InstP &I = ctx->ip[k];
+        if (I.large)
+            for (int l = 0; l < I.n; l += 256) large.push_back(make_int2(k, l));
+        else
+            for (int l = 0; l < I.n; l += 32) small.push_back(make_int2(k, l));
+    }
+    std::vector<int2> items(small);
+    items.insert(items.end(), large.begin(), large.end());
+    if (dalloc(ctx, &ctx->items_d, items.size())) {
+        sis_gpu_destroy(ctx);
+        return SIS_ERR_NOMEM;
+    }
+    ctx->plan.small_items = ctx->items_d;
+    ctx->plan.n_small_items = (int)small.size();
+    ctx->plan.small_grid = std::max(1, std::min((int)small.size(), 4096));
+    ctx->plan.large_items = ctx->items_d + small.size();
+    ctx->plan.n_large_items = (int)large.size();
+    ctx->plan.large_grid = std::max(1, std::min((int)large.size(), 2048));
+    // uploads
+    bool ok = true;
+    ok &= cudaMemcpy(D.binfo, ctx->binfo.data(), sizeof(int4) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(D.mdc, mdc.data(), sizeof(double4) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(D.mass, ctx->mass.data(), sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(bpp_d, ctx->bpp, sizeof(BPP) * MAX_BP_TYPES, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(hash_d, hash.data(), sizeof(short) * 4097, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(dH_d, dH.data(), sizeof(double) * 469, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(dS_d, dS.data(), sizeof(double) * 469, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(ctx->ip_d, ctx->ip.data(), sizeof(InstP) * ni, cudaMemcpyHostToDevice) == cudaSuccess;
+    ok &= cudaMemcpy(ctx->items_d, items.data(), sizeof(int2) * std::max<size_t>(1, items.size()), cudaMemcpyHostToDevice) ==
+          cudaSuccess;
+    if (!ok) {
+        sis_gpu_destroy(ctx);
+        return SIS_ERR_CUDA;
+    }
+    // lanes per bead from the expected list length
+    ctx->G = 8;
+    *out = ctx;
+    return SIS_OK;
+}
+
+extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
+    if (!ctx) return;
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    for (void *q : ctx->allocs) cudaFree(q);
+    if (ctx->noise_d) cudaFree(ctx->noise_d);
+    if (ctx->flush_d) cudaFree(ctx->flush_d);
+    if (ctx->pin) cudaFreeHost(ctx->pin);
+    for (int e = 0; e < kEvents; ++e)
+        if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+extern "C" int sis_gpu_nmp(const sis_ctx *ctx, int32_t inst) {
+    if (!ctx || inst < -1 || inst >= ctx->n_inst) return SIS_ERR_ARG;
+    return inst < 0 ? ctx->n : ctx->ip[inst].n;
+}
+
+extern "C" int sis_gpu_set_state(sis_ctx *ctx, int32_t inst, const double *xyz, const double *velos, const double *accels) {
+    if (!ctx) return SIS_ERR_ARG;
+    int off, cnt;
+    if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
+    if (!ctx->pin) CK(cudaMallocHost((void **)&ctx->pin, sizeof(double4) * ctx->n));
+    double4 *h = ctx->pin;
+    const double *src[3] = {xyz, velos, accels};
+    double4 *dst[3] = {ctx->D.x[ctx->cur], ctx->D.v, ctx->D.beta};
+    for (int f = 0; f < 3; ++f) {
+        if (!src[f]) continue;
+        for (int i = 0; i < cnt; ++i) h[i] = make_double4(src[f][3 * i], src[f][3 * i + 1], src[f][3 * i + 2], 0.0);
+        CK(cudaMemcpyAsync(dst[f] + off, h, sizeof(double4) * cnt, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    if (xyz) {
+        CK(launch_mirror(ctx->D, ctx->g, ctx->cur, ctx->st));
+        ctx->launches++;
+        ctx->lists_valid = false;
+        ctx->bp_cache = false;
+        if (inst < 0) ctx->state_set = true;
+        else ctx->state_set = true;
+    }
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_get_state(sis_ctx *ctx, int32_t inst, double *xyz, double *velos, double *accels) {
+    if (!ctx) return SIS_ERR_ARG;
+    int off, cnt;
+    if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
+    if (!ctx->pin) CK(cudaMallocHost((void **)&ctx->pin, sizeof(double4) * ctx->n));
+    double4 *h = ctx->pin;
+    double *dst[3] = {xyz, velos, accels};
+    const double4 *src[3] = {ctx->D.x[ctx->cur], ctx->D.v, ctx->D.beta};
+    for (int f = 0; f < 3; ++f) {
+        if (!dst[f]) continue;
+        CK(cudaMemcpyAsync(h, src[f] + off, sizeof(double4) * cnt, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int i = 0; i < cnt; ++i) {
+            dst[f][3 * i] = h[i].x;
+            dst[f][3 * i + 1] = h[i].y;
+            dst[f][3 * i + 2] = h[i].z;
+        }
+    }
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_init_velocities(sis_ctx *ctx) {
+    if (!ctx) return SIS_ERR_ARG;
+    const unsigned long long ctr = (1ull << 62) + 2ull * (unsigned long long)(ctx->n_vel_init++);
+    CK(launch_init_velocities(ctx->D, ctx->g, ctr, ctx->st));
+    ctx->launches++;
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_neighbor_list(sis_ctx *ctx, int32_t inst) {
+    if (!ctx || inst < -1 || inst >= ctx->n_inst) return SIS_ERR_ARG;
+    if (!ctx->state_set) return fail(ctx, SIS_ERR_STATE, "coordinates have not been set");
+    if (!ctx->lists_valid) inst = -1;
+    int rc = flag_all(ctx, inst);
+    if (rc) return rc;
+    rc = run_rebuild(ctx);
+    if (rc) return rc;
+    ctx->lists_valid = true;
+    ctx->bp_cache = false;
+    CK(cudaStreamSynchronize(ctx->st));
+    return check_err(ctx);
+}
+
+extern "C" int sis_gpu_get_list(sis_ctx *ctx, int32_t inst, int32_t kind, int32_t *out, int32_t cap, int32_t *n_out) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || kind < 0 || kind > 2 || !n_out) return SIS_ERR_ARG;
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    const InstP &I = ctx->ip[inst];
+    const int off = I.bead_off, cnt = I.n;
+    std::vector<int> res;
+    if (kind < 2) {
+        std::vector<int> nn(cnt), nb((size_t)cnt * ctx->g.cap);
+        CK(cudaMemcpyAsync(nn.data(), ctx->D.nnbr + off, sizeof(int) * cnt, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaMemcpyAsync(nb.data(), ctx->D.nbr + (size_t)off * ctx->g.cap, sizeof(int) * nb.size(), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        const int bit = kind == 0 ? WCA_BIT : ELE_BIT;
+        for (int i = 0; i < cnt; ++i) {
+            const int c = std::min(nn[i], ctx->g.cap);
+            for (int k = 0; k < c; ++k) {
+                const int e = nb[(size_t)i * ctx->g.cap + k];
+                const int j = (e & IDX_MASK) - off;
+                if ((e & bit) && j > i) {
+                    res.push_back(i + 1);
+                    res.push_back(j + 1);
+                }
+            }
+        }
+        *n_out = (int)(res.size() / 2);
+        if (out) memcpy(out, res.data(), sizeof(int) * std::min<size_t>(res.size(), (size_t)cap * 2));
+    } else {
+        int c = 0;
+        CK(cudaMemcpyAsync(&c, ctx->D.bp_cnt + inst, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        c = std::min(c, I.bp_cap);
+        std::vector<int4> r(std::max(c, 1)), q(std::max(c, 1));
+        CK(cudaMemcpyAsync(r.data(), ctx->D.bps + I.bp_off, sizeof(int4) * c, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaMemcpyAsync(q.data(), ctx->D.bps_n + I.bp_off, sizeof(int4) * c, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int k = 0; k < c; ++k) {
+            const int rec[7] = {r[k].x - off + 1, r[k].y - off + 1, q[k].x - off + 1, q[k].y - off + 1,
+                                q[k].z - off + 1, q[k].w - off + 1, r[k].z & 0xff};
+            res.insert(res.end(), rec, rec + 7);
+        }
+        *n_out = c;
+        if (out) memcpy(out, res.data(), sizeof(int) * std::min<size_t>(res.size(), (size_t)cap * 7));
+    }
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_get_bp_coef(sis_ctx *ctx, int32_t inst, double *out, int32_t cap, int32_t *n_out) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || !n_out) return SIS_ERR_ARG;
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    const InstP &I = ctx->ip[inst];
+    int c = 0;
+    CK(cudaMemcpyAsync(&c, ctx->D.bp_cnt + inst, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    c = std::min(c, I.bp_cap);
+    std::vector<int4> r(std::max(c, 1));
+    std::vector<double> dH(469), dS(469);
+    CK(cudaMemcpyAsync(r.data(), ctx->D.bps + I.bp_off, sizeof(int4) * c, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(dH.data(), ctx->D.bp3_dH, sizeof(double) * 469, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(dS.data(), ctx->D.bp3_dS, sizeof(double) * 469, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int k = 0; k < c && k < cap; ++k) {
+        const int h = r[k].z >> 8;
+        out[2 * k] = dH[h];
+        out[2 * k + 1] = dS[h];
+    }
+    *n_out = c;
+    return SIS_OK;
+}
+
+static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
+    int off, cnt;
+    if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    if ((mask & 8) && ctx->g.bp_model > 0) {
+        CK(launch_bp(ctx->D, ctx->g, ctx->cur, 0, -1.0, bp_blocks(ctx), ctx->st));
+        ctx->launches++;
+        ctx->bp_cache = true;
+    }
+    CK(launch_force(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->fout_d, mask, ctx->st));
+    ctx->launches++;
+    if (forces) CK(cudaMemcpyAsync(forces, ctx->fout_d + 3 * (size_t)off, sizeof(double) * 3 * cnt, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return check_err(ctx);
+}
+
+extern "C" int sis_gpu_force(sis_ctx *ctx, int32_t inst, double *forces) {
+    if (!ctx) return SIS_ERR_ARG;
+    return force_common(ctx, inst, 63, forces);
+}
+
+extern "C" int sis_gpu_force_term(sis_ctx *ctx, int32_t inst, int32_t term, double *forces) {
+    if (!ctx || term < 1 || term > 6) return SIS_ERR_ARG;
+    return force_common(ctx, inst, 1 << (term - 1), forces);
+}
+
+extern "C" int sis_gpu_invalidate_bp_cache(sis_ctx *ctx) {
+    if (!ctx) return SIS_ERR_ARG;
+    ctx->bp_cache = false;
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_energy_sumup(sis_ctx *ctx, int32_t inst, double tempK, double *E) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || !E) return SIS_ERR_ARG;
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    if (!ctx->bp_cache && ctx->g.bp_model > 0) {
+        CK(launch_bp(ctx->D, ctx->g, ctx->cur, 1, tempK, bp_blocks(ctx), ctx->st));
+        ctx->launches++;
+    }
+    CK(cudaMemsetAsync(ctx->D.ene, 0, sizeof(double) * 12 * ctx->n_inst, ctx->st));
+    CK(launch_energy(ctx->D, ctx->g, ctx->cur, ctx->st));
+    ctx->launches += 2;
+    double h[12];
+    CK(cudaMemcpyAsync(h, ctx->D.ene + 12 * (size_t)inst, sizeof(double) * 12, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int k = 0; k <= SIS_ENE_MAX; ++k) E[k] = k == 0 ? 0.0 : h[k];
+    double tot = 0.0;
+    for (int k = 1; k <= SIS_ENE_MAX; ++k) tot += E[k];
+    E[0] = tot;
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_energy_kinetic(sis_ctx *ctx, int32_t inst, double *ekin) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || !ekin) return SIS_ERR_ARG;
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(ctx->D.ene, 0, sizeof(double) * 12 * ctx->n_inst, ctx->st));
+    CK(launch_energy(ctx->D, ctx->g, ctx->cur, ctx->st));
+    ctx->launches += 2;
+    double h[12];
+    CK(cudaMemcpyAsync(h, ctx->D.ene + 12 * (size_t)inst, sizeof(double) * 12, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    *ekin = h[11];
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
+    if (!ctx || nsteps < 0) return SIS_ERR_ARG;
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    if (noise) {
+        const size_t need = (size_t)nsteps * ctx->n * 3;
+        if (need > ctx->noise_cap) {
+            if (ctx->noise_d) cudaFree(ctx->noise_d);
+            ctx->noise_d = nullptr;
+            if (cudaMalloc(&ctx->noise_d, sizeof(double) * need) != cudaSuccess) return fail(ctx, SIS_ERR_NOMEM, "noise buffer");
+            ctx->noise_cap = need;
+        }
+        CK(cudaMemcpyAsync(ctx->noise_d, noise, sizeof(double) * need, cudaMemcpyHostToDevice, ctx->st));
+    }
+    for (int64_t s = 0; s < nsteps; ++s) {
+        rc = enqueue_step(ctx, noise ? ctx->noise_d : nullptr, (long long)s);
+        if (rc) return rc;
+    }
+    ctx->steps += nsteps;
+    ctx->bp_cache = true;
+    CK(cudaStreamSynchronize(ctx->st));
+    return check_err(ctx);
+}
+
+extern "C" int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || tempK <= 0 || ionic <= 0) return SIS_ERR_ARG;
+    ctx->ip[inst].tempK = tempK;
+    ctx->ionic[inst] = ionic;
+    set_ele(ctx, inst);
+    std::vector<double4> mdc;
+    md_coefs(ctx, mdc);
+    const InstP &I = ctx->ip[inst];
+    CK(cudaMemcpyAsync(ctx->D.mdc + I.bead_off, mdc.data() + I.bead_off, sizeof(double4) * I.n, cudaMemcpyHostToDevice, ctx->st));
+    int rc = upload_ip(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *o) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || !o) return SIS_ERR_ARG;
+    const InstP &I = ctx->ip[inst];
+    o[0] = I.ele_coef;
+    o[1] = 1.0 / I.rcdist;
+    o[2] = I.ele_cut;
+    o[3] = diele_of(ctx, inst);
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
+    if (!ctx || !s) return SIS_ERR_ARG;
+    memset(s, 0, sizeof(*s));
+    s->steps = ctx->steps;
+    s->n_beads = ctx->n;
+    s->n_inst = ctx->n_inst;
+    s->lanes_per_bead = ctx->G;
+    long long rb = 0;
+    int e = 0;
+    CK(cudaMemcpyAsync(&rb, ctx->D.rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(&e, ctx->D.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    std::vector<int> nn(ctx->n), bc(ctx->n_inst);
+    CK(cudaMemcpyAsync(nn.data(), ctx->D.nnbr, sizeof(int) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(bc.data(), ctx->D.bp_cnt, sizeof(int) * ctx->n_inst, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    s->rebuilds = rb;
+    s->error_flags = e;
+    for (int i = 0; i < ctx->n; ++i) s->pair_entries += std::min(nn[i], ctx->g.cap);
+    for (int k = 0; k < ctx->n_inst; ++k) s->bp_pairs += std::min(bc[k], ctx->ip[k].bp_cap);
+    return SIS_OK;
+}
+
+extern "C" const char *sis_gpu_last_error(const sis_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+extern "C" int sis_gpu_event_record(sis_ctx *ctx, int32_t slot) {
+    if (!ctx || slot < 0 || slot >= kEvents) return SIS_ERR_ARG;
+    CK(cudaEventRecord(ctx->ev[slot], ctx->st));
+    return SIS_OK;
+}
+extern "C" int sis_gpu_event_elapsed(sis_ctx *ctx, int32_t a, int32_t b, float *ms) {
+    if (!ctx || a < 0 || b < 0 || a >= kEvents || b >= kEvents || !ms) return SIS_ERR_ARG;
+    CK(cudaEventSynchronize(ctx->ev[b]));
+    CK(cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]));
+    return SIS_OK;
+}
+extern "C" int sis_gpu_synchronize(sis_ctx *ctx) {
+    if (!ctx) return SIS_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+extern "C" int sis_gpu_flush_l2(sis_ctx *ctx) {
+    if (!ctx) return SIS_ERR_ARG;
+    if (!ctx->flush_d) {
+        ctx->flush_bytes = (size_t)512 << 20;
+        if (cudaMalloc(&ctx->flush_d, ctx->flush_bytes) != cudaSuccess) return fail(ctx, SIS_ERR_NOMEM, "flush buffer");
+    }
+    CK(cudaMemsetAsync(ctx->flush_d, ctx->launches & 0xff, ctx->flush_bytes, ctx->st));
+    return SIS_OK;
+}
+extern "C" int64_t sis_gpu_kernel_launches(const sis_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
+    if (!ctx || nsteps < 0 || !ms3) return SIS_ERR_ARG;
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    double acc[3] = {0.0, 0.0, 0.0};
+    cudaEvent_t *e = ctx->ev + 8; // events 8..11
+    for (int64_t s = 0; s < nsteps; ++s) {
+        CK(cudaEventRecord(e[0], ctx->st));
+        if (ctx->g.bp_model > 0) {
+            CK(launch_bp(ctx->D, ctx->g, ctx->cur, 0, -1.0, bp_blocks(ctx), ctx->st));
+            ctx->launches++;
+        }
+        CK(cudaEventRecord(e[1], ctx->st));
+        CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
+        ctx->launches++;
+        ctx->cur ^= 1;
+        CK(cudaEventRecord(e[2], ctx->st));
+        rc = run_rebuild(ctx);
+        if (rc) return rc;
+        CK(cudaEventRecord(e[3], ctx->st));
+        CK(cudaEventSynchronize(e[3]));
+        float t;
+        for (int k = 0; k < 3; ++k) {
+            CK(cudaEventElapsedTime(&t, e[k], e[k + 1]));
+            acc[k] += t;
+        }
+    }
+    ctx->steps += nsteps;
+    ctx->bp_cache = true;
+    for (int k = 0; k < 3; ++k) ms3[k] = (float)acc[k];
+    return check_err(ctx);
+}

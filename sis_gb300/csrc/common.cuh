@@ -1,0 +1,195 @@
+// Internal device structures and helpers of libsisgpu (SIS hot path on sm_103a).
+//
+// Device data layout (n = beads of all instances, flat, instance-major):
+//   x[2]      double4   FP64 positions, double-buffered across steps (w unused)
+//   mir[2]    uint4     fixed-point mirror of x: per component llrint(x*S) mod 2^32;
+//                       the int32 difference of two mirrors is the exact
+//                       minimum-image separation in units of 1/S (PBC: S = 2^32/L,
+//                       so the box maps onto the 32-bit ring; no PBC: S = 2^20/A)
+//   v, beta   double4   velocities and GJF-2GJ noise term (reference: velos, accels)
+//   move      double4   displacement since the last rebuild (reference: xyz_move)
+//   mdc       double4   per-bead integrator coefficients (a, sqrt(b)h/m, sqrt(b)h, noise)
+//   fbp       double4   base-pair forces of the current step (atomic scatter target)
+//   binfo     int4      (instance, chain start, chain length | circ<<31,
+//                        local index | seq<<24 | charge<<28)
+//   nbr       int32     per-bead pair list, stride cap: j | WCA<<31 | ELE<<30
+//   nnbr      int32     entries per bead
+//   bps/bps_n int4      base-pair candidates in per-instance segments:
+//                       (i, j, type|hash<<8, inst) and neighbour beads
+//                       (i-1, j-1, i+1, j+1); a prefix over instance counts
+//                       maps a global record index to its segment slot
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sisg {
+
+constexpr int WCA_BIT = 1 << 31;
+constexpr int ELE_BIT = 1 << 30;
+constexpr int IDX_MASK = (1 << 30) - 1;
+constexpr int MAX_BP_TYPES = 7;
+
+// error flag bits
+constexpr int ERR_PAIR_OVERFLOW = 1;
+constexpr int ERR_BP_OVERFLOW = 2;
+constexpr int ERR_NONFINITE = 4;
+
+struct InstP {
+    double box[3];     // PBC box (0 when pbc == 0)
+    double half[3];    // box / 2
+    double fsc[3];     // fixed-point scale, units per Angstrom
+    float finv[3];     // Angstrom per unit
+    int pbc;
+    int bead_off, n;   // beads [bead_off, bead_off + n)
+    int bp_off, bp_cap;// base-pair staging segment
+    double tempK;
+    double ele_coef, rcdist, ele_cut, ele_cut2, diele_dTcoef;
+    float ele_coef_f, rcdist_f, ele_cut2_f;
+    double wca_nl_cut2, ele_nl_cut2, bp_nl_cut2;
+    // cell grid of large PBC instances (large == 0: all-pairs scan)
+    int large, cell_base, nc[3];
+    double cell_len[3];
+    // noise stream of the instance: Philox counter (local bead, step - step0, stream)
+    unsigned int stream;
+    unsigned long long step0;
+};
+
+struct GlobP {
+    int n, n_inst, cap, prec, integrator;
+    int angl_reb, dih_type, bp_model, flg_ele, temp_indep;
+    int bp_min_loop, bp_jnext_compat, ele_excl_bond, ele_excl_angle;
+    double bond_k, bond_r0, angl_k, angl_t0, cos_t0, dih_k, dih_w, dih_p0;
+    double wca_sigma, wca_eps, wca_sig2, wca_coef;
+    double bp_cutoff_energy, nl_margin;
+    float f_bond_k, f_bond_r0, f_angl_k, f_angl_t0, f_cos_t0, f_dih_k, f_dih_w, f_dih_p0;
+    float f_wca_sig2, f_wca_coef, f_wca_sigma, f_wca_eps;
+    unsigned long long seed;
+};
+
+// base-pair parameter record (var_potential.F90 basepair_parameters), index 1..6
+struct BPP {
+    double cutoff_ddist, U0, bond_k, bond_r;
+    double angl_k[4], angl_theta[4];
+    double dihd_k[2], dihd_phi[2];
+};
+
+// all device pointers of one context (passed by value to kernels)
+struct Dev {
+    double4 *x[2];
+    uint4 *mir[2];
+    double4 *v, *beta, *move, *mdc, *fbp;
+    int4 *binfo;
+    double *mass;
+    int *nbr, *nnbr;
+    // base-pair lists
+    int4 *bps, *bps_n;      // per-instance staging segments (records, neighbour beads)
+    int *bp_cnt;            // [2*n_inst] staging counts, then their exclusive prefix
+    int *bp_total;          // [1] records over all instances
+    double *ene_bp;         // per staging slot
+    unsigned char *bp_status;
+    const BPP *bpp;         // [7]
+    const short *bp3_hash;  // [4097]
+    const double *bp3_dH, *bp3_dS; // [469]
+    const InstP *ip;
+    // rebuild trigger
+    unsigned long long *m1, *m2; // [n_inst] top-2 displacement^2 (bit patterns)
+    int *flag;              // [n_inst] rebuild requested
+    int *any;               // [1] any flag set
+    unsigned int *ticket;   // [2] last-block tickets (step, rebuild)
+    unsigned long long *step_ctr; // [1] Philox step counter
+    int *err;               // [1] error flags
+    int *max_need;          // [2] largest pair / bp count seen
+    long long *rebuilds;    // [1]
+    // cell lists of large PBC instances
+    int *bead_cell, *cell_cnt, *cell_start, *cell_beads;
+    int n_cells;
+    // energies [n_inst][12] (slots 0..10 + kinetic)
+    double *ene;
+};
+
+// ----------------------------------------------------------------- vectors
+template <typename R> struct V3 {
+    R x, y, z;
+};
+template <typename R> __device__ __forceinline__ V3<R> mk(R a, R b, R c) { return V3<R>{a, b, c}; }
+template <typename R> __device__ __forceinline__ R dot3(const V3<R> &a, const V3<R> &b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <typename R> __device__ __forceinline__ V3<R> cross3(const V3<R> &a, const V3<R> &b) {
+    return mk<R>(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <typename R> __device__ __forceinline__ V3<R> operator+(V3<R> a, V3<R> b) { return mk<R>(a.x + b.x, a.y + b.y, a.z + b.z); }
+template <typename R> __device__ __forceinline__ V3<R> operator-(V3<R> a, V3<R> b) { return mk<R>(a.x - b.x, a.y - b.y, a.z - b.z); }
+template <typename R> __device__ __forceinline__ V3<R> operator*(R s, V3<R> a) { return mk<R>(s * a.x, s * a.y, s * a.z); }
+template <typename R> __device__ __forceinline__ V3<R> operator-(V3<R> a) { return mk<R>(-a.x, -a.y, -a.z); }
+
+// ------------------------------------------------------- relative position
+// FP64: the reference's pbc_vec_d (pbc.F90:140-165), single shift.
+__device__ __forceinline__ V3<double> dvec64(const double4 &a, const double4 &b, const InstP &ip) {
+    V3<double> v = mk<double>(a.x - b.x, a.y - b.y, a.z - b.z);
+    if (ip.pbc) {
+        if (v.x > ip.half[0]) v.x = v.x - ip.box[0];
+        else if (v.x < -ip.half[0]) v.x = v.x + ip.box[0];
+        if (v.y > ip.half[1]) v.y = v.y - ip.box[1];
+        else if (v.y < -ip.half[1]) v.y = v.y + ip.box[1];
+        if (v.z > ip.half[2]) v.z = v.z - ip.box[2];
+        else if (v.z < -ip.half[2]) v.z = v.z + ip.box[2];
+    }
+    return v;
+}
+// FP32: from the fixed-point mirror; the wrap of the 32-bit difference is the
+// minimum image for PBC instances.
+__device__ __forceinline__ V3<float> dvec32(const uint4 &a, const uint4 &b, const InstP &ip) {
+    return mk<float>((float)(int)(a.x - b.x) * ip.finv[0], (float)(int)(a.y - b.y) * ip.finv[1],
+                     (float)(int)(a.z - b.z) * ip.finv[2]);
+}
+
+template <typename R> struct Pos;
+template <> struct Pos<double> {
+    const double4 *x;
+    __device__ __forceinline__ V3<double> d(int a, int b, const InstP &ip) const { return dvec64(x[a], x[b], ip); }
+};
+template <> struct Pos<float> {
+    const uint4 *m;
+    __device__ __forceinline__ V3<float> d(int a, int b, const InstP &ip) const { return dvec32(m[a], m[b], ip); }
+};
+
+__device__ __forceinline__ unsigned int fixed1(double x, double s) { return (unsigned int)(unsigned long long)llrint(x * s); }
+
+// -------------------------------------------------------- bead information
+__device__ __forceinline__ int bi_inst(const int4 &b) { return b.x; }
+__device__ __forceinline__ int bi_cstart(const int4 &b) { return b.y; }
+__device__ __forceinline__ int bi_clen(const int4 &b) { return b.z & 0x7fffffff; }
+__device__ __forceinline__ bool bi_circ(const int4 &b) { return (b.z >> 31) & 1; }
+__device__ __forceinline__ int bi_lidx(const int4 &b) { return b.w & 0xffffff; }
+__device__ __forceinline__ int bi_seq(const int4 &b) { return (b.w >> 24) & 0xf; }
+__device__ __forceinline__ bool bi_charge(const int4 &b) { return (b.w >> 28) & 1; }
+
+// bead of local index k of the chain (modular for circular chains); -1 if none
+__device__ __forceinline__ int chain_bead(const int4 &b, int k) {
+    const int n = bi_clen(b);
+    if (bi_circ(b)) {
+        k %= n;
+        if (k < 0) k += n;
+        return bi_cstart(b) + k;
+    }
+    return (k >= 0 && k < n) ? bi_cstart(b) + k : -1;
+}
+
+// ------------------------------------------------------------------ Philox
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), written from the paper.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+    const unsigned int M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const unsigned int hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+        const unsigned int hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += W0;
+        k.y += W1;
+    }
+    return c;
+}
+
+} // namespace sisg

@@ -1,0 +1,23 @@
+// Kernel launchers of libsisgpu (host side declarations).
+#pragma once
+
+#include "common.cuh"
+
+namespace sisg {
+
+struct RebuildPlan {
+    const int2 *small_items; // device: (instance, first local bead), 32 beads per item
+    int n_small_items, small_grid;
+    const int2 *large_items; // device: (instance, first local bead), 256 beads per item
+    int n_large_items, large_grid;
+};
+
+cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long noise_step, cudaStream_t st);
+cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
+cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int mode, double tK, int nblocks, cudaStream_t st);
+cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
+cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st);
+cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, cudaStream_t st);
+
+} // namespace sisg

@@ -1,0 +1,368 @@
+// Force and energy terms of the SIS model, templated on the arithmetic type.
+// Each function restates one Fortran routine of the reference; the file:line
+// of that routine is given at the function.  FP64 instantiations keep the
+// reference's expression order; FP32 instantiations are used by the mixed
+// precision path, which re-evaluates angle terms near cos = +-1 in FP64 from
+// the FP64 positions.
+#pragma once
+
+#include "common.cuh"
+
+namespace sisg {
+
+template <typename R> __device__ __forceinline__ R pick(double d, float f);
+template <> __device__ __forceinline__ double pick<double>(double d, float) { return d; }
+template <> __device__ __forceinline__ float pick<float>(double, float f) { return f; }
+
+template <typename R> __device__ __forceinline__ V3<R> to(const V3<double> &a) { return mk<R>((R)a.x, (R)a.y, (R)a.z); }
+
+constexpr float NEAR_ONE = 0.99f;
+
+// ------------------------------------------------------------- bond
+// force_bond.F90:33-57: v = x1 - x2, f = k (d - r0)/d v, F1 -= f, F2 += f
+template <typename R>
+__device__ __forceinline__ V3<R> bond_force(const V3<R> &v, int p, const GlobP &g) {
+    const R d = sqrt(dot3(v, v));
+    const R delta = d - pick<R>(g.bond_r0, g.f_bond_r0);
+    const V3<R> f = (pick<R>(g.bond_k, g.f_bond_k) * delta / d) * v;
+    return p == 0 ? -f : f;
+}
+// energy_bond.F90:17-28
+template <typename R> __device__ __forceinline__ R bond_energy(const V3<R> &v, const GlobP &g) {
+    const R d = sqrt(dot3(v, v));
+    const R dd = d - pick<R>(g.bond_r0, g.f_bond_r0);
+    return R(0.5) * pick<R>(g.bond_k, g.f_bond_k) * (dd * dd);
+}
+
+// ------------------------------------------------------------- angle
+// force_angl.F90:35-83 with v21 = x2 - x1, v32 = x3 - x2; returns the force on
+// participant p (0,1,2).  *cos_out receives the cosine before clamping.
+template <typename T>
+__device__ __forceinline__ V3<T> angle_force_core(const V3<T> &v21, const V3<T> &v32, int p, T k, T t0, T *cos_out) {
+    const T d21 = dot3(v21, v21), d32 = dot3(v32, v32), d2132 = dot3(v32, v21);
+    T cosine = -d2132 / sqrt(d21 * d32);
+    *cos_out = cosine;
+    if (fabs(cosine) > T(1)) cosine = copysign(T(1), cosine);
+    const T delta = acos(cosine) - t0;
+    T t = d21 * d32 - d2132 * d2132;
+    if (t <= T(1)) t = T(1);
+    const T f = k * delta / sqrt(t);
+    const V3<T> f21 = f * ((d2132 / d21) * v21 - v32);
+    const V3<T> f32 = f * ((d2132 / d32) * v32 - v21);
+    if (p == 0) return -f21;
+    if (p == 1) return f21 - f32;
+    return f32;
+}
+// force_angl_ReB.F90:36-74 with v12 = x1 - x2, v32 = x3 - x2
+template <typename T>
+__device__ __forceinline__ V3<T> angle_reb_force_core(const V3<T> &v12, const V3<T> &v32, int p, T k, T co0, T *cos_out) {
+    const T d12 = dot3(v12, v12), d32 = dot3(v32, v32);
+    const T a1232 = sqrt(d12 * d32);
+    const T cosine = dot3(v12, v32) / a1232;
+    *cos_out = cosine;
+    const T omc = T(1) - cosine * cosine;
+    const T f = -k * (cosine - co0) * (T(1) - cosine * co0) / (omc * omc);
+    const V3<T> f1 = f * ((T(1) / a1232) * v32 - (cosine / d12) * v12);
+    const V3<T> f3 = f * ((T(1) / a1232) * v12 - (cosine / d32) * v32);
+    if (p == 0) return f1;
+    if (p == 1) return -(f1 + f3);
+    return f3;
+}
+// energy_angl.F90:18-41 / energy_angl_ReB.F90 with v12 = x1 - x2, v32 = x3 - x2
+template <typename T> __device__ __forceinline__ T angle_energy_core(const V3<T> &v12, const V3<T> &v32, const GlobP &g, T *cos_out) {
+    T t = dot3(v32, v12) / sqrt(dot3(v12, v12) * dot3(v32, v32));
+    *cos_out = t;
+    const T k = pick<T>(g.angl_k, g.f_angl_k);
+    if (g.angl_reb) {
+        const T c0 = pick<T>(g.cos_t0, g.f_cos_t0);
+        return T(0.5) * k * ((t - c0) * (t - c0)) / (T(1) - t * t);
+    }
+    if (t > T(1)) t = T(1);
+    else if (t < T(-1)) t = T(-1);
+    t = acos(t);
+    const T t0 = pick<T>(g.angl_t0, g.f_angl_t0);
+    return T(0.5) * k * ((t - t0) * (t - t0));
+}
+
+// ---------------------------------------------------------- dihedral
+// force_dih_cos.F90:19-60 / force_dih_exp.F90:36-95 with vij = x1 - x2,
+// vkj = x3 - x2, vkl = x3 - x4; force on participant p (0..3)
+template <typename T>
+__device__ __forceinline__ V3<T> dih_force_core(const V3<T> &vij, const V3<T> &vkj, const V3<T> &vkl, int p, const GlobP &g) {
+    const V3<T> m = cross3(vij, vkj), n = cross3(vkj, vkl);
+    const T akj2 = dot3(vkj, vkj), akj = sqrt(akj2);
+    const T dih = atan2(akj * dot3(vij, n), dot3(m, n));
+    const T k = pick<T>(g.dih_k, g.f_dih_k), p0 = pick<T>(g.dih_p0, g.f_dih_p0);
+    T pre;
+    if (g.dih_type == 1) {
+        pre = -k * sin(dih + p0) * akj;
+    } else {
+        const T w = pick<T>(g.dih_w, g.f_dih_w);
+        const T dd = dih - p0;
+        pre = (k * w) * dd * exp((T(-0.5) * w) * (dd * dd)) * akj;
+    }
+    const V3<T> fi = (-pre / dot3(m, m)) * m;
+    const V3<T> fl = (pre / dot3(n, n)) * n;
+    if (p == 0) return fi;
+    if (p == 3) return fl;
+    const T a = dot3(vij, vkj) / akj2, b = dot3(vkl, vkj) / akj2;
+    if (p == 1) return (T(-1) + a) * fi + (-b) * fl;
+    return (-a) * fi + (T(-1) + b) * fl;
+}
+// energy_dih_cos.F90:18-39 / energy_dih_exp.F90 (same angle as the force routine)
+template <typename T>
+__device__ __forceinline__ T dih_energy_core(const V3<T> &vij, const V3<T> &vkj, const V3<T> &vkl, const GlobP &g) {
+    const V3<T> m = cross3(vij, vkj), n = cross3(vkj, vkl);
+    const T akj = sqrt(dot3(vkj, vkj));
+    const T dih = atan2(akj * dot3(vij, n), dot3(m, n));
+    const T k = pick<T>(g.dih_k, g.f_dih_k), p0 = pick<T>(g.dih_p0, g.f_dih_p0);
+    if (g.dih_type == 1) return k * (T(1) + cos(dih + p0));
+    const T w = pick<T>(g.dih_w, g.f_dih_w);
+    const T dd = dih - p0;
+    return -k * exp((T(-0.5) * w) * (dd * dd));
+}
+
+// ------------------------------------------------ bonded gather per bead
+// The bonded terms touching bead i: slot 0,1 bonds (l-1,l),(l,l+1); slots
+// 2..4 angles starting at l-2, l-1, l; slots 5..8 dihedrals starting at
+// l-3..l.  Terms exist as list_local.F90:1-126 creates them (linear chains
+// within the chain, circular chains modular).  Returns the force on bead i.
+template <typename R>
+__device__ V3<R> bonded_slot(int t, int i, const int4 &bi, const Pos<R> &P, const double4 *x64, const InstP &ip, const GlobP &g) {
+    const int l = bi_lidx(bi);
+    int start, nb, p;
+    if (t < 2) {
+        nb = 2; start = l - 1 + t; p = 1 - t;
+    } else if (t < 5) {
+        nb = 3; start = l - 2 + (t - 2); p = 2 - (t - 2);
+    } else {
+        if (g.dih_type == 0) return mk<R>(0, 0, 0);
+        nb = 4; start = l - 3 + (t - 5); p = 3 - (t - 5);
+    }
+    int q[4];
+    for (int k = 0; k < nb; ++k) {
+        q[k] = chain_bead(bi, start + k);
+        if (q[k] < 0) return mk<R>(0, 0, 0);
+    }
+    if (bi_circ(bi) && bi_clen(bi) < nb) return mk<R>(0, 0, 0);
+    if (nb == 2) return bond_force<R>(P.d(q[0], q[1], ip), p, g);
+    if (nb == 3) {
+        R c;
+        V3<R> f;
+        if (!g.angl_reb) {
+            f = angle_force_core<R>(P.d(q[1], q[0], ip), P.d(q[2], q[1], ip), p, pick<R>(g.angl_k, g.f_angl_k),
+                                    pick<R>(g.angl_t0, g.f_angl_t0), &c);
+        } else {
+            f = angle_reb_force_core<R>(P.d(q[0], q[1], ip), P.d(q[2], q[1], ip), p, pick<R>(g.angl_k, g.f_angl_k),
+                                        pick<R>(g.cos_t0, g.f_cos_t0), &c);
+        }
+        if (sizeof(R) == 4 && fabs((float)c) > NEAR_ONE) {
+            double cd;
+            V3<double> fd;
+            if (!g.angl_reb)
+                fd = angle_force_core<double>(dvec64(x64[q[1]], x64[q[0]], ip), dvec64(x64[q[2]], x64[q[1]], ip), p, g.angl_k,
+                                              g.angl_t0, &cd);
+            else
+                fd = angle_reb_force_core<double>(dvec64(x64[q[0]], x64[q[1]], ip), dvec64(x64[q[2]], x64[q[1]], ip), p,
+                                                  g.angl_k, g.cos_t0, &cd);
+            f = to<R>(fd);
+        }
+        return f;
+    }
+    return dih_force_core<R>(P.d(q[0], q[1], ip), P.d(q[2], q[1], ip), P.d(q[2], q[3], ip), p, g);
+}
+
+// bonded energies owned by bead i (terms whose first bead is i)
+template <typename R>
+__device__ void bonded_energy_owned(int i, const int4 &bi, const Pos<R> &P, const double4 *x64, const InstP &ip, const GlobP &g,
+                                    double *eb, double *ea, double *ed) {
+    const int l = bi_lidx(bi);
+    const int n = bi_clen(bi);
+    const bool circ = bi_circ(bi);
+    *eb = *ea = *ed = 0.0;
+    int q[4];
+    bool ok = true;
+    for (int k = 0; k < 4; ++k) q[k] = chain_bead(bi, l + k);
+    if (q[1] >= 0 && (!circ || n >= 2)) *eb = (double)bond_energy<R>(P.d(q[0], q[1], ip), g);
+    if (q[1] >= 0 && q[2] >= 0 && (!circ || n >= 3)) {
+        R c;
+        double e = (double)angle_energy_core<R>(P.d(q[0], q[1], ip), P.d(q[2], q[1], ip), g, &c);
+        if (sizeof(R) == 4 && fabs((float)c) > NEAR_ONE) {
+            double cd;
+            e = angle_energy_core<double>(dvec64(x64[q[0]], x64[q[1]], ip), dvec64(x64[q[2]], x64[q[1]], ip), g, &cd);
+        }
+        *ea = e;
+    }
+    for (int k = 0; k < 4; ++k) ok = ok && q[k] >= 0;
+    if (g.dih_type != 0 && ok && (!circ || n >= 4))
+        *ed = (double)dih_energy_core<R>(P.d(q[0], q[1], ip), P.d(q[2], q[1], ip), P.d(q[2], q[3], ip), g);
+}
+
+// -------------------------------------------------------- pair terms
+// force_wca.F90:34-67 and force_ele_DH.F90:39-82 folded into one scalar c
+// with F_i += c * (x_i - x_j).  The DH force on i is dvdw_dr * (x_i - x_j).
+template <typename R>
+__device__ __forceinline__ R pair_coef(int e, R d2, R sig2, R wcoef, R ecoef, R rc, R cut2, int mask) {
+    R c = R(0);
+    if ((e & WCA_BIT) && (mask & 16) && d2 < sig2) {
+        const R s = sig2 / d2;
+        const R s2 = s * s, s4 = s2 * s2;
+        c += wcoef * (s4 * s2 * s - s4);
+    }
+    if ((e & ELE_BIT) && (mask & 32) && d2 <= cut2) {
+        const R r = sqrt(d2);
+        const R ri = R(1) / r;
+        c += ecoef * ri * ri * (ri + rc) * exp(-r * rc);
+    }
+    return c;
+}
+// FP32 variant with a reciprocal square root in place of sqrt and divisions
+__device__ __forceinline__ float pair_coef_f(int e, float d2, float sig2, float wcoef, float ecoef, float rc, float cut2, int mask) {
+    float c = 0.f;
+    const float ri = rsqrtf(d2);
+    if ((e & WCA_BIT) && (mask & 16) && d2 < sig2) {
+        const float s = sig2 * ri * ri;
+        const float s2 = s * s, s4 = s2 * s2;
+        c += wcoef * (s4 * s2 * s - s4);
+    }
+    if ((e & ELE_BIT) && (mask & 32) && d2 <= cut2) {
+        const float r = d2 * ri;
+        c += ecoef * ri * ri * (ri + rc) * __expf(-r * rc);
+    }
+    return c;
+}
+// energy_wca.F90:19-33, energy_ele_DH.F90:20-37 for one (ordered) list entry
+template <typename R>
+__device__ __forceinline__ void pair_energy(int e, R d2, const InstP &ip, const GlobP &g, double *ew, double *ee) {
+    const R d = sqrt(d2);
+    if (e & WCA_BIT) {
+        const R sg = pick<R>(g.wca_sigma, g.f_wca_sigma);
+        if (d < sg) {
+            const R s = sg / d;
+            const R s6 = s * s * s * s * s * s;
+            *ew += (double)(pick<R>(g.wca_eps, g.f_wca_eps) * (s6 * s6 - R(2) * s6 + R(1)));
+        }
+    }
+    if ((e & ELE_BIT) && g.flg_ele) {
+        if ((double)d <= ip.ele_cut) {
+            const R rc = pick<R>(ip.rcdist, ip.rcdist_f);
+            const R coef = pick<R>(ip.ele_coef, ip.ele_coef_f);
+            if (g.temp_indep == 0) {
+                *ee += (double)(coef / d * exp(-d * rc));
+            } else {
+                const R rk = d * rc;
+                *ee += (double)(coef / d * exp(-rk) * (-(R(1) + R(0.5) * rk) * (R)ip.diele_dTcoef));
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------------- base pair
+// force_bp.F90:44-204 / force_bp_triplet.F90:62-240 for one record.  Vectors
+// v12 = x1-x2, v13 = x1-x3, v15 = x1-x5, v42 = x4-x2, v62 = x6-x2 (bead roles
+// 1 imp, 2 jmp, 3 imp-1, 4 jmp-1, 5 imp+1, 6 jmp+1).  Returns false if the
+// pair is outside cutoff_ddist.  f[6] receives dU-weighted forces before the
+// final multiplication by the energy (as f_bp in the reference); *u_out the
+// exponent u; *near is set when an angle cosine is within 1 - NEAR_ONE of +-1.
+template <typename T>
+__device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v15, const V3<T> &v42, const V3<T> &v62,
+                              const BPP &b, V3<T> f[6], T *u_out, bool *near) {
+    const T d1212 = dot3(v12, v12);
+    const T a12 = sqrt(d1212);
+    T d = a12 - (T)b.bond_r;
+    if (fabs(d) > (T)b.cutoff_ddist) return false;
+    *near = false;
+    T u = (T)b.bond_k * (d * d);
+    V3<T> fi = ((T)2 * (T)b.bond_k * d / a12) * v12, fk, fl;
+    f[0] = fi;
+    f[1] = -fi;
+    const T d1313 = dot3(v13, v13), d4242 = dot3(v42, v42), d1213 = dot3(v12, v13), d1242 = dot3(v12, v42);
+    const T d1215 = dot3(v12, v15), d1515 = dot3(v15, v15), d1262 = dot3(v12, v62), d6262 = dot3(v62, v62);
+    const T o13 = d1213 / d1212, o42 = d1242 / d1212, o15 = d1215 / d1212, o62 = d1262 / d1212;
+    T cosine, pre;
+    // 3-1=2 (imp-1 -- imp -- jmp)
+    cosine = d1213 / (sqrt(d1313) * a12);
+    *near |= fabs((float)cosine) > NEAR_ONE;
+    d = acos(cosine) - (T)b.angl_theta[1];
+    pre = (T)2 * (T)b.angl_k[1] * d / sqrt(d1313 * d1212 - d1213 * d1213);
+    u = u + (T)b.angl_k[1] * (d * d);
+    fi = pre * (v12 - (d1213 / d1313) * v13);
+    fk = pre * (v13 - o13 * v12);
+    f[0] = f[0] - fi - fk;
+    f[1] = f[1] + fk;
+    f[2] = fi;
+    // 1=2-4 (imp -- jmp -- jmp-1)
+    cosine = d1242 / (a12 * sqrt(d4242));
+    *near |= fabs((float)cosine) > NEAR_ONE;
+    d = acos(cosine) - (T)b.angl_theta[0];
+    u = u + (T)b.angl_k[0] * (d * d);
+    pre = (T)2 * (T)b.angl_k[0] * d / sqrt(d1212 * d4242 - d1242 * d1242);
+    fi = -pre * (v42 - o42 * v12);
+    fk = -pre * (v12 - (d1242 / d4242) * v42);
+    f[0] = f[0] + fi;
+    f[1] = f[1] - fi - fk;
+    f[3] = fk;
+    // 5-1=2 (imp+1 -- imp -- jmp)
+    cosine = d1215 / (sqrt(d1515) * a12);
+    *near |= fabs((float)cosine) > NEAR_ONE;
+    d = acos(cosine) - (T)b.angl_theta[3];
+    u = u + (T)b.angl_k[3] * (d * d);
+    pre = (T)2 * (T)b.angl_k[3] * d / sqrt(d1515 * d1212 - d1215 * d1215);
+    fi = pre * (v12 - (d1215 / d1515) * v15);
+    fk = pre * (v15 - o15 * v12);
+    f[0] = f[0] - fi - fk;
+    f[1] = f[1] + fk;
+    f[4] = fi;
+    // 1=2-6 (imp -- jmp -- jmp+1)
+    cosine = d1262 / (a12 * sqrt(d6262));
+    *near |= fabs((float)cosine) > NEAR_ONE;
+    d = acos(cosine) - (T)b.angl_theta[2];
+    u = u + (T)b.angl_k[2] * (d * d);
+    pre = (T)2 * (T)b.angl_k[2] * d / sqrt(d1212 * d6262 - d1262 * d1262);
+    fi = -pre * (v62 - o62 * v12);
+    fk = -pre * (v12 - (d1262 / d6262) * v62);
+    f[0] = f[0] + fi;
+    f[1] = f[1] - fi - fk;
+    f[5] = fk;
+    // dihedral 4-2=1=3
+    V3<T> m = cross3(v42, v12), n = cross3(v12, v13);
+    T dih = atan2(dot3(v42, n) * a12, dot3(m, n));
+    d = dih + (T)b.dihd_phi[0];
+    u = u + (T)b.dihd_k[0] * ((T)1 + cos(d));
+    pre = -(T)b.dihd_k[0] * sin(d) * a12;
+    fi = (pre / dot3(m, m)) * m;
+    fl = (-pre / dot3(n, n)) * n;
+    f[3] = f[3] + fi;
+    f[1] = f[1] + ((T)-1 + o42) * fi - o13 * fl;
+    f[0] = f[0] + ((T)-1 + o13) * fl - o42 * fi;
+    f[2] = f[2] + fl;
+    // dihedral 6-2=1=5
+    m = cross3(v62, v12);
+    n = cross3(v12, v15);
+    dih = atan2(dot3(v62, n) * a12, dot3(m, n));
+    d = dih + (T)b.dihd_phi[1];
+    u = u + (T)b.dihd_k[1] * ((T)1 + cos(d));
+    pre = -(T)b.dihd_k[1] * sin(d) * a12;
+    fi = (pre / dot3(m, m)) * m;
+    fl = (-pre / dot3(n, n)) * n;
+    f[5] = f[5] + fi;
+    f[1] = f[1] + ((T)-1 + o62) * fi - o15 * fl;
+    f[0] = f[0] + ((T)-1 + o15) * fl - o62 * fi;
+    f[4] = f[4] + fl;
+    *u_out = u;
+    return true;
+}
+
+// energy_bp.F90 mp_angle (clamped) and mp_dihedral
+template <typename T> __device__ __forceinline__ T mp_angle(const V3<T> &v12, const V3<T> &v32) {
+    T co = dot3(v32, v12) / sqrt(dot3(v12, v12) * dot3(v32, v32));
+    if (co > T(1)) co = T(1);
+    else if (co < T(-1)) co = T(-1);
+    return acos(co);
+}
+template <typename T> __device__ __forceinline__ T mp_dihedral(const V3<T> &v12, const V3<T> &v32, const V3<T> &v34) {
+    const V3<T> m = cross3(v12, v32), n = cross3(v32, v34);
+    return atan2(dot3(v12, n) * sqrt(dot3(v32, v32)), dot3(m, n));
+}
+
+} // namespace sisg

@@ -1,0 +1,168 @@
+"""Host-side mirror of the reference's hot-path interface over libsisgpu.
+
+The reference's Fortran routines act on module state for replica ``irep``:
+``force(irep, forces)`` (src/force.F90:1), ``energy_sumup(irep, tempK_in,
+energies)`` (src/energy_sumup.F90:1), ``neighbor_list(irep)``
+(src/neighbor_list.F90:1) and the time loop of ``job_md``
+(src/job_md.F90:360-460).  :class:`Engine` exposes the same operations with
+0-based instance indices; arrays are numpy, shaped (nmp, 3) where the
+reference uses (3, nmp).  Every call goes through the C ABI of
+include/sis_gpu.h; a failing call raises :class:`SisError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import SisError, ptr
+from .model import MIXED, System
+
+ENE_NAMES = ["total", "bond", "angl", "dihe", "bp", "exv", "ele", "stage", "twz", "rg", "rest"]
+
+
+class Engine:
+    def __init__(self, system: System, precision: int = MIXED, seed: int = 12345, nbr_cap: int = 0, bp_cap: int = 0,
+                 streams: Optional[Sequence[int]] = None):
+        self.L = _abi.lib()
+        self.system = system
+        self.precision = precision
+        self._topo = _abi.TopologyArrays(system, streams)
+        self._par = _abi.pack_params(system, precision, seed, nbr_cap, bp_cap)
+        h = C.c_void_p()
+        rc = self.L.sis_gpu_create(C.byref(self._topo.struct), C.byref(self._par), C.byref(h))
+        if rc != 0:
+            raise SisError(rc, "sis_gpu_create failed")
+        self.h = h
+        self.n_inst = len(system.instances)
+        self.offsets = system.offsets()
+        self.n = int(self.offsets[-1])
+        if all(i.xyz is not None for i in system.instances):
+            self.set_state(-1, np.concatenate([np.asarray(i.xyz, dtype=np.float64) for i in system.instances]))
+
+    # ------------------------------------------------------------- plumbing
+    def _ck(self, rc: int):
+        if rc != 0:
+            raise SisError(rc, self.L.sis_gpu_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sis_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def nmp(self, inst: int = -1) -> int:
+        return self.n if inst < 0 else int(self.offsets[inst + 1] - self.offsets[inst])
+
+    # ---------------------------------------------------------------- state
+    def set_state(self, inst: int, xyz=None, velos=None, accels=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (xyz, velos, accels)]
+        for a in arrs:
+            if a is not None and a.size != 3 * self.nmp(inst):
+                raise ValueError("state array size does not match the instance")
+        self._ck(self.L.sis_gpu_set_state(self.h, inst, *(ptr(a) for a in arrs)))
+
+    def get_state(self, inst: int = -1):
+        n = self.nmp(inst)
+        x, v, a = (np.empty((n, 3)) for _ in range(3))
+        self._ck(self.L.sis_gpu_get_state(self.h, inst, ptr(x), ptr(v), ptr(a)))
+        return x, v, a
+
+    def init_velocities(self):
+        self._ck(self.L.sis_gpu_init_velocities(self.h))
+
+    # ---------------------------------------------------- reference interface
+    def neighbor_list(self, inst: int = -1):
+        self._ck(self.L.sis_gpu_neighbor_list(self.h, inst))
+
+    def get_list(self, inst: int, kind: int) -> np.ndarray:
+        """kind 0 wca (n,2), 1 ele (n,2), 2 bp (n,7); 1-based local indices."""
+        w = 7 if kind == 2 else 2
+        n = C.c_int32()
+        self._ck(self.L.sis_gpu_get_list(self.h, inst, kind, None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), w), dtype=np.int32)
+        self._ck(self.L.sis_gpu_get_list(self.h, inst, kind, ptr(out), n.value, C.byref(n)))
+        return out[: n.value]
+
+    def get_bp_coef(self, inst: int) -> np.ndarray:
+        n = C.c_int32()
+        self._ck(self.L.sis_gpu_get_bp_coef(self.h, inst, None, 0, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 2))
+        self._ck(self.L.sis_gpu_get_bp_coef(self.h, inst, ptr(out), n.value, C.byref(n)))
+        return out[: n.value]
+
+    def force(self, inst: int = 0) -> np.ndarray:
+        out = np.empty((self.nmp(inst), 3))
+        self._ck(self.L.sis_gpu_force(self.h, inst, ptr(out)))
+        return out
+
+    def force_term(self, inst: int, term: int) -> np.ndarray:
+        out = np.empty((self.nmp(inst), 3))
+        self._ck(self.L.sis_gpu_force_term(self.h, inst, term, ptr(out)))
+        return out
+
+    def energy_sumup(self, inst: int = 0, tempK: Optional[float] = None) -> np.ndarray:
+        T = self.system.instances[inst].tempK if tempK is None else tempK
+        out = np.zeros(11)
+        self._ck(self.L.sis_gpu_energy_sumup(self.h, inst, float(T), ptr(out)))
+        return out
+
+    def energy_kinetic(self, inst: int = 0) -> float:
+        e = C.c_double()
+        self._ck(self.L.sis_gpu_energy_kinetic(self.h, inst, C.byref(e)))
+        return e.value
+
+    def invalidate_bp_cache(self):
+        self._ck(self.L.sis_gpu_invalidate_bp_cache(self.h))
+
+    def step(self, nsteps: int, noise: Optional[np.ndarray] = None):
+        if noise is not None:
+            noise = np.ascontiguousarray(noise, dtype=np.float64)
+            if noise.size != nsteps * self.n * 3:
+                raise ValueError("noise must hold nsteps * n_beads * 3 values")
+        self._ck(self.L.sis_gpu_step(self.h, int(nsteps), ptr(noise)))
+
+    def set_condition(self, inst: int, tempK: float, ionic_strength: float):
+        self._ck(self.L.sis_gpu_set_condition(self.h, inst, float(tempK), float(ionic_strength)))
+        self.system.instances[inst].tempK = tempK
+        self.system.instances[inst].ionic_strength = ionic_strength
+
+    def get_ele(self, inst: int) -> np.ndarray:
+        out = np.zeros(4)
+        self._ck(self.L.sis_gpu_get_ele(self.h, inst, ptr(out)))
+        return out
+
+    def stats(self) -> dict:
+        s = _abi.sis_stats()
+        self._ck(self.L.sis_gpu_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    # --------------------------------------------------------------- timing
+    def event(self, slot: int):
+        self._ck(self.L.sis_gpu_event_record(self.h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_float()
+        self._ck(self.L.sis_gpu_event_elapsed(self.h, a, b, C.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        self._ck(self.L.sis_gpu_synchronize(self.h))
+
+    def flush_l2(self):
+        self._ck(self.L.sis_gpu_flush_l2(self.h))
+
+    def step_profiled(self, nsteps: int):
+        ms = (C.c_float * 3)()
+        self._ck(self.L.sis_gpu_step_profiled(self.h, int(nsteps), ms))
+        return list(ms)
+
+    def kernel_launches(self) -> int:
+        return int(self.L.sis_gpu_kernel_launches(self.h))

@@ -1,0 +1,168 @@
+"""Readers for the reference's input formats.
+
+* ``.ff`` force-field TOML (``src/read_force_field.F90:32-372``);
+* input TOML sections used by the hot path (``src/read_input.F90``);
+* FASTA (``src/read_fasta.F90``), XYZ (``src/read_xyz.F90``) and PDB
+  coordinate records (``src/read_pdb.F90``).
+
+TOML parsing uses Python's ``tomllib``; the reference uses the toml-f library
+(``subprojects/toml-f``, not vendored), whose key semantics are restated here.
+"""
+from __future__ import annotations
+
+import tomllib
+from pathlib import Path
+from typing import Dict, List, Tuple
+
+import numpy as np
+
+from .model import (BD_EM, BP_FIELDS, GJF2GJ, MOLT_CIRC, MOLT_LINEAR, NN_NAMES, NNEND_NAMES, SEQT, Chain,
+                    ForceField, Options)
+
+
+class InputError(ValueError):
+    """Raised where the reference calls sis_abort on an invalid input."""
+
+
+def _lower_keys(d):
+    if isinstance(d, dict):
+        return {k.lower() if isinstance(k, str) else k: _lower_keys(v) for k, v in d.items()}
+    return d
+
+
+def parse_ff(text: str, bp_model: int = 1) -> ForceField:
+    """Force-field file semantics of read_force_field.F90:80-372."""
+    t = tomllib.loads(text)
+    pot = t.get("potential")
+    if pot is None:
+        raise InputError("[potential] required in FF file")
+    ff = ForceField()
+    bond = pot.get("bond")
+    if bond is None:
+        raise InputError("[bond] parameters required in FF file")
+    ff.bond_k, ff.bond_r0 = float(bond["k"]), float(bond["r0"])
+    angle, reb = pot.get("angle"), pot.get("angle_ReB")
+    if angle is not None and reb is not None:
+        raise InputError("[angle] and [angle_ReB] cannot be specified together in FF file.")
+    if angle is None and reb is None:
+        raise InputError("Either [angle] or [angle_ReB] parameters are required in FF file")
+    a = angle if angle is not None else reb
+    ff.angl_reb = reb is not None
+    ff.angl_k, ff.angl_t0 = float(a["k"]), float(a["a0"])
+    dcos, dexp = pot.get("dihedral"), pot.get("dihedral_exp")
+    ff.dih_type = 0
+    if dcos is not None:
+        ff.dih_type, ff.dih_k, ff.dih_p0 = 1, float(dcos["k"]), float(dcos["phi0"])
+    if dexp is not None:
+        ff.dih_type, ff.dih_k, ff.dih_w, ff.dih_p0 = 2, float(dexp["k"]), float(dexp["w"]), float(dexp["phi0"])
+    bp = pot.get("basepair")
+    if bp is None:
+        raise InputError("[basepair] parameters required in FF file")
+    ff.bp_cutoff_energy = float(bp.get("cutoff_energy", 0.001))
+    ff.coef_dG = float(bp.get("coef_dG", 1.0))
+    ff.dH0 = float(bp.get("dH0", 0.0))
+    ff.dS0 = float(bp.get("dS0", 0.0))
+    ff.nnend = bool(bp.get("NNend", False))
+    ff.dHend0 = float(bp.get("dHend0", 0.0))
+    ff.dSend0 = float(bp.get("dSend0", 0.0))
+    for name in ("GC", "AU", "GU"):
+        sub = bp.get(name)
+        if sub is not None:
+            ff.bp[name] = {k: float(sub[k]) for k in BP_FIELDS}
+    wca = pot.get("wca")
+    if wca is None:
+        raise InputError("[wca] parameters required in FF file")
+    ff.wca_sigma, ff.wca_eps = float(wca["sigma"]), float(wca["epsilon"])
+    if bp_model == 5:
+        nn = t.get("NN")
+        if nn is None or "dH" not in nn or "dS" not in nn:
+            raise InputError("[NN.dH] and [NN.dS] required in FF file")
+        ff.nn_dH = [float(nn["dH"][k]) for k in NN_NAMES]
+        ff.nn_dS = [float(nn["dS"][k]) for k in NN_NAMES]
+        if ff.nnend:
+            ne = t.get("NNend")
+            if ne is None:
+                raise InputError("[NNend] required in FF file")
+            ff.nnend_dH = [float(ne["dH"][k]) for k in NNEND_NAMES]
+            ff.nnend_dS = [float(ne["dS"][k]) for k in NNEND_NAMES]
+    return ff
+
+
+def read_ff(path, bp_model: int = 1) -> ForceField:
+    return parse_ff(Path(path).read_text(), bp_model)
+
+
+def parse_input(text: str) -> Tuple[Options, Dict]:
+    """Hot-path options from an input TOML (section names are case-insensitive
+    in the reference's reader).  Returns (Options, condition dict)."""
+    t = _lower_keys(tomllib.loads(text))
+    o = Options()
+    md = t.get("md", {})
+    integ = md.get("integrator", "GJF-2GJ")
+    if integ == "GJF-2GJ":
+        o.integrator = GJF2GJ
+    elif integ == "Ermak-McCammon":
+        o.integrator = BD_EM
+    else:
+        raise InputError(f"invalid integrator {integ!r}")
+    o.dt = float(md.get("dt", o.dt))
+    m = float(md.get("neighbor_list_margin", -1.0))
+    o.nl_margin = 10.0 if m < 0 else m
+    v = float(md.get("viscosity_pas", -1.0))
+    o.viscosity_Pas = 1e-5 if v < 0 else v
+    bp = t.get("basepair")
+    if bp is None:
+        # read_input.F90:674-679
+        o.bp_model, o.bp_min_loop = 5, 3
+    else:
+        o.bp_model = int(bp.get("model", 1))
+        o.bp_min_loop = int(bp.get("min_loop", 3))
+    ele = t.get("electrostatic")
+    o.flg_ele = ele is not None
+    if ele is not None:
+        o.ele_cutoff_type = int(ele.get("cutoff_type", 1))
+        o.ele_cutoff = float(ele.get("cutoff", 50.0))
+        o.length_per_charge = float(ele.get("length_per_charge", o.length_per_charge))
+        o.ele_excl_bond = bool(ele.get("exclude_covalent_bond_pairs", True))
+        o.ele_excl_angle = bool(ele.get("exclude_covalent_angle_pairs", True))
+    cond = t.get("condition", {})
+    o.temp_independent = int(cond.get("temp_independent", 0))
+    o.tempK_ref = float(cond.get("tempk_ref", 0.0))
+    c = {"tempK": float(cond.get("tempk", 300.0)), "rng_seed": int(cond.get("rng_seed", 0)),
+         "ionic_strength": float(ele.get("ionic_strength", 0.15)) if ele else 0.15}
+    pbc = t.get("pbc_box")
+    if pbc is not None:
+        c["box"] = [float(pbc["x"]), float(pbc["y"]), float(pbc["z"])]
+    return o, c
+
+
+def read_fasta(path) -> List[Chain]:
+    chains: List[Chain] = []
+    cur: List[str] = []
+    for line in Path(path).read_text().splitlines():
+        line = line.strip()
+        if not line:
+            continue
+        if line.startswith(">"):
+            if cur:
+                chains.append(Chain.from_string("".join(cur)))
+            cur = []
+        else:
+            cur.append(line)
+    if cur:
+        chains.append(Chain.from_string("".join(cur)))
+    return chains
+
+
+def read_xyz(path) -> np.ndarray:
+    lines = Path(path).read_text().splitlines()
+    n = int(lines[0].split()[0])
+    return np.array([[float(v) for v in lines[2 + i].split()[1:4]] for i in range(n)])
+
+
+def read_pdb(path) -> np.ndarray:
+    xyz = []
+    for line in Path(path).read_text().splitlines():
+        if line.startswith(("ATOM", "HETATM")):
+            xyz.append([float(line[30:38]), float(line[38:46]), float(line[46:54])])
+    return np.array(xyz)

@@ -1,0 +1,79 @@
+"""The C-ABI library: builds, loads without a GPU, exports every entry point
+declared in include/sis_gpu.h, and its structs have the layout the Python
+binding assumes.  No compute call is made here."""
+import ctypes as C
+import re
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "sis_gpu.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from sis_gb300.build import build_lib
+
+    build_lib()
+    from sis_gb300 import _abi
+
+    return _abi.lib()
+
+
+def declared():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(sis_gpu_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    from sis_gb300 import _abi
+
+    assert set(names) == set(_abi.EXPORTS)
+
+
+def test_no_oracle_symbols_in_product(lib):
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", str(ROOT / "sis_gb300" / "_lib" / "libsisgpu.so")], capture_output=True, text=True).stdout
+    assert "or_force" not in out and "or_create" not in out
+
+
+def test_struct_layout_matches_header(tmp_path):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from sis_gb300 import _abi
+
+    src = tmp_path / "layout.c"
+    fields = {s.__name__: [f for f, _ in s._fields_] for s in (_abi.sis_params, _abi.sis_topology, _abi.sis_stats)}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
+    for s, fs in fields.items():
+        lines.append(f'printf("{s} %zu\\n", sizeof({s}));')
+        for f in fs:
+            lines.append(f'printf("{s}.{f} %zu\\n", offsetof({s}, {f}));')
+    lines.append("return 0;}")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())
+    for s in (_abi.sis_params, _abi.sis_topology, _abi.sis_stats):
+        assert int(got[s.__name__]) == C.sizeof(s), s.__name__
+        for f, _ in s._fields_:
+            assert int(got[f"{s.__name__}.{f}"]) == getattr(s, f).offset, f
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    from sis_gb300 import _abi
+
+    monkeypatch.setattr(_abi, "_lib", None)
+    monkeypatch.setattr(_abi, "LIB_PATH", tmp_path / "absent.so")
+    with pytest.raises(RuntimeError):
+        _abi.lib()

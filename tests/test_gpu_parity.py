@@ -1,0 +1,235 @@
+"""GPU parity: libsisgpu (through the C ABI) against the FP64 oracle.
+
+Bars (from the engine's specification):
+* list membership (WCA, DH, base-pair records and their dH/dS) bit-exact;
+* FP64 path: forces per term within 1e-12 (norm-wise, per bead relative to
+  max(|F_ref|, rms F_ref)), energies within 1e-12 relative;
+* mixed path (FP32 terms, FP64 accumulation/integration): force RMS relative
+  error <= 1e-5;
+* a Langevin run fed the oracle's noise array matches its positions to 1e-10
+  after 10 steps (FP64 path).
+"""
+import numpy as np
+import pytest
+
+from helpers import cag47_system, max_rel, pbc_md_system, rms_rel, t2s2hp_system
+from oracle.oracle import Oracle
+from sis_gb300 import FP64, MIXED
+from sis_gb300._abi import SisError
+from sis_gb300.coil import crowded_box, random_coil, single_chain, uneven_batch
+from sis_gb300.engine import Engine
+from sis_gb300.model import MOLT_CIRC, Chain, Instance, Options, System
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL_FP64 = 1e-12
+ENERGY_TOL_FP64 = 1e-12
+FORCE_RMS_TOL_MIXED = 1e-5
+
+
+def compact_system(ff):
+    rng = np.random.default_rng(5)
+    x = random_coil(rng, 30, amin_deg=60.0, amax_deg=100.0, rmin=3.0)
+    inst = Instance([Chain.from_string("GGGGCAAAAGCCCCAAAAGGGGAAAACCCC")], tempK=300.0, ionic_strength=0.15, xyz=x)
+    return System(ff, Options(bp_model=1), [inst])
+
+
+def circ_system(ff):
+    rng = np.random.default_rng(9)
+    seq = rng.integers(0, 4, 48).astype(np.int32)
+    t = np.linspace(0, 2 * np.pi, 48, endpoint=False)
+    x = np.stack([45 * np.cos(t), 45 * np.sin(t), 8 * np.sin(3 * t)], axis=1) + rng.normal(scale=0.3, size=(48, 3))
+    inst = Instance([Chain(seq, MOLT_CIRC)], tempK=310.0, ionic_strength=0.1, xyz=x)
+    return System(ff, Options(bp_model=3), [inst])
+
+
+def cell_system(ff):
+    return crowded_box(ff, n_chains=12, n=500, molar=0.05, seed=21)
+
+
+SYSTEMS = {
+    "cag47": lambda ff, nn: cag47_system(7),
+    "chain64": lambda ff, nn: single_chain(ff, n=64, seed=1001),
+    "pbc564": lambda ff, nn: pbc_md_system(ff, 1),
+    "t2s2hp_model5": lambda ff, nn: t2s2hp_system(nn),
+    "compact_bp": lambda ff, nn: compact_system(ff),
+    "circ": lambda ff, nn: circ_system(ff),
+    "cells6000": lambda ff, nn: cell_system(ff),
+}
+
+
+@pytest.fixture(scope="module")
+def systems(sis_ff, nn_ff):
+    return {k: f(sis_ff, nn_ff) for k, f in SYSTEMS.items()}
+
+
+def oracle_for(sysm, k=0):
+    o = Oracle.from_instance(sysm, k)
+    o.neighbor_list(0)
+    return o
+
+
+def as_set(a):
+    return set(map(tuple, np.asarray(a).tolist()))
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_lists_bit_exact(name, systems):
+    sysm = systems[name]
+    orc = oracle_for(sysm)
+    eng = Engine(sysm, precision=FP64)
+    eng.neighbor_list(-1)
+    for kind in (0, 1, 2):
+        assert as_set(eng.get_list(0, kind)) == as_set(orc.get_list(0, kind)), (name, kind)
+    # dH/dS of each base-pair record
+    g = {tuple(r): tuple(c) for r, c in zip(eng.get_list(0, 2).tolist(), eng.get_bp_coef(0).tolist())}
+    o = {tuple(r): tuple(c) for r, c in zip(orc.get_list(0, 2).tolist(), orc.get_bp_coef(0).tolist())}
+    assert g == o
+    # wrapped coordinates after the rebuild (pbc_wrap) are bit-identical
+    assert np.array_equal(eng.get_state(0)[0], orc.get_xyz(0))
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_fp64_forces_per_term(name, systems):
+    sysm = systems[name]
+    orc = oracle_for(sysm)
+    eng = Engine(sysm, precision=FP64)
+    for term in range(1, 7):
+        ref = orc.force_term(0, term)
+        got = eng.force_term(0, term)
+        if not np.any(ref):
+            assert not np.any(got), (name, term)
+            continue
+        assert max_rel(got, ref) < FORCE_TOL_FP64, (name, term, max_rel(got, ref))
+    ref = orc.force(0)
+    assert max_rel(eng.force(0), ref) < FORCE_TOL_FP64
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_fp64_energies(name, systems):
+    sysm = systems[name]
+    orc = oracle_for(sysm)
+    eng = Engine(sysm, precision=FP64)
+    orc.set_bp_energy_flag(0)
+    ref = orc.energy_sumup(0)
+    eng.invalidate_bp_cache()
+    got = eng.energy_sumup(0)
+    scale = np.abs(ref[1:7]).sum()
+    for k in range(1, 7):
+        assert abs(got[k] - ref[k]) <= ENERGY_TOL_FP64 * max(abs(ref[k]), 1e-3 * scale), (name, k, got[k], ref[k])
+    # bp energies cached by the force call (flg_bp_energy) equal the recomputed ones
+    eng.force(0)
+    assert abs(eng.energy_sumup(0)[4] - ref[4]) <= 1e-12 * max(1.0, abs(ref[4]))
+
+
+@pytest.mark.parametrize("name", list(SYSTEMS))
+def test_mixed_precision_force_error(name, systems):
+    sysm = systems[name]
+    orc = oracle_for(sysm)
+    eng = Engine(sysm, precision=MIXED)
+    ref = orc.force(0)
+    err = rms_rel(eng.force(0), ref)
+    assert err <= FORCE_RMS_TOL_MIXED, (name, err)
+    orc.set_bp_energy_flag(0)
+    eref = orc.energy_sumup(0)
+    eng.invalidate_bp_cache()
+    e = eng.energy_sumup(0)
+    assert abs(e[0] - eref[0]) <= 1e-5 * np.abs(eref[1:7]).sum()
+
+
+def test_batched_instances_match_their_own_oracles(sis_ff):
+    sysm = uneven_batch(sis_ff, n_inst=8, lmin=20, lmax=120, seed=77)
+    eng = Engine(sysm, precision=FP64)
+    for k in range(len(sysm.instances)):
+        orc = oracle_for(sysm, k)
+        for kind in (0, 1, 2):
+            assert as_set(eng.get_list(k, kind)) == as_set(orc.get_list(0, kind))
+        assert max_rel(eng.force(k), orc.force(0)) < FORCE_TOL_FP64
+        assert np.allclose(eng.get_ele(k)[:3], orc.get_ele(0)[:3], rtol=1e-15, atol=0)
+
+
+@pytest.mark.parametrize("name", ["chain64", "pbc564", "t2s2hp_model5", "compact_bp"])
+def test_fed_noise_trajectory_matches_oracle(name, systems):
+    sysm = systems[name]
+    n = sysm.nmp
+    rng = np.random.default_rng(42)
+    v0 = rng.normal(size=(n, 3)) * 0.04
+    a0 = rng.normal(size=(n, 3)) * 0.01
+    noise = rng.normal(size=(10, 1, n, 3))
+    orc = Oracle.from_instance(sysm, 0)
+    orc.set_velos(0, v0)
+    orc.set_accels(0, a0)
+    orc.md_init()
+    orc.run(10, noise)
+    eng = Engine(sysm, precision=FP64)
+    eng.set_state(0, None, v0, a0)
+    eng.step(10, noise.reshape(10, n, 3))
+    x, v, a = eng.get_state(0)
+    scale = np.abs(orc.get_xyz(0)).max()
+    assert np.abs(x - orc.get_xyz(0)).max() <= 1e-10 * scale
+    assert np.abs(v - orc.get_velos(0)).max() <= 1e-10 * np.abs(orc.get_velos(0)).max()
+    assert np.array_equal(a, orc.get_accels(0))
+
+
+def test_rebuild_trigger_matches_oracle(sis_ff):
+    """Large early displacements from a 4 A random-coil contact set force several
+    displacement-triggered rebuilds; positions still agree with the oracle."""
+    sysm = single_chain(sis_ff, n=64, seed=1001)
+    n = sysm.nmp
+    rng = np.random.default_rng(1)
+    noise = rng.normal(size=(60, 1, n, 3))
+    orc = Oracle.from_instance(sysm, 0)
+    orc.md_init()
+    nreb = orc.run(60, noise)
+    eng = Engine(sysm, precision=FP64)
+    eng.step(60, noise.reshape(60, n, 3))
+    st = eng.stats()
+    assert st["rebuilds"] - 1 == nreb  # minus the initial build
+    x = eng.get_state(0)[0]
+    assert np.abs(x - orc.get_xyz(0)).max() <= 1e-8 * np.abs(x).max()
+
+
+def test_instance_alone_equals_instance_in_batch(sis_ff):
+    big = uneven_batch(sis_ff, n_inst=6, lmin=30, lmax=80, seed=5)
+    alone = System(big.ff, big.opts, [big.instances[3]])
+    e1 = Engine(big, precision=MIXED, seed=99)
+    # the noise of an instance is keyed by its stream id (here the batch index)
+    e2 = Engine(alone, precision=MIXED, seed=99, streams=[3])
+    e1.step(50)
+    e2.step(50)
+    x1 = e1.get_state(3)[0]
+    x2 = e2.get_state(0)[0]
+    assert np.array_equal(x1, x2)
+
+
+def test_philox_thermostat_kinetic_temperature(sis_ff):
+    sysm = single_chain(sis_ff, n=64, seed=1001)
+    eng = Engine(sysm, precision=MIXED, seed=3)
+    eng.init_velocities()
+    eng.step(2000)
+    kB = 0.0019872042586408316
+    ek = []
+    for _ in range(40):
+        eng.step(50)
+        ek.append(eng.energy_kinetic(0))
+    T = np.mean(ek) / (1.5 * 64 * kB)
+    assert abs(T - 300.0) < 25.0
+
+
+def test_nonfinite_coordinates_are_reported(sis_ff):
+    sysm = single_chain(sis_ff, n=32, seed=2)
+    eng = Engine(sysm, precision=MIXED)
+    x = eng.get_state(0)[0]
+    x[5, 1] = np.nan
+    eng.set_state(0, x)
+    with pytest.raises(SisError) as ei:
+        eng.step(2)
+    assert ei.value.code == -4
+
+
+def test_pair_list_overflow_is_reported(sis_ff):
+    sysm = compact_system(sis_ff)
+    eng = Engine(sysm, precision=MIXED, nbr_cap=4)
+    with pytest.raises(SisError) as ei:
+        eng.neighbor_list(-1)
+    assert ei.value.code == -3

@@ -1,0 +1,182 @@
+"""CPU checks of the FP64 oracle against the reference's golden vectors and
+known-answer tests.
+
+* CAG47 energies of the reference's regression test
+  (check/test_DCD_CAG47: OpenMM energies of 25 DCD frames);
+* MT19937 known answers (the C++ standard's mt19937 requirement: the 10000th
+  output of the default seed 5489 is 4123659995);
+* force = -grad(energy) by central differences, the reference's own
+  consistency check (src/job_check_force.F90:57-82);
+* neighbour-list membership recomputed independently with numpy.
+"""
+import numpy as np
+import pytest
+
+from helpers import cag47_system, rms_rel, t2s2hp_system, pbc_md_system
+from oracle.oracle import MT, Oracle
+from sis_gb300.coil import random_coil, single_chain
+from sis_gb300.model import Chain, Instance, Options, System
+
+
+def test_cag47_energies_match_openmm_golden():
+    z = np.load(__import__("helpers").GOLDEN / "cag47.npz")
+    sysm = cag47_system(0)
+    orc = Oracle.from_instance(sysm, 0)
+    for f in range(len(z["xyz"])):
+        orc.set_xyz(0, z["xyz"][f].astype(np.float64))
+        orc.neighbor_list(0)
+        orc.set_bp_energy_flag(0)
+        e = orc.energy_sumup(0)
+        g = z["energy"][f]
+        # columns: step, Ebond, Eangl, Eexv, Eele, -, Ebp, -; coordinates are float32
+        assert abs(e[1] - g[1]) <= 1e-4 * abs(g[1]) + 1e-4
+        assert abs(e[2] - g[2]) <= 1e-4 * abs(g[2]) + 1e-4
+        assert abs(e[5] - g[3]) <= 2e-3 * abs(g[3]) + 1e-5
+        # OpenMM used slightly different electrostatic constants (closer to the
+        # reference's _HTN_CONSISTENT build): agreement to 0.6 %
+        assert abs(e[6] - g[4]) <= 6e-3 * abs(g[4])
+
+
+def test_mt19937_known_answers():
+    m = MT(5489)
+    first = m.int32()
+    assert first == 3499211612
+    for _ in range(9998):
+        m.int32()
+    assert m.int32() == 4123659995
+
+
+def test_mt_double_ranges_and_boxmuller_moments():
+    m = MT(123)
+    u = np.array([m.double1() for _ in range(20000)])
+    assert u.min() >= 0.0 and u.max() <= 1.0 and abs(u.mean() - 0.5) < 0.01
+    g = np.array([m.boxmuller() for _ in range(100000)])
+    assert abs(g.mean()) < 0.015 and abs(g.var() - 1.0) < 0.015
+
+
+def _fd_check(orc, beads, h=1e-5):
+    x0 = orc.get_xyz(0)
+    orc.set_bp_energy_flag(0)
+    f = orc.force(0)
+    worst = 0.0
+    scale = np.sqrt(np.mean(np.sum(f ** 2, axis=1)))
+    for i in beads:
+        for k in range(3):
+            xp = x0.copy()
+            xp[i, k] += h
+            orc.set_xyz(0, xp)
+            orc.set_bp_energy_flag(0)
+            ep = orc.energy_sumup(0)[0]
+            xp[i, k] -= 2 * h
+            orc.set_xyz(0, xp)
+            orc.set_bp_energy_flag(0)
+            em = orc.energy_sumup(0)[0]
+            fd = -(ep - em) / (2 * h)
+            worst = max(worst, abs(fd - f[i, k]) / max(abs(f[i, k]), scale))
+    orc.set_xyz(0, x0)
+    return worst
+
+
+def test_force_is_minus_energy_gradient_model1(sis_ff):
+    sysm = single_chain(sis_ff, n=40, seed=11)
+    orc = Oracle.from_instance(sysm, 0)
+    orc.neighbor_list(0)
+    assert _fd_check(orc, range(0, 40, 3)) < 2e-5
+
+
+def test_force_is_minus_energy_gradient_model5_reb_expdih(nn_ff):
+    sysm = t2s2hp_system(nn_ff)
+    orc = Oracle.from_instance(sysm, 0)
+    orc.neighbor_list(0)
+    assert _fd_check(orc, range(27)) < 2e-5
+
+
+def test_force_is_minus_energy_gradient_with_pairs(sis_ff):
+    """A compact structure so that WCA, DH and base pairs all contribute."""
+    rng = np.random.default_rng(5)
+    n = 30
+    x = random_coil(rng, n, amin_deg=60.0, amax_deg=100.0, rmin=3.0)
+    inst = Instance([Chain.from_string("GGGGCAAAAGCCCCAAAAGGGGAAAACCCC")], tempK=300.0, ionic_strength=0.15, xyz=x)
+    orc = Oracle.from_instance(System(sis_ff, Options(bp_model=1), [inst]), 0)
+    orc.neighbor_list(0)
+    assert len(orc.get_list(0, 0)) > 0
+    assert _fd_check(orc, range(n)) < 5e-5
+
+
+def _ref_lists(sysm):
+    """neighbor_list.F90 membership recomputed with numpy (no bp)."""
+    inst = sysm.instances[0]
+    o = sysm.opts
+    x = np.array(inst.xyz, dtype=np.float64)
+    n = len(x)
+    if inst.box is not None:
+        L = np.array(inst.box)
+        for k in range(3):
+            hi = x[:, k] > L[k]
+            lo = x[:, k] < 0
+            x[hi, k] = x[hi, k] - L[k] * (np.trunc((x[hi, k] - L[k]) / L[k]) + 1)
+            x[lo, k] = x[lo, k] + L[k] * (np.trunc((0 - x[lo, k]) / L[k]) + 1)
+    chain = np.concatenate([[c] * len(ch) for c, ch in enumerate(inst.chains)])
+    loc = np.concatenate([np.arange(1, len(ch) + 1) for ch in inst.chains])
+    wca, ele = set(), set()
+    wc2 = (sysm.ff.wca_sigma + o.nl_margin) ** 2
+    ec2 = (o.ele_cutoff + o.nl_margin) ** 2
+    for i in range(n):
+        v = x[i] - x[i + 1:]
+        if inst.box is not None:
+            for k in range(3):
+                c = v[:, k]
+                c[c > L[k] / 2] -= L[k]
+                c[c < -L[k] / 2] += L[k]
+        d2 = v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1] + v[:, 2] * v[:, 2]
+        for jj in np.nonzero(d2 <= max(wc2, ec2))[0]:
+            j = i + 1 + jj
+            same = chain[i] == chain[j]
+            if d2[jj] <= wc2 and not (same and loc[i] + 2 >= loc[j]):
+                wca.add((i + 1, j + 1))
+            if d2[jj] <= ec2 and not (same and loc[j] - loc[i] in (1, 2)):
+                ele.add((i + 1, j + 1))
+    return wca, ele
+
+
+@pytest.mark.parametrize("which", ["cag47", "test_md_pbc"])
+def test_neighbor_list_membership_matches_numpy(which, sis_ff):
+    sysm = cag47_system(3) if which == "cag47" else pbc_md_system(sis_ff, 1)
+    orc = Oracle.from_instance(sysm, 0)
+    orc.neighbor_list(0)
+    wca, ele = _ref_lists(sysm)
+    assert set(map(tuple, orc.get_list(0, 0).tolist())) == wca
+    assert set(map(tuple, orc.get_list(0, 1).tolist())) == ele
+
+
+def test_gjf2gj_one_step_matches_update_formula(sis_ff):
+    sysm = single_chain(sis_ff, n=32, seed=3)
+    orc = Oracle.from_instance(sysm, 0)
+    orc.md_init()
+    rng = np.random.default_rng(0)
+    v0 = rng.normal(size=(32, 3)) * 0.03
+    a0 = rng.normal(size=(32, 3)) * 0.01
+    orc.set_velos(0, v0)
+    orc.set_accels(0, a0)
+    x0 = orc.get_xyz(0)
+    f = orc.force(0)
+    xi = rng.normal(size=(1, 1, 32, 3))
+    orc.run(1, xi)
+    c = orc.get_md_coef(0)
+    bn = c[:, 3:4] * xi[0, 0]
+    v1 = c[:, 0:1] * v0 + c[:, 1:2] * f + (a0 + bn)
+    x1 = x0 + c[:, 2:3] * v1
+    assert np.allclose(orc.get_velos(0), v1, rtol=1e-14, atol=0)
+    assert np.allclose(orc.get_xyz(0), x1, rtol=1e-15, atol=0)
+    assert np.allclose(orc.get_accels(0), bn, rtol=0, atol=0)
+
+
+def test_set_ele_values_are_physical(sis_ff):
+    sysm = single_chain(sis_ff, n=8, seed=1)
+    orc = Oracle.from_instance(sysm, 0)
+    ele_coef, lam, cut, diele = orc.get_ele(0)
+    assert 77.0 < diele < 78.5  # water at 300 K (Malmberg-Maryott)
+    assert 7.6 < lam < 8.2  # Debye length at 150 mM
+    assert cut == 50.0
+    kB = orc.L.or_const(1)
+    assert abs(kB - 0.0019872) < 1e-6
