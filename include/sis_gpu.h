@@ -179,6 +179,11 @@ int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise);
 /* set_ele + set_md_coef for one instance at a new temperature / salt
  * (src/set_ele.F90, src/job_md.F90:700-767). */
 int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic_strength);
+/* Caps the magnitude of every bead's total force at fmax (kcal/mol/A) in
+ * sis_gpu_step; 0 removes the cap.  An equilibration aid for starting
+ * structures with overlapping beads; it has no counterpart in the reference
+ * and is off unless set. */
+int sis_gpu_set_force_cap(sis_ctx *ctx, double fmax);
 /* derived per-instance electrostatic values [ele_coef, lambdaD, ele_cutoff, diele] */
 int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *out4);
 

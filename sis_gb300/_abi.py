@@ -85,6 +85,7 @@ EXPORTS = {
     "sis_gpu_step": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "sis_gpu_set_condition": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),
     "sis_gpu_get_ele": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "sis_gpu_set_force_cap": (C.c_int, [C.c_void_p, C.c_double]),
     "sis_gpu_get_stats": (C.c_int, [C.c_void_p, C.POINTER(sis_stats)]),
     "sis_gpu_last_error": (C.c_char_p, [C.c_void_p]),
     "sis_gpu_event_record": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -85,6 +85,7 @@ struct sis_ctx {
     cudaGraphExec_t gexec = nullptr;
     int graph_steps = 0;
     int n_vel_init = 0;
+    bool tuned = false;
 };
 
 namespace {
@@ -236,9 +237,9 @@ int upload_ip(sis_ctx *ctx) {
 
 int ensure_lists(sis_ctx *ctx);
 
-int run_rebuild(sis_ctx *ctx) {
+int run_rebuild(sis_ctx *ctx, int after_step = 0) {
     ctx->launches += 2 + (ctx->plan.n_small_items > 0) + 5 * (ctx->plan.n_large_items > 0);
-    CK(launch_rebuild(ctx->D, ctx->g, ctx->cur, ctx->plan, ctx->st));
+    CK(launch_rebuild(ctx->D, ctx->g, ctx->cur, ctx->plan, after_step, step_blocks(ctx->G, ctx->n), ctx->st));
     return SIS_OK;
 }
 
@@ -280,17 +281,45 @@ int inst_range(const sis_ctx *ctx, int inst, int &off, int &cnt) {
     return SIS_OK;
 }
 
-int bp_blocks(const sis_ctx *ctx) { return 2 * 152; }
+int bp_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? 4 * 152 : 0; }
 
 int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
-    if (ctx->g.bp_model > 0) {
-        CK(launch_bp(ctx->D, ctx->g, ctx->cur, 0, -1.0, bp_blocks(ctx), ctx->st));
-        ctx->launches++;
-    }
+    CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st));
+    ctx->launches++;
     CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, noise, ns, ctx->st));
     ctx->launches++;
     ctx->cur ^= 1;
-    return run_rebuild(ctx);
+    return run_rebuild(ctx, 1);
+}
+
+// Picks the lanes-per-bead width G of the step kernel by timing force-only
+// launches (no state changes: they read positions and write a scratch force
+// array; the base-pair buffer they consume is zero between steps).
+int autotune(sis_ctx *ctx) {
+    if (ctx->tuned) return SIS_OK;
+    const int cand[4] = {2, 4, 8, 16};
+    float best = 1e30f;
+    int bestG = ctx->G;
+    cudaEvent_t e0 = ctx->ev[12], e1 = ctx->ev[13];
+    CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, 0, 0, ctx->st));
+    ctx->launches++;
+    for (int c = 0; c < 4; ++c) {
+        CK(launch_force(cand[c], ctx->D, ctx->g, ctx->cur, ctx->fout_d, 55, ctx->st)); // warm-up (mask without base pairs)
+        CK(cudaEventRecord(e0, ctx->st));
+        for (int r = 0; r < 3; ++r) CK(launch_force(cand[c], ctx->D, ctx->g, ctx->cur, ctx->fout_d, 55, ctx->st));
+        CK(cudaEventRecord(e1, ctx->st));
+        CK(cudaEventSynchronize(e1));
+        float ms;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        ctx->launches += 4;
+        if (ms < best) {
+            best = ms;
+            bestG = cand[c];
+        }
+    }
+    ctx->G = bestG;
+    ctx->tuned = true;
+    return SIS_OK;
 }
 
 } // namespace
@@ -471,9 +500,20 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.ene_bp, bp_total_cap);
     rc |= dalloc(ctx, &D.bp_status, bp_total_cap);
     BPP *bpp_d;
+    BPPf *bppf_d;
     short *hash_d;
     double *dH_d, *dS_d;
     rc |= dalloc(ctx, &bpp_d, MAX_BP_TYPES);
+    rc |= dalloc(ctx, &bppf_d, MAX_BP_TYPES);
+    if (p.precision == SIS_PREC_FP64) {
+        double4 *sl;
+        rc |= dalloc(ctx, &sl, (size_t)8 * n);
+        D.slot = sl;
+    } else {
+        float4 *sl;
+        rc |= dalloc(ctx, &sl, (size_t)8 * n);
+        D.slot = sl;
+    }
     rc |= dalloc(ctx, &hash_d, 4097);
     rc |= dalloc(ctx, &dH_d, 469);
     rc |= dalloc(ctx, &dS_d, 469);
@@ -483,6 +523,8 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.flag, ni);
     rc |= dalloc(ctx, &D.any, 1);
     rc |= dalloc(ctx, &D.ticket, 2);
+    rc |= dalloc(ctx, &D.part_inst, (size_t)2 * step_blocks(32, n));
+    rc |= dalloc(ctx, &D.part_m, (size_t)4 * step_blocks(32, n));
     rc |= dalloc(ctx, &D.step_ctr, 1);
     rc |= dalloc(ctx, &D.err, 1);
     rc |= dalloc(ctx, &D.max_need, 2);
@@ -499,6 +541,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     }
     D.n_cells = ncells;
     D.bpp = bpp_d;
+    D.bppf = bppf_d;
     D.bp3_hash = hash_d;
     D.bp3_dH = dH_d;
     D.bp3_dS = dS_d;
@@ -532,6 +575,27 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     ok &= cudaMemcpy(D.mdc, mdc.data(), sizeof(double4) * n, cudaMemcpyHostToDevice) == cudaSuccess;
     ok &= cudaMemcpy(D.mass, ctx->mass.data(), sizeof(double) * n, cudaMemcpyHostToDevice) == cudaSuccess;
     ok &= cudaMemcpy(bpp_d, ctx->bpp, sizeof(BPP) * MAX_BP_TYPES, cudaMemcpyHostToDevice) == cudaSuccess;
+    {
+        BPPf bf[MAX_BP_TYPES];
+        memset(bf, 0, sizeof(bf));
+        for (int t = 1; t < MAX_BP_TYPES; ++t) {
+            const BPP &b = ctx->bpp[t];
+            BPPf &f = bf[t];
+            f.cutoff_ddist = (float)b.cutoff_ddist; f.U0 = (float)b.U0; f.bond_k = (float)b.bond_k; f.bond_r = (float)b.bond_r;
+            for (int a = 0; a < 4; ++a) {
+                f.angl_k[a] = (float)b.angl_k[a];
+                f.angl_theta[a] = (float)b.angl_theta[a];
+            }
+            for (int a = 0; a < 2; ++a) {
+                f.dihd_k[a] = (float)b.dihd_k[a];
+                f.dihd_phi[a] = (float)b.dihd_phi[a];
+            }
+            const double lo = std::max(0.0, b.bond_r - b.cutoff_ddist), hi = b.bond_r + b.cutoff_ddist;
+            f.lo2 = (float)(lo * lo);
+            f.hi2 = (float)(hi * hi);
+        }
+        ok &= cudaMemcpy(bppf_d, bf, sizeof(bf), cudaMemcpyHostToDevice) == cudaSuccess;
+    }
     ok &= cudaMemcpy(hash_d, hash.data(), sizeof(short) * 4097, cudaMemcpyHostToDevice) == cudaSuccess;
     ok &= cudaMemcpy(dH_d, dH.data(), sizeof(double) * 469, cudaMemcpyHostToDevice) == cudaSuccess;
     ok &= cudaMemcpy(dS_d, dS.data(), sizeof(double) * 469, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -711,11 +775,10 @@ static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
     if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
     int rc = ensure_lists(ctx);
     if (rc) return rc;
-    if ((mask & 8) && ctx->g.bp_model > 0) {
-        CK(launch_bp(ctx->D, ctx->g, ctx->cur, 0, -1.0, bp_blocks(ctx), ctx->st));
-        ctx->launches++;
-        ctx->bp_cache = true;
-    }
+    const int do_bp = (mask & 8) && ctx->g.bp_model > 0;
+    CK(launch_pre(ctx->D, ctx->g, ctx->cur, (mask & 7) != 0, do_bp, bp_blocks(ctx), ctx->st));
+    ctx->launches++;
+    if (do_bp) ctx->bp_cache = true;
     CK(launch_force(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->fout_d, mask, ctx->st));
     ctx->launches++;
     if (forces) CK(cudaMemcpyAsync(forces, ctx->fout_d + 3 * (size_t)off, sizeof(double) * 3 * cnt, cudaMemcpyDeviceToHost, ctx->st));
@@ -744,7 +807,7 @@ extern "C" int sis_gpu_energy_sumup(sis_ctx *ctx, int32_t inst, double tempK, do
     int rc = ensure_lists(ctx);
     if (rc) return rc;
     if (!ctx->bp_cache && ctx->g.bp_model > 0) {
-        CK(launch_bp(ctx->D, ctx->g, ctx->cur, 1, tempK, bp_blocks(ctx), ctx->st));
+        CK(launch_bp_energy(ctx->D, ctx->g, ctx->cur, tempK, bp_blocks(ctx), ctx->st));
         ctx->launches++;
     }
     CK(cudaMemsetAsync(ctx->D.ene, 0, sizeof(double) * 12 * ctx->n_inst, ctx->st));
@@ -778,6 +841,7 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     if (!ctx || nsteps < 0) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
+    if (!noise && nsteps >= 64 && (rc = autotune(ctx))) return rc;
     if (noise) {
         const size_t need = (size_t)nsteps * ctx->n * 3;
         if (need > ctx->noise_cap) {
@@ -810,6 +874,12 @@ extern "C" int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, d
     int rc = upload_ip(ctx);
     if (rc) return rc;
     CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_set_force_cap(sis_ctx *ctx, double fmax) {
+    if (!ctx || fmax < 0.0) return SIS_ERR_ARG;
+    ctx->g.fcap = fmax;
     return SIS_OK;
 }
 
@@ -878,20 +948,19 @@ extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
     if (!ctx || nsteps < 0 || !ms3) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
+    if ((rc = autotune(ctx))) return rc;
     double acc[3] = {0.0, 0.0, 0.0};
     cudaEvent_t *e = ctx->ev + 8; // events 8..11
     for (int64_t s = 0; s < nsteps; ++s) {
         CK(cudaEventRecord(e[0], ctx->st));
-        if (ctx->g.bp_model > 0) {
-            CK(launch_bp(ctx->D, ctx->g, ctx->cur, 0, -1.0, bp_blocks(ctx), ctx->st));
-            ctx->launches++;
-        }
+        CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st));
+        ctx->launches++;
         CK(cudaEventRecord(e[1], ctx->st));
         CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
         ctx->launches++;
         ctx->cur ^= 1;
         CK(cudaEventRecord(e[2], ctx->st));
-        rc = run_rebuild(ctx);
+        rc = run_rebuild(ctx, 1);
         if (rc) return rc;
         CK(cudaEventRecord(e[3], ctx->st));
         CK(cudaEventSynchronize(e[3]));

@@ -65,6 +65,7 @@ struct GlobP {
     float f_bond_k, f_bond_r0, f_angl_k, f_angl_t0, f_cos_t0, f_dih_k, f_dih_w, f_dih_p0;
     float f_wca_sig2, f_wca_coef, f_wca_sigma, f_wca_eps;
     unsigned long long seed;
+    double fcap; // > 0: per-bead force magnitude cap (equilibration only)
 };
 
 // base-pair parameter record (var_potential.F90 basepair_parameters), index 1..6
@@ -72,6 +73,15 @@ struct BPP {
     double cutoff_ddist, U0, bond_k, bond_r;
     double angl_k[4], angl_theta[4];
     double dihd_k[2], dihd_phi[2];
+};
+
+// FP32 copy of BPP for the mixed path, plus the squared distance window
+// (bond_r -+ cutoff_ddist)^2 of the early rejection test
+struct BPPf {
+    float cutoff_ddist, U0, bond_k, bond_r;
+    float angl_k[4], angl_theta[4];
+    float dihd_k[2], dihd_phi[2];
+    float lo2, hi2;
 };
 
 // all device pointers of one context (passed by value to kernels)
@@ -89,6 +99,8 @@ struct Dev {
     double *ene_bp;         // per staging slot
     unsigned char *bp_status;
     const BPP *bpp;         // [7]
+    const BPPf *bppf;       // [7]
+    void *slot;             // [n][8] bonded forces per term start (float4 or double4)
     const short *bp3_hash;  // [4097]
     const double *bp3_dH, *bp3_dS; // [469]
     const InstP *ip;
@@ -96,7 +108,9 @@ struct Dev {
     unsigned long long *m1, *m2; // [n_inst] top-2 displacement^2 (bit patterns)
     int *flag;              // [n_inst] rebuild requested
     int *any;               // [1] any flag set
-    unsigned int *ticket;   // [2] last-block tickets (step, rebuild)
+    unsigned int *ticket;   // [2] last-block tickets (trigger, rebuild)
+    int *part_inst;         // [2 * step blocks] per-block trigger partials: instance
+    unsigned long long *part_m; // [4 * step blocks] and its top-two displacement^2
     unsigned long long *step_ctr; // [1] Philox step counter
     int *err;               // [1] error flags
     int *max_need;          // [2] largest pair / bp count seen

@@ -15,6 +15,8 @@
 #include "kernels.h"
 #include "terms.cuh"
 
+#include <algorithm>
+
 namespace sisg {
 
 template <typename R> __device__ __forceinline__ Pos<R> pos_of(const Dev &D, int cur);
@@ -50,180 +52,32 @@ template <> __device__ __forceinline__ double gauss3<double>(unsigned long long 
     return sqrt(-2.0 * log(u1)) * (c == 1 ? sn : cs);
 }
 
-// ------------------------------------------------------------------ k_step
-// MODE 0: full MD step (forces + integration + trigger)
-// MODE 1: forces only, written to fout[3*i+c] (terms selected by mask)
-template <typename R, int G, int MODE>
-__global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
-                                              double *__restrict__ fout, int mask) {
-    __shared__ unsigned long long s_m1[32], s_m2[32];
-    __shared__ int s_lo, s_cnt;
-    __shared__ int s_last;
-    const int bpb = blockDim.x / G;
-    const int i_raw = blockIdx.x * bpb + threadIdx.x / G;
-    const int lane = threadIdx.x % G;
-    const bool active = i_raw < g.n;
-    const int i = active ? i_raw : g.n - 1;
-    if (MODE == 0) {
-        if (threadIdx.x < 32) {
-            s_m1[threadIdx.x] = 0ull;
-            s_m2[threadIdx.x] = 0ull;
-        }
-        if (threadIdx.x == 0) {
-            const int i0 = blockIdx.x * bpb;
-            const int i1 = min(i0 + bpb - 1, g.n - 1);
-            s_lo = D.binfo[i0].x;
-            s_cnt = D.binfo[i1].x - s_lo + 1;
-        }
-        __syncthreads();
-    }
-    const int4 bi = D.binfo[i];
-    const InstP &ip = D.ip[bi.x];
-    const Pos<R> P = pos_of<R>(D, cur);
-    const double4 *__restrict__ x64 = D.x[cur];
+template <typename R> struct Vec4;
+template <> struct Vec4<float> {
+    using type = float4;
+    __device__ static float4 make(const V3<float> &a) { return make_float4(a.x, a.y, a.z, 0.f); }
+};
+template <> struct Vec4<double> {
+    using type = double4;
+    __device__ static double4 make(const V3<double> &a) { return make_double4(a.x, a.y, a.z, 0.0); }
+};
+template <typename V> __device__ __forceinline__ V3<float> v3of(const float4 &a) { return mk<float>(a.x, a.y, a.z); }
+__device__ __forceinline__ V3<float> v3(const float4 &a) { return mk<float>(a.x, a.y, a.z); }
+__device__ __forceinline__ V3<double> v3(const double4 &a) { return mk<double>(a.x, a.y, a.z); }
 
-    // non-bonded pair terms over the full list
-    V3<R> an = mk<R>(0, 0, 0);
-    if (mask & 48) {
-        const int cnt = min(D.nnbr[i], g.cap);
-        const int *__restrict__ nb = D.nbr + (size_t)i * g.cap;
-        const R sig2 = pick<R>(g.wca_sig2, g.f_wca_sig2), wcoef = pick<R>(g.wca_coef, g.f_wca_coef);
-        const R ecoef = pick<R>(ip.ele_coef, ip.ele_coef_f), rc = pick<R>(ip.rcdist, ip.rcdist_f);
-        const R cut2 = g.flg_ele ? pick<R>(ip.ele_cut2, ip.ele_cut2_f) : R(-1);
-        for (int k = lane; k < cnt; k += G) {
-            const int e = __ldg(nb + k);
-            const int j = e & IDX_MASK;
-            const V3<R> v = P.d(i, j, ip);
-            const R d2 = dot3(v, v);
-            R c;
-            if (sizeof(R) == 4)
-                c = (R)pair_coef_f(e, (float)d2, (float)sig2, (float)wcoef, (float)ecoef, (float)rc, (float)cut2, mask);
-            else
-                c = pair_coef<R>(e, d2, sig2, wcoef, ecoef, rc, cut2, mask);
-            an = an + c * v;
-        }
-    }
-    // bonded terms touching bead i
-    V3<R> ab = mk<R>(0, 0, 0);
-    if (mask & 7) {
-        for (int t = lane; t < 9; t += G) {
-            const int cls = t < 2 ? 1 : (t < 5 ? 2 : 4);
-            if (mask & cls) ab = ab + bonded_slot<R>(t, i, bi, P, x64, ip, g);
-        }
-    }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) {
-        an.x += __shfl_xor_sync(0xffffffffu, an.x, o);
-        an.y += __shfl_xor_sync(0xffffffffu, an.y, o);
-        an.z += __shfl_xor_sync(0xffffffffu, an.z, o);
-        ab.x += __shfl_xor_sync(0xffffffffu, ab.x, o);
-        ab.y += __shfl_xor_sync(0xffffffffu, ab.y, o);
-        ab.z += __shfl_xor_sync(0xffffffffu, ab.z, o);
-    }
-    // per-bead FP64 accumulation
-    V3<double> F = mk<double>((double)an.x + (double)ab.x, (double)an.y + (double)ab.y, (double)an.z + (double)ab.z);
-    if (mask & 8) {
-        const double4 fb = D.fbp[i];
-        F = mk<double>(F.x + fb.x, F.y + fb.y, F.z + fb.z);
-        __syncwarp();
-        if (active && lane == 0) D.fbp[i] = make_double4(0.0, 0.0, 0.0, 0.0);
-    }
-    if (MODE == 1) {
-        if (active)
-            for (int c = lane; c < 3; c += G) fout[3 * (size_t)i + c] = comp(F, c);
-        return;
-    }
-
-    // ---------------------------------------------- GJF-2GJ / Ermak-McCammon
-    const int nxt = cur ^ 1;
-    const unsigned long long step = *D.step_ctr;
-    double mv0 = 0.0, mv1 = 0.0, mv2 = 0.0;
-    if (active) {
-        const double4 m = D.mdc[i];
-        for (int c = lane; c < 3; c += G) {
-            const double Fc = comp(F, c);
-            const double xi =
-                noise ? noise[((size_t)noise_step * g.n + i) * 3 + c]
-                      : gauss3<R>(g.seed, i - ip.bead_off, step - ip.step0, c, ip.stream);
-            const double xc = ((const double *)(x64 + i))[c];
-            double dx;
-            if (g.integrator == 1) {
-                double *vp = (double *)(D.v + i) + c;
-                double *bp = (double *)(D.beta + i) + c;
-                const double bn = m.w * xi;
-                const double vn = m.x * (*vp) + m.y * Fc + (*bp + bn);
-                *bp = bn;
-                *vp = vn;
-                dx = m.z * vn;
-            } else {
-                dx = m.x * Fc + m.w * xi;
-            }
-            const double xn = xc + dx;
-            ((double *)(D.x[nxt] + i))[c] = xn;
-            double *mp = (double *)(D.move + i) + c;
-            const double mn = *mp + dx;
-            *mp = mn;
-            if (c == 0) mv0 = mn;
-            else if (c == 1) mv1 = mn;
-            else mv2 = mn;
-            ((unsigned int *)(D.mir[nxt] + i))[c] = fixed1(xn, ip.fsc[c]);
-        }
-    }
-    // displacement^2 of the bead (unfused, as dot_product in FP64)
-    const int base = (threadIdx.x & 31) - lane;
-    const double mx = __shfl_sync(0xffffffffu, mv0, base + (0 % G));
-    const double my = __shfl_sync(0xffffffffu, mv1, base + (1 % G));
-    const double mz = __shfl_sync(0xffffffffu, mv2, base + (2 % G));
-    if (active && lane == 0) {
-        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
-        if (!isfinite(d2)) atomicOr(D.err, ERR_NONFINITE);
-        const unsigned long long b = (unsigned long long)__double_as_longlong(d2);
-        const int k = bi.x - s_lo;
-        if (s_cnt <= 32) {
-            const unsigned long long old = atomicMax(&s_m1[k], b);
-            atomicMax(&s_m2[k], old < b ? old : b);
-        } else {
-            const unsigned long long old = atomicMax(&D.m1[bi.x], b);
-            atomicMax(&D.m2[bi.x], old < b ? old : b);
-        }
-    }
-    __syncthreads();
-    if (s_cnt <= 32 && (int)threadIdx.x < s_cnt) {
-        const unsigned long long b1 = s_m1[threadIdx.x], b2 = s_m2[threadIdx.x];
-        const int inst = s_lo + threadIdx.x;
-        const unsigned long long old = atomicMax(&D.m1[inst], b1);
-        const unsigned long long c2 = old < b1 ? old : b1;
-        atomicMax(&D.m2[inst], c2 > b2 ? c2 : b2);
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(&D.ticket[0], 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (s_last) {
-        __threadfence();
-        int any = 0;
-        for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) {
-            const double a = __longlong_as_double((long long)atomicExch(&D.m1[k], 0ull));
-            const double b = __longlong_as_double((long long)atomicExch(&D.m2[k], 0ull));
-            if (sqrt(a) + sqrt(b) > g.nl_margin) {
-                D.flag[k] = 1;
-                any = 1;
-            }
-        }
-        if (any) atomicOr(D.any, 1);
-        if (threadIdx.x == 0) {
-            D.ticket[0] = 0u;
-            D.step_ctr[0] = step + 1ull;
-        }
-    }
-}
-
-// -------------------------------------------------------------------- k_bp
-// Base-pair records, grid-stride over the candidate list.  The global record
-// index is mapped to (instance, slot) by binary search over the per-instance
-// prefix counts written by the last list rebuild.
-__device__ __forceinline__ bool bp_record(const Dev &D, int r, int n_inst, int &slot) {
-    const int total = *D.bp_total;
+// --------------------------------------------------------------- k_pre
+// Term-parallel pass before the step kernel.
+//  * blocks [0, nbond_blocks): thread s evaluates the bond (s,s+1), the angle
+//    (s,s+1,s+2) and the dihedral (s..s+3) of list_local.F90 (all three term
+//    types in every thread, so warps do not diverge) and stores their forces
+//    in slot[s][0..7]: bond force on s+1; angle forces on s, s+1, s+2;
+//    dihedral forces on s..s+3.  Absent terms store zeros.
+//  * blocks from nbond_blocks on: base-pair records (force_bp*.F90), grid
+//    stride; mode 0 scatters forces into fbp and caches ene_bp/bp_status,
+//    mode 1 computes energies only (energy_bp*.F90) at temperature tK_in.
+// The global record index is mapped to (instance, slot) by binary search
+// over the per-instance prefix counts written by the last list rebuild.
+__device__ __forceinline__ bool bp_record(const Dev &D, int r, int total, int n_inst, int &slot) {
     if (r >= total) return false;
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
@@ -235,122 +89,527 @@ __device__ __forceinline__ bool bp_record(const Dev &D, int r, int n_inst, int &
     return true;
 }
 
-// mode 0: forces (+ cached energies); mode 1: energies only at temperature tK
-// (tK < 0: the instance's own temperature)
 template <typename R>
-__global__ void __launch_bounds__(128) k_bp(Dev D, GlobP g, int cur, int mode, double tK_in) {
+__device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int cur, int s) {
+    using V4 = typename Vec4<R>::type;
+    V4 *S = (V4 *)D.slot + (size_t)s * 8;
+    const int4 bi = D.binfo[s];
+    const InstP &ip = D.ip[bi.x];
     const Pos<R> P = pos_of<R>(D, cur);
+    const double4 *__restrict__ x64 = D.x[cur];
+    const int l = bi_lidx(bi), n = bi_clen(bi);
+    const bool circ = bi_circ(bi);
+    const int q1 = chain_bead(bi, l + 1), q2 = chain_bead(bi, l + 2), q3 = chain_bead(bi, l + 3);
+    const V3<R> z = mk<R>(0, 0, 0);
+    // bond (s, s+1)
+    V3<R> fb = z;
+    if (q1 >= 0 && (!circ || n >= 2)) fb = bond_f<R>(P.d(s, q1, ip), g);
+    S[0] = Vec4<R>::make(fb);
+    // angle (s, s+1, s+2)
+    V3<R> Fa[3] = {z, z, z};
+    if (q2 >= 0 && (!circ || n >= 3)) {
+        R c;
+        angle_forces<R>(P.d(q1, s, ip), P.d(q2, q1, ip), g, Fa, &c);
+        if constexpr (sizeof(R) == 4) {
+            if (fabsf(c) > NEAR_ONE) {
+                V3<double> Fd[3];
+                double cd;
+                angle_forces<double>(dvec64(x64[q1], x64[s], ip), dvec64(x64[q2], x64[q1], ip), g, Fd, &cd);
+                for (int k = 0; k < 3; ++k) Fa[k] = to<R>(Fd[k]);
+            }
+        }
+    }
+    S[1] = Vec4<R>::make(Fa[0]);
+    S[2] = Vec4<R>::make(Fa[1]);
+    S[3] = Vec4<R>::make(Fa[2]);
+    // dihedral (s, s+1, s+2, s+3)
+    V3<R> Fd[4] = {z, z, z, z};
+    if (g.dih_type != 0 && q3 >= 0 && (!circ || n >= 4)) {
+        bool nr;
+        dih_forces<R>(P.d(s, q1, ip), P.d(q2, q1, ip), P.d(q2, q3, ip), g, Fd, &nr);
+        if constexpr (sizeof(R) == 4) {
+            if (nr) {
+                V3<double> F64[4];
+                dih_forces<double>(dvec64(x64[s], x64[q1], ip), dvec64(x64[q2], x64[q1], ip), dvec64(x64[q2], x64[q3], ip), g, F64,
+                                   &nr);
+                for (int k = 0; k < 4; ++k) Fd[k] = to<R>(F64[k]);
+            }
+        }
+    }
+    S[4] = Vec4<R>::make(Fd[0]);
+    S[5] = Vec4<R>::make(Fd[1]);
+    S[6] = Vec4<R>::make(Fd[2]);
+    S[7] = Vec4<R>::make(Fd[3]);
+}
+
+// window and free-energy test of one record (force mode); returns true when
+// the 6-bead term has to be evaluated.  Records that fail are given zero
+// energy and status, as force_bp*.F90 zero ene_bp/bp_status before the loop.
+template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, const GlobP &g, int cur, int slot) {
+    const int4 rec = D.bps[slot];
+    const int type = rec.z & 0xff;
+    const InstP &ip = D.ip[rec.w];
+    bool pass;
+    if constexpr (sizeof(R) == 4) {
+        const BPPf &bf = D.bppf[type];
+        const V3<float> v = dvec32(D.mir[cur][rec.x], D.mir[cur][rec.y], ip);
+        const float d2 = fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z));
+        // window widened by 1e-5 relative; the exact test follows
+        pass = d2 >= bf.lo2 * 0.99999f && d2 <= bf.hi2 * 1.00001f;
+    } else {
+        const BPP &b = D.bpp[type];
+        const V3<double> v = dvec64(D.x[cur][rec.x], D.x[cur][rec.y], ip);
+        pass = fabs(sqrt(dot3(v, v)) - b.bond_r) <= b.cutoff_ddist;
+    }
+    if (pass && (g.bp_model == 4 || g.bp_model == 5)) {
+        const int h = rec.z >> 8;
+        pass = D.bp3_dH[h] - ip.tempK * D.bp3_dS[h] < 0.0;
+    }
+    if (!pass) {
+        D.ene_bp[slot] = 0.0;
+        D.bp_status[slot] = 0;
+    }
+    return pass;
+}
+
+// force_bp.F90:44-204 / force_bp_triplet.F90:62-240 for one record that
+// passed bp_test: forces scattered into fbp, energy and status cached.
+template <typename R> __device__ __noinline__ void bp_eval(const Dev &D, const GlobP &g, int cur, int slot) {
+    const Pos<R> P = pos_of<R>(D, cur);
+    const double4 *__restrict__ x64 = D.x[cur];
+    const int4 rec = D.bps[slot];
+    const int4 nb = D.bps_n[slot];
+    const int i1 = rec.x, i2 = rec.y, type = rec.z & 0xff, h = rec.z >> 8;
+    const InstP &ip = D.ip[rec.w];
+    const bool triplet = g.bp_model == 4 || g.bp_model == 5;
+    const double dG = triplet ? D.bp3_dH[h] - ip.tempK * D.bp3_dS[h] : 1.0;
+    V3<double> fd[6];
+    double ud = 0.0;
+    bool ok;
+    if constexpr (sizeof(R) == 4) {
+        V3<float> f[6];
+        float u;
+        bool nr = false;
+        ok = bp_force_core<float, BPPf>(P.d(i1, i2, ip), P.d(i1, nb.x, ip), P.d(i1, nb.z, ip), P.d(nb.y, i2, ip), P.d(nb.w, i2, ip),
+                                        D.bppf[type], f, &u, &nr);
+        if (ok && nr) {
+            bool nr2;
+            ok = bp_force_core<double, BPP>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[i1], x64[nb.x], ip),
+                                            dvec64(x64[i1], x64[nb.z], ip), dvec64(x64[nb.y], x64[i2], ip),
+                                            dvec64(x64[nb.w], x64[i2], ip), D.bpp[type], fd, &ud, &nr2);
+        } else if (ok) {
+            for (int q = 0; q < 6; ++q) fd[q] = mk<double>((double)f[q].x, (double)f[q].y, (double)f[q].z);
+            ud = (double)u;
+        }
+    } else {
+        bool nr;
+        ok = bp_force_core<double, BPP>(P.d(i1, i2, ip), P.d(i1, nb.x, ip), P.d(i1, nb.z, ip), P.d(nb.y, i2, ip), P.d(nb.w, i2, ip),
+                                        D.bpp[type], fd, &ud, &nr);
+    }
+    double ene = 0.0;
+    unsigned char st = 0;
+    if (ok) {
+        const BPP &b = D.bpp[type];
+        const double e = triplet ? b.U0 * dG * exp(-ud) : b.U0 * exp(-ud);
+        if (e <= g.bp_cutoff_energy) {
+            ene = e;
+            st = 1;
+            const int ids[6] = {i1, i2, nb.x, nb.y, nb.z, nb.w};
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                atomicAdd(&D.fbp[ids[q]].x, e * fd[q].x);
+                atomicAdd(&D.fbp[ids[q]].y, e * fd[q].y);
+                atomicAdd(&D.fbp[ids[q]].z, e * fd[q].z);
+            }
+        }
+    }
+    D.ene_bp[slot] = ene;
+    D.bp_status[slot] = st;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_blocks, int do_bp) {
+    if ((int)blockIdx.x < nbond_blocks) {
+        const int s = blockIdx.x * blockDim.x + threadIdx.x;
+        if (s < g.n) bonded_terms<R>(D, g, cur, s);
+        return;
+    }
+    if (!do_bp) return;
+    // Base-pair records: each warp tests 32 records at a time and queues the
+    // few that pass the distance window; full warps of queued records are
+    // evaluated together so that the expensive 6-bead term runs without
+    // divergence.
+    __shared__ int q[8][64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int total = *D.bp_total;
+    const int nwarps = (gridDim.x - nbond_blocks) * 8;
+    int qn = 0;
+    for (int base = ((blockIdx.x - nbond_blocks) * 8 + warp) * 32; base < total; base += nwarps * 32) {
+        const int r = base + lane;
+        int slot = -1;
+        bool pass = false;
+        if (bp_record(D, r, total, g.n_inst, slot)) pass = bp_test<R>(D, g, cur, slot);
+        const unsigned bal = __ballot_sync(0xffffffffu, pass);
+        if (pass) q[warp][qn + __popc(bal & ((1u << lane) - 1u))] = slot;
+        qn += __popc(bal);
+        __syncwarp();
+        if (qn >= 32) {
+            bp_eval<R>(D, g, cur, q[warp][lane]);
+            __syncwarp();
+            if (lane < qn - 32) q[warp][lane] = q[warp][lane + 32];
+            qn -= 32;
+            __syncwarp();
+        }
+    }
+    if (lane < qn) bp_eval<R>(D, g, cur, q[warp][lane]);
+}
+
+// energy_bp.F90 / energy_bp_triplet.F90 for every record at temperature tK
+// (tK < 0: each instance's own): clamped angles, FP64 from the FP64 positions.
+__global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, double tK_in) {
     const double4 *__restrict__ x64 = D.x[cur];
     const int total = *D.bp_total;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < total; r += gridDim.x * blockDim.x) {
         int slot;
-        if (!bp_record(D, r, g.n_inst, slot)) break;
+        if (!bp_record(D, r, total, g.n_inst, slot)) break;
         const int4 rec = D.bps[slot];
         const int4 nb = D.bps_n[slot];
         const int i1 = rec.x, i2 = rec.y, type = rec.z & 0xff, h = rec.z >> 8;
         const InstP &ip = D.ip[rec.w];
         const BPP &b = D.bpp[type];
         const bool triplet = g.bp_model == 4 || g.bp_model == 5;
-        double ene = 0.0;
+        double ene = 0.0, dG = 1.0;
         unsigned char st = 0;
-        double dG = 1.0;
         bool skip = false;
         if (triplet) {
-            double tK = mode == 0 ? ip.tempK : (tK_in < 0 ? ip.tempK : tK_in);
-            if (mode == 1 && g.temp_indep) tK = 0.0;
+            double tK = tK_in < 0 ? ip.tempK : tK_in;
+            if (g.temp_indep) tK = 0.0;
             dG = D.bp3_dH[h] - tK * D.bp3_dS[h];
-            if (dG >= 0.0) skip = true;
+            skip = dG >= 0.0;
         }
-        if (!skip && mode == 0) {
-            V3<R> f[6];
-            R u;
-            bool nr = false;
-            bool ok = bp_force_core<R>(P.d(i1, i2, ip), P.d(i1, nb.x, ip), P.d(i1, nb.z, ip), P.d(nb.y, i2, ip), P.d(nb.w, i2, ip), b,
-                                       f, &u, &nr);
-            V3<double> fd[6];
-            double ud = 0.0;
-            if (ok && sizeof(R) == 4 && nr) {
-                bool nr2;
-                ok = bp_force_core<double>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[i1], x64[nb.x], ip),
-                                           dvec64(x64[i1], x64[nb.z], ip), dvec64(x64[nb.y], x64[i2], ip),
-                                           dvec64(x64[nb.w], x64[i2], ip), b, fd, &ud, &nr2);
-            } else if (ok) {
-                for (int q = 0; q < 6; ++q) fd[q] = mk<double>((double)f[q].x, (double)f[q].y, (double)f[q].z);
-                ud = (double)u;
-            }
-            if (ok) {
-                const double e = triplet ? b.U0 * dG * exp(-ud) : b.U0 * exp(-ud);
-                if (e <= g.bp_cutoff_energy) {
-                    ene = e;
-                    st = 1;
-                    const int ids[6] = {i1, i2, nb.x, nb.y, nb.z, nb.w};
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) {
-                        atomicAdd(&D.fbp[ids[q]].x, e * fd[q].x);
-                        atomicAdd(&D.fbp[ids[q]].y, e * fd[q].y);
-                        atomicAdd(&D.fbp[ids[q]].z, e * fd[q].z);
-                    }
-                }
-            }
-        } else if (!skip) {
-            // energy_bp.F90 / energy_bp_triplet.F90 (clamped angles)
-            double u = 0.0;
-            bool ok;
-            if constexpr (sizeof(R) == 8) {
-                const V3<double> v = dvec64(x64[i1], x64[i2], ip);
-                const double d = sqrt(dot3(v, v)) - b.bond_r;
-                ok = fabs(d) <= b.cutoff_ddist;
-                if (ok) {
-                    u = b.bond_k * (d * d);
-                    double th = mp_angle<double>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[nb.y], x64[i2], ip));
-                    u = u + b.angl_k[0] * ((th - b.angl_theta[0]) * (th - b.angl_theta[0]));
-                    th = mp_angle<double>(dvec64(x64[nb.x], x64[i1], ip), dvec64(x64[i2], x64[i1], ip));
-                    u = u + b.angl_k[1] * ((th - b.angl_theta[1]) * (th - b.angl_theta[1]));
-                    th = mp_angle<double>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[nb.w], x64[i2], ip));
-                    u = u + b.angl_k[2] * ((th - b.angl_theta[2]) * (th - b.angl_theta[2]));
-                    th = mp_angle<double>(dvec64(x64[nb.z], x64[i1], ip), dvec64(x64[i2], x64[i1], ip));
-                    u = u + b.angl_k[3] * ((th - b.angl_theta[3]) * (th - b.angl_theta[3]));
-                    double ph = mp_dihedral<double>(dvec64(x64[nb.x], x64[i1], ip), dvec64(x64[i2], x64[i1], ip),
-                                                    dvec64(x64[i2], x64[nb.y], ip));
-                    u = u + b.dihd_k[0] * (1.0 + cos(ph + b.dihd_phi[0]));
-                    ph = mp_dihedral<double>(dvec64(x64[nb.z], x64[i1], ip), dvec64(x64[i2], x64[i1], ip),
-                                             dvec64(x64[i2], x64[nb.w], ip));
-                    u = u + b.dihd_k[1] * (1.0 + cos(ph + b.dihd_phi[1]));
-                }
-            } else {
-                const V3<float> v = P.d(i1, i2, ip);
-                const float d = sqrtf(dot3(v, v)) - (float)b.bond_r;
-                ok = fabsf(d) <= (float)b.cutoff_ddist;
-                if (ok) {
-                    // angles and dihedrals in FP64 from the FP64 positions
-                    double dd = sqrt(dot3(dvec64(x64[i1], x64[i2], ip), dvec64(x64[i1], x64[i2], ip))) - b.bond_r;
-                    u = b.bond_k * (dd * dd);
-                    double th = mp_angle<double>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[nb.y], x64[i2], ip));
-                    u = u + b.angl_k[0] * ((th - b.angl_theta[0]) * (th - b.angl_theta[0]));
-                    th = mp_angle<double>(dvec64(x64[nb.x], x64[i1], ip), dvec64(x64[i2], x64[i1], ip));
-                    u = u + b.angl_k[1] * ((th - b.angl_theta[1]) * (th - b.angl_theta[1]));
-                    th = mp_angle<double>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[nb.w], x64[i2], ip));
-                    u = u + b.angl_k[2] * ((th - b.angl_theta[2]) * (th - b.angl_theta[2]));
-                    th = mp_angle<double>(dvec64(x64[nb.z], x64[i1], ip), dvec64(x64[i2], x64[i1], ip));
-                    u = u + b.angl_k[3] * ((th - b.angl_theta[3]) * (th - b.angl_theta[3]));
-                    double ph = mp_dihedral<double>(dvec64(x64[nb.x], x64[i1], ip), dvec64(x64[i2], x64[i1], ip),
-                                                    dvec64(x64[i2], x64[nb.y], ip));
-                    u = u + b.dihd_k[0] * (1.0 + cos(ph + b.dihd_phi[0]));
-                    ph = mp_dihedral<double>(dvec64(x64[nb.z], x64[i1], ip), dvec64(x64[i2], x64[i1], ip),
-                                             dvec64(x64[i2], x64[nb.w], ip));
-                    u = u + b.dihd_k[1] * (1.0 + cos(ph + b.dihd_phi[1]));
-                }
-            }
-            if (ok) {
-                const double e = triplet ? b.U0 * dG * exp(-u) : b.U0 * exp(-u);
-                if (e <= g.bp_cutoff_energy) {
-                    ene = e;
-                    st = 1;
-                }
+        const V3<double> v = dvec64(x64[i1], x64[i2], ip);
+        const double d = sqrt(dot3(v, v)) - b.bond_r;
+        if (!skip && fabs(d) <= b.cutoff_ddist) {
+            double u = b.bond_k * (d * d);
+            double th = mp_angle<double>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[nb.y], x64[i2], ip));
+            u = u + b.angl_k[0] * ((th - b.angl_theta[0]) * (th - b.angl_theta[0]));
+            th = mp_angle<double>(dvec64(x64[nb.x], x64[i1], ip), dvec64(x64[i2], x64[i1], ip));
+            u = u + b.angl_k[1] * ((th - b.angl_theta[1]) * (th - b.angl_theta[1]));
+            th = mp_angle<double>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[nb.w], x64[i2], ip));
+            u = u + b.angl_k[2] * ((th - b.angl_theta[2]) * (th - b.angl_theta[2]));
+            th = mp_angle<double>(dvec64(x64[nb.z], x64[i1], ip), dvec64(x64[i2], x64[i1], ip));
+            u = u + b.angl_k[3] * ((th - b.angl_theta[3]) * (th - b.angl_theta[3]));
+            double ph = mp_dihedral<double>(dvec64(x64[nb.x], x64[i1], ip), dvec64(x64[i2], x64[i1], ip),
+                                            dvec64(x64[i2], x64[nb.y], ip));
+            u = u + b.dihd_k[0] * (1.0 + cos(ph + b.dihd_phi[0]));
+            ph = mp_dihedral<double>(dvec64(x64[nb.z], x64[i1], ip), dvec64(x64[i2], x64[i1], ip),
+                                     dvec64(x64[i2], x64[nb.w], ip));
+            u = u + b.dihd_k[1] * (1.0 + cos(ph + b.dihd_phi[1]));
+            const double e = triplet ? b.U0 * dG * exp(-u) : b.U0 * exp(-u);
+            if (e <= g.bp_cutoff_energy) {
+                ene = e;
+                st = 1;
             }
         }
         D.ene_bp[slot] = ene;
         D.bp_status[slot] = st;
+    }
+}
+
+// ------------------------------------------------------------------ k_step
+// Phase A (G lanes per bead): WCA + Debye-Hueckel over the bead's full pair
+// list and the gather of the bead's bonded slot forces, reduced over the
+// lanes; the per-bead sums go to shared memory.
+// Phase B (one thread per bead component, packed): FP64 accumulation of the
+// force (pair + bonded + base pair) and the GJF-2GJ / Ermak-McCammon update
+// (job_md.F90:415-456).  Packing the FP64 work onto whole warps keeps the
+// reduced-rate FP64 pipe busy with useful lanes only.
+// Phase C (one thread per bead): displacement^2 since the last rebuild and
+// its top two per instance; the last block evaluates the rebuild trigger of
+// every instance (job_md.F90:376-395).
+// MODE 1 computes forces only (terms selected by mask) into fout.
+
+template <typename R, int G, int MODE>
+__global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
+                                              double *__restrict__ fout, int mask) {
+    constexpr int BPB = 256 / G;
+    __shared__ R sA[3][BPB], sB[3][BPB];
+    __shared__ float sScale[BPB];
+    __shared__ double sM[3][BPB];
+    __shared__ unsigned long long s_m1[32], s_m2[32];
+    __shared__ int s_lo, s_cnt;
+    const int b = threadIdx.x / G;
+    const int lane = threadIdx.x % G;
+    const int i0 = blockIdx.x * BPB;
+    const int i_raw = i0 + b;
+    const bool active = i_raw < g.n;
+    const int i = active ? i_raw : g.n - 1;
+    if (MODE == 0) {
+        if (threadIdx.x < 32) {
+            s_m1[threadIdx.x] = 0ull;
+            s_m2[threadIdx.x] = 0ull;
+        }
+        if (threadIdx.x == 0) {
+            const int i1 = min(i0 + BPB - 1, g.n - 1);
+            s_lo = D.binfo[i0].x;
+            s_cnt = D.binfo[i1].x - s_lo + 1;
+        }
+    }
+    const int4 bi = D.binfo[i];
+    const InstP &ip = D.ip[bi.x];
+
+    // -------------------------------------------------------------- phase A
+    V3<R> an = mk<R>(0, 0, 0);
+    if (mask & 48) {
+        const int cnt = min(D.nnbr[i], g.cap);
+        const int *__restrict__ nb = D.nbr + (size_t)i * g.cap;
+        if constexpr (sizeof(R) == 4) {
+            const uint4 mi = D.mir[cur][i];
+            const uint4 *__restrict__ mir = D.mir[cur];
+            const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
+            const float sig2 = g.f_wca_sig2, wcoef = g.f_wca_coef;
+            const float ecoef = ip.ele_coef_f, rc = ip.rcdist_f;
+            const float cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+#pragma unroll 2
+            for (int k = lane; k < cnt; k += G) {
+                const int e = __ldg(nb + k);
+                const uint4 mj = __ldg(mir + (e & IDX_MASK));
+                const float vx = (float)(int)(mi.x - mj.x) * f0;
+                const float vy = (float)(int)(mi.y - mj.y) * f1;
+                const float vz = (float)(int)(mi.z - mj.z) * f2;
+                const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+                float c = 0.f;
+                if ((e & WCA_BIT) && (mask & 16) && d2 < sig2) {
+                    const float sq = __fdiv_rn(sig2, d2);
+                    const float s2 = sq * sq, s4 = s2 * s2;
+                    c += wcoef * (s4 * s2 * sq - s4);
+                }
+                if ((e & ELE_BIT) && (mask & 32) && d2 <= cut2) {
+                    float ri = rsqrtf(d2);
+                    ri = ri * fmaf(-0.5f * d2 * ri, ri, 1.5f);
+                    const float r = d2 * ri;
+                    c += ecoef * ri * ri * (ri + rc) * __expf(-r * rc);
+                }
+                an.x = fmaf(c, vx, an.x);
+                an.y = fmaf(c, vy, an.y);
+                an.z = fmaf(c, vz, an.z);
+            }
+        } else {
+            const R sig2 = g.wca_sig2, wcoef = g.wca_coef;
+            const R ecoef = ip.ele_coef, rc = ip.rcdist;
+            const R cut2 = g.flg_ele ? ip.ele_cut2 : R(-1);
+            const Pos<R> P = pos_of<R>(D, cur);
+            for (int k = lane; k < cnt; k += G) {
+                const int e = __ldg(nb + k);
+                const V3<R> v = P.d(i, e & IDX_MASK, ip);
+                const R c = pair_coef<R>(e, dot3(v, v), sig2, wcoef, ecoef, rc, cut2, mask);
+                an = an + c * v;
+            }
+        }
+    }
+    // bonded: gather of slot forces, 9 contributions spread over the lanes
+    V3<R> ab = mk<R>(0, 0, 0);
+    if (mask & 7) {
+        using V4 = typename Vec4<R>::type;
+        const V4 *__restrict__ S = (const V4 *)D.slot;
+        const int l = bi_lidx(bi);
+        for (int t = lane; t < 9; t += G) {
+            // t: 0 bond(l-1,l) 1 bond(l,l+1) 2 angle@l-2 3 angle@l-1 4 angle@l 5..8 dihedral@l-3..l
+            int start, k, cls;
+            R sgn = R(1);
+            if (t < 2) {
+                cls = 1;
+                start = l - 1 + t;
+                k = 0;
+                if (t == 1) sgn = R(-1);
+            } else if (t < 5) {
+                cls = 2;
+                start = l - 2 + (t - 2);
+                k = 1 + (2 - (t - 2));
+            } else {
+                cls = 4;
+                start = l - 3 + (t - 5);
+                k = 4 + (3 - (t - 5));
+            }
+            const int q = chain_bead(bi, start);
+            if ((mask & cls) && q >= 0) ab = ab + sgn * v3(S[(size_t)q * 8 + k]);
+        }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        an.x += __shfl_xor_sync(0xffffffffu, an.x, o, G);
+        an.y += __shfl_xor_sync(0xffffffffu, an.y, o, G);
+        an.z += __shfl_xor_sync(0xffffffffu, an.z, o, G);
+        ab.x += __shfl_xor_sync(0xffffffffu, ab.x, o, G);
+        ab.y += __shfl_xor_sync(0xffffffffu, ab.y, o, G);
+        ab.z += __shfl_xor_sync(0xffffffffu, ab.z, o, G);
+    }
+    if (lane == 0) {
+        sA[0][b] = an.x;
+        sA[1][b] = an.y;
+        sA[2][b] = an.z;
+        sB[0][b] = ab.x;
+        sB[1][b] = ab.y;
+        sB[2][b] = ab.z;
+        float sc = 1.f;
+        if (MODE == 0 && g.fcap > 0.0) {
+            const double4 fb = D.fbp[i];
+            const float fx = (float)(an.x + ab.x) + (float)fb.x, fy = (float)(an.y + ab.y) + (float)fb.y,
+                        fz = (float)(an.z + ab.z) + (float)fb.z;
+            const float fm = sqrtf(fx * fx + fy * fy + fz * fz);
+            if (fm > (float)g.fcap) sc = (float)g.fcap / fm;
+        }
+        sScale[b] = sc;
+    }
+    __syncthreads();
+
+    // -------------------------------------------------------------- phase B
+    const unsigned long long step = MODE == 0 ? *D.step_ctr : 0ull;
+    for (int t = threadIdx.x; t < 3 * BPB; t += blockDim.x) {
+        const int bb = t % BPB, c = t / BPB;
+        const int ii = i0 + bb;
+        if (ii >= g.n) continue;
+        double Fc = (double)sA[c][bb] + (double)sB[c][bb];
+        if (mask & 8) {
+            double *fp = (double *)(D.fbp + ii) + c;
+            Fc += *fp;
+            *fp = 0.0;
+        }
+        if (MODE == 1) {
+            fout[3 * (size_t)ii + c] = Fc;
+            continue;
+        }
+        Fc *= (double)sScale[bb];
+        const int4 bj = D.binfo[ii];
+        const InstP &jp = D.ip[bj.x];
+        const double4 m = D.mdc[ii];
+        const double xi = noise ? noise[((size_t)noise_step * g.n + ii) * 3 + c]
+                                : gauss3<R>(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
+        const double xc = ((const double *)(D.x[cur] + ii))[c];
+        double dx;
+        if (g.integrator == 1) {
+            double *vp = (double *)(D.v + ii) + c;
+            double *bp = (double *)(D.beta + ii) + c;
+            const double bn = m.w * xi;
+            const double vn = m.x * (*vp) + m.y * Fc + (*bp + bn);
+            *bp = bn;
+            *vp = vn;
+            dx = m.z * vn;
+        } else {
+            dx = m.x * Fc + m.w * xi;
+        }
+        const double xn = xc + dx;
+        if (!isfinite(xn)) atomicOr(D.err, ERR_NONFINITE);
+        ((double *)(D.x[cur ^ 1] + ii))[c] = xn;
+        double *mp = (double *)(D.move + ii) + c;
+        const double mn = *mp + dx;
+        *mp = mn;
+        sM[c][bb] = mn;
+        ((unsigned int *)(D.mir[cur ^ 1] + ii))[c] = fixed1(xn, jp.fsc[c]);
+    }
+    if (MODE == 1) return;
+    __syncthreads();
+
+    // -------------------------------------------------------------- phase C
+    // displacement^2 per bead and its top two per instance (shared memory);
+    // the block's result goes to its partial record, reduced by k_trigger
+    for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
+        const int ii = i0 + bb;
+        if (ii >= g.n) continue;
+        const double mx = sM[0][bb], my = sM[1][bb], mz = sM[2][bb];
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
+        if (!isfinite(d2)) atomicOr(D.err, ERR_NONFINITE);
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(d2);
+        const int inst = D.binfo[ii].x;
+        if (s_cnt <= 32) {
+            const int k = inst - s_lo;
+            const unsigned long long old = atomicMax(&s_m1[k], bits);
+            atomicMax(&s_m2[k], old < bits ? old : bits);
+        } else {
+            const unsigned long long old = atomicMax(&D.m1[inst], bits);
+            atomicMax(&D.m2[inst], old < bits ? old : bits);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        const int k = threadIdx.x;
+        const bool mine = s_cnt <= 2 && k < s_cnt;
+        D.part_inst[2 * blockIdx.x + k] = mine ? s_lo + k : -1;
+        D.part_m[4 * blockIdx.x + 2 * k] = mine ? s_m1[k] : 0ull;
+        D.part_m[4 * blockIdx.x + 2 * k + 1] = mine ? s_m2[k] : 0ull;
+    }
+    if (s_cnt > 2 && s_cnt <= 32 && (int)threadIdx.x < s_cnt) {
+        const unsigned long long b1 = s_m1[threadIdx.x], b2 = s_m2[threadIdx.x];
+        const int inst = s_lo + threadIdx.x;
+        const unsigned long long old = atomicMax(&D.m1[inst], b1);
+        const unsigned long long c2 = old < b1 ? old : b1;
+        atomicMax(&D.m2[inst], c2 > b2 ? c2 : b2);
+    }
+}
+
+// Rebuild trigger (job_md.F90:376-395): reduces the step kernel's per-block
+// top-two displacements per instance, then the last block sets the rebuild
+// flag of every instance with sqrt(d2max) + sqrt(d2max_2nd) > margin, clears
+// the base-pair staging count of flagged instances and advances the Philox
+// step counter.
+__device__ __forceinline__ void top2_merge(unsigned long long &a1, unsigned long long &a2, unsigned long long b1,
+                                           unsigned long long b2) {
+    const unsigned long long lo = a1 < b1 ? a1 : b1;
+    a1 = a1 > b1 ? a1 : b1;
+    const unsigned long long m = a2 > b2 ? a2 : b2;
+    a2 = lo > m ? lo : m;
+}
+
+__global__ void __launch_bounds__(256) k_trigger(Dev D, GlobP g, int nparts) {
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < 2 * nparts; base += gridDim.x * blockDim.x) {
+        const int r = base + threadIdx.x;
+        int inst = r < 2 * nparts ? D.part_inst[r] : -1;
+        unsigned long long a1 = 0ull, a2 = 0ull;
+        if (inst >= 0) {
+            a1 = D.part_m[2 * r];
+            a2 = D.part_m[2 * r + 1];
+        }
+        const int i0 = __shfl_sync(0xffffffffu, inst, 0);
+        const bool uniform = __all_sync(0xffffffffu, inst == i0 || inst < 0) && i0 >= 0;
+        if (uniform) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long b1 = __shfl_xor_sync(0xffffffffu, a1, o), b2 = __shfl_xor_sync(0xffffffffu, a2, o);
+                top2_merge(a1, a2, b1, b2);
+            }
+            if (lane == 0) {
+                const unsigned long long old = atomicMax(&D.m1[i0], a1);
+                const unsigned long long c2 = old < a1 ? old : a1;
+                atomicMax(&D.m2[i0], c2 > a2 ? c2 : a2);
+            }
+        } else if (inst >= 0) {
+            const unsigned long long old = atomicMax(&D.m1[inst], a1);
+            const unsigned long long c2 = old < a1 ? old : a1;
+            atomicMax(&D.m2[inst], c2 > a2 ? c2 : a2);
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(&D.ticket[0], 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    int any = 0;
+    for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) {
+        const double a = __longlong_as_double((long long)atomicExch(&D.m1[k], 0ull));
+        const double b = __longlong_as_double((long long)atomicExch(&D.m2[k], 0ull));
+        if (sqrt(a) + sqrt(b) > g.nl_margin) {
+            D.flag[k] = 1;
+            D.bp_cnt[k] = 0;
+            any = 1;
+        }
+    }
+    if (any) atomicOr(D.any, 1);
+    if (threadIdx.x == 0) {
+        D.ticket[0] = 0u;
+        D.step_ctr[0] += 1ull;
     }
 }
 
@@ -440,7 +699,7 @@ __global__ void k_mirror(Dev D, GlobP g, int cur) {
 template <typename R, int G, int MODE>
 static cudaError_t launch_step_g(const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, double *fout, int mask,
                                  cudaStream_t st) {
-    const int bpb = 256 / G;
+    constexpr int bpb = 256 / G;
     const int grid = (g.n + bpb - 1) / bpb;
     k_step<R, G, MODE><<<grid, 256, 0, st>>>(D, g, cur, noise, ns, fout, mask);
     return cudaGetLastError();
@@ -469,11 +728,28 @@ cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *f
     return launch_step_r<float, 1>(G, D, g, cur, nullptr, 0, fout, mask, st);
 }
 
-cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int mode, double tK, int nblocks, cudaStream_t st) {
-    if (g.prec == 0) k_bp<double><<<nblocks, 128, 0, st>>>(D, g, cur, mode, tK);
-    else k_bp<float><<<nblocks, 128, 0, st>>>(D, g, cur, mode, tK);
+// bonded terms (if do_bonded) and base-pair forces (if do_bp) of one step
+cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st) {
+    const int nb = do_bonded ? (g.n + 255) / 256 : 0;
+    const int grid = nb + (do_bp ? bp_blocks : 0);
+    if (grid == 0) return cudaSuccess;
+    if (g.prec == 0) k_pre<double><<<grid, 256, 0, st>>>(D, g, cur, nb, do_bp);
+    else k_pre<float><<<grid, 256, 0, st>>>(D, g, cur, nb, do_bp);
     return cudaGetLastError();
 }
+
+cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st) {
+    k_bp_energy<<<bp_blocks, 256, 0, st>>>(D, g, cur, tK);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st) {
+    const int grid = std::max(1, std::min(64, (2 * nparts + 255) / 256));
+    k_trigger<<<grid, 256, 0, st>>>(D, g, nparts);
+    return cudaGetLastError();
+}
+
+int step_blocks(int G, int n) { return (n + 256 / G - 1) / (256 / G); }
 
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
     const int grid = (g.n + 255) / 256;

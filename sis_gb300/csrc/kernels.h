@@ -14,10 +14,15 @@ struct RebuildPlan {
 
 cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long noise_step, cudaStream_t st);
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
-cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int mode, double tK, int nblocks, cudaStream_t st);
+cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st);
+cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st);
+cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st);
+int step_blocks(int G, int n);
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
-cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, cudaStream_t st);
+// after_step: the rebuild follows a step (k_trigger decides the flags);
+// otherwise the flags were set by the host and k_rebuild_begin starts it
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, cudaStream_t st);
 
 } // namespace sisg

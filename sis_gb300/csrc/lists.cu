@@ -410,9 +410,15 @@ __global__ void k_rebuild_begin(Dev D, GlobP g) {
         if (D.flag[k]) D.bp_cnt[k] = 0;
 }
 
-cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, cudaStream_t st) {
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts,
+                           cudaStream_t st) {
     const float slack = 1.001f;
-    k_rebuild_begin<<<(g.n_inst + 255) / 256, 256, 0, st>>>(D, g);
+    if (after_step) {
+        cudaError_t e = launch_trigger(D, g, nparts, st);
+        if (e != cudaSuccess) return e;
+    } else {
+        k_rebuild_begin<<<(g.n_inst + 255) / 256, 256, 0, st>>>(D, g);
+    }
     if (pl.n_small_items > 0) k_rebuild_small<<<pl.small_grid, 256, 0, st>>>(D, g, cur, pl.small_items, pl.n_small_items, slack);
     if (pl.n_large_items > 0) {
         k_cell_bin<<<pl.large_grid, 256, 0, st>>>(D, g, cur, pl.large_items, pl.n_large_items);

@@ -10,6 +10,27 @@
 
 namespace sisg {
 
+// Math functions with explicit single/double overloads, so that FP32
+// instantiations never promote to the FP64 pipe.
+namespace fm {
+__device__ __forceinline__ float sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+__device__ __forceinline__ float acos(float x) { return acosf(x); }
+__device__ __forceinline__ double acos(double x) { return ::acos(x); }
+__device__ __forceinline__ float atan2(float y, float x) { return atan2f(y, x); }
+__device__ __forceinline__ double atan2(double y, double x) { return ::atan2(y, x); }
+__device__ __forceinline__ float sin(float x) { return sinf(x); }
+__device__ __forceinline__ double sin(double x) { return ::sin(x); }
+__device__ __forceinline__ float cos(float x) { return cosf(x); }
+__device__ __forceinline__ double cos(double x) { return ::cos(x); }
+__device__ __forceinline__ float exp(float x) { return expf(x); }
+__device__ __forceinline__ double exp(double x) { return ::exp(x); }
+__device__ __forceinline__ float fabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double fabs(double x) { return ::fabs(x); }
+__device__ __forceinline__ float copysign(float a, float b) { return copysignf(a, b); }
+__device__ __forceinline__ double copysign(double a, double b) { return ::copysign(a, b); }
+} // namespace fm
+
 template <typename R> __device__ __forceinline__ R pick(double d, float f);
 template <> __device__ __forceinline__ double pick<double>(double d, float) { return d; }
 template <> __device__ __forceinline__ float pick<float>(double, float f) { return f; }
@@ -19,17 +40,44 @@ template <typename R> __device__ __forceinline__ V3<R> to(const V3<double> &a) {
 constexpr float NEAR_ONE = 0.99f;
 
 // ------------------------------------------------------------- bond
-// force_bond.F90:33-57: v = x1 - x2, f = k (d - r0)/d v, F1 -= f, F2 += f
+// force_bond.F90:33-57: v = x1 - x2, f = k (d - r0)/d v, F1 -= f, F2 += f.
+// Returns f (the force on the second bead).
+template <typename R> __device__ __forceinline__ V3<R> bond_f(const V3<R> &v, const GlobP &g);
+template <> __device__ __forceinline__ V3<double> bond_f<double>(const V3<double> &v, const GlobP &g) {
+    const double d = fm::sqrt(dot3(v, v));
+    const double delta = d - g.bond_r0;
+    return (g.bond_k * delta / d) * v;
+}
+// FP32: d - r0 cancels; it is formed as (d^2 - r0^2)/(d + r0) with d^2 - r0^2
+// accumulated from exact products (fmaf residuals) and error-free sums, so
+// that its relative error stays near one float ulp.
+__device__ __forceinline__ float two_sum(float a, float b, float &err) {
+    const float s = a + b;
+    const float bb = s - a;
+    err = (a - (s - bb)) + (b - bb);
+    return s;
+}
+template <> __device__ __forceinline__ V3<float> bond_f<float>(const V3<float> &v, const GlobP &g) {
+    const float px = v.x * v.x, py = v.y * v.y, pz = v.z * v.z;
+    const float ex = fmaf(v.x, v.x, -px), ey = fmaf(v.y, v.y, -py), ez = fmaf(v.z, v.z, -pz);
+    float e1, e2;
+    const float s1 = two_sum(px, py, e1);
+    const float s2 = two_sum(s1, pz, e2);
+    const float r0 = g.f_bond_r0;
+    const float r0sq = r0 * r0, r0sq_lo = fmaf(r0, r0, -r0sq);
+    const float diff = (s2 - r0sq) + ((e1 + e2) + (ex + ey + ez) - r0sq_lo);
+    const float d = sqrtf(s2);
+    const float delta = diff / (d + r0);
+    return (g.f_bond_k * delta / d) * v;
+}
 template <typename R>
 __device__ __forceinline__ V3<R> bond_force(const V3<R> &v, int p, const GlobP &g) {
-    const R d = sqrt(dot3(v, v));
-    const R delta = d - pick<R>(g.bond_r0, g.f_bond_r0);
-    const V3<R> f = (pick<R>(g.bond_k, g.f_bond_k) * delta / d) * v;
+    const V3<R> f = bond_f<R>(v, g);
     return p == 0 ? -f : f;
 }
 // energy_bond.F90:17-28
 template <typename R> __device__ __forceinline__ R bond_energy(const V3<R> &v, const GlobP &g) {
-    const R d = sqrt(dot3(v, v));
+    const R d = fm::sqrt(dot3(v, v));
     const R dd = d - pick<R>(g.bond_r0, g.f_bond_r0);
     return R(0.5) * pick<R>(g.bond_k, g.f_bond_k) * (dd * dd);
 }
@@ -40,13 +88,13 @@ template <typename R> __device__ __forceinline__ R bond_energy(const V3<R> &v, c
 template <typename T>
 __device__ __forceinline__ V3<T> angle_force_core(const V3<T> &v21, const V3<T> &v32, int p, T k, T t0, T *cos_out) {
     const T d21 = dot3(v21, v21), d32 = dot3(v32, v32), d2132 = dot3(v32, v21);
-    T cosine = -d2132 / sqrt(d21 * d32);
+    T cosine = -d2132 / fm::sqrt(d21 * d32);
     *cos_out = cosine;
-    if (fabs(cosine) > T(1)) cosine = copysign(T(1), cosine);
-    const T delta = acos(cosine) - t0;
+    if (fm::fabs(cosine) > T(1)) cosine = fm::copysign(T(1), cosine);
+    const T delta = fm::acos(cosine) - t0;
     T t = d21 * d32 - d2132 * d2132;
     if (t <= T(1)) t = T(1);
-    const T f = k * delta / sqrt(t);
+    const T f = k * delta / fm::sqrt(t);
     const V3<T> f21 = f * ((d2132 / d21) * v21 - v32);
     const V3<T> f32 = f * ((d2132 / d32) * v32 - v21);
     if (p == 0) return -f21;
@@ -57,7 +105,7 @@ __device__ __forceinline__ V3<T> angle_force_core(const V3<T> &v21, const V3<T> 
 template <typename T>
 __device__ __forceinline__ V3<T> angle_reb_force_core(const V3<T> &v12, const V3<T> &v32, int p, T k, T co0, T *cos_out) {
     const T d12 = dot3(v12, v12), d32 = dot3(v32, v32);
-    const T a1232 = sqrt(d12 * d32);
+    const T a1232 = fm::sqrt(d12 * d32);
     const T cosine = dot3(v12, v32) / a1232;
     *cos_out = cosine;
     const T omc = T(1) - cosine * cosine;
@@ -68,9 +116,45 @@ __device__ __forceinline__ V3<T> angle_reb_force_core(const V3<T> &v12, const V3
     if (p == 1) return -(f1 + f3);
     return f3;
 }
+// all three forces of one angle term (harmonic or ReB); *c receives the cosine
+template <typename T>
+__device__ __forceinline__ void angle_forces(const V3<T> &x21, const V3<T> &x32, const GlobP &g, V3<T> F[3], T *c) {
+    // x21 = x2 - x1, x32 = x3 - x2
+    if (!g.angl_reb) {
+        const T d21 = dot3(x21, x21), d32 = dot3(x32, x32), d2132 = dot3(x32, x21);
+        T cosine = -d2132 / fm::sqrt(d21 * d32);
+        *c = cosine;
+        if (fm::fabs(cosine) > T(1)) cosine = fm::copysign(T(1), cosine);
+        const T delta = fm::acos(cosine) - pick<T>(g.angl_t0, g.f_angl_t0);
+        T t = d21 * d32 - d2132 * d2132;
+        if (t <= T(1)) t = T(1);
+        const T f = pick<T>(g.angl_k, g.f_angl_k) * delta / fm::sqrt(t);
+        const V3<T> f21 = f * ((d2132 / d21) * x21 - x32);
+        const V3<T> f32 = f * ((d2132 / d32) * x32 - x21);
+        F[0] = -f21;
+        F[1] = f21 - f32;
+        F[2] = f32;
+    } else {
+        // v12 = x1 - x2 = -x21, v32 = x3 - x2 = x32
+        const V3<T> v12 = -x21;
+        const T k = pick<T>(g.angl_k, g.f_angl_k), co0 = pick<T>(g.cos_t0, g.f_cos_t0);
+        const T d12 = dot3(v12, v12), d32 = dot3(x32, x32);
+        const T a1232 = fm::sqrt(d12 * d32);
+        const T cosine = dot3(v12, x32) / a1232;
+        *c = cosine;
+        const T omc = T(1) - cosine * cosine;
+        const T f = -k * (cosine - co0) * (T(1) - cosine * co0) / (omc * omc);
+        const V3<T> f1 = f * ((T(1) / a1232) * x32 - (cosine / d12) * v12);
+        const V3<T> f3 = f * ((T(1) / a1232) * v12 - (cosine / d32) * x32);
+        F[0] = f1;
+        F[1] = -(f1 + f3);
+        F[2] = f3;
+    }
+}
+
 // energy_angl.F90:18-41 / energy_angl_ReB.F90 with v12 = x1 - x2, v32 = x3 - x2
 template <typename T> __device__ __forceinline__ T angle_energy_core(const V3<T> &v12, const V3<T> &v32, const GlobP &g, T *cos_out) {
-    T t = dot3(v32, v12) / sqrt(dot3(v12, v12) * dot3(v32, v32));
+    T t = dot3(v32, v12) / fm::sqrt(dot3(v12, v12) * dot3(v32, v32));
     *cos_out = t;
     const T k = pick<T>(g.angl_k, g.f_angl_k);
     if (g.angl_reb) {
@@ -79,7 +163,7 @@ template <typename T> __device__ __forceinline__ T angle_energy_core(const V3<T>
     }
     if (t > T(1)) t = T(1);
     else if (t < T(-1)) t = T(-1);
-    t = acos(t);
+    t = fm::acos(t);
     const T t0 = pick<T>(g.angl_t0, g.f_angl_t0);
     return T(0.5) * k * ((t - t0) * (t - t0));
 }
@@ -90,16 +174,16 @@ template <typename T> __device__ __forceinline__ T angle_energy_core(const V3<T>
 template <typename T>
 __device__ __forceinline__ V3<T> dih_force_core(const V3<T> &vij, const V3<T> &vkj, const V3<T> &vkl, int p, const GlobP &g) {
     const V3<T> m = cross3(vij, vkj), n = cross3(vkj, vkl);
-    const T akj2 = dot3(vkj, vkj), akj = sqrt(akj2);
-    const T dih = atan2(akj * dot3(vij, n), dot3(m, n));
+    const T akj2 = dot3(vkj, vkj), akj = fm::sqrt(akj2);
+    const T dih = fm::atan2(akj * dot3(vij, n), dot3(m, n));
     const T k = pick<T>(g.dih_k, g.f_dih_k), p0 = pick<T>(g.dih_p0, g.f_dih_p0);
     T pre;
     if (g.dih_type == 1) {
-        pre = -k * sin(dih + p0) * akj;
+        pre = -k * fm::sin(dih + p0) * akj;
     } else {
         const T w = pick<T>(g.dih_w, g.f_dih_w);
         const T dd = dih - p0;
-        pre = (k * w) * dd * exp((T(-0.5) * w) * (dd * dd)) * akj;
+        pre = (k * w) * dd * fm::exp((T(-0.5) * w) * (dd * dd)) * akj;
     }
     const V3<T> fi = (-pre / dot3(m, m)) * m;
     const V3<T> fl = (pre / dot3(n, n)) * n;
@@ -109,67 +193,44 @@ __device__ __forceinline__ V3<T> dih_force_core(const V3<T> &vij, const V3<T> &v
     if (p == 1) return (T(-1) + a) * fi + (-b) * fl;
     return (-a) * fi + (T(-1) + b) * fl;
 }
+// *near: a flanking bond angle has |cos| > NEAR_ONE (|m| or |n| small)
+template <typename T>
+__device__ __forceinline__ void dih_forces(const V3<T> &vij, const V3<T> &vkj, const V3<T> &vkl, const GlobP &g, V3<T> F[4],
+                                           bool *near) {
+    const V3<T> m = cross3(vij, vkj), n = cross3(vkj, vkl);
+    const T akj2 = dot3(vkj, vkj), akj = fm::sqrt(akj2);
+    const T s2 = T(1) - T(NEAR_ONE) * T(NEAR_ONE);
+    *near = dot3(m, m) < s2 * dot3(vij, vij) * akj2 || dot3(n, n) < s2 * akj2 * dot3(vkl, vkl);
+    const T dih = fm::atan2(akj * dot3(vij, n), dot3(m, n));
+    const T k = pick<T>(g.dih_k, g.f_dih_k), p0 = pick<T>(g.dih_p0, g.f_dih_p0);
+    T pre;
+    if (g.dih_type == 1) {
+        pre = -k * fm::sin(dih + p0) * akj;
+    } else {
+        const T w = pick<T>(g.dih_w, g.f_dih_w);
+        const T dd = dih - p0;
+        pre = (k * w) * dd * fm::exp((T(-0.5) * w) * (dd * dd)) * akj;
+    }
+    const V3<T> fi = (-pre / dot3(m, m)) * m;
+    const V3<T> fl = (pre / dot3(n, n)) * n;
+    const T a = dot3(vij, vkj) / akj2, b = dot3(vkl, vkj) / akj2;
+    F[0] = fi;
+    F[1] = (T(-1) + a) * fi + (-b) * fl;
+    F[2] = (-a) * fi + (T(-1) + b) * fl;
+    F[3] = fl;
+}
+
 // energy_dih_cos.F90:18-39 / energy_dih_exp.F90 (same angle as the force routine)
 template <typename T>
 __device__ __forceinline__ T dih_energy_core(const V3<T> &vij, const V3<T> &vkj, const V3<T> &vkl, const GlobP &g) {
     const V3<T> m = cross3(vij, vkj), n = cross3(vkj, vkl);
-    const T akj = sqrt(dot3(vkj, vkj));
-    const T dih = atan2(akj * dot3(vij, n), dot3(m, n));
+    const T akj = fm::sqrt(dot3(vkj, vkj));
+    const T dih = fm::atan2(akj * dot3(vij, n), dot3(m, n));
     const T k = pick<T>(g.dih_k, g.f_dih_k), p0 = pick<T>(g.dih_p0, g.f_dih_p0);
-    if (g.dih_type == 1) return k * (T(1) + cos(dih + p0));
+    if (g.dih_type == 1) return k * (T(1) + fm::cos(dih + p0));
     const T w = pick<T>(g.dih_w, g.f_dih_w);
     const T dd = dih - p0;
-    return -k * exp((T(-0.5) * w) * (dd * dd));
-}
-
-// ------------------------------------------------ bonded gather per bead
-// The bonded terms touching bead i: slot 0,1 bonds (l-1,l),(l,l+1); slots
-// 2..4 angles starting at l-2, l-1, l; slots 5..8 dihedrals starting at
-// l-3..l.  Terms exist as list_local.F90:1-126 creates them (linear chains
-// within the chain, circular chains modular).  Returns the force on bead i.
-template <typename R>
-__device__ V3<R> bonded_slot(int t, int i, const int4 &bi, const Pos<R> &P, const double4 *x64, const InstP &ip, const GlobP &g) {
-    const int l = bi_lidx(bi);
-    int start, nb, p;
-    if (t < 2) {
-        nb = 2; start = l - 1 + t; p = 1 - t;
-    } else if (t < 5) {
-        nb = 3; start = l - 2 + (t - 2); p = 2 - (t - 2);
-    } else {
-        if (g.dih_type == 0) return mk<R>(0, 0, 0);
-        nb = 4; start = l - 3 + (t - 5); p = 3 - (t - 5);
-    }
-    int q[4];
-    for (int k = 0; k < nb; ++k) {
-        q[k] = chain_bead(bi, start + k);
-        if (q[k] < 0) return mk<R>(0, 0, 0);
-    }
-    if (bi_circ(bi) && bi_clen(bi) < nb) return mk<R>(0, 0, 0);
-    if (nb == 2) return bond_force<R>(P.d(q[0], q[1], ip), p, g);
-    if (nb == 3) {
-        R c;
-        V3<R> f;
-        if (!g.angl_reb) {
-            f = angle_force_core<R>(P.d(q[1], q[0], ip), P.d(q[2], q[1], ip), p, pick<R>(g.angl_k, g.f_angl_k),
-                                    pick<R>(g.angl_t0, g.f_angl_t0), &c);
-        } else {
-            f = angle_reb_force_core<R>(P.d(q[0], q[1], ip), P.d(q[2], q[1], ip), p, pick<R>(g.angl_k, g.f_angl_k),
-                                        pick<R>(g.cos_t0, g.f_cos_t0), &c);
-        }
-        if (sizeof(R) == 4 && fabs((float)c) > NEAR_ONE) {
-            double cd;
-            V3<double> fd;
-            if (!g.angl_reb)
-                fd = angle_force_core<double>(dvec64(x64[q[1]], x64[q[0]], ip), dvec64(x64[q[2]], x64[q[1]], ip), p, g.angl_k,
-                                              g.angl_t0, &cd);
-            else
-                fd = angle_reb_force_core<double>(dvec64(x64[q[0]], x64[q[1]], ip), dvec64(x64[q[2]], x64[q[1]], ip), p,
-                                                  g.angl_k, g.cos_t0, &cd);
-            f = to<R>(fd);
-        }
-        return f;
-    }
-    return dih_force_core<R>(P.d(q[0], q[1], ip), P.d(q[2], q[1], ip), P.d(q[2], q[3], ip), p, g);
+    return -k * fm::exp((T(-0.5) * w) * (dd * dd));
 }
 
 // bonded energies owned by bead i (terms whose first bead is i)
@@ -187,7 +248,7 @@ __device__ void bonded_energy_owned(int i, const int4 &bi, const Pos<R> &P, cons
     if (q[1] >= 0 && q[2] >= 0 && (!circ || n >= 3)) {
         R c;
         double e = (double)angle_energy_core<R>(P.d(q[0], q[1], ip), P.d(q[2], q[1], ip), g, &c);
-        if (sizeof(R) == 4 && fabs((float)c) > NEAR_ONE) {
+        if (sizeof(R) == 4 && fm::fabs((float)c) > NEAR_ONE) {
             double cd;
             e = angle_energy_core<double>(dvec64(x64[q[0]], x64[q[1]], ip), dvec64(x64[q[2]], x64[q[1]], ip), g, &cd);
         }
@@ -210,9 +271,9 @@ __device__ __forceinline__ R pair_coef(int e, R d2, R sig2, R wcoef, R ecoef, R 
         c += wcoef * (s4 * s2 * s - s4);
     }
     if ((e & ELE_BIT) && (mask & 32) && d2 <= cut2) {
-        const R r = sqrt(d2);
+        const R r = fm::sqrt(d2);
         const R ri = R(1) / r;
-        c += ecoef * ri * ri * (ri + rc) * exp(-r * rc);
+        c += ecoef * ri * ri * (ri + rc) * fm::exp(-r * rc);
     }
     return c;
 }
@@ -234,7 +295,7 @@ __device__ __forceinline__ float pair_coef_f(int e, float d2, float sig2, float 
 // energy_wca.F90:19-33, energy_ele_DH.F90:20-37 for one (ordered) list entry
 template <typename R>
 __device__ __forceinline__ void pair_energy(int e, R d2, const InstP &ip, const GlobP &g, double *ew, double *ee) {
-    const R d = sqrt(d2);
+    const R d = fm::sqrt(d2);
     if (e & WCA_BIT) {
         const R sg = pick<R>(g.wca_sigma, g.f_wca_sigma);
         if (d < sg) {
@@ -248,10 +309,10 @@ __device__ __forceinline__ void pair_energy(int e, R d2, const InstP &ip, const 
             const R rc = pick<R>(ip.rcdist, ip.rcdist_f);
             const R coef = pick<R>(ip.ele_coef, ip.ele_coef_f);
             if (g.temp_indep == 0) {
-                *ee += (double)(coef / d * exp(-d * rc));
+                *ee += (double)(coef / d * fm::exp(-d * rc));
             } else {
                 const R rk = d * rc;
-                *ee += (double)(coef / d * exp(-rk) * (-(R(1) + R(0.5) * rk) * (R)ip.diele_dTcoef));
+                *ee += (double)(coef / d * fm::exp(-rk) * (-(R(1) + R(0.5) * rk) * (R)ip.diele_dTcoef));
             }
         }
     }
@@ -264,13 +325,13 @@ __device__ __forceinline__ void pair_energy(int e, R d2, const InstP &ip, const 
 // pair is outside cutoff_ddist.  f[6] receives dU-weighted forces before the
 // final multiplication by the energy (as f_bp in the reference); *u_out the
 // exponent u; *near is set when an angle cosine is within 1 - NEAR_ONE of +-1.
-template <typename T>
+template <typename T, typename P>
 __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v15, const V3<T> &v42, const V3<T> &v62,
-                              const BPP &b, V3<T> f[6], T *u_out, bool *near) {
+                              const P &b, V3<T> f[6], T *u_out, bool *near) {
     const T d1212 = dot3(v12, v12);
-    const T a12 = sqrt(d1212);
+    const T a12 = fm::sqrt(d1212);
     T d = a12 - (T)b.bond_r;
-    if (fabs(d) > (T)b.cutoff_ddist) return false;
+    if (fm::fabs(d) > (T)b.cutoff_ddist) return false;
     *near = false;
     T u = (T)b.bond_k * (d * d);
     V3<T> fi = ((T)2 * (T)b.bond_k * d / a12) * v12, fk, fl;
@@ -281,10 +342,10 @@ __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v
     const T o13 = d1213 / d1212, o42 = d1242 / d1212, o15 = d1215 / d1212, o62 = d1262 / d1212;
     T cosine, pre;
     // 3-1=2 (imp-1 -- imp -- jmp)
-    cosine = d1213 / (sqrt(d1313) * a12);
-    *near |= fabs((float)cosine) > NEAR_ONE;
-    d = acos(cosine) - (T)b.angl_theta[1];
-    pre = (T)2 * (T)b.angl_k[1] * d / sqrt(d1313 * d1212 - d1213 * d1213);
+    cosine = d1213 / (fm::sqrt(d1313) * a12);
+    *near |= fm::fabs((float)cosine) > NEAR_ONE;
+    d = fm::acos(cosine) - (T)b.angl_theta[1];
+    pre = (T)2 * (T)b.angl_k[1] * d / fm::sqrt(d1313 * d1212 - d1213 * d1213);
     u = u + (T)b.angl_k[1] * (d * d);
     fi = pre * (v12 - (d1213 / d1313) * v13);
     fk = pre * (v13 - o13 * v12);
@@ -292,33 +353,33 @@ __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v
     f[1] = f[1] + fk;
     f[2] = fi;
     // 1=2-4 (imp -- jmp -- jmp-1)
-    cosine = d1242 / (a12 * sqrt(d4242));
-    *near |= fabs((float)cosine) > NEAR_ONE;
-    d = acos(cosine) - (T)b.angl_theta[0];
+    cosine = d1242 / (a12 * fm::sqrt(d4242));
+    *near |= fm::fabs((float)cosine) > NEAR_ONE;
+    d = fm::acos(cosine) - (T)b.angl_theta[0];
     u = u + (T)b.angl_k[0] * (d * d);
-    pre = (T)2 * (T)b.angl_k[0] * d / sqrt(d1212 * d4242 - d1242 * d1242);
+    pre = (T)2 * (T)b.angl_k[0] * d / fm::sqrt(d1212 * d4242 - d1242 * d1242);
     fi = -pre * (v42 - o42 * v12);
     fk = -pre * (v12 - (d1242 / d4242) * v42);
     f[0] = f[0] + fi;
     f[1] = f[1] - fi - fk;
     f[3] = fk;
     // 5-1=2 (imp+1 -- imp -- jmp)
-    cosine = d1215 / (sqrt(d1515) * a12);
-    *near |= fabs((float)cosine) > NEAR_ONE;
-    d = acos(cosine) - (T)b.angl_theta[3];
+    cosine = d1215 / (fm::sqrt(d1515) * a12);
+    *near |= fm::fabs((float)cosine) > NEAR_ONE;
+    d = fm::acos(cosine) - (T)b.angl_theta[3];
     u = u + (T)b.angl_k[3] * (d * d);
-    pre = (T)2 * (T)b.angl_k[3] * d / sqrt(d1515 * d1212 - d1215 * d1215);
+    pre = (T)2 * (T)b.angl_k[3] * d / fm::sqrt(d1515 * d1212 - d1215 * d1215);
     fi = pre * (v12 - (d1215 / d1515) * v15);
     fk = pre * (v15 - o15 * v12);
     f[0] = f[0] - fi - fk;
     f[1] = f[1] + fk;
     f[4] = fi;
     // 1=2-6 (imp -- jmp -- jmp+1)
-    cosine = d1262 / (a12 * sqrt(d6262));
-    *near |= fabs((float)cosine) > NEAR_ONE;
-    d = acos(cosine) - (T)b.angl_theta[2];
+    cosine = d1262 / (a12 * fm::sqrt(d6262));
+    *near |= fm::fabs((float)cosine) > NEAR_ONE;
+    d = fm::acos(cosine) - (T)b.angl_theta[2];
     u = u + (T)b.angl_k[2] * (d * d);
-    pre = (T)2 * (T)b.angl_k[2] * d / sqrt(d1212 * d6262 - d1262 * d1262);
+    pre = (T)2 * (T)b.angl_k[2] * d / fm::sqrt(d1212 * d6262 - d1262 * d1262);
     fi = -pre * (v62 - o62 * v12);
     fk = -pre * (v12 - (d1262 / d6262) * v62);
     f[0] = f[0] + fi;
@@ -326,10 +387,10 @@ __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v
     f[5] = fk;
     // dihedral 4-2=1=3
     V3<T> m = cross3(v42, v12), n = cross3(v12, v13);
-    T dih = atan2(dot3(v42, n) * a12, dot3(m, n));
+    T dih = fm::atan2(dot3(v42, n) * a12, dot3(m, n));
     d = dih + (T)b.dihd_phi[0];
-    u = u + (T)b.dihd_k[0] * ((T)1 + cos(d));
-    pre = -(T)b.dihd_k[0] * sin(d) * a12;
+    u = u + (T)b.dihd_k[0] * ((T)1 + fm::cos(d));
+    pre = -(T)b.dihd_k[0] * fm::sin(d) * a12;
     fi = (pre / dot3(m, m)) * m;
     fl = (-pre / dot3(n, n)) * n;
     f[3] = f[3] + fi;
@@ -339,10 +400,10 @@ __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v
     // dihedral 6-2=1=5
     m = cross3(v62, v12);
     n = cross3(v12, v15);
-    dih = atan2(dot3(v62, n) * a12, dot3(m, n));
+    dih = fm::atan2(dot3(v62, n) * a12, dot3(m, n));
     d = dih + (T)b.dihd_phi[1];
-    u = u + (T)b.dihd_k[1] * ((T)1 + cos(d));
-    pre = -(T)b.dihd_k[1] * sin(d) * a12;
+    u = u + (T)b.dihd_k[1] * ((T)1 + fm::cos(d));
+    pre = -(T)b.dihd_k[1] * fm::sin(d) * a12;
     fi = (pre / dot3(m, m)) * m;
     fl = (-pre / dot3(n, n)) * n;
     f[5] = f[5] + fi;
@@ -355,14 +416,14 @@ __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v
 
 // energy_bp.F90 mp_angle (clamped) and mp_dihedral
 template <typename T> __device__ __forceinline__ T mp_angle(const V3<T> &v12, const V3<T> &v32) {
-    T co = dot3(v32, v12) / sqrt(dot3(v12, v12) * dot3(v32, v32));
+    T co = dot3(v32, v12) / fm::sqrt(dot3(v12, v12) * dot3(v32, v32));
     if (co > T(1)) co = T(1);
     else if (co < T(-1)) co = T(-1);
-    return acos(co);
+    return fm::acos(co);
 }
 template <typename T> __device__ __forceinline__ T mp_dihedral(const V3<T> &v12, const V3<T> &v32, const V3<T> &v34) {
     const V3<T> m = cross3(v12, v32), n = cross3(v32, v34);
-    return atan2(dot3(v12, n) * sqrt(dot3(v32, v32)), dot3(m, n));
+    return fm::atan2(dot3(v12, n) * fm::sqrt(dot3(v32, v32)), dot3(m, n));
 }
 
 } // namespace sisg

@@ -134,6 +134,18 @@ class Engine:
         self.system.instances[inst].tempK = tempK
         self.system.instances[inst].ionic_strength = ionic_strength
 
+    def set_force_cap(self, fmax: float):
+        """Equilibration aid: caps each bead's force magnitude (0 = off)."""
+        self._ck(self.L.sis_gpu_set_force_cap(self.h, float(fmax)))
+
+    def relax(self, capped_steps: int = 3000, fmax: float = 1000.0, free_steps: int = 2000):
+        """Force-capped dynamics followed by uncapped dynamics; removes the
+        bead overlaps of random-coil starts before production steps."""
+        self.set_force_cap(fmax)
+        self.step(capped_steps)
+        self.set_force_cap(0.0)
+        self.step(free_steps)
+
     def get_ele(self, inst: int) -> np.ndarray:
         out = np.zeros(4)
         self._ck(self.L.sis_gpu_get_ele(self.h, inst, ptr(out)))
