@@ -164,11 +164,16 @@ def run_gpu(args):
     # relax the random-coil starts (4 A contacts) before timing: force-capped
     # dynamics, then uncapped dynamics; neither is timed
     eng.relax(capped_steps=args.relax, fmax=1000.0, free_steps=args.relax)
+    # singularity guard for the production steps: the cosine dihedral force of
+    # the model (force_dih_cos.F90) diverges as a bond angle reaches 180 degrees;
+    # a per-bead cap far above thermal forces keeps such events finite
+    eng.set_force_cap(args.force_cap)
     for _ in range(args.warmup):
         eng.flush_l2()
         eng.step(S)
     launches0 = eng.kernel_launches()
     st0 = eng.stats()
+    cap0 = st0["capped"]
     times = []
     barrier(world)
     with Clocks(local) as clk:
@@ -203,6 +208,7 @@ def run_gpu(args):
     x, v, a = eng.get_state(-1)
     e64 = Engine(sysm, precision=FP64, seed=2024 + rank)
     e64.set_state(-1, x, v, a)
+    e64.set_force_cap(args.force_cap)
     f64 = np.concatenate([e64.force(k) for k in range(e64.n_inst)])
     eng.set_state(-1, x, v, a)
     f32 = np.concatenate([eng.force(k) for k in range(eng.n_inst)])
@@ -236,6 +242,7 @@ def run_gpu(args):
            "list_entries_per_bead": round(L, 3), "steps_per_rebuild": k_rebuild, "lanes_per_bead": st1["lanes_per_bead"],
            "l2": "flushed between timed steps (512 MiB write)", "fp64_value": fp64_value,
            "speedup_vs_fp64": value / fp64_value, "force_rms_rel_err_vs_fp64": err, "relax_steps": args.relax,
+           "force_cap": args.force_cap, "capped_bead_steps": st1["capped"] - cap0,
            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -323,6 +330,7 @@ def main():
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--relax", type=int, default=3000)
     ap.add_argument("--ref-sample", type=int, default=10)
+    ap.add_argument("--force-cap", type=float, default=1000.0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()

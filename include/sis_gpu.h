@@ -125,6 +125,7 @@ typedef struct sis_stats {
     int32_t n_beads;
     int32_t n_inst;
     int32_t lanes_per_bead; /* autotuned group width of the step kernel */
+    int64_t capped;         /* bead-steps at which sis_gpu_set_force_cap's cap bound */
 } sis_stats;
 
 /* Creates a context and uploads topology and parameters.  Replaces the
@@ -184,8 +185,20 @@ int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic
  * structures with overlapping beads; it has no counterpart in the reference
  * and is off unless set. */
 int sis_gpu_set_force_cap(sis_ctx *ctx, double fmax);
+/* per-bead integrator coefficients of instance inst, 4 per bead: GJF-2GJ
+ * md_coef(1:3) and md_coef_rep(1) (src/job_md.F90:700-767) */
+int sis_gpu_get_md_coef(sis_ctx *ctx, int32_t inst, double *out4);
 /* derived per-instance electrostatic values [ele_coef, lambdaD, ele_cutoff, diele] */
 int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *out4);
+
+/* Philox step counter of the noise stream (restart files store it in place
+ * of the reference's MT19937 state, src/write_rst.F90 PRNG block). */
+int sis_gpu_get_step(sis_ctx *ctx, uint64_t *step);
+int sis_gpu_set_step(sis_ctx *ctx, uint64_t step);
+
+/* Lanes per bead of the step kernel (1, 2, 4, 8, 16 or 32); 0 re-enables
+ * the autotuner that picks it on the first long run. */
+int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes);
 
 int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *st);
 /* Human-readable description of the last error on this context. */

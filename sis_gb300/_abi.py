@@ -63,7 +63,7 @@ class sis_stats(C.Structure):
     _fields_ = [
         ("steps", C.c_int64), ("rebuilds", C.c_int64), ("pair_entries", C.c_int64), ("wca_pairs", C.c_int64),
         ("ele_pairs", C.c_int64), ("bp_pairs", C.c_int64), ("error_flags", C.c_int32), ("n_beads", C.c_int32),
-        ("n_inst", C.c_int32), ("lanes_per_bead", C.c_int32),
+        ("n_inst", C.c_int32), ("lanes_per_bead", C.c_int32), ("capped", C.c_int64),
     ]
 
 
@@ -85,8 +85,12 @@ EXPORTS = {
     "sis_gpu_step": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "sis_gpu_set_condition": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),
     "sis_gpu_get_ele": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "sis_gpu_get_md_coef": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "sis_gpu_set_force_cap": (C.c_int, [C.c_void_p, C.c_double]),
     "sis_gpu_get_stats": (C.c_int, [C.c_void_p, C.POINTER(sis_stats)]),
+    "sis_gpu_get_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "sis_gpu_set_lanes": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sis_gpu_set_step": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sis_gpu_last_error": (C.c_char_p, [C.c_void_p]),
     "sis_gpu_event_record": (C.c_int, [C.c_void_p, C.c_int32]),
     "sis_gpu_event_elapsed": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),

@@ -264,10 +264,12 @@ int ensure_lists(sis_ctx *ctx) {
     return SIS_OK;
 }
 
+// Reads and clears the device error flags: an error is reported once.
 int check_err(sis_ctx *ctx) {
     int e = 0;
     CK(cudaMemcpyAsync(&e, ctx->D.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    if (e) CK(cudaMemsetAsync(ctx->D.err, 0, sizeof(int), ctx->st));
     if (e & ERR_PAIR_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "pair list capacity exceeded");
     if (e & ERR_BP_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "base-pair list capacity exceeded");
     if (e & ERR_NONFINITE) return fail(ctx, SIS_ERR_NONFINITE, "non-finite displacement");
@@ -529,6 +531,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.err, 1);
     rc |= dalloc(ctx, &D.max_need, 2);
     rc |= dalloc(ctx, &D.rebuilds, 1);
+    rc |= dalloc(ctx, &D.capped, 1);
     rc |= dalloc(ctx, &D.bead_cell, n);
     rc |= dalloc(ctx, &D.cell_cnt, ncells);
     rc |= dalloc(ctx, &D.cell_start, ncells + 1);
@@ -883,6 +886,15 @@ extern "C" int sis_gpu_set_force_cap(sis_ctx *ctx, double fmax) {
     return SIS_OK;
 }
 
+extern "C" int sis_gpu_get_md_coef(sis_ctx *ctx, int32_t inst, double *o) {
+    if (!ctx || !o) return SIS_ERR_ARG;
+    int off, cnt;
+    if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
+    CK(cudaMemcpyAsync(o, ctx->D.mdc + off, sizeof(double4) * cnt, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
 extern "C" int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *o) {
     if (!ctx || inst < 0 || inst >= ctx->n_inst || !o) return SIS_ERR_ARG;
     const InstP &I = ctx->ip[inst];
@@ -890,6 +902,35 @@ extern "C" int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *o) {
     o[1] = 1.0 / I.rcdist;
     o[2] = I.ele_cut;
     o[3] = diele_of(ctx, inst);
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_get_step(sis_ctx *ctx, uint64_t *step) {
+    if (!ctx || !step) return SIS_ERR_ARG;
+    unsigned long long v = 0;
+    CK(cudaMemcpyAsync(&v, ctx->D.step_ctr, sizeof(v), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    *step = v;
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_set_step(sis_ctx *ctx, uint64_t step) {
+    if (!ctx) return SIS_ERR_ARG;
+    unsigned long long v = step;
+    CK(cudaMemcpyAsync(ctx->D.step_ctr, &v, sizeof(v), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes) {
+    if (!ctx || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32))
+        return SIS_ERR_ARG;
+    if (lanes == 0) {
+        ctx->tuned = false;
+    } else {
+        ctx->G = lanes;
+        ctx->tuned = true;
+    }
     return SIS_OK;
 }
 
@@ -901,14 +942,17 @@ extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
     s->n_inst = ctx->n_inst;
     s->lanes_per_bead = ctx->G;
     long long rb = 0;
+    unsigned long long cp = 0;
     int e = 0;
     CK(cudaMemcpyAsync(&rb, ctx->D.rebuilds, sizeof(long long), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(&cp, ctx->D.capped, sizeof(cp), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaMemcpyAsync(&e, ctx->D.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     std::vector<int> nn(ctx->n), bc(ctx->n_inst);
     CK(cudaMemcpyAsync(nn.data(), ctx->D.nnbr, sizeof(int) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaMemcpyAsync(bc.data(), ctx->D.bp_cnt, sizeof(int) * ctx->n_inst, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     s->rebuilds = rb;
+    s->capped = (int64_t)cp;
     s->error_flags = e;
     for (int i = 0; i < ctx->n; ++i) s->pair_entries += std::min(nn[i], ctx->g.cap);
     for (int k = 0; k < ctx->n_inst; ++k) s->bp_pairs += std::min(bc[k], ctx->ip[k].bp_cap);

@@ -115,6 +115,7 @@ struct Dev {
     int *err;               // [1] error flags
     int *max_need;          // [2] largest pair / bp count seen
     long long *rebuilds;    // [1]
+    unsigned long long *capped; // [1] bead-steps at which the force cap bound
     // cell lists of large PBC instances
     int *bead_cell, *cell_cnt, *cell_start, *cell_beads;
     int n_cells;

@@ -89,18 +89,21 @@ __device__ __forceinline__ bool bp_record(const Dev &D, int r, int total, int n_
     return true;
 }
 
+// Bonded terms starting at bead s (list_local.F90 order).  The FP32 path
+// flags angle terms with |cos| > NEAR_ONE and dihedrals whose flanking angle
+// is that close to 180 degrees; the caller re-evaluates those in FP64.
 template <typename R>
-__device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int cur, int s) {
+__device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int cur, int s, bool *angle_near, bool *dih_near) {
     using V4 = typename Vec4<R>::type;
     V4 *S = (V4 *)D.slot + (size_t)s * 8;
     const int4 bi = D.binfo[s];
     const InstP &ip = D.ip[bi.x];
     const Pos<R> P = pos_of<R>(D, cur);
-    const double4 *__restrict__ x64 = D.x[cur];
     const int l = bi_lidx(bi), n = bi_clen(bi);
     const bool circ = bi_circ(bi);
     const int q1 = chain_bead(bi, l + 1), q2 = chain_bead(bi, l + 2), q3 = chain_bead(bi, l + 3);
     const V3<R> z = mk<R>(0, 0, 0);
+    *angle_near = *dih_near = false;
     // bond (s, s+1)
     V3<R> fb = z;
     if (q1 >= 0 && (!circ || n >= 2)) fb = bond_f<R>(P.d(s, q1, ip), g);
@@ -110,14 +113,7 @@ __device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int c
     if (q2 >= 0 && (!circ || n >= 3)) {
         R c;
         angle_forces<R>(P.d(q1, s, ip), P.d(q2, q1, ip), g, Fa, &c);
-        if constexpr (sizeof(R) == 4) {
-            if (fabsf(c) > NEAR_ONE) {
-                V3<double> Fd[3];
-                double cd;
-                angle_forces<double>(dvec64(x64[q1], x64[s], ip), dvec64(x64[q2], x64[q1], ip), g, Fd, &cd);
-                for (int k = 0; k < 3; ++k) Fa[k] = to<R>(Fd[k]);
-            }
-        }
+        if (sizeof(R) == 4) *angle_near = fm::fabs(c) > R(NEAR_ONE_STRICT);
     }
     S[1] = Vec4<R>::make(Fa[0]);
     S[2] = Vec4<R>::make(Fa[1]);
@@ -127,19 +123,34 @@ __device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int c
     if (g.dih_type != 0 && q3 >= 0 && (!circ || n >= 4)) {
         bool nr;
         dih_forces<R>(P.d(s, q1, ip), P.d(q2, q1, ip), P.d(q2, q3, ip), g, Fd, &nr);
-        if constexpr (sizeof(R) == 4) {
-            if (nr) {
-                V3<double> F64[4];
-                dih_forces<double>(dvec64(x64[s], x64[q1], ip), dvec64(x64[q2], x64[q1], ip), dvec64(x64[q2], x64[q3], ip), g, F64,
-                                   &nr);
-                for (int k = 0; k < 4; ++k) Fd[k] = to<R>(F64[k]);
-            }
-        }
+        if (sizeof(R) == 4) *dih_near = nr;
     }
     S[4] = Vec4<R>::make(Fd[0]);
     S[5] = Vec4<R>::make(Fd[1]);
     S[6] = Vec4<R>::make(Fd[2]);
     S[7] = Vec4<R>::make(Fd[3]);
+}
+
+// FP64 re-evaluation of a flagged angle (kind 0) or dihedral (kind 1) term
+// starting at bead s; overwrites its FP32 slot forces.
+__device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, int s, int kind) {
+    float4 *S = (float4 *)D.slot + (size_t)s * 8;
+    const int4 bi = D.binfo[s];
+    const InstP &ip = D.ip[bi.x];
+    const double4 *__restrict__ x64 = D.x[cur];
+    const int l = bi_lidx(bi);
+    const int q1 = chain_bead(bi, l + 1), q2 = chain_bead(bi, l + 2), q3 = chain_bead(bi, l + 3);
+    if (kind == 0) {
+        V3<double> F[3];
+        double c;
+        angle_forces<double>(dvec64(x64[q1], x64[s], ip), dvec64(x64[q2], x64[q1], ip), g, F, &c);
+        for (int k = 0; k < 3; ++k) S[1 + k] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
+    } else {
+        V3<double> F[4];
+        bool nr;
+        dih_forces<double>(dvec64(x64[s], x64[q1], ip), dvec64(x64[q2], x64[q1], ip), dvec64(x64[q2], x64[q3], ip), g, F, &nr);
+        for (int k = 0; k < 4; ++k) S[4 + k] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
+    }
 }
 
 // window and free-energy test of one record (force mode); returns true when
@@ -174,38 +185,14 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
 
 // force_bp.F90:44-204 / force_bp_triplet.F90:62-240 for one record that
 // passed bp_test: forces scattered into fbp, energy and status cached.
-template <typename R> __device__ __noinline__ void bp_eval(const Dev &D, const GlobP &g, int cur, int slot) {
-    const Pos<R> P = pos_of<R>(D, cur);
-    const double4 *__restrict__ x64 = D.x[cur];
-    const int4 rec = D.bps[slot];
-    const int4 nb = D.bps_n[slot];
-    const int i1 = rec.x, i2 = rec.y, type = rec.z & 0xff, h = rec.z >> 8;
-    const InstP &ip = D.ip[rec.w];
+// bp_finish applies the energy cut and the scatter; in the FP32 path,
+// contributions with exp(-u) < 2e-9 (u > 20) are not scattered (their forces
+// are below the FP32 rounding of the remaining terms) but their energy is
+// still cached.
+__device__ __forceinline__ void bp_finish(const Dev &D, const GlobP &g, int slot, const int4 &rec, const int4 &nb, double dG,
+                                          const V3<double> *fd, double ud, bool ok, bool scatter_all) {
+    const int type = rec.z & 0xff;
     const bool triplet = g.bp_model == 4 || g.bp_model == 5;
-    const double dG = triplet ? D.bp3_dH[h] - ip.tempK * D.bp3_dS[h] : 1.0;
-    V3<double> fd[6];
-    double ud = 0.0;
-    bool ok;
-    if constexpr (sizeof(R) == 4) {
-        V3<float> f[6];
-        float u;
-        bool nr = false;
-        ok = bp_force_core<float, BPPf>(P.d(i1, i2, ip), P.d(i1, nb.x, ip), P.d(i1, nb.z, ip), P.d(nb.y, i2, ip), P.d(nb.w, i2, ip),
-                                        D.bppf[type], f, &u, &nr);
-        if (ok && nr) {
-            bool nr2;
-            ok = bp_force_core<double, BPP>(dvec64(x64[i1], x64[i2], ip), dvec64(x64[i1], x64[nb.x], ip),
-                                            dvec64(x64[i1], x64[nb.z], ip), dvec64(x64[nb.y], x64[i2], ip),
-                                            dvec64(x64[nb.w], x64[i2], ip), D.bpp[type], fd, &ud, &nr2);
-        } else if (ok) {
-            for (int q = 0; q < 6; ++q) fd[q] = mk<double>((double)f[q].x, (double)f[q].y, (double)f[q].z);
-            ud = (double)u;
-        }
-    } else {
-        bool nr;
-        ok = bp_force_core<double, BPP>(P.d(i1, i2, ip), P.d(i1, nb.x, ip), P.d(i1, nb.z, ip), P.d(nb.y, i2, ip), P.d(nb.w, i2, ip),
-                                        D.bpp[type], fd, &ud, &nr);
-    }
     double ene = 0.0;
     unsigned char st = 0;
     if (ok) {
@@ -214,12 +201,14 @@ template <typename R> __device__ __noinline__ void bp_eval(const Dev &D, const G
         if (e <= g.bp_cutoff_energy) {
             ene = e;
             st = 1;
-            const int ids[6] = {i1, i2, nb.x, nb.y, nb.z, nb.w};
+            if (scatter_all || ud <= 20.0) {
+                const int ids[6] = {rec.x, rec.y, nb.x, nb.y, nb.z, nb.w};
 #pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                atomicAdd(&D.fbp[ids[q]].x, e * fd[q].x);
-                atomicAdd(&D.fbp[ids[q]].y, e * fd[q].y);
-                atomicAdd(&D.fbp[ids[q]].z, e * fd[q].z);
+                for (int q = 0; q < 6; ++q) {
+                    atomicAdd(&D.fbp[ids[q]].x, e * fd[q].x);
+                    atomicAdd(&D.fbp[ids[q]].y, e * fd[q].y);
+                    atomicAdd(&D.fbp[ids[q]].z, e * fd[q].z);
+                }
             }
         }
     }
@@ -227,23 +216,96 @@ template <typename R> __device__ __noinline__ void bp_eval(const Dev &D, const G
     D.bp_status[slot] = st;
 }
 
+__device__ __forceinline__ double bp_dG(const Dev &D, const GlobP &g, const int4 &rec) {
+    if (!(g.bp_model == 4 || g.bp_model == 5)) return 1.0;
+    const int h = rec.z >> 8;
+    return D.bp3_dH[h] - D.ip[rec.w].tempK * D.bp3_dS[h];
+}
+
+// FP64 evaluation (FP64 path, and records flagged near +-1 by the FP32 path)
+__device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, int slot) {
+    const double4 *__restrict__ x64 = D.x[cur];
+    const int4 rec = D.bps[slot];
+    const int4 nb = D.bps_n[slot];
+    const InstP &ip = D.ip[rec.w];
+    V3<double> fd[6];
+    double ud = 0.0;
+    bool nr;
+    const bool ok = bp_force_core<double, BPP>(dvec64(x64[rec.x], x64[rec.y], ip), dvec64(x64[rec.x], x64[nb.x], ip),
+                                               dvec64(x64[rec.x], x64[nb.z], ip), dvec64(x64[nb.y], x64[rec.y], ip),
+                                               dvec64(x64[nb.w], x64[rec.y], ip), D.bpp[rec.z & 0xff], fd, &ud, &nr);
+    bp_finish(D, g, slot, rec, nb, bp_dG(D, g, rec), fd, ud, ok, g.prec == 0);
+}
+
+// FP32 evaluation; returns true (and writes nothing) when an angle cosine is
+// within 1 - NEAR_ONE of +-1, so that the caller queues the record for FP64
+__device__ __noinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, int slot) {
+    const uint4 *__restrict__ m = D.mir[cur];
+    const int4 rec = D.bps[slot];
+    const int4 nb = D.bps_n[slot];
+    const InstP &ip = D.ip[rec.w];
+    V3<float> f[6];
+    float u;
+    bool nr = false;
+    const BPPf &bf = D.bppf[rec.z & 0xff];
+    const bool ok = bp_force_core<float, BPPf>(dvec32(m[rec.x], m[rec.y], ip), dvec32(m[rec.x], m[nb.x], ip),
+                                               dvec32(m[rec.x], m[nb.z], ip), dvec32(m[nb.y], m[rec.y], ip),
+                                               dvec32(m[nb.w], m[rec.y], ip), bf, f, &u, &nr);
+    if (ok && nr) return true;
+    const bool triplet = g.bp_model == 4 || g.bp_model == 5;
+    if (!ok || u > 20.f) {
+        // no force worth scattering: cache the energy without FP64 work
+        float e = 0.f;
+        unsigned char st = 0;
+        if (ok) {
+            e = triplet ? bf.U0 * (float)bp_dG(D, g, rec) * __expf(-u) : bf.U0 * __expf(-u);
+            st = e <= (float)g.bp_cutoff_energy;
+            if (!st) e = 0.f;
+        }
+        D.ene_bp[slot] = (double)e;
+        D.bp_status[slot] = st;
+        return false;
+    }
+    V3<double> fd[6];
+    for (int q = 0; q < 6; ++q) fd[q] = mk<double>((double)f[q].x, (double)f[q].y, (double)f[q].z);
+    bp_finish(D, g, slot, rec, nb, bp_dG(D, g, rec), fd, (double)u, ok, false);
+    return false;
+}
+
 template <typename R>
 __global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_blocks, int do_bp) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if ((int)blockIdx.x < nbond_blocks) {
+        // bonded terms, one start bead per thread; flagged terms are queued in
+        // shared memory and re-evaluated in FP64 on packed warps
+        __shared__ int qa[256], qd[256];
+        __shared__ int na, nd;
+        if (threadIdx.x == 0) na = nd = 0;
+        __syncthreads();
         const int s = blockIdx.x * blockDim.x + threadIdx.x;
-        if (s < g.n) bonded_terms<R>(D, g, cur, s);
+        if (s < g.n) {
+            bool an, dn;
+            bonded_terms<R>(D, g, cur, s, &an, &dn);
+            if (an) qa[atomicAdd(&na, 1)] = s;
+            if (dn) qd[atomicAdd(&nd, 1)] = s;
+        }
+        __syncthreads();
+        if constexpr (sizeof(R) == 4) {
+            for (int k = threadIdx.x; k < na; k += blockDim.x) bonded_fp64(D, g, cur, qa[k], 0);
+            for (int k = threadIdx.x; k < nd; k += blockDim.x) bonded_fp64(D, g, cur, qd[k], 1);
+        }
         return;
     }
     if (!do_bp) return;
     // Base-pair records: each warp tests 32 records at a time and queues the
-    // few that pass the distance window; full warps of queued records are
-    // evaluated together so that the expensive 6-bead term runs without
-    // divergence.
-    __shared__ int q[8][64];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // ones inside the distance window (q); full warps of queued records are
+    // evaluated together, so the 6-bead term runs without divergence.  In
+    // the FP32 path, records with an angle cosine near +-1 go to a second
+    // queue (nq) that is evaluated in FP64, again by whole warps.
+    __shared__ int q[8][64], nq[8][64];
     const int total = *D.bp_total;
     const int nwarps = (gridDim.x - nbond_blocks) * 8;
-    int qn = 0;
+    int qn = 0, nn = 0;
     for (int base = ((blockIdx.x - nbond_blocks) * 8 + warp) * 32; base < total; base += nwarps * 32) {
         const int r = base + lane;
         int slot = -1;
@@ -254,14 +316,38 @@ __global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_
         qn += __popc(bal);
         __syncwarp();
         if (qn >= 32) {
-            bp_eval<R>(D, g, cur, q[warp][lane]);
+            const int sl = q[warp][lane];
+            bool near = false;
+            if constexpr (sizeof(R) == 4) near = bp_eval_f(D, g, cur, sl);
+            else bp_eval_d(D, g, cur, sl);
             __syncwarp();
             if (lane < qn - 32) q[warp][lane] = q[warp][lane + 32];
             qn -= 32;
+            const unsigned nb = __ballot_sync(0xffffffffu, near);
+            if (near) nq[warp][nn + __popc(nb & ((1u << lane) - 1u))] = sl;
+            nn += __popc(nb);
             __syncwarp();
+            if (nn >= 32) {
+                bp_eval_d(D, g, cur, nq[warp][lane]);
+                __syncwarp();
+                if (lane < nn - 32) nq[warp][lane] = nq[warp][lane + 32];
+                nn -= 32;
+                __syncwarp();
+            }
         }
     }
-    if (lane < qn) bp_eval<R>(D, g, cur, q[warp][lane]);
+    bool near = false;
+    int sl = -1;
+    if (lane < qn) {
+        sl = q[warp][lane];
+        if constexpr (sizeof(R) == 4) near = bp_eval_f(D, g, cur, sl);
+        else bp_eval_d(D, g, cur, sl);
+    }
+    const unsigned nb = __ballot_sync(0xffffffffu, near);
+    if (near) nq[warp][nn + __popc(nb & ((1u << lane) - 1u))] = sl;
+    nn += __popc(nb);
+    __syncwarp();
+    for (int k = lane; k < nn; k += 32) bp_eval_d(D, g, cur, nq[warp][k]);
 }
 
 // energy_bp.F90 / energy_bp_triplet.F90 for every record at temperature tK
@@ -313,6 +399,36 @@ __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, doub
         }
         D.ene_bp[slot] = ene;
         D.bp_status[slot] = st;
+    }
+}
+
+// three Gaussian deviates of one bead from one Philox4x32-10 block
+// (Box-Muller on the pairs (r.x, r.y) and (r.z, r.w)); equal to gauss3 for
+// components 0, 1, 2
+template <typename R>
+__device__ __forceinline__ void gauss_bead(unsigned long long seed, int i, unsigned long long s, unsigned stream, double *xi) {
+    const uint4 r = philox4x32_10(make_uint4((unsigned)i, (unsigned)s, (unsigned)(s >> 32), stream),
+                                  make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    if constexpr (sizeof(R) == 4) {
+        const float u1 = (float)((r.x >> 8) + 1u) * (1.0f / 16777216.0f), u2 = (float)(r.y >> 8) * (1.0f / 16777216.0f);
+        const float u3 = (float)((r.z >> 8) + 1u) * (1.0f / 16777216.0f), u4 = (float)(r.w >> 8) * (1.0f / 16777216.0f);
+        float s1, c1, s2, c2;
+        sincospif(2.0f * u2, &s1, &c1);
+        sincospif(2.0f * u4, &s2, &c2);
+        const float r1 = sqrtf(-2.0f * logf(u1)), r2 = sqrtf(-2.0f * logf(u3));
+        xi[0] = (double)(r1 * c1);
+        xi[1] = (double)(r1 * s1);
+        xi[2] = (double)(r2 * c2);
+    } else {
+        const double u1 = ((double)r.x + 1.0) * (1.0 / 4294967296.0), u2 = (double)r.y * (1.0 / 4294967296.0);
+        const double u3 = ((double)r.z + 1.0) * (1.0 / 4294967296.0), u4 = (double)r.w * (1.0 / 4294967296.0);
+        double s1, c1, s2, c2;
+        sincospi(2.0 * u2, &s1, &c1);
+        sincospi(2.0 * u4, &s2, &c2);
+        const double r1 = sqrt(-2.0 * log(u1)), r2 = sqrt(-2.0 * log(u3));
+        xi[0] = r1 * c1;
+        xi[1] = r1 * s1;
+        xi[2] = r2 * c2;
     }
 }
 
@@ -370,7 +486,7 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
             const float sig2 = g.f_wca_sig2, wcoef = g.f_wca_coef;
             const float ecoef = ip.ele_coef_f, rc = ip.rcdist_f;
             const float cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
-#pragma unroll 2
+#pragma unroll 4
             for (int k = lane; k < cnt; k += G) {
                 const int e = __ldg(nb + k);
                 const uint4 mj = __ldg(mir + (e & IDX_MASK));
@@ -457,7 +573,10 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
             const float fx = (float)(an.x + ab.x) + (float)fb.x, fy = (float)(an.y + ab.y) + (float)fb.y,
                         fz = (float)(an.z + ab.z) + (float)fb.z;
             const float fm = sqrtf(fx * fx + fy * fy + fz * fz);
-            if (fm > (float)g.fcap) sc = (float)g.fcap / fm;
+            if (fm > (float)g.fcap) {
+                sc = (float)g.fcap / fm;
+                if (active) atomicAdd(D.capped, 1ull);
+            }
         }
         sScale[b] = sc;
     }
@@ -465,47 +584,65 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
 
     // -------------------------------------------------------------- phase B
     const unsigned long long step = MODE == 0 ? *D.step_ctr : 0ull;
-    for (int t = threadIdx.x; t < 3 * BPB; t += blockDim.x) {
-        const int bb = t % BPB, c = t / BPB;
+    for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
-        double Fc = (double)sA[c][bb] + (double)sB[c][bb];
+        double F[3];
+        double4 fb = make_double4(0.0, 0.0, 0.0, 0.0);
         if (mask & 8) {
-            double *fp = (double *)(D.fbp + ii) + c;
-            Fc += *fp;
-            *fp = 0.0;
+            fb = D.fbp[ii];
+            D.fbp[ii] = make_double4(0.0, 0.0, 0.0, 0.0);
         }
+        F[0] = (double)sA[0][bb] + (double)sB[0][bb] + fb.x;
+        F[1] = (double)sA[1][bb] + (double)sB[1][bb] + fb.y;
+        F[2] = (double)sA[2][bb] + (double)sB[2][bb] + fb.z;
         if (MODE == 1) {
-            fout[3 * (size_t)ii + c] = Fc;
+            fout[3 * (size_t)ii + 0] = F[0];
+            fout[3 * (size_t)ii + 1] = F[1];
+            fout[3 * (size_t)ii + 2] = F[2];
             continue;
         }
-        Fc *= (double)sScale[bb];
+        const double sc = (double)sScale[bb];
         const int4 bj = D.binfo[ii];
         const InstP &jp = D.ip[bj.x];
         const double4 m = D.mdc[ii];
-        const double xi = noise ? noise[((size_t)noise_step * g.n + ii) * 3 + c]
-                                : gauss3<R>(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
-        const double xc = ((const double *)(D.x[cur] + ii))[c];
-        double dx;
-        if (g.integrator == 1) {
-            double *vp = (double *)(D.v + ii) + c;
-            double *bp = (double *)(D.beta + ii) + c;
-            const double bn = m.w * xi;
-            const double vn = m.x * (*vp) + m.y * Fc + (*bp + bn);
-            *bp = bn;
-            *vp = vn;
-            dx = m.z * vn;
+        double xi[3];
+        if (noise) {
+            for (int c = 0; c < 3; ++c) xi[c] = noise[((size_t)noise_step * g.n + ii) * 3 + c];
         } else {
-            dx = m.x * Fc + m.w * xi;
+            gauss_bead<R>(g.seed, ii - jp.bead_off, step - jp.step0, jp.stream, xi);
         }
-        const double xn = xc + dx;
-        if (!isfinite(xn)) atomicOr(D.err, ERR_NONFINITE);
-        ((double *)(D.x[cur ^ 1] + ii))[c] = xn;
-        double *mp = (double *)(D.move + ii) + c;
-        const double mn = *mp + dx;
-        *mp = mn;
-        sM[c][bb] = mn;
-        ((unsigned int *)(D.mir[cur ^ 1] + ii))[c] = fixed1(xn, jp.fsc[c]);
+        const double4 x0 = D.x[cur][ii];
+        double4 v = D.v[ii], be = D.beta[ii], mv = D.move[ii];
+        const double xc[3] = {x0.x, x0.y, x0.z};
+        double vc[3] = {v.x, v.y, v.z}, bc[3] = {be.x, be.y, be.z}, mc[3] = {mv.x, mv.y, mv.z}, xn[3];
+        unsigned int mirn[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double Fc = F[c] * sc;
+            double dx;
+            if (g.integrator == 1) {
+                const double bn = m.w * xi[c];
+                const double vn = m.x * vc[c] + m.y * Fc + (bc[c] + bn);
+                bc[c] = bn;
+                vc[c] = vn;
+                dx = m.z * vn;
+            } else {
+                dx = m.x * Fc + m.w * xi[c];
+            }
+            xn[c] = xc[c] + dx;
+            if (!isfinite(xn[c])) atomicOr(D.err, ERR_NONFINITE);
+            mc[c] = mc[c] + dx;
+            sM[c][bb] = mc[c];
+            mirn[c] = fixed1(xn[c], jp.fsc[c]);
+        }
+        D.x[cur ^ 1][ii] = make_double4(xn[0], xn[1], xn[2], 0.0);
+        if (g.integrator == 1) {
+            D.v[ii] = make_double4(vc[0], vc[1], vc[2], 0.0);
+            D.beta[ii] = make_double4(bc[0], bc[1], bc[2], 0.0);
+        }
+        D.move[ii] = make_double4(mc[0], mc[1], mc[2], 0.0);
+        D.mir[cur ^ 1][ii] = make_uint4(mirn[0], mirn[1], mirn[2], 0u);
     }
     if (MODE == 1) return;
     __syncthreads();

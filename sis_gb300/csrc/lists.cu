@@ -141,6 +141,16 @@ __device__ __forceinline__ int pair_flags(const GlobP &g, const InstP &ip, const
 
 // Tests bead gi against candidate gj and appends the results.  Returns the
 // list flag word (0 if not listed).
+// Tests bead gi against candidate gj and appends base-pair records.  Returns
+// the list flag word (0 if not listed).  Membership is decided from the
+// float distance when it lies outside a 1e-4 relative band around every
+// cutoff (its error is below 1e-6 relative); inside the band the squared
+// distance is recomputed exactly as the reference computes it (FP64, wrapped
+// coordinates, lower index first, unfused).
+__device__ __forceinline__ bool near_cut(float d2f, double c2) {
+    const float c = (float)c2;
+    return d2f > c * 0.9999f && d2f < c * 1.0001f;
+}
 __device__ __forceinline__ int test_pair(const Dev &D, const GlobP &g, const InstP &ip, int cur, int gi, const int4 &bii,
                                          const uint4 &mi, const double4 &xi_w, int gj, float maxcut2f, int inst) {
     const uint4 mj = D.mir[cur][gj];
@@ -148,9 +158,12 @@ __device__ __forceinline__ int test_pair(const Dev &D, const GlobP &g, const Ins
     const float d2f = vf.x * vf.x + vf.y * vf.y + vf.z * vf.z;
     if (!(d2f <= maxcut2f)) return 0;
     const int4 bij = D.binfo[gj];
-    const double4 xj_w = wrap_pos(D.x[cur][gj], ip);
     const bool ilo = gi < gj;
-    const double d2 = ilo ? exact_d2(xi_w, xj_w, ip) : exact_d2(xj_w, xi_w, ip);
+    double d2 = (double)d2f;
+    if (near_cut(d2f, ip.wca_nl_cut2) || near_cut(d2f, ip.ele_nl_cut2) || near_cut(d2f, ip.bp_nl_cut2)) {
+        const double4 xj_w = wrap_pos(D.x[cur][gj], ip);
+        d2 = ilo ? exact_d2(xi_w, xj_w, ip) : exact_d2(xj_w, xi_w, ip);
+    }
     const int4 &bl = ilo ? bii : bij;
     const int4 &bh = ilo ? bij : bii;
     const int f = pair_flags(g, ip, bl, bh, d2);

@@ -37,7 +37,11 @@ template <> __device__ __forceinline__ float pick<float>(double, float f) { retu
 
 template <typename R> __device__ __forceinline__ V3<R> to(const V3<double> &a) { return mk<R>((R)a.x, (R)a.y, (R)a.z); }
 
+// |cos| above which FP32 angle evaluations are redone in FP64: NEAR_ONE for
+// the base-pair angles (acos form), NEAR_ONE_STRICT for the bonded angle and
+// dihedral terms, whose FP32 forms are cancellation-free
 constexpr float NEAR_ONE = 0.99f;
+constexpr float NEAR_ONE_STRICT = 0.9999f;
 
 // ------------------------------------------------------------- bond
 // force_bond.F90:33-57: v = x1 - x2, f = k (d - r0)/d v, F1 -= f, F2 += f.
@@ -116,10 +120,62 @@ __device__ __forceinline__ V3<T> angle_reb_force_core(const V3<T> &v12, const V3
     if (p == 1) return -(f1 + f3);
     return f3;
 }
+// a*b - c*d with one rounding (Kahan's difference of products); keeps cross
+// products of nearly parallel vectors accurate in FP32
+__device__ __forceinline__ float dop(float a, float b, float c, float d) {
+    const float w = c * d;
+    const float e = fmaf(-c, d, w);
+    const float f = fmaf(a, b, -w);
+    return f + e;
+}
+__device__ __forceinline__ V3<float> cross_acc(const V3<float> &a, const V3<float> &b) {
+    return mk<float>(dop(a.y, b.z, a.z, b.y), dop(a.z, b.x, a.x, b.z), dop(a.x, b.y, a.y, b.x));
+}
+
 // all three forces of one angle term (harmonic or ReB); *c receives the cosine
 template <typename T>
+__device__ __forceinline__ void angle_forces(const V3<T> &x21, const V3<T> &x32, const GlobP &g, V3<T> F[3], T *c);
+
+// FP32: the angle is atan2(|x21 x x32|, -x21.x32) and t = |x21 x x32|^2
+// (Lagrange's identity for the reference's d21*d32 - d2132**2), both free of
+// the cancellation that acos and the difference form suffer near 0 and 180
+// degrees; the reference's clamps (|cos| <= 1, t >= 1) are kept.
+template <>
+__device__ __forceinline__ void angle_forces<float>(const V3<float> &x21, const V3<float> &x32, const GlobP &g, V3<float> F[3],
+                                                    float *c) {
+    const float d21 = dot3(x21, x21), d32 = dot3(x32, x32), d2132 = dot3(x32, x21);
+    const V3<float> cr = cross_acc(x21, x32);
+    float t = dot3(cr, cr);
+    const float cosine = -d2132 * rsqrtf(d21 * d32);
+    *c = cosine;
+    if (!g.angl_reb) {
+        const float delta = atan2f(sqrtf(t), -d2132) - g.f_angl_t0;
+        if (t <= 1.f) t = 1.f;
+        const float f = g.f_angl_k * delta / sqrtf(t);
+        const V3<float> f21 = f * ((d2132 / d21) * x21 - x32);
+        const V3<float> f32 = f * ((d2132 / d32) * x32 - x21);
+        F[0] = -f21;
+        F[1] = f21 - f32;
+        F[2] = f32;
+    } else {
+        // v12 = -x21; cos = v12.x32/|v12||x32|; 1 - cos^2 = t/(d12 d32)
+        const V3<float> v12 = -x21;
+        const float k = g.f_angl_k, co0 = g.f_cos_t0;
+        const float a1232 = sqrtf(d21 * d32);
+        const float cs = -d2132 / a1232;
+        const float omc = t / (d21 * d32);
+        const float f = -k * (cs - co0) * (1.f - cs * co0) / (omc * omc);
+        const V3<float> f1 = f * ((1.f / a1232) * x32 - (cs / d21) * v12);
+        const V3<float> f3 = f * ((1.f / a1232) * v12 - (cs / d32) * x32);
+        F[0] = f1;
+        F[1] = -(f1 + f3);
+        F[2] = f3;
+    }
+}
+
+template <typename T>
 __device__ __forceinline__ void angle_forces(const V3<T> &x21, const V3<T> &x32, const GlobP &g, V3<T> F[3], T *c) {
-    // x21 = x2 - x1, x32 = x3 - x2
+    // x21 = x2 - x1, x32 = x3 - x2 (FP64: the reference's formulas)
     if (!g.angl_reb) {
         const T d21 = dot3(x21, x21), d32 = dot3(x32, x32), d2132 = dot3(x32, x21);
         T cosine = -d2132 / fm::sqrt(d21 * d32);
@@ -197,9 +253,16 @@ __device__ __forceinline__ V3<T> dih_force_core(const V3<T> &vij, const V3<T> &v
 template <typename T>
 __device__ __forceinline__ void dih_forces(const V3<T> &vij, const V3<T> &vkj, const V3<T> &vkl, const GlobP &g, V3<T> F[4],
                                            bool *near) {
-    const V3<T> m = cross3(vij, vkj), n = cross3(vkj, vkl);
+    V3<T> m, n;
+    if constexpr (sizeof(T) == 4) {
+        m = cross_acc(vij, vkj);
+        n = cross_acc(vkj, vkl);
+    } else {
+        m = cross3(vij, vkj);
+        n = cross3(vkj, vkl);
+    }
     const T akj2 = dot3(vkj, vkj), akj = fm::sqrt(akj2);
-    const T s2 = T(1) - T(NEAR_ONE) * T(NEAR_ONE);
+    const T s2 = T(1) - T(NEAR_ONE_STRICT) * T(NEAR_ONE_STRICT);
     *near = dot3(m, m) < s2 * dot3(vij, vij) * akj2 || dot3(n, n) < s2 * akj2 * dot3(vkl, vkl);
     const T dih = fm::atan2(akj * dot3(vij, n), dot3(m, n));
     const T k = pick<T>(g.dih_k, g.f_dih_k), p0 = pick<T>(g.dih_p0, g.f_dih_p0);

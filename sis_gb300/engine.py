@@ -146,10 +146,27 @@ class Engine:
         self.set_force_cap(0.0)
         self.step(free_steps)
 
+    def get_md_coef(self, inst: int = -1) -> np.ndarray:
+        out = np.zeros((self.nmp(inst), 4))
+        self._ck(self.L.sis_gpu_get_md_coef(self.h, inst, ptr(out)))
+        return out
+
     def get_ele(self, inst: int) -> np.ndarray:
         out = np.zeros(4)
         self._ck(self.L.sis_gpu_get_ele(self.h, inst, ptr(out)))
         return out
+
+    def set_lanes(self, lanes: int):
+        """Lanes per bead of the step kernel; 0 lets the autotuner choose."""
+        self._ck(self.L.sis_gpu_set_lanes(self.h, int(lanes)))
+
+    def get_step(self) -> int:
+        v = C.c_uint64()
+        self._ck(self.L.sis_gpu_get_step(self.h, C.byref(v)))
+        return int(v.value)
+
+    def set_step(self, step: int):
+        self._ck(self.L.sis_gpu_set_step(self.h, int(step)))
 
     def stats(self) -> dict:
         s = _abi.sis_stats()
