@@ -239,7 +239,7 @@ def run_gpu(args):
     e2e_value = world * N * S * args.steps / e2e_s
     cfg = {"workload": args.workload, "description": WORKLOADS[args.workload], "n_beads": N,
            "n_instances": len(sysm.instances), "md_steps_per_step": S, "precision": "FP32 terms / FP64 accumulate+integrate",
-           "list_entries_per_bead": round(L, 3), "steps_per_rebuild": k_rebuild, "lanes_per_bead": st1["lanes_per_bead"],
+           "list_entries_per_bead": round(L, 3), "steps_per_rebuild": k_rebuild, "lanes_per_bead": st1["lanes_per_bead"], "bp_blocks": st1["bp_blocks"],
            "l2": "flushed between timed steps (512 MiB write)", "fp64_value": fp64_value,
            "speedup_vs_fp64": value / fp64_value, "force_rms_rel_err_vs_fp64": err, "relax_steps": args.relax,
            "force_cap": args.force_cap, "capped_bead_steps": st1["capped"] - cap0,

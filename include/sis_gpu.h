@@ -126,6 +126,8 @@ typedef struct sis_stats {
     int32_t n_inst;
     int32_t lanes_per_bead; /* autotuned group width of the step kernel */
     int64_t capped;         /* bead-steps at which sis_gpu_set_force_cap's cap bound */
+    int32_t bp_blocks;      /* autotuned block count of the base-pair pass */
+    int32_t reserved;
 } sis_stats;
 
 /* Creates a context and uploads topology and parameters.  Replaces the

@@ -20,7 +20,7 @@ OBJ = ROOT / "_build"
 LIB = PKG / "_lib" / "libsisgpu.so"
 SOURCES = ["kernels.cu", "lists.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-Wno-deprecated-declarations", "-diag-suppress", "1444"]
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-Wno-deprecated-declarations,-ffp-contract=off", "-diag-suppress", "1444"]
 
 
 def nvcc() -> str:

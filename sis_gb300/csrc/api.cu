@@ -59,6 +59,7 @@ struct sis_ctx {
     GlobP g{};
     sis_params p{};
     int n = 0, n_inst = 0, cur = 0, G = 8;
+    int bpb = 2 * 152; // base-pair blocks of k_pre (tuned)
     std::vector<InstP> ip;
     std::vector<int4> binfo;
     std::vector<int> seq;
@@ -68,6 +69,9 @@ struct sis_ctx {
     InstP *ip_d = nullptr;
     BPP bpp[MAX_BP_TYPES]{};
     double bp_cutoff_dist = 0.0;
+    std::vector<double> bp3_dH, bp3_dS; // triplet free-energy tables [469]
+    std::vector<float> dgf;             // [n_inst][469] FP32 dH - T dS
+    float *dgf_d = nullptr;
     RebuildPlan plan{};
     int2 *items_d = nullptr;
     cudaStream_t st = nullptr;
@@ -235,6 +239,25 @@ int upload_ip(sis_ctx *ctx) {
     return SIS_OK;
 }
 
+// Row k of the FP32 triplet free-energy table at instance k's temperature.
+// dG = dH - T dS is rounded once per operation (as the FP64 kernels and the
+// FP64 restatement evaluate it), and the FP32 copy keeps the sign of the FP64
+// value, so the dG < 0 test of the mixed path decides as the FP64 path does.
+int upload_dgf(sis_ctx *ctx, int k) {
+    const double T = ctx->ip[k].tempK;
+    float *row = ctx->dgf.data() + (size_t)k * 469;
+    for (int h = 0; h < 469; ++h) {
+        const double p = T * ctx->bp3_dS[h];
+        const double v = ctx->bp3_dH[h] - p;
+        float f = (float)v;
+        if (v < 0.0 && !(f < 0.f)) f = -1.17549435e-38f;
+        if (!(v < 0.0) && !(f >= 0.f)) f = 0.f;
+        row[h] = f;
+    }
+    CK(cudaMemcpyAsync(ctx->dgf_d + (size_t)k * 469, row, sizeof(float) * 469, cudaMemcpyHostToDevice, ctx->st));
+    return SIS_OK;
+}
+
 int ensure_lists(sis_ctx *ctx);
 
 int run_rebuild(sis_ctx *ctx, int after_step = 0) {
@@ -283,7 +306,7 @@ int inst_range(const sis_ctx *ctx, int inst, int &off, int &cnt) {
     return SIS_OK;
 }
 
-int bp_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? 4 * 152 : 0; }
+int bp_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? ctx->bpb : 0; }
 
 int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
     CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st));
@@ -320,6 +343,28 @@ int autotune(sis_ctx *ctx) {
         }
     }
     ctx->G = bestG;
+    // base-pair blocks: fewer, longer-lived blocks fill their evaluation
+    // queues more often; more blocks hide more gather latency
+    if (ctx->g.bp_model > 0) {
+        const int bcand[4] = {152, 304, 608, 1216};
+        best = 1e30f;
+        for (int c = 0; c < 4; ++c) {
+            CK(launch_pre(ctx->D, ctx->g, ctx->cur, 0, 1, bcand[c], ctx->st));
+            CK(cudaEventRecord(e0, ctx->st));
+            for (int r = 0; r < 3; ++r) CK(launch_pre(ctx->D, ctx->g, ctx->cur, 0, 1, bcand[c], ctx->st));
+            CK(cudaEventRecord(e1, ctx->st));
+            CK(cudaEventSynchronize(e1));
+            float ms;
+            CK(cudaEventElapsedTime(&ms, e0, e1));
+            ctx->launches += 4;
+            if (ms < best) {
+                best = ms;
+                ctx->bpb = bcand[c];
+            }
+        }
+        // the trial launches scattered base-pair forces: clear them
+        CK(cudaMemsetAsync(ctx->D.fbp, 0, sizeof(double4) * ctx->n, ctx->st));
+    }
     ctx->tuned = true;
     return SIS_OK;
 }
@@ -466,6 +511,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     g.wca_sig2 = p.wca_sigma * p.wca_sigma;
     g.wca_coef = 12.0 * p.wca_eps / g.wca_sig2;
     g.bp_cutoff_energy = p.bp_cutoff_energy;
+    g.f_bp_cutoff_energy = (float)p.bp_cutoff_energy;
     g.nl_margin = p.nl_margin;
     g.f_bond_k = (float)g.bond_k; g.f_bond_r0 = (float)g.bond_r0;
     g.f_angl_k = (float)g.angl_k; g.f_angl_t0 = (float)g.angl_t0; g.f_cos_t0 = (float)g.cos_t0;
@@ -486,6 +532,8 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.x[1], n);
     rc |= dalloc(ctx, &D.mir[0], n);
     rc |= dalloc(ctx, &D.mir[1], n);
+    rc |= dalloc(ctx, &D.res[0], n);
+    rc |= dalloc(ctx, &D.res[1], n);
     rc |= dalloc(ctx, &D.v, n);
     rc |= dalloc(ctx, &D.beta, n);
     rc |= dalloc(ctx, &D.move, n);
@@ -519,6 +567,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &hash_d, 4097);
     rc |= dalloc(ctx, &dH_d, 469);
     rc |= dalloc(ctx, &dS_d, 469);
+    rc |= dalloc(ctx, &ctx->dgf_d, (size_t)469 * ni);
     rc |= dalloc(ctx, &ctx->ip_d, ni);
     rc |= dalloc(ctx, &D.m1, ni);
     rc |= dalloc(ctx, &D.m2, ni);
@@ -548,6 +597,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     D.bp3_hash = hash_d;
     D.bp3_dH = dH_d;
     D.bp3_dS = dS_d;
+    D.bp_dgf = ctx->dgf_d;
     D.ip = ctx->ip_d;
     std::vector<double4> mdc;
     md_coefs(ctx, mdc);
@@ -603,6 +653,11 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     ok &= cudaMemcpy(dH_d, dH.data(), sizeof(double) * 469, cudaMemcpyHostToDevice) == cudaSuccess;
     ok &= cudaMemcpy(dS_d, dS.data(), sizeof(double) * 469, cudaMemcpyHostToDevice) == cudaSuccess;
     ok &= cudaMemcpy(ctx->ip_d, ctx->ip.data(), sizeof(InstP) * ni, cudaMemcpyHostToDevice) == cudaSuccess;
+    ctx->bp3_dH = dH;
+    ctx->bp3_dS = dS;
+    ctx->dgf.assign((size_t)469 * ni, 0.f);
+    for (int k = 0; k < ni && ok; ++k) ok &= upload_dgf(ctx, k) == SIS_OK;
+    ok &= cudaStreamSynchronize(ctx->st) == cudaSuccess;
     ok &= cudaMemcpy(ctx->items_d, items.data(), sizeof(int2) * std::max<size_t>(1, items.size()), cudaMemcpyHostToDevice) ==
           cudaSuccess;
     if (!ok) {
@@ -875,6 +930,7 @@ extern "C" int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, d
     const InstP &I = ctx->ip[inst];
     CK(cudaMemcpyAsync(ctx->D.mdc + I.bead_off, mdc.data() + I.bead_off, sizeof(double4) * I.n, cudaMemcpyHostToDevice, ctx->st));
     int rc = upload_ip(ctx);
+    if (!rc) rc = upload_dgf(ctx, inst);
     if (rc) return rc;
     CK(cudaStreamSynchronize(ctx->st));
     return SIS_OK;
@@ -941,6 +997,7 @@ extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
     s->n_beads = ctx->n;
     s->n_inst = ctx->n_inst;
     s->lanes_per_bead = ctx->G;
+    s->bp_blocks = bp_blocks(ctx);
     long long rb = 0;
     unsigned long long cp = 0;
     int e = 0;

@@ -6,10 +6,17 @@
 //                       the int32 difference of two mirrors is the exact
 //                       minimum-image separation in units of 1/S (PBC: S = 2^32/L,
 //                       so the box maps onto the 32-bit ring; no PBC: S = 2^20/A)
+//   res[2]    float4    residual x*S - llrint(x*S) of each mirror component, for
+//                       the rare nearly-collinear terms that need separations
+//                       beyond the mirror's resolution
 //   v, beta   double4   velocities and GJF-2GJ noise term (reference: velos, accels)
 //   move      double4   displacement since the last rebuild (reference: xyz_move)
 //   mdc       double4   per-bead integrator coefficients (a, sqrt(b)h/m, sqrt(b)h, noise)
-//   fbp       double4   base-pair forces of the current step (atomic scatter target)
+//   fbp       double4   base-pair forces of the current step (atomic scatter
+//                       target): FP64 values in the FP64 path; in the mixed path
+//                       the same words hold int64 fixed point (units of 2^-32
+//                       kcal/mol/A), so that the sum is exact and independent
+//                       of the order in which records arrive
 //   binfo     int4      (instance, chain start, chain length | circ<<31,
 //                        local index | seq<<24 | charge<<28)
 //   nbr       int32     per-bead pair list, stride cap: j | WCA<<31 | ELE<<30
@@ -34,6 +41,24 @@ constexpr int MAX_BP_TYPES = 7;
 constexpr int ERR_PAIR_OVERFLOW = 1;
 constexpr int ERR_BP_OVERFLOW = 2;
 constexpr int ERR_NONFINITE = 4;
+
+// Fixed-point base-pair force accumulation of the mixed path: one unit is
+// 2^-32 kcal/mol/A; contributions of magnitude 2^30 or more are reported as
+// non-finite (no physical step survives such a force).
+constexpr float FX_LIMIT = 1073741824.0f;
+constexpr double FX_UNIT = 1.0 / 4294967296.0;
+
+// round(v * 2^32) for |v| < 2^30 from FP32 and 32-bit integer operations:
+// a = v*2^32 is exact; h = trunc(a/2^31) and l = a - h*2^31 are exact, and
+// l is rounded to an integer only when |a| < 2^31 (then h = 0).
+__device__ __forceinline__ long long fx_of(float v) {
+    const float a = v * 4294967296.0f;
+    const float h = truncf(a * 4.656612873077392578125e-10f);
+    const float l = fmaf(h, -2147483648.0f, a);
+    return (long long)__float2int_rz(h) * 2147483648LL + (long long)__float2int_rn(l);
+}
+__device__ __forceinline__ long long fx_of(double v) { return __double2ll_rn(v * 4294967296.0); }
+__device__ __forceinline__ double fx_value(double word) { return (double)__double_as_longlong(word) * FX_UNIT; }
 
 struct InstP {
     double box[3];     // PBC box (0 when pbc == 0)
@@ -62,6 +87,7 @@ struct GlobP {
     double bond_k, bond_r0, angl_k, angl_t0, cos_t0, dih_k, dih_w, dih_p0;
     double wca_sigma, wca_eps, wca_sig2, wca_coef;
     double bp_cutoff_energy, nl_margin;
+    float f_bp_cutoff_energy;
     float f_bond_k, f_bond_r0, f_angl_k, f_angl_t0, f_cos_t0, f_dih_k, f_dih_w, f_dih_p0;
     float f_wca_sig2, f_wca_coef, f_wca_sigma, f_wca_eps;
     unsigned long long seed;
@@ -88,6 +114,7 @@ struct BPPf {
 struct Dev {
     double4 *x[2];
     uint4 *mir[2];
+    float4 *res[2];         // mirror residuals x*S - q (units), w unused
     double4 *v, *beta, *move, *mdc, *fbp;
     int4 *binfo;
     double *mass;
@@ -103,6 +130,8 @@ struct Dev {
     void *slot;             // [n][8] bonded forces per term start (float4 or double4)
     const short *bp3_hash;  // [4097]
     const double *bp3_dH, *bp3_dS; // [469]
+    const float *bp_dgf;    // [n_inst][469] FP32 dH - T dS at each instance's
+                            // temperature; its sign equals that of the FP64 value
     const InstP *ip;
     // rebuild trigger
     unsigned long long *m1, *m2; // [n_inst] top-2 displacement^2 (bit patterns)
@@ -170,7 +199,38 @@ template <> struct Pos<float> {
     __device__ __forceinline__ V3<float> d(int a, int b, const InstP &ip) const { return dvec32(m[a], m[b], ip); }
 };
 
-__device__ __forceinline__ unsigned int fixed1(double x, double s) { return (unsigned int)(unsigned long long)llrint(x * s); }
+// mirror component q = llrint(x*S) mod 2^32 and the residual x*S - q (units
+// of 1/S, |r| <= 1/2) that the mirror drops
+__device__ __forceinline__ unsigned int fixed_res(double x, double s, float &r) {
+    const double t = x * s;
+    const double q = rint(t);
+    r = (float)(t - q);
+    return (unsigned int)(unsigned long long)(long long)q;
+}
+
+// A separation in fixed-point units: the exact mirror difference d (int32,
+// the minimum image under PBC) and the residual difference (FP32).
+struct FxV {
+    int x, y, z;
+    float rx, ry, rz;
+};
+__device__ __forceinline__ FxV fxv(const uint4 *m, const float4 *r, int i, int j) {
+    const uint4 a = m[i], b = m[j];
+    const float4 ra = r[i], rb = r[j];
+    return FxV{(int)(a.x - b.x), (int)(a.y - b.y), (int)(a.z - b.z), ra.x - rb.x, ra.y - rb.y, ra.z - rb.z};
+}
+// a x b in A^2: the product of the mirror differences is exact in int64 and
+// rounded once to FP32; the first-order residual terms are added in FP32
+// (the second-order term is below 1 unit^2).  Accurate to a few FP32 ulps of
+// |a x b| however nearly parallel a and b are, unlike a cross product of
+// FP32 separation vectors, which inherits their ~1e-7 relative rounding.
+__device__ __forceinline__ V3<float> cross_fx(const FxV &a, const FxV &b, const InstP &ip) {
+    const float ax = (float)a.x, ay = (float)a.y, az = (float)a.z, bx = (float)b.x, by = (float)b.y, bz = (float)b.z;
+    const float cx = (float)((long long)a.y * b.z - (long long)a.z * b.y) + ((ay * b.rz - az * b.ry) + (a.ry * bz - a.rz * by));
+    const float cy = (float)((long long)a.z * b.x - (long long)a.x * b.z) + ((az * b.rx - ax * b.rz) + (a.rz * bx - a.rx * bz));
+    const float cz = (float)((long long)a.x * b.y - (long long)a.y * b.x) + ((ax * b.ry - ay * b.rx) + (a.rx * by - a.ry * bx));
+    return mk<float>(cx * (ip.finv[1] * ip.finv[2]), cy * (ip.finv[2] * ip.finv[0]), cz * (ip.finv[0] * ip.finv[1]));
+}
 
 // -------------------------------------------------------- bead information
 __device__ __forceinline__ int bi_inst(const int4 &b) { return b.x; }

@@ -1,16 +1,19 @@
 // Step, force, base-pair and energy kernels of libsisgpu.
 //
-// One MD step (job_md.F90:360-460) is two kernels:
-//   k_bp    base-pair 6-bead terms over the candidate list (force_bp*.F90),
-//           scattered into fbp with FP64 atomics (few records pass the
-//           distance test, so the scatter is cheap);
+// One MD step (job_md.F90:360-460) is two kernels plus the list check:
+//   k_pre   bonded terms, one thread per term start bead, written to per-term
+//           force slots (no atomics); and the base-pair 6-bead terms over the
+//           candidate list (force_bp*.F90), compacted per warp to the records
+//           inside the distance window and scattered into fbp (FP64 atomics
+//           in the FP64 path, exact int64 fixed-point atomics in the mixed
+//           path);
 //   k_step  one group of G lanes per bead: gathers the WCA and Debye-Hueckel
-//           pair forces over the bead's full pair list and the bonded terms
+//           pair forces over the bead's full pair list and the bonded slots
 //           touching the bead, adds fbp, and applies the GJF-2GJ (or
-//           Ermak-McCammon) update in FP64; its last block evaluates the
-//           displacement trigger of every instance (job_md.F90:376-395).
-// The list rebuild (k_rebuild in lists.cu) follows and exits at once when no
-// instance asked for one.
+//           Ermak-McCammon) update in FP64; per-block partials of the
+//           displacement trigger (job_md.F90:376-395) are merged by k_trigger.
+// The list rebuild (lists.cu) follows and exits at once when no instance
+// asked for one.
 #include "common.cuh"
 #include "kernels.h"
 #include "terms.cuh"
@@ -174,7 +177,8 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
     }
     if (pass && (g.bp_model == 4 || g.bp_model == 5)) {
         const int h = rec.z >> 8;
-        pass = D.bp3_dH[h] - ip.tempK * D.bp3_dS[h] < 0.0;
+        if constexpr (sizeof(R) == 4) pass = D.bp_dgf[rec.w * 469 + h] < 0.f;
+        else pass = __dsub_rn(D.bp3_dH[h], __dmul_rn(ip.tempK, D.bp3_dS[h])) < 0.0;
     }
     if (!pass) {
         D.ene_bp[slot] = 0.0;
@@ -185,10 +189,17 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
 
 // force_bp.F90:44-204 / force_bp_triplet.F90:62-240 for one record that
 // passed bp_test: forces scattered into fbp, energy and status cached.
-// bp_finish applies the energy cut and the scatter; in the FP32 path,
+// bp_finish applies the energy cut and the scatter.  In the mixed path,
 // contributions with exp(-u) < 2e-9 (u > 20) are not scattered (their forces
 // are below the FP32 rounding of the remaining terms) but their energy is
-// still cached.
+// still cached, and forces go to fbp as fixed point.
+__device__ __forceinline__ void fx_scatter(const Dev &D, int i, long long fx, long long fy, long long fz) {
+    unsigned long long *p = reinterpret_cast<unsigned long long *>(D.fbp + i);
+    atomicAdd(p + 0, (unsigned long long)fx);
+    atomicAdd(p + 1, (unsigned long long)fy);
+    atomicAdd(p + 2, (unsigned long long)fz);
+}
+
 __device__ __forceinline__ void bp_finish(const Dev &D, const GlobP &g, int slot, const int4 &rec, const int4 &nb, double dG,
                                           const V3<double> *fd, double ud, bool ok, bool scatter_all) {
     const int type = rec.z & 0xff;
@@ -205,9 +216,18 @@ __device__ __forceinline__ void bp_finish(const Dev &D, const GlobP &g, int slot
                 const int ids[6] = {rec.x, rec.y, nb.x, nb.y, nb.z, nb.w};
 #pragma unroll
                 for (int q = 0; q < 6; ++q) {
-                    atomicAdd(&D.fbp[ids[q]].x, e * fd[q].x);
-                    atomicAdd(&D.fbp[ids[q]].y, e * fd[q].y);
-                    atomicAdd(&D.fbp[ids[q]].z, e * fd[q].z);
+                    if (g.prec == 0) {
+                        atomicAdd(&D.fbp[ids[q]].x, e * fd[q].x);
+                        atomicAdd(&D.fbp[ids[q]].y, e * fd[q].y);
+                        atomicAdd(&D.fbp[ids[q]].z, e * fd[q].z);
+                    } else {
+                        const V3<double> c = e * fd[q];
+                        if (!(fabs(c.x) < FX_LIMIT && fabs(c.y) < FX_LIMIT && fabs(c.z) < FX_LIMIT)) {
+                            atomicOr(D.err, ERR_NONFINITE);
+                            continue;
+                        }
+                        fx_scatter(D, ids[q], fx_of(c.x), fx_of(c.y), fx_of(c.z));
+                    }
                 }
             }
         }
@@ -219,7 +239,7 @@ __device__ __forceinline__ void bp_finish(const Dev &D, const GlobP &g, int slot
 __device__ __forceinline__ double bp_dG(const Dev &D, const GlobP &g, const int4 &rec) {
     if (!(g.bp_model == 4 || g.bp_model == 5)) return 1.0;
     const int h = rec.z >> 8;
-    return D.bp3_dH[h] - D.ip[rec.w].tempK * D.bp3_dS[h];
+    return __dsub_rn(D.bp3_dH[h], __dmul_rn(D.ip[rec.w].tempK, D.bp3_dS[h]));
 }
 
 // FP64 evaluation (FP64 path, and records flagged near +-1 by the FP32 path)
@@ -237,8 +257,11 @@ __device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, in
     bp_finish(D, g, slot, rec, nb, bp_dG(D, g, rec), fd, ud, ok, g.prec == 0);
 }
 
-// FP32 evaluation; returns true (and writes nothing) when an angle cosine is
-// within 1 - NEAR_ONE of +-1, so that the caller queues the record for FP64
+// FP32 evaluation.  A record with a bond angle within 0.03 rad of 0 or 180
+// degrees is evaluated again with its four cross products from the exact
+// mirror differences and residuals (cross_fx); only if an angle is within
+// 1e-6 rad does it return true (writing nothing), so that the caller redoes
+// the record in FP64.
 __device__ __noinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, int slot) {
     const uint4 *__restrict__ m = D.mir[cur];
     const int4 rec = D.bps[slot];
@@ -248,28 +271,51 @@ __device__ __noinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, in
     float u;
     bool nr = false;
     const BPPf &bf = D.bppf[rec.z & 0xff];
-    const bool ok = bp_force_core<float, BPPf>(dvec32(m[rec.x], m[rec.y], ip), dvec32(m[rec.x], m[nb.x], ip),
-                                               dvec32(m[rec.x], m[nb.z], ip), dvec32(m[nb.y], m[rec.y], ip),
-                                               dvec32(m[nb.w], m[rec.y], ip), bf, f, &u, &nr);
-    if (ok && nr) return true;
-    const bool triplet = g.bp_model == 4 || g.bp_model == 5;
-    if (!ok || u > 20.f) {
-        // no force worth scattering: cache the energy without FP64 work
-        float e = 0.f;
-        unsigned char st = 0;
-        if (ok) {
-            e = triplet ? bf.U0 * (float)bp_dG(D, g, rec) * __expf(-u) : bf.U0 * __expf(-u);
-            st = e <= (float)g.bp_cutoff_energy;
-            if (!st) e = 0.f;
-        }
-        D.ene_bp[slot] = (double)e;
-        D.bp_status[slot] = st;
-        return false;
+    const V3<float> v12 = dvec32(m[rec.x], m[rec.y], ip), v13 = dvec32(m[rec.x], m[nb.x], ip),
+                    v15 = dvec32(m[rec.x], m[nb.z], ip), v42 = dvec32(m[nb.y], m[rec.y], ip),
+                    v62 = dvec32(m[nb.w], m[rec.y], ip);
+    bool ok = bp_force_core_f(v12, v13, v15, v42, v62, bf, nullptr, f, &u, &nr);
+    if (ok && nr) {
+        const float4 *r = D.res[cur];
+        const FxV a12 = fxv(m, r, rec.x, rec.y);
+        const V3<float> cc[4] = {cross_fx(a12, fxv(m, r, rec.x, nb.x), ip), cross_fx(a12, fxv(m, r, rec.x, nb.z), ip),
+                                 cross_fx(fxv(m, r, nb.y, rec.y), a12, ip), cross_fx(fxv(m, r, nb.w, rec.y), a12, ip)};
+        ok = bp_force_core_f(v12, v13, v15, v42, v62, bf, cc, f, &u, &nr);
     }
-    V3<double> fd[6];
-    for (int q = 0; q < 6; ++q) fd[q] = mk<double>((double)f[q].x, (double)f[q].y, (double)f[q].z);
-    bp_finish(D, g, slot, rec, nb, bp_dG(D, g, rec), fd, (double)u, ok, false);
+    if (ok && nr) return true;
+    float e = 0.f;
+    unsigned char st = 0;
+    if (ok) {
+        const bool triplet = g.bp_model == 4 || g.bp_model == 5;
+        const float ex = expf(-u);
+        e = triplet ? bf.U0 * D.bp_dgf[rec.w * 469 + (rec.z >> 8)] * ex : bf.U0 * ex;
+        st = e <= g.f_bp_cutoff_energy;
+        if (!st) {
+            e = 0.f;
+        } else if (u <= 20.f) {
+            const int ids[6] = {rec.x, rec.y, nb.x, nb.y, nb.z, nb.w};
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float cx = e * f[q].x, cy = e * f[q].y, cz = e * f[q].z;
+                if (!(fabsf(cx) < FX_LIMIT && fabsf(cy) < FX_LIMIT && fabsf(cz) < FX_LIMIT)) {
+                    atomicOr(D.err, ERR_NONFINITE);
+                    continue;
+                }
+                fx_scatter(D, ids[q], fx_of(cx), fx_of(cy), fx_of(cz));
+            }
+        }
+    }
+    D.ene_bp[slot] = (double)e;
+    D.bp_status[slot] = st;
     return false;
+}
+
+template <typename R> __device__ __forceinline__ void bp_eval(const Dev &D, const GlobP &g, int cur, int slot) {
+    if constexpr (sizeof(R) == 4) {
+        if (bp_eval_f(D, g, cur, slot)) bp_eval_d(D, g, cur, slot);
+    } else {
+        bp_eval_d(D, g, cur, slot);
+    }
 }
 
 template <typename R>
@@ -297,57 +343,38 @@ __global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_
         return;
     }
     if (!do_bp) return;
-    // Base-pair records: each warp tests 32 records at a time and queues the
-    // ones inside the distance window (q); full warps of queued records are
-    // evaluated together, so the 6-bead term runs without divergence.  In
-    // the FP32 path, records with an angle cosine near +-1 go to a second
-    // queue (nq) that is evaluated in FP64, again by whole warps.
-    __shared__ int q[8][64], nq[8][64];
+    // Base-pair records: the block tests 256 records at a time and appends the
+    // ones inside the distance window to a shared queue; whenever the queue
+    // holds 256, every thread evaluates one, so the 6-bead term runs on full
+    // warps (about one candidate in ten passes the window, too few to fill a
+    // warp from a single test round).  In the FP32 path, a record with a bond
+    // angle within 0.03 rad of 0 or 180 degrees (~0.3%) is redone in FP64 at once.
+    __shared__ int q[512];
+    __shared__ int qn_s;
+    if (threadIdx.x == 0) qn_s = 0;
+    __syncthreads();
     const int total = *D.bp_total;
-    const int nwarps = (gridDim.x - nbond_blocks) * 8;
-    int qn = 0, nn = 0;
-    for (int base = ((blockIdx.x - nbond_blocks) * 8 + warp) * 32; base < total; base += nwarps * 32) {
-        const int r = base + lane;
+    const int nbp = gridDim.x - nbond_blocks;
+    for (int base = ((int)blockIdx.x - nbond_blocks) * 256; base < total; base += nbp * 256) {
         int slot = -1;
         bool pass = false;
-        if (bp_record(D, r, total, g.n_inst, slot)) pass = bp_test<R>(D, g, cur, slot);
+        if (bp_record(D, base + (int)threadIdx.x, total, g.n_inst, slot)) pass = bp_test<R>(D, g, cur, slot);
         const unsigned bal = __ballot_sync(0xffffffffu, pass);
-        if (pass) q[warp][qn + __popc(bal & ((1u << lane) - 1u))] = slot;
-        qn += __popc(bal);
-        __syncwarp();
-        if (qn >= 32) {
-            const int sl = q[warp][lane];
-            bool near = false;
-            if constexpr (sizeof(R) == 4) near = bp_eval_f(D, g, cur, sl);
-            else bp_eval_d(D, g, cur, sl);
-            __syncwarp();
-            if (lane < qn - 32) q[warp][lane] = q[warp][lane + 32];
-            qn -= 32;
-            const unsigned nb = __ballot_sync(0xffffffffu, near);
-            if (near) nq[warp][nn + __popc(nb & ((1u << lane) - 1u))] = sl;
-            nn += __popc(nb);
-            __syncwarp();
-            if (nn >= 32) {
-                bp_eval_d(D, g, cur, nq[warp][lane]);
-                __syncwarp();
-                if (lane < nn - 32) nq[warp][lane] = nq[warp][lane + 32];
-                nn -= 32;
-                __syncwarp();
-            }
+        int wb = 0;
+        if (lane == 0 && bal) wb = atomicAdd(&qn_s, __popc(bal));
+        wb = __shfl_sync(0xffffffffu, wb, 0);
+        if (pass) q[wb + __popc(bal & ((1u << lane) - 1u))] = slot;
+        __syncthreads();
+        const int qn = qn_s;
+        if (qn >= 256) {
+            bp_eval<R>(D, g, cur, q[threadIdx.x]);
+            __syncthreads();
+            if ((int)threadIdx.x < qn - 256) q[threadIdx.x] = q[threadIdx.x + 256];
+            if (threadIdx.x == 0) qn_s = qn - 256;
         }
+        __syncthreads();
     }
-    bool near = false;
-    int sl = -1;
-    if (lane < qn) {
-        sl = q[warp][lane];
-        if constexpr (sizeof(R) == 4) near = bp_eval_f(D, g, cur, sl);
-        else bp_eval_d(D, g, cur, sl);
-    }
-    const unsigned nb = __ballot_sync(0xffffffffu, near);
-    if (near) nq[warp][nn + __popc(nb & ((1u << lane) - 1u))] = sl;
-    nn += __popc(nb);
-    __syncwarp();
-    for (int k = lane; k < nn; k += 32) bp_eval_d(D, g, cur, nq[warp][k]);
+    if ((int)threadIdx.x < qn_s) bp_eval<R>(D, g, cur, q[threadIdx.x]);
 }
 
 // energy_bp.F90 / energy_bp_triplet.F90 for every record at temperature tK
@@ -370,7 +397,7 @@ __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, doub
         if (triplet) {
             double tK = tK_in < 0 ? ip.tempK : tK_in;
             if (g.temp_indep) tK = 0.0;
-            dG = D.bp3_dH[h] - tK * D.bp3_dS[h];
+            dG = __dsub_rn(D.bp3_dH[h], __dmul_rn(tK, D.bp3_dS[h]));
             skip = dG >= 0.0;
         }
         const V3<double> v = dvec64(x64[i1], x64[i2], ip);
@@ -570,8 +597,10 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
         float sc = 1.f;
         if (MODE == 0 && g.fcap > 0.0) {
             const double4 fb = D.fbp[i];
-            const float fx = (float)(an.x + ab.x) + (float)fb.x, fy = (float)(an.y + ab.y) + (float)fb.y,
-                        fz = (float)(an.z + ab.z) + (float)fb.z;
+            const float bx = sizeof(R) == 4 ? (float)fx_value(fb.x) : (float)fb.x;
+            const float by = sizeof(R) == 4 ? (float)fx_value(fb.y) : (float)fb.y;
+            const float bz = sizeof(R) == 4 ? (float)fx_value(fb.z) : (float)fb.z;
+            const float fx = (float)(an.x + ab.x) + bx, fy = (float)(an.y + ab.y) + by, fz = (float)(an.z + ab.z) + bz;
             const float fm = sqrtf(fx * fx + fy * fy + fz * fz);
             if (fm > (float)g.fcap) {
                 sc = (float)g.fcap / fm;
@@ -592,6 +621,7 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
         if (mask & 8) {
             fb = D.fbp[ii];
             D.fbp[ii] = make_double4(0.0, 0.0, 0.0, 0.0);
+            if constexpr (sizeof(R) == 4) fb = make_double4(fx_value(fb.x), fx_value(fb.y), fx_value(fb.z), 0.0);
         }
         F[0] = (double)sA[0][bb] + (double)sB[0][bb] + fb.x;
         F[1] = (double)sA[1][bb] + (double)sB[1][bb] + fb.y;
@@ -617,6 +647,7 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
         const double xc[3] = {x0.x, x0.y, x0.z};
         double vc[3] = {v.x, v.y, v.z}, bc[3] = {be.x, be.y, be.z}, mc[3] = {mv.x, mv.y, mv.z}, xn[3];
         unsigned int mirn[3];
+        float resn[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const double Fc = F[c] * sc;
@@ -634,7 +665,7 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
             if (!isfinite(xn[c])) atomicOr(D.err, ERR_NONFINITE);
             mc[c] = mc[c] + dx;
             sM[c][bb] = mc[c];
-            mirn[c] = fixed1(xn[c], jp.fsc[c]);
+            mirn[c] = fixed_res(xn[c], jp.fsc[c], resn[c]);
         }
         D.x[cur ^ 1][ii] = make_double4(xn[0], xn[1], xn[2], 0.0);
         if (g.integrator == 1) {
@@ -643,6 +674,7 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
         }
         D.move[ii] = make_double4(mc[0], mc[1], mc[2], 0.0);
         D.mir[cur ^ 1][ii] = make_uint4(mirn[0], mirn[1], mirn[2], 0u);
+        D.res[cur ^ 1][ii] = make_float4(resn[0], resn[1], resn[2], 0.f);
     }
     if (MODE == 1) return;
     __syncthreads();
@@ -829,7 +861,9 @@ __global__ void k_mirror(Dev D, GlobP g, int cur) {
     if (i >= g.n) return;
     const InstP &ip = D.ip[D.binfo[i].x];
     const double4 x = D.x[cur][i];
-    D.mir[cur][i] = make_uint4(fixed1(x.x, ip.fsc[0]), fixed1(x.y, ip.fsc[1]), fixed1(x.z, ip.fsc[2]), 0u);
+    float r[3];
+    D.mir[cur][i] = make_uint4(fixed_res(x.x, ip.fsc[0], r[0]), fixed_res(x.y, ip.fsc[1], r[1]), fixed_res(x.z, ip.fsc[2], r[2]), 0u);
+    D.res[cur][i] = make_float4(r[0], r[1], r[2], 0.f);
 }
 
 // ------------------------------------------------------------- launchers

@@ -387,7 +387,8 @@ __device__ __forceinline__ void pair_energy(int e, R d2, const InstP &ip, const 
 // 1 imp, 2 jmp, 3 imp-1, 4 jmp-1, 5 imp+1, 6 jmp+1).  Returns false if the
 // pair is outside cutoff_ddist.  f[6] receives dU-weighted forces before the
 // final multiplication by the energy (as f_bp in the reference); *u_out the
-// exponent u; *near is set when an angle cosine is within 1 - NEAR_ONE of +-1.
+// exponent u; *near is set when an angle cosine is within 1 - NEAR_ONE of +-1
+// (FP64 form; the FP32 specialization below uses its own, far tighter, test).
 template <typename T, typename P>
 __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v15, const V3<T> &v42, const V3<T> &v62,
                               const P &b, V3<T> f[6], T *u_out, bool *near) {
@@ -473,6 +474,109 @@ __device__ bool bp_force_core(const V3<T> &v12, const V3<T> &v13, const V3<T> &v
     f[1] = f[1] + ((T)-1 + o62) * fi - o15 * fl;
     f[0] = f[0] + ((T)-1 + o15) * fl - o62 * fi;
     f[4] = f[4] + fl;
+    *u_out = u;
+    return true;
+}
+
+// FP32 form of the same term, free of the cancellation that the acos and
+// sqrt(|a|^2 |b|^2 - (a.b)^2) forms suffer near 0 and 180 degrees: each angle
+// is atan2(|a x b|, a.b) (Lagrange's identity makes |a x b| the reference's
+// square root), and each perpendicular vector a - (a.b / |b|^2) b is formed
+// as b x (a x b) / |b|^2 (the vector triple product), which cancels nothing.
+// The four cross products v12 x v13, v12 x v15, v42 x v12 and v62 x v12 are
+// also the m and n vectors of the two dihedrals, and they alone carry the
+// conditioning of the term: both force directions are set by the offsets
+// |a| sin(theta).  Without cc they are formed from the FP32 separations,
+// whose ~1e-6 A rounding is then amplified by 1/sin(theta), and *near is set
+// (nothing else computed) when a bond angle is within 0.03 rad of 0 or 180
+// degrees; with cc (cross products from cross_fx, accurate to FP32 ulps)
+// only within 1e-6 rad, where the force direction itself is ill-defined.
+__device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<float> &v13, const V3<float> &v15,
+                                                const V3<float> &v42, const V3<float> &v62, const BPPf &b,
+                                                const V3<float> *cc, V3<float> f[6], float *u_out, bool *near) {
+    const float d1212 = dot3(v12, v12);
+    const float a12 = sqrtf(d1212);
+    float d = a12 - b.bond_r;
+    if (fabsf(d) > b.cutoff_ddist) return false;
+    const float d1313 = dot3(v13, v13), d4242 = dot3(v42, v42), d1515 = dot3(v15, v15), d6262 = dot3(v62, v62);
+    const V3<float> c13 = cc ? cc[0] : cross_acc(v12, v13), c15 = cc ? cc[1] : cross_acc(v12, v15);
+    const V3<float> m42 = cc ? cc[2] : cross_acc(v42, v12), m62 = cc ? cc[3] : cross_acc(v62, v12);
+    const float s13 = dot3(c13, c13), s15 = dot3(c15, c15), s42 = dot3(m42, m42), s62 = dot3(m62, m62);
+    const float kSin2 = cc ? 1e-12f : 9e-4f;
+    *near = s13 < kSin2 * d1212 * d1313 || s15 < kSin2 * d1212 * d1515 || s42 < kSin2 * d1212 * d4242 ||
+            s62 < kSin2 * d1212 * d6262;
+    if (*near) return true;
+    const float d1213 = dot3(v12, v13), d1242 = dot3(v12, v42), d1215 = dot3(v12, v15), d1262 = dot3(v12, v62);
+    const float o13 = d1213 / d1212, o42 = d1242 / d1212, o15 = d1215 / d1212, o62 = d1262 / d1212;
+    float u = b.bond_k * (d * d);
+    const V3<float> fb = (2.f * b.bond_k * d / a12) * v12;
+    V3<float> f0 = fb, f1 = -fb, fi, fk, fl;
+    float r, pre;
+    // 3-1=2 (imp-1 -- imp -- jmp)
+    r = sqrtf(s13);
+    d = atan2f(r, d1213) - b.angl_theta[1];
+    u += b.angl_k[1] * (d * d);
+    pre = 2.f * b.angl_k[1] * d / r;
+    fi = (pre / d1313) * cross3(v13, c13);
+    fk = (pre / d1212) * cross3(c13, v12);
+    f0 = f0 - fi - fk;
+    f1 = f1 + fk;
+    f[2] = fi;
+    // 1=2-4 (imp -- jmp -- jmp-1)
+    r = sqrtf(s42);
+    d = atan2f(r, d1242) - b.angl_theta[0];
+    u += b.angl_k[0] * (d * d);
+    pre = 2.f * b.angl_k[0] * d / r;
+    fi = (-pre / d1212) * cross3(v12, m42);
+    fk = (-pre / d4242) * cross3(m42, v42);
+    f0 = f0 + fi;
+    f1 = f1 - fi - fk;
+    f[3] = fk;
+    // 5-1=2 (imp+1 -- imp -- jmp)
+    r = sqrtf(s15);
+    d = atan2f(r, d1215) - b.angl_theta[3];
+    u += b.angl_k[3] * (d * d);
+    pre = 2.f * b.angl_k[3] * d / r;
+    fi = (pre / d1515) * cross3(v15, c15);
+    fk = (pre / d1212) * cross3(c15, v12);
+    f0 = f0 - fi - fk;
+    f1 = f1 + fk;
+    f[4] = fi;
+    // 1=2-6 (imp -- jmp -- jmp+1)
+    r = sqrtf(s62);
+    d = atan2f(r, d1262) - b.angl_theta[2];
+    u += b.angl_k[2] * (d * d);
+    pre = 2.f * b.angl_k[2] * d / r;
+    fi = (-pre / d1212) * cross3(v12, m62);
+    fk = (-pre / d6262) * cross3(m62, v62);
+    f0 = f0 + fi;
+    f1 = f1 - fi - fk;
+    f[5] = fk;
+    // dihedral 4-2=1=3: m = v42 x v12, n = v12 x v13
+    float sn, cs;
+    d = atan2f(dot3(v42, c13) * a12, dot3(m42, c13)) + b.dihd_phi[0];
+    sincosf(d, &sn, &cs);
+    u += b.dihd_k[0] * (1.f + cs);
+    pre = -b.dihd_k[0] * sn * a12;
+    fi = (pre / s42) * m42;
+    fl = (-pre / s13) * c13;
+    f[3] = f[3] + fi;
+    f1 = f1 + (o42 - 1.f) * fi - o13 * fl;
+    f0 = f0 + (o13 - 1.f) * fl - o42 * fi;
+    f[2] = f[2] + fl;
+    // dihedral 6-2=1=5: m = v62 x v12, n = v12 x v15
+    d = atan2f(dot3(v62, c15) * a12, dot3(m62, c15)) + b.dihd_phi[1];
+    sincosf(d, &sn, &cs);
+    u += b.dihd_k[1] * (1.f + cs);
+    pre = -b.dihd_k[1] * sn * a12;
+    fi = (pre / s62) * m62;
+    fl = (-pre / s15) * c15;
+    f[5] = f[5] + fi;
+    f1 = f1 + (o62 - 1.f) * fi - o15 * fl;
+    f0 = f0 + (o15 - 1.f) * fl - o62 * fi;
+    f[4] = f[4] + fl;
+    f[0] = f0;
+    f[1] = f1;
     *u_out = u;
     return true;
 }

@@ -34,6 +34,23 @@ def compact_system(ff):
     return System(ff, Options(bp_model=1), [inst])
 
 
+def near_collinear_bp_system(ff, sin_theta):
+    """One G-C base-pair record (strands GGG / CCC, middle beads paired) whose
+    flanking bond angle imp+1 -- imp -- jmp has sine sin_theta (nearly 0 deg);
+    the other three flanking angles sit near their minima."""
+    u12 = np.array([-1.0, 0.0, 0.0])
+
+    def arm(theta, e):
+        e = np.asarray(e, float) / np.linalg.norm(e)
+        return 5.84 * (np.cos(theta) * u12 + np.sin(theta) * e)
+
+    x1, x2 = np.zeros(3), np.array([13.8, 0.0, 0.0])
+    xyz = np.stack([x1 - arm(1.83, [0, 0.6, 0.8]), x1, x1 - arm(np.arcsin(sin_theta), [0, 1, 0.3]),
+                    x2 + arm(1.83, [0, -0.8, 0.6]), x2, x2 + arm(0.94, [0, 0.28, -0.96])])
+    inst = Instance([Chain.from_string("GGG"), Chain.from_string("CCC")], tempK=300.0, ionic_strength=0.15, xyz=xyz)
+    return System(ff, Options(bp_model=1), [inst])
+
+
 def circ_system(ff):
     rng = np.random.default_rng(9)
     seq = rng.integers(0, 4, 48).astype(np.int32)
@@ -135,6 +152,26 @@ def test_mixed_precision_force_error(name, systems):
     eng.invalidate_bp_cache()
     e = eng.energy_sumup(0)
     assert abs(e[0] - eref[0]) <= 1e-5 * np.abs(eref[1:7]).sum()
+
+
+@pytest.mark.parametrize("sin_theta", [0.1, 0.031, 0.029, 1e-3, 3e-5])
+def test_base_pair_near_collinear_angle(sin_theta, sis_ff):
+    """sin >= 0.03: the FP32 base-pair term (atan2 angles, compensated cross
+    products of FP32 separations) keeps the 1e-5 bar where acos would not;
+    below, the mixed path recomputes the four cross products exactly from the
+    fixed-point mirror and its residuals.  The reference's angle forces divide
+    by sqrt(|a|^2 |b|^2 - (a.b)^2), whose rounding error grows as
+    eps / sin^2: FP64 results that round differently (FMA contraction) agree
+    with the oracle to that bound, not to 1e-12, at the smallest angles."""
+    sysm = near_collinear_bp_system(sis_ff, sin_theta)
+    orc = oracle_for(sysm)
+    ref = orc.force_term(0, 4)
+    assert len(orc.get_list(0, 2)) == 1 and np.abs(ref).max() > 1e-3
+    tol64 = max(FORCE_TOL_FP64, 2.2e-16 / sin_theta ** 2)
+    for prec, tol in ((FP64, tol64), (MIXED, FORCE_RMS_TOL_MIXED)):
+        eng = Engine(sysm, precision=prec)
+        got = eng.force_term(0, 4)
+        assert max_rel(got, ref) < tol, (prec, max_rel(got, ref))
 
 
 def test_batched_instances_match_their_own_oracles(sis_ff):
