@@ -39,7 +39,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "bead·steps/s batched-FP32 vs plain-FP64 on 1 GB300 at stated force err; p99 job ms"
 UNIT = "bead*steps/s"
 WORKLOADS = {
-    "crowded": "200 chains x 500 nt (100,000 beads), cubic PBC box at 10 mM nucleotide, 150 mM salt, 300 K",
+    "crowded": "200 chains x 500 nt (100,000 beads), cubic PBC box at 10 mM nucleotide, 150 mM salt, 300 K; "
+               "random-coil start with non-bonded pairs >= 10 A apart",
     "uneven": "256 independent chains, lengths U[20,500], salt U[20,500] mM, T U[280,340] K",
     "remd": "64 replicas x 120 nt, T geometric 280-360 K",
     "chain64": "one 64-nt chain, 300 K, 150 mM, no PBC",
@@ -260,41 +261,61 @@ def run_gpu(args):
     return out, rank
 
 
-def cpu_baseline(args, sysm, eng=None, sample_steps=None):
+class CpuSampler:
     """The FP64 oracle (C++ restatement of the reference, OpenMP over all host
-    threads) on a bounded sample of the same workload."""
-    from oracle.oracle import Oracle
+    threads) on up to 8 instances of the workload.  Its lists are built once
+    (untimed); each sample then runs MD until the displacement trigger has
+    rebuilt the lists once, so the reference's O(N^2) rebuild enters at its
+    natural rate: one rebuild per rebuild interval."""
 
-    cores = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    N = sysm.nmp
-    # about 20 s of CPU work: scale the step count to the system size
-    if sample_steps is None:
-        sample_steps = max(2, int(2e7 / max(N, 1) / 4))
-        sample_steps = min(sample_steps, 200)
-    x = None
-    if eng is not None:
-        x, v, a = eng.get_state(-1)
-    t_total, beads_steps = 0.0, 0
-    insts = range(len(sysm.instances))
-    if len(sysm.instances) > 8:
-        insts = range(0, len(sysm.instances), max(1, len(sysm.instances) // 8))
-    off = sysm.offsets()
-    for k in insts:
-        o = Oracle.from_instance(sysm, k)
-        if x is not None:
-            o.set_xyz(0, x[off[k]:off[k + 1]])
-            o.set_velos(0, v[off[k]:off[k + 1]])
-            o.set_accels(0, a[off[k]:off[k + 1]])
-        o.seed(1234 + k)
-        o.md_init()
-        t0 = time.perf_counter()
-        o.run(sample_steps)
-        t_total += time.perf_counter() - t0
-        beads_steps += o.nmp * sample_steps
-    return {"value": beads_steps / t_total, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{sample_steps} MD steps of {len(list(insts))} instance(s) ({beads_steps // sample_steps} beads) after "
-                      f"the initial list build; FP64 C++ restatement of the reference with OpenMP"}
+    def __init__(self, sysm, eng=None, seed=1234):
+        from oracle.oracle import Oracle
+
+        self.cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(self.cores))
+        n_inst = len(sysm.instances)
+        insts = range(0, n_inst, max(1, n_inst // 8)) if n_inst > 8 else range(n_inst)
+        off = sysm.offsets()
+        state = eng.get_state(-1) if eng is not None else None
+        self.oracles = []
+        for k in insts:
+            o = Oracle.from_instance(sysm, k)
+            if state is not None:
+                x, v, a = state
+                o.set_xyz(0, x[off[k]:off[k + 1]])
+                o.set_velos(0, v[off[k]:off[k + 1]])
+                o.set_accels(0, a[off[k]:off[k + 1]])
+            o.seed(seed + k)
+            o.md_init()
+            self.oracles.append(o)
+        self.start = "relaxed GPU state" if state is not None else "the workload's start"
+
+    def sample(self, max_seconds=30.0, max_steps=4000, chunk=10):
+        """Per instance: steps in chunks until a rebuild happened (or the caps)."""
+        bead_steps, secs, steps, rebuilds = 0, 0.0, 0, 0
+        for o in self.oracles:
+            t0 = time.perf_counter()
+            s = r = 0
+            while r == 0 and s < max_steps and time.perf_counter() - t0 < max_seconds:
+                r += o.run(chunk)
+                s += chunk
+            secs += time.perf_counter() - t0
+            bead_steps += o.nmp * s
+            steps += s
+            rebuilds += r
+        return bead_steps, secs, steps, rebuilds
+
+    def describe(self, steps, rebuilds):
+        n = sum(o.nmp for o in self.oracles)
+        return (f"{steps} MD steps over {len(self.oracles)} instance(s) ({n} beads) from {self.start}, each run until the "
+                f"displacement trigger rebuilt its lists ({rebuilds} O(N^2) rebuilds timed); FP64 C++ restatement of the "
+                f"reference with OpenMP")
+
+
+def cpu_baseline(args, sysm, eng=None):
+    smp = CpuSampler(sysm, eng)
+    bs, secs, steps, reb = smp.sample()
+    return {"value": bs / secs, "unit": UNIT, "cores": smp.cores, "kind": "port", "sample": smp.describe(steps, reb)}
 
 
 def run_reference(args):
@@ -302,17 +323,20 @@ def run_reference(args):
     if rank != 0:
         return None, rank
     sysm = make_system(args.workload)
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(args, sysm, sample_steps=2)
+    smp = CpuSampler(sysm)
+    # warm-up: the first sample leaves the start's transient and ends right
+    # after a rebuild, so every timed sample spans one rebuild interval
+    for w in range(args.warmup):
+        smp.sample() if w == 0 else smp.sample(max_steps=2)
+    tot_bs, tot_s, tot_steps, tot_reb = 0, 0.0, 0, 0
     for _ in range(args.steps):
-        vals.append(cpu_baseline(args, sysm, sample_steps=max(2, args.ref_sample)))
-    value = statistics.median(v["value"] for v in vals)
-    cb = dict(vals[-1])
-    cb["value"] = value
+        bs, secs, steps, reb = smp.sample()
+        tot_bs, tot_s, tot_steps, tot_reb = tot_bs + bs, tot_s + secs, tot_steps + steps, tot_reb + reb
+    value = tot_bs / tot_s
+    cb = {"value": value, "unit": UNIT, "cores": smp.cores, "kind": "port", "sample": smp.describe(tot_steps, tot_reb)}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-           "data": "synthetic (seeded sequences and random-coil starts)", "impl": "reference",
+           "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "fp64", "data": "synthetic (seeded sequences and random-coil starts)", "impl": "reference",
            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "n_beads": sysm.nmp,
                       "note": "Fortran reference unavailable on this box (no Fortran compiler, toml-f not vendored); "
                               "timed arm is the FP64 C++ restatement of its algorithms"},
@@ -329,7 +353,6 @@ def main():
     ap.add_argument("--workload", default="crowded", choices=list(WORKLOADS))
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--relax", type=int, default=3000)
-    ap.add_argument("--ref-sample", type=int, default=10)
     ap.add_argument("--force-cap", type=float, default=1000.0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

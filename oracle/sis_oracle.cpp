@@ -540,7 +540,20 @@ extern "C" double or_const(int32_t w) {
 }
 
 /* ---------------------------------------------------------- neighbour list */
-/* neighbor_list.F90:1-233 */
+/* neighbor_list.F90:1-233.  The O(N^2) scan runs over rows (chain ic, chain
+ * jc >= ic, a block of 64 beads i of ic) in parallel; each row appends to its
+ * own buffers, which are joined in row order, so the lists come out in the
+ * reference's serial (ic, jc, i, j) order whatever the thread count. */
+namespace {
+struct NlRow {
+    int ic, jc, i0, i1;
+};
+struct NlOut {
+    std::vector<int> wca, ele, bp;
+    std::vector<double> coef;
+};
+} // namespace
+
 extern "C" void or_neighbor_list(or_system *s, int32_t irep) {
     Rep &R = s->rep[irep];
     const or_params &p = s->p;
@@ -556,70 +569,83 @@ extern "C" void or_neighbor_list(or_system *s, int32_t irep) {
     }
     const double wca_nl_cut2 = (p.wca_sigma + p.nl_margin) * (p.wca_sigma + p.nl_margin);
     const double bp_nl_cut2 = (s->bp_cutoff_dist + p.nl_margin) * (s->bp_cutoff_dist + p.nl_margin);
+    std::vector<NlRow> rows;
     for (int ic = 0; ic < s->nchains; ++ic)
-        for (int jc = ic; jc < s->nchains; ++jc) {
-            const int ni = s->nmp_chain[ic], nj = s->nmp_chain[jc];
-            for (int i = 1; i <= ni; ++i) {
-                const int imp = s->chain_start[ic] + i;
-                const int iseq = s->seq[imp - 1];
-                const int j_start = (ic == jc) ? i + 1 : 1;
-                for (int j = j_start; j <= nj; ++j) {
-                    const int jmp = s->chain_start[jc] + j;
-                    const int jseq = s->seq[jmp - 1];
-                    double v[3];
-                    pbc_vec_d(s, X(s, irep, imp), X(s, irep, jmp), v);
-                    const double d2 = dot(v, v);
-                    if (iseq != SD && jseq != SD && d2 <= wca_nl_cut2) {
-                        bool add = true;
-                        if (ic == jc) {
-                            if (i + 2 >= j) add = false;
-                            else if (s->moltype[ic] == MOLT_CIRC && j + 2 >= i + ni) add = false;
-                        }
-                        if (add) {
-                            R.wca_mp.push_back(imp);
-                            R.wca_mp.push_back(jmp);
-                        }
+        for (int jc = ic; jc < s->nchains; ++jc)
+            for (int i0 = 1; i0 <= s->nmp_chain[ic]; i0 += 64) rows.push_back({ic, jc, i0, std::min(i0 + 63, s->nmp_chain[ic])});
+    std::vector<NlOut> out(rows.size());
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long r = 0; r < (long)rows.size(); ++r) {
+        const int ic = rows[r].ic, jc = rows[r].jc;
+        NlOut &o = out[r];
+        const int ni = s->nmp_chain[ic], nj = s->nmp_chain[jc];
+        for (int i = rows[r].i0; i <= rows[r].i1; ++i) {
+            const int imp = s->chain_start[ic] + i;
+            const int iseq = s->seq[imp - 1];
+            const int j_start = (ic == jc) ? i + 1 : 1;
+            for (int j = j_start; j <= nj; ++j) {
+                const int jmp = s->chain_start[jc] + j;
+                const int jseq = s->seq[jmp - 1];
+                double v[3];
+                pbc_vec_d(s, X(s, irep, imp), X(s, irep, jmp), v);
+                const double d2 = dot(v, v);
+                if (iseq != SD && jseq != SD && d2 <= wca_nl_cut2) {
+                    bool add = true;
+                    if (ic == jc) {
+                        if (i + 2 >= j) add = false;
+                        else if (s->moltype[ic] == MOLT_CIRC && j + 2 >= i + ni) add = false;
                     }
-                    if (p.flg_ele && d2 <= ele_nl_cut2 && s->has_charge[imp - 1] && s->has_charge[jmp - 1]) {
-                        bool add = true;
-                        if (ic == jc) {
-                            if (j == i + 1 && p.ele_excl_bond) add = false;
-                            if (j == i + 2 && p.ele_excl_angle) add = false;
-                            if (s->moltype[ic] == MOLT_CIRC) {
-                                if (i == 1) {
-                                    if (j == ni && p.ele_excl_bond) add = false;
-                                    if (j == ni - 1 && p.ele_excl_angle) add = false;
-                                } else if (i == 2) {
-                                    if (j == ni && p.ele_excl_angle) add = false;
-                                }
+                    if (add) {
+                        o.wca.push_back(imp);
+                        o.wca.push_back(jmp);
+                    }
+                }
+                if (p.flg_ele && d2 <= ele_nl_cut2 && s->has_charge[imp - 1] && s->has_charge[jmp - 1]) {
+                    bool add = true;
+                    if (ic == jc) {
+                        if (j == i + 1 && p.ele_excl_bond) add = false;
+                        if (j == i + 2 && p.ele_excl_angle) add = false;
+                        if (s->moltype[ic] == MOLT_CIRC) {
+                            if (i == 1) {
+                                if (j == ni && p.ele_excl_bond) add = false;
+                                if (j == ni - 1 && p.ele_excl_angle) add = false;
+                            } else if (i == 2) {
+                                if (j == ni && p.ele_excl_angle) add = false;
                             }
                         }
-                        if (add) {
-                            R.ele_mp.push_back(imp);
-                            R.ele_mp.push_back(jmp);
-                        }
                     }
-                    if (d2 <= bp_nl_cut2) {
-                        int bp3;
-                        int type = bp_candidate(s, imp, jmp, &bp3);
-                        if (bp3 > 0) {
-                            int rec[7];
-                            rec[0] = imp;
-                            rec[1] = jmp;
-                            rec[2] = (i == 1) ? imp + ni - 1 : imp - 1;
-                            rec[3] = (j == 1) ? jmp + nj - 1 : jmp - 1;
-                            rec[4] = (i == ni) ? imp + 1 - ni : imp + 1;
-                            const int jend = p.bp_jnext_compat ? ni : nj; /* neighbor_list.F90:212 */
-                            rec[5] = (j == jend) ? jmp + 1 - nj : jmp + 1;
-                            rec[6] = type;
-                            R.bp_mp.insert(R.bp_mp.end(), rec, rec + 7);
-                            R.bp_coef.push_back(s->bp3_dH[bp3]);
-                            R.bp_coef.push_back(s->bp3_dS[bp3]);
-                        }
+                    if (add) {
+                        o.ele.push_back(imp);
+                        o.ele.push_back(jmp);
+                    }
+                }
+                if (d2 <= bp_nl_cut2) {
+                    int bp3;
+                    int type = bp_candidate(s, imp, jmp, &bp3);
+                    if (bp3 > 0) {
+                        int rec[7];
+                        rec[0] = imp;
+                        rec[1] = jmp;
+                        rec[2] = (i == 1) ? imp + ni - 1 : imp - 1;
+                        rec[3] = (j == 1) ? jmp + nj - 1 : jmp - 1;
+                        rec[4] = (i == ni) ? imp + 1 - ni : imp + 1;
+                        const int jend = p.bp_jnext_compat ? ni : nj; /* neighbor_list.F90:212 */
+                        rec[5] = (j == jend) ? jmp + 1 - nj : jmp + 1;
+                        rec[6] = type;
+                        o.bp.insert(o.bp.end(), rec, rec + 7);
+                        o.coef.push_back(s->bp3_dH[bp3]);
+                        o.coef.push_back(s->bp3_dS[bp3]);
                     }
                 }
             }
         }
+    }
+    for (const NlOut &o : out) {
+        R.wca_mp.insert(R.wca_mp.end(), o.wca.begin(), o.wca.end());
+        R.ele_mp.insert(R.ele_mp.end(), o.ele.begin(), o.ele.end());
+        R.bp_mp.insert(R.bp_mp.end(), o.bp.begin(), o.bp.end());
+        R.bp_coef.insert(R.bp_coef.end(), o.coef.begin(), o.coef.end());
+    }
     const size_t nbp = R.bp_mp.size() / 7;
     R.ene_bp.assign(nbp, 0.0);
     R.bp_status.assign(nbp, 0);

@@ -131,13 +131,18 @@ def single_chain(ff: ForceField, n: int = 64, seed: int = 1001, tempK: float = 3
 
 
 def crowded_box(ff: ForceField, n_chains: int = 200, n: int = 500, molar: float = 0.01, seed: int = 1002,
-                tempK: float = 300.0, salt: float = 0.15) -> System:
-    """n_chains x n nt in a cubic PBC box at `molar` nucleotide concentration."""
+                tempK: float = 300.0, salt: float = 0.15, rmin: float = 10.0) -> System:
+    """n_chains x n nt in a cubic PBC box at `molar` nucleotide concentration.
+
+    Non-bonded pairs (|i-j| >= 3 in a chain, every pair between chains) start
+    at least rmin apart.  The default is the WCA sigma (10 A), so the start
+    carries no WCA overlap and any engine can step it without a force-capped
+    relaxation; rmin = 4 gives the coil recipe's closer contacts."""
     rng = np.random.default_rng(seed)
     L = box_for_concentration(n_chains * n, molar)
     chains = [Chain(random_sequence(rng, n)) for _ in range(n_chains)]
-    coils = [random_coil(rng, n) for _ in range(n_chains)]
-    xyz = np.concatenate(place_chains(rng, coils, L))
+    coils = [random_coil(rng, n, rmin=rmin) for _ in range(n_chains)]
+    xyz = np.concatenate(place_chains(rng, coils, L, rmin=rmin))
     inst = Instance(chains, tempK=tempK, ionic_strength=salt, box=(L, L, L), xyz=xyz)
     return System(ff, sis_options(), [inst])
 
