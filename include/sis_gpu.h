@@ -219,6 +219,21 @@ int64_t sis_gpu_kernel_launches(const sis_ctx *ctx);
  * base-pair, step and rebuild kernels.  For roofline measurements. */
 int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3);
 
+/* No counterpart in the reference.  sis_gpu_step with host noise (same
+ * layout: nsteps x nmp x 3 doubles, step-major), but allocating nothing: it
+ * stages one step's noise at a time through a fixed static device buffer
+ * of 65,536 beads (1.5 MiB), where sis_gpu_step grows a per-context buffer
+ * with cudaMalloc/cudaFree when a call needs more than the last one.
+ * Callers that cannot allocate are those whose device memory is already
+ * handed out by a fixed budget (a long job that must not fail with an
+ * out-of-memory error midway), and those that must not stall other work on
+ * the device: cudaFree waits for the whole device, including other
+ * contexts' and other threads' work in flight.  Contexts of more than
+ * 65,536 beads get SIS_ERR_ARG and a message.  The first call on a device
+ * looks the buffer's address up (cudaGetSymbolAddress); the buffer is shared
+ * by all contexts on that device, so calls must not overlap in time. */
+int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const double *noise);
+
 #ifdef __cplusplus
 }
 #endif

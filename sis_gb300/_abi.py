@@ -99,6 +99,7 @@ EXPORTS = {
     "sis_gpu_flush_l2": (C.c_int, [C.c_void_p]),
     "sis_gpu_kernel_launches": (C.c_int64, [C.c_void_p]),
     "sis_gpu_step_profiled": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
+    "sis_gpu_step_noise_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
 }
 
 _lib = None

@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1074,5 +1075,66 @@ extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
     ctx->steps += nsteps;
     ctx->bp_cache = true;
     for (int k = 0; k < 3; ++k) ms3[k] = (float)acc[k];
+    return check_err(ctx);
+}
+
+// ============================================ allocation-free fed-noise step
+// sis_gpu_step_noise_static: sis_gpu_step with host noise, staged one step at
+// a time through a fixed static device buffer instead of the context's noise
+// buffer (which sis_gpu_step grows with cudaMalloc/cudaFree at call time).
+// Nothing in the buffer has to start at zero: each step's copy overwrites all
+// 3n doubles that step's kernel reads.  The buffer is one per device and
+// shared by every context on it, so calls that overlap in time on one device
+// race on it; callers serialise them.
+constexpr int kStaticNoiseBeads = 65536; // 3 x 65536 doubles = 1.5 MiB
+static __device__ __align__(256) double g_noise_scratch[3 * kStaticNoiseBeads];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noise_mu;
+double *g_noise_addr[kMaxDevices] = {};
+
+// Address of g_noise_scratch on the current device, looked up once per
+// device with that device current (the first call on a device does this
+// set-up; a caller that captures its stream should make that first call
+// before it starts capturing).
+int noise_scratch(sis_ctx *ctx, double **out) {
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(ctx, SIS_ERR_ARG, "sis_gpu_step_noise_static: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noise_mu);
+    if (!g_noise_addr[dev]) {
+        void *p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noise_scratch));
+        g_noise_addr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noise_addr[dev];
+    return SIS_OK;
+}
+
+} // namespace
+
+extern "C" int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const double *noise) {
+    if (!ctx || nsteps < 0 || (nsteps > 0 && !noise)) return SIS_ERR_ARG;
+    if (ctx->n > kStaticNoiseBeads)
+        return fail(ctx, SIS_ERR_ARG,
+                    "sis_gpu_step_noise_static: " + std::to_string(ctx->n) + " beads exceed the static noise buffer (" +
+                        std::to_string(kStaticNoiseBeads) + " beads); use sis_gpu_step");
+    double *buf = nullptr;
+    int rc = noise_scratch(ctx, &buf);
+    if (rc) return rc;
+    rc = ensure_lists(ctx);
+    if (rc) return rc;
+    const size_t per = (size_t)ctx->n * 3;
+    for (int64_t s = 0; s < nsteps; ++s) {
+        // stream-ordered: the copy waits for the previous step's kernels
+        CK(cudaMemcpyAsync(buf, noise + (size_t)s * per, sizeof(double) * per, cudaMemcpyHostToDevice, ctx->st));
+        rc = enqueue_step(ctx, buf, 0);
+        if (rc) return rc;
+    }
+    ctx->steps += nsteps;
+    ctx->bp_cache = true;
+    CK(cudaStreamSynchronize(ctx->st));
     return check_err(ctx);
 }
