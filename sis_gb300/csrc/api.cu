@@ -87,8 +87,14 @@ struct sis_ctx {
     size_t flush_bytes = 0;
     std::vector<void *> allocs;
     double4 *pin = nullptr; // pinned staging buffer for state transfers (n double4)
+    // steady-state step graph (kGraphSteps steps, rebuild bodies behind
+    // conditional nodes) and the parameters it was captured with
     cudaGraphExec_t gexec = nullptr;
-    int graph_steps = 0;
+    cudaStream_t st2 = nullptr; // captures the conditional rebuild bodies
+    int graph_cur = -1, graph_G = 0, graph_bpb = 0;
+    GlobP graph_g{};
+    unsigned long long graph_passes = 0; // D.rebuilds[1] already counted in launches
+    bool use_graphs = true;
     int n_vel_init = 0;
     bool tuned = false;
 };
@@ -316,6 +322,86 @@ int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
     ctx->launches++;
     ctx->cur ^= 1;
     return run_rebuild(ctx, 1);
+}
+
+// ----------------------------------------------------------- step graphs
+// kGraphSteps MD steps captured as one graph: per step k_pre, k_step,
+// k_trigger and a conditional (IF) node whose body is the rebuild; k_trigger
+// sets the node's condition on the device, so a step without a rebuild runs
+// three kernels and no early-exit launches.  An even step count leaves the
+// position buffer parity unchanged, so one graph serves every launch.
+constexpr int kGraphSteps = 20;
+
+cudaError_t add_rebuild_node(sis_ctx *ctx, cudaGraphConditionalHandle cond, int cur) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(ctx->st, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
+    if (e != cudaSuccess) return e;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(ctx->st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return e;
+    cudaError_t eb = launch_rebuild_body(ctx->D, ctx->g, cur, ctx->plan, 1, ctx->st2);
+    cudaGraph_t got = nullptr;
+    e = cudaStreamEndCapture(ctx->st2, &got);
+    if (eb != cudaSuccess) return eb;
+    if (e != cudaSuccess) return e;
+    return cudaStreamUpdateCaptureDependencies(ctx->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+}
+
+int build_step_graph(sis_ctx *ctx) {
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    ctx->gexec = nullptr;
+    if (!ctx->st2) CK(cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    CK(cudaGraphCreate(&graph, 0));
+    cudaError_t e = cudaSuccess;
+    cudaGraphConditionalHandle cond[kGraphSteps];
+    for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k)
+        e = cudaGraphConditionalHandleCreate(&cond[k], graph, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(ctx->st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+        int cur = ctx->cur;
+        for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k) {
+            e = launch_pre(ctx->D, ctx->g, cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st);
+            if (e == cudaSuccess) e = launch_step(ctx->G, ctx->D, ctx->g, cur, nullptr, 0, ctx->st);
+            cur ^= 1;
+            if (e == cudaSuccess) e = launch_trigger(ctx->D, ctx->g, step_blocks(ctx->G, ctx->n), ctx->st, &cond[k]);
+            if (e == cudaSuccess) e = add_rebuild_node(ctx, cond[k], cur);
+        }
+        cudaGraph_t got = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(ctx->st, &got);
+        if (e == cudaSuccess) e = ee;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        ctx->gexec = nullptr;
+        cudaGetLastError();
+        return fail(ctx, SIS_ERR_CUDA, std::string("step graph: ") + cudaGetErrorString(e));
+    }
+    ctx->graph_cur = ctx->cur;
+    ctx->graph_G = ctx->G;
+    ctx->graph_bpb = ctx->bpb;
+    ctx->graph_g = ctx->g;
+    return SIS_OK;
+}
+
+// the step graph for the current parameters, captured again when they changed
+int ensure_step_graph(sis_ctx *ctx) {
+    if (ctx->gexec && ctx->graph_cur == ctx->cur && ctx->graph_G == ctx->G && ctx->graph_bpb == ctx->bpb &&
+        memcmp(&ctx->graph_g, &ctx->g, sizeof(GlobP)) == 0)
+        return SIS_OK;
+    return build_step_graph(ctx);
 }
 
 // Picks the lanes-per-bead width G of the step kernel by timing force-only
@@ -580,7 +666,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.step_ctr, 1);
     rc |= dalloc(ctx, &D.err, 1);
     rc |= dalloc(ctx, &D.max_need, 2);
-    rc |= dalloc(ctx, &D.rebuilds, 1);
+    rc |= dalloc(ctx, &D.rebuilds, 2); // [0] instance rebuilds, [1] rebuild passes run by step graphs
     rc |= dalloc(ctx, &D.capped, 1);
     rc |= dalloc(ctx, &D.bead_cell, n);
     rc |= dalloc(ctx, &D.cell_cnt, ncells);
@@ -682,6 +768,7 @@ extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
     for (int e = 0; e < kEvents; ++e)
         if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
     if (ctx->st) cudaStreamDestroy(ctx->st);
+    if (ctx->st2) cudaStreamDestroy(ctx->st2);
     delete ctx;
 }
 
@@ -911,13 +998,28 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
         }
         CK(cudaMemcpyAsync(ctx->noise_d, noise, sizeof(double) * need, cudaMemcpyHostToDevice, ctx->st));
     }
-    for (int64_t s = 0; s < nsteps; ++s) {
+    int64_t s = 0;
+    bool graphs = false;
+    if (!noise && ctx->use_graphs && nsteps >= kGraphSteps) {
+        if ((rc = ensure_step_graph(ctx))) return rc;
+        for (; s + kGraphSteps <= nsteps; s += kGraphSteps) CK(cudaGraphLaunch(ctx->gexec, ctx->st));
+        ctx->launches += 3 * s;
+        graphs = true;
+    }
+    for (; s < nsteps; ++s) {
         rc = enqueue_step(ctx, noise ? ctx->noise_d : nullptr, (long long)s);
         if (rc) return rc;
     }
     ctx->steps += nsteps;
     ctx->bp_cache = true;
     CK(cudaStreamSynchronize(ctx->st));
+    if (graphs) {
+        // rebuild bodies the graphs actually ran
+        unsigned long long passes = 0;
+        CK(cudaMemcpy(&passes, ctx->D.rebuilds + 1, sizeof(passes), cudaMemcpyDeviceToHost));
+        ctx->launches += (long long)(passes - ctx->graph_passes) * rebuild_body_kernels(ctx->plan);
+        ctx->graph_passes = passes;
+    }
     return check_err(ctx);
 }
 

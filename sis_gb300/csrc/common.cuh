@@ -143,7 +143,7 @@ struct Dev {
     unsigned long long *step_ctr; // [1] Philox step counter
     int *err;               // [1] error flags
     int *max_need;          // [2] largest pair / bp count seen
-    long long *rebuilds;    // [1]
+    long long *rebuilds;    // [2] instance rebuilds, rebuild passes run by step graphs
     unsigned long long *capped; // [1] bead-steps at which the force cap bound
     // cell lists of large PBC instances
     int *bead_cell, *cell_cnt, *cell_start, *cell_beads;

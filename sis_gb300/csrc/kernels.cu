@@ -432,32 +432,6 @@ __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, doub
 // three Gaussian deviates of one bead from one Philox4x32-10 block
 // (Box-Muller on the pairs (r.x, r.y) and (r.z, r.w)); equal to gauss3 for
 // components 0, 1, 2
-template <typename R>
-__device__ __forceinline__ void gauss_bead(unsigned long long seed, int i, unsigned long long s, unsigned stream, double *xi) {
-    const uint4 r = philox4x32_10(make_uint4((unsigned)i, (unsigned)s, (unsigned)(s >> 32), stream),
-                                  make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
-    if constexpr (sizeof(R) == 4) {
-        const float u1 = (float)((r.x >> 8) + 1u) * (1.0f / 16777216.0f), u2 = (float)(r.y >> 8) * (1.0f / 16777216.0f);
-        const float u3 = (float)((r.z >> 8) + 1u) * (1.0f / 16777216.0f), u4 = (float)(r.w >> 8) * (1.0f / 16777216.0f);
-        float s1, c1, s2, c2;
-        sincospif(2.0f * u2, &s1, &c1);
-        sincospif(2.0f * u4, &s2, &c2);
-        const float r1 = sqrtf(-2.0f * logf(u1)), r2 = sqrtf(-2.0f * logf(u3));
-        xi[0] = (double)(r1 * c1);
-        xi[1] = (double)(r1 * s1);
-        xi[2] = (double)(r2 * c2);
-    } else {
-        const double u1 = ((double)r.x + 1.0) * (1.0 / 4294967296.0), u2 = (double)r.y * (1.0 / 4294967296.0);
-        const double u3 = ((double)r.z + 1.0) * (1.0 / 4294967296.0), u4 = (double)r.w * (1.0 / 4294967296.0);
-        double s1, c1, s2, c2;
-        sincospi(2.0 * u2, &s1, &c1);
-        sincospi(2.0 * u4, &s2, &c2);
-        const double r1 = sqrt(-2.0 * log(u1)), r2 = sqrt(-2.0 * log(u3));
-        xi[0] = r1 * c1;
-        xi[1] = r1 * s1;
-        xi[2] = r2 * c2;
-    }
-}
 
 // ------------------------------------------------------------------ k_step
 // Phase A (G lanes per bead): WCA + Debye-Hueckel over the bead's full pair
@@ -612,69 +586,57 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
     __syncthreads();
 
     // -------------------------------------------------------------- phase B
+    // One thread per (component, bead): the components of the GJF-2GJ /
+    // Ermak-McCammon update are independent, and FP64 runs at a small
+    // fraction of the FP32 rate on this part, so the block spreads it over
+    // 3*BPB threads (whole warps) instead of BPB.
     const unsigned long long step = MODE == 0 ? *D.step_ctr : 0ull;
-    for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
+    for (int t = threadIdx.x; t < 3 * BPB; t += blockDim.x) {
+        const int c = t / BPB, bb = t - c * BPB;
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
-        double F[3];
-        double4 fb = make_double4(0.0, 0.0, 0.0, 0.0);
+        double fb = 0.0;
         if (mask & 8) {
-            fb = D.fbp[ii];
-            D.fbp[ii] = make_double4(0.0, 0.0, 0.0, 0.0);
-            if constexpr (sizeof(R) == 4) fb = make_double4(fx_value(fb.x), fx_value(fb.y), fx_value(fb.z), 0.0);
+            double *fp = reinterpret_cast<double *>(D.fbp + ii) + c;
+            fb = *fp;
+            *fp = 0.0;
+            if constexpr (sizeof(R) == 4) fb = fx_value(fb);
         }
-        F[0] = (double)sA[0][bb] + (double)sB[0][bb] + fb.x;
-        F[1] = (double)sA[1][bb] + (double)sB[1][bb] + fb.y;
-        F[2] = (double)sA[2][bb] + (double)sB[2][bb] + fb.z;
+        double Fc;
+        if constexpr (sizeof(R) == 4) Fc = (double)(sA[c][bb] + sB[c][bb]) + fb;
+        else Fc = sA[c][bb] + sB[c][bb] + fb;
         if (MODE == 1) {
-            fout[3 * (size_t)ii + 0] = F[0];
-            fout[3 * (size_t)ii + 1] = F[1];
-            fout[3 * (size_t)ii + 2] = F[2];
+            fout[3 * (size_t)ii + c] = Fc;
             continue;
         }
-        const double sc = (double)sScale[bb];
+        Fc = Fc * (double)sScale[bb];
         const int4 bj = D.binfo[ii];
         const InstP &jp = D.ip[bj.x];
         const double4 m = D.mdc[ii];
-        double xi[3];
-        if (noise) {
-            for (int c = 0; c < 3; ++c) xi[c] = noise[((size_t)noise_step * g.n + ii) * 3 + c];
-        } else {
-            gauss_bead<R>(g.seed, ii - jp.bead_off, step - jp.step0, jp.stream, xi);
-        }
-        const double4 x0 = D.x[cur][ii];
-        double4 v = D.v[ii], be = D.beta[ii], mv = D.move[ii];
-        const double xc[3] = {x0.x, x0.y, x0.z};
-        double vc[3] = {v.x, v.y, v.z}, bc[3] = {be.x, be.y, be.z}, mc[3] = {mv.x, mv.y, mv.z}, xn[3];
-        unsigned int mirn[3];
-        float resn[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const double Fc = F[c] * sc;
-            double dx;
-            if (g.integrator == 1) {
-                const double bn = m.w * xi[c];
-                const double vn = m.x * vc[c] + m.y * Fc + (bc[c] + bn);
-                bc[c] = bn;
-                vc[c] = vn;
-                dx = m.z * vn;
-            } else {
-                dx = m.x * Fc + m.w * xi[c];
-            }
-            xn[c] = xc[c] + dx;
-            if (!isfinite(xn[c])) atomicOr(D.err, ERR_NONFINITE);
-            mc[c] = mc[c] + dx;
-            sM[c][bb] = mc[c];
-            mirn[c] = fixed_res(xn[c], jp.fsc[c], resn[c]);
-        }
-        D.x[cur ^ 1][ii] = make_double4(xn[0], xn[1], xn[2], 0.0);
+        const double xi = noise ? noise[((size_t)noise_step * g.n + ii) * 3 + c]
+                                : gauss3<R>(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
+        double *vp = reinterpret_cast<double *>(D.v + ii) + c;
+        double *bp = reinterpret_cast<double *>(D.beta + ii) + c;
+        double *mp = reinterpret_cast<double *>(D.move + ii) + c;
+        double dx;
         if (g.integrator == 1) {
-            D.v[ii] = make_double4(vc[0], vc[1], vc[2], 0.0);
-            D.beta[ii] = make_double4(bc[0], bc[1], bc[2], 0.0);
+            const double bn = m.w * xi;
+            const double vn = m.x * *vp + m.y * Fc + (*bp + bn);
+            *bp = bn;
+            *vp = vn;
+            dx = m.z * vn;
+        } else {
+            dx = m.x * Fc + m.w * xi;
         }
-        D.move[ii] = make_double4(mc[0], mc[1], mc[2], 0.0);
-        D.mir[cur ^ 1][ii] = make_uint4(mirn[0], mirn[1], mirn[2], 0u);
-        D.res[cur ^ 1][ii] = make_float4(resn[0], resn[1], resn[2], 0.f);
+        const double xn = reinterpret_cast<const double *>(D.x[cur] + ii)[c] + dx;
+        if (!isfinite(xn)) atomicOr(D.err, ERR_NONFINITE);
+        const double mc = *mp + dx;
+        *mp = mc;
+        sM[c][bb] = mc;
+        reinterpret_cast<double *>(D.x[cur ^ 1] + ii)[c] = xn;
+        float r;
+        reinterpret_cast<unsigned int *>(D.mir[cur ^ 1] + ii)[c] = fixed_res(xn, jp.fsc[c], r);
+        reinterpret_cast<float *>(D.res[cur ^ 1] + ii)[c] = r;
     }
     if (MODE == 1) return;
     __syncthreads();
@@ -729,7 +691,10 @@ __device__ __forceinline__ void top2_merge(unsigned long long &a1, unsigned long
     a2 = lo > m ? lo : m;
 }
 
-__global__ void __launch_bounds__(256) k_trigger(Dev D, GlobP g, int nparts) {
+// The last block also sets the graph conditional cond (use_cond: launched as
+// a node of a captured step graph) to whether any instance asked for a
+// rebuild, so that the graph runs its rebuild body only then.
+__global__ void __launch_bounds__(256) k_trigger(Dev D, GlobP g, int nparts, cudaGraphConditionalHandle cond, int use_cond) {
     __shared__ int s_last;
     const int lane = threadIdx.x & 31;
     for (int base = blockIdx.x * blockDim.x; base < 2 * nparts; base += gridDim.x * blockDim.x) {
@@ -776,9 +741,11 @@ __global__ void __launch_bounds__(256) k_trigger(Dev D, GlobP g, int nparts) {
         }
     }
     if (any) atomicOr(D.any, 1);
+    __syncthreads();
     if (threadIdx.x == 0) {
         D.ticket[0] = 0u;
         D.step_ctr[0] += 1ull;
+        if (use_cond) cudaGraphSetConditional(cond, *(volatile int *)D.any ? 1u : 0u);
     }
 }
 
@@ -914,9 +881,9 @@ cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st) {
+cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st, const cudaGraphConditionalHandle *cond) {
     const int grid = std::max(1, std::min(64, (2 * nparts + 255) / 256));
-    k_trigger<<<grid, 256, 0, st>>>(D, g, nparts);
+    k_trigger<<<grid, 256, 0, st>>>(D, g, nparts, cond ? *cond : cudaGraphConditionalHandle{}, cond != nullptr);
     return cudaGetLastError();
 }
 

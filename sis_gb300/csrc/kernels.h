@@ -16,7 +16,8 @@ cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const doub
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
 cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st);
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st);
-cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st);
+cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st,
+                           const cudaGraphConditionalHandle *cond = nullptr);
 int step_blocks(int G, int n);
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st);
@@ -24,5 +25,11 @@ cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st
 // after_step: the rebuild follows a step (k_trigger decides the flags);
 // otherwise the flags were set by the host and k_rebuild_begin starts it
 cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, cudaStream_t st);
+// the rebuild proper (every kernel after k_trigger / k_rebuild_begin); in_graph:
+// it is the body of a step graph's conditional node, whose passes are counted
+// in D.rebuilds[1]
+cudaError_t launch_rebuild_body(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int in_graph, cudaStream_t st);
+// kernels launch_rebuild_body enqueues
+int rebuild_body_kernels(const RebuildPlan &pl);
 
 } // namespace sisg

@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(256) k_cell_search(Dev D, GlobP g, int cur, co
 // ------------------------------------------------------------ finish
 // One block: base-pair prefix counts, rebuild bookkeeping, reset of flags
 // and cell counters.
-__global__ void __launch_bounds__(1024) k_rebuild_finish(Dev D, GlobP g) {
+__global__ void __launch_bounds__(1024) k_rebuild_finish(Dev D, GlobP g, int in_graph) {
     if (*(volatile int *)D.any == 0) return;
     __shared__ int s[1024];
     const int n = g.n_inst;
@@ -413,7 +413,10 @@ __global__ void __launch_bounds__(1024) k_rebuild_finish(Dev D, GlobP g) {
     if (nflag) atomicAdd((unsigned long long *)D.rebuilds, (unsigned long long)nflag);
     for (int c = threadIdx.x; c < D.n_cells; c += blockDim.x) D.cell_cnt[c] = 0;
     __syncthreads();
-    if (threadIdx.x == 0) *D.any = 0;
+    if (threadIdx.x == 0) {
+        *D.any = 0;
+        if (in_graph) atomicAdd((unsigned long long *)(D.rebuilds + 1), 1ull);
+    }
 }
 
 // Clears the base-pair staging count of flagged instances; first kernel of a rebuild.
@@ -423,15 +426,8 @@ __global__ void k_rebuild_begin(Dev D, GlobP g) {
         if (D.flag[k]) D.bp_cnt[k] = 0;
 }
 
-cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts,
-                           cudaStream_t st) {
+cudaError_t launch_rebuild_body(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int in_graph, cudaStream_t st) {
     const float slack = 1.001f;
-    if (after_step) {
-        cudaError_t e = launch_trigger(D, g, nparts, st);
-        if (e != cudaSuccess) return e;
-    } else {
-        k_rebuild_begin<<<(g.n_inst + 255) / 256, 256, 0, st>>>(D, g);
-    }
     if (pl.n_small_items > 0) k_rebuild_small<<<pl.small_grid, 256, 0, st>>>(D, g, cur, pl.small_items, pl.n_small_items, slack);
     if (pl.n_large_items > 0) {
         k_cell_bin<<<pl.large_grid, 256, 0, st>>>(D, g, cur, pl.large_items, pl.n_large_items);
@@ -440,8 +436,21 @@ cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildP
         k_cell_sort<<<(D.n_cells + 255) / 256, 256, 0, st>>>(D);
         k_cell_search<<<pl.large_grid, 256, 0, st>>>(D, g, cur, pl.large_items, pl.n_large_items, slack);
     }
-    k_rebuild_finish<<<1, 1024, 0, st>>>(D, g);
+    k_rebuild_finish<<<1, 1024, 0, st>>>(D, g, in_graph);
     return cudaGetLastError();
+}
+
+int rebuild_body_kernels(const RebuildPlan &pl) { return (pl.n_small_items > 0) + 5 * (pl.n_large_items > 0) + 1; }
+
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts,
+                           cudaStream_t st) {
+    if (after_step) {
+        cudaError_t e = launch_trigger(D, g, nparts, st);
+        if (e != cudaSuccess) return e;
+    } else {
+        k_rebuild_begin<<<(g.n_inst + 255) / 256, 256, 0, st>>>(D, g);
+    }
+    return launch_rebuild_body(D, g, cur, pl, 0, st);
 }
 
 } // namespace sisg

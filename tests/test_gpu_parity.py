@@ -14,7 +14,7 @@ import pytest
 
 from helpers import cag47_system, max_rel, pbc_md_system, rms_rel, t2s2hp_system
 from oracle.oracle import Oracle
-from sis_gb300 import FP64, MIXED
+from sis_gb300 import BD_EM, FP64, GJF2GJ, MIXED
 from sis_gb300._abi import SisError
 from sis_gb300.coil import crowded_box, random_coil, single_chain, uneven_batch
 from sis_gb300.engine import Engine
@@ -208,6 +208,69 @@ def test_fed_noise_trajectory_matches_oracle(name, systems):
     assert np.array_equal(a, orc.get_accels(0))
 
 
+@pytest.mark.parametrize("name", ["chain64", "pbc564", "compact_bp"])
+def test_one_fed_noise_step_matches_oracle(name, systems):
+    """One GJF-2GJ step fed the oracle's Gaussian array: positions to 1e-12."""
+    sysm = systems[name]
+    n = sysm.nmp
+    rng = np.random.default_rng(8)
+    v0 = rng.normal(size=(n, 3)) * 0.04
+    a0 = rng.normal(size=(n, 3)) * 0.01
+    noise = rng.normal(size=(1, 1, n, 3))
+    orc = Oracle.from_instance(sysm, 0)
+    orc.set_velos(0, v0)
+    orc.set_accels(0, a0)
+    orc.md_init()
+    orc.run(1, noise)
+    eng = Engine(sysm, precision=FP64)
+    eng.set_state(0, None, v0, a0)
+    eng.step(1, noise.reshape(1, n, 3))
+    x = eng.get_state(0)[0]
+    assert np.abs(x - orc.get_xyz(0)).max() <= 1e-12 * np.abs(orc.get_xyz(0)).max()
+
+
+@pytest.mark.parametrize("name", ["chain64", "pbc564"])
+def test_fed_noise_ermak_mccammon_matches_oracle(name, sis_ff):
+    """Ermak-McCammon Brownian dynamics (job_md.F90:446-456), 10 fed steps, at
+    water viscosity: with the MD default (1e-5 Pa s) the explicit BD step
+    h/gamma * k_bond exceeds 1 and amplifies every rounding difference.
+    Positions compare modulo the box: the engine wraps when it rebuilds after
+    a step, the oracle when it rebuilds before the next one."""
+    if name == "chain64":  # a coil without WCA overlap (the 4 A contacts of the recipe kick beads far)
+        rng = np.random.default_rng(1001)
+        x = random_coil(rng, 64, rmin=10.0)
+        sysm = System(sis_ff, Options(bp_model=1), [Instance([Chain(rng.integers(0, 4, 64).astype(np.int32))],
+                                                             tempK=300.0, ionic_strength=0.15, xyz=x)])
+    else:
+        sysm = pbc_md_system(sis_ff, 1)
+    sysm.opts.integrator = BD_EM
+    sysm.opts.viscosity_Pas = 8.9e-4
+    n = sysm.nmp
+    noise = np.random.default_rng(4).normal(size=(10, 1, n, 3))
+    orc = Oracle.from_instance(sysm, 0)
+    orc.md_init()
+    orc.run(10, noise)
+    eng = Engine(sysm, precision=FP64)
+    eng.step(10, noise.reshape(10, n, 3))
+    d = eng.get_state(0)[0] - orc.get_xyz(0)
+    box = sysm.instances[0].box
+    if box is not None and box[0] > 0:
+        d -= np.asarray(box) * np.round(d / np.asarray(box))
+    assert np.abs(d).max() <= 1e-10 * np.abs(orc.get_xyz(0)).max()
+
+
+@pytest.mark.parametrize("integrator", [GJF2GJ, BD_EM])
+def test_md_coefficients_match_oracle(integrator, sis_ff):
+    """set_md_coef (job_md.F90:700-767): per-bead coefficients of every instance."""
+    sysm = uneven_batch(sis_ff, n_inst=3, lmin=20, lmax=60, seed=9)
+    sysm.opts.integrator = integrator
+    eng = Engine(sysm, precision=FP64)
+    for k in range(3):
+        orc = Oracle.from_instance(sysm, k)
+        orc.md_init()
+        assert np.allclose(eng.get_md_coef(k), orc.get_md_coef(0), rtol=1e-14, atol=0), k
+
+
 def test_rebuild_trigger_matches_oracle(sis_ff):
     """Large early displacements from a 4 A random-coil contact set force several
     displacement-triggered rebuilds; positions still agree with the oracle."""
@@ -224,6 +287,34 @@ def test_rebuild_trigger_matches_oracle(sis_ff):
     assert st["rebuilds"] - 1 == nreb  # minus the initial build
     x = eng.get_state(0)[0]
     assert np.abs(x - orc.get_xyz(0)).max() <= 1e-8 * np.abs(x).max()
+
+
+@pytest.mark.parametrize("name", ["chain64", "cells6000"])
+@pytest.mark.parametrize("prec", [MIXED, FP64])
+def test_step_graph_equals_single_steps(name, prec, systems, sis_ff):
+    """sis_gpu_step runs 20-step graphs whose rebuilds sit behind conditional
+    nodes; single-step calls launch every kernel.  Same state, same rebuilds.
+    Both starts carry 4 A contacts, so the trigger fires within the run (the
+    cell-list box under the force cap that guards such starts)."""
+    sysm = systems[name] if name == "chain64" else crowded_box(sis_ff, n_chains=12, n=500, molar=0.05, seed=22, rmin=4.0)
+    a = Engine(sysm, precision=prec, seed=5)
+    b = Engine(sysm, precision=prec, seed=5)
+    for e in (a, b):
+        e.set_lanes(8)
+        e.set_force_cap(1000.0)
+        e.init_velocities()
+    nsteps = 60 if name == "chain64" else 100
+    a.step(nsteps)
+    for _ in range(nsteps):
+        b.step(1)
+    for u, w in zip(a.get_state(-1), b.get_state(-1)):
+        if prec == MIXED:
+            assert np.array_equal(u, w)
+        else:  # FP64 base-pair scatter: atomic arrival order moves the last bits
+            assert np.abs(u - w).max() <= 1e-12 * np.abs(w).max()
+    sa, sb = a.stats(), b.stats()
+    assert sa["rebuilds"] == sb["rebuilds"] and sa["rebuilds"] > 1
+    assert a.get_step() == b.get_step() == nsteps
 
 
 def test_instance_alone_equals_instance_in_batch(sis_ff):
