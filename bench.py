@@ -161,6 +161,10 @@ def run_gpu(args):
     S = args.md_steps
     N = sysm.nmp
     eng = Engine(sysm, precision=MIXED, seed=2024 + rank)
+    if args.lanes:  # fixed lanes per bead (no autotuning): reproducible launch sequences for profiling
+        eng.set_lanes(args.lanes)
+    if args.no_graphs:  # every kernel launched from the host (what per-kernel profilers can see)
+        eng.set_graphs(False)
     eng.init_velocities()
     # equilibrate before timing (force-capped, then free dynamics; neither is
     # timed): the coil start has no WCA overlap but is far from equilibrium
@@ -245,7 +249,7 @@ def run_gpu(args):
            "speedup_vs_fp64": value / fp64_value, "force_rms_rel_err_vs_fp64": err,
            "relax_steps": {"force_capped": args.relax, "free": args.relax},
            "force_cap": args.force_cap, "capped_bead_steps": st1["capped"] - cap0,
-           "launches_before_timed": int(launches0),
+           "launches_before_timed": int(launches0), "step_graphs": not args.no_graphs,
            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -356,6 +360,8 @@ def main():
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--relax", type=int, default=1000)
     ap.add_argument("--force-cap", type=float, default=1000.0)
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per bead of the step kernel (0: autotune)")
+    ap.add_argument("--no-graphs", action="store_true", help="launch every kernel from the host instead of step graphs")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()

@@ -201,6 +201,11 @@ int sis_gpu_set_step(sis_ctx *ctx, uint64_t step);
 /* Lanes per bead of the step kernel (1, 2, 4, 8, 16 or 32); 0 re-enables
  * the autotuner that picks it on the first long run. */
 int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes);
+/* 1 (default): sis_gpu_step runs steady-state steps as captured CUDA graphs
+ * (20 steps each, the rebuild behind a device-set conditional node); 0:
+ * every kernel is launched from the host.  Results are identical; per-kernel
+ * profilers see only the second form. */
+int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable);
 
 int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *st);
 /* Human-readable description of the last error on this context. */

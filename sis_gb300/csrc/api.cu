@@ -1093,6 +1093,12 @@ extern "C" int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes) {
     return SIS_OK;
 }
 
+extern "C" int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable) {
+    if (!ctx || (enable != 0 && enable != 1)) return SIS_ERR_ARG;
+    ctx->use_graphs = enable != 0;
+    return SIS_OK;
+}
+
 extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
     if (!ctx || !s) return SIS_ERR_ARG;
     memset(s, 0, sizeof(*s));

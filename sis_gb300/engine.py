@@ -160,6 +160,10 @@ class Engine:
         """Lanes per bead of the step kernel; 0 lets the autotuner choose."""
         self._ck(self.L.sis_gpu_set_lanes(self.h, int(lanes)))
 
+    def set_graphs(self, enable: bool):
+        """Run steady-state steps as CUDA graphs (default) or launch by launch."""
+        self._ck(self.L.sis_gpu_set_graphs(self.h, int(bool(enable))))
+
     def get_step(self) -> int:
         v = C.c_uint64()
         self._ck(self.L.sis_gpu_get_step(self.h, C.byref(v)))
