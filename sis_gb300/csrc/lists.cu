@@ -281,30 +281,53 @@ __global__ void k_cell_bin(Dev D, GlobP g, int cur, const int2 *litems, int n_li
     }
 }
 
-// exclusive scan of cell counts (one block); counts are reset to serve as fill cursors
+// exclusive scan of cell counts (one block, coalesced tiles of 4096 cells);
+// counts are reset to serve as fill cursors
 __global__ void __launch_bounds__(1024) k_cell_scan(Dev D) {
     if (*(volatile int *)D.any == 0) return;
-    __shared__ int s[1024];
+    __shared__ int s_warp[32];
+    __shared__ int s_carry;
     const int n = D.n_cells;
-    const int per = (n + 1023) / 1024;
-    const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
-    int sum = 0;
-    for (int c = lo; c < hi; ++c) sum += D.cell_cnt[c];
-    s[threadIdx.x] = sum;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = 0;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
-        const int v = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0;
+    for (int base = 0; base < n; base += 4096) {
+        const int c0 = base + 4 * threadIdx.x;
+        int v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[q] = c0 + q < n ? D.cell_cnt[c0 + q] : 0;
+        const int tsum = v[0] + v[1] + v[2] + v[3];
+        int incl = tsum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) s_warp[warp] = incl;
         __syncthreads();
-        s[threadIdx.x] += v;
+        if (warp == 0) {
+            int w = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            s_warp[lane] = w;
+        }
+        __syncthreads();
+        int run = s_carry + (warp ? s_warp[warp - 1] : 0) + incl - tsum;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (c0 + q < n) {
+                D.cell_start[c0 + q] = run;
+                D.cell_cnt[c0 + q] = 0;
+                run += v[q];
+            }
+        __syncthreads();
+        if (threadIdx.x == 1023) s_carry += s_warp[31];
         __syncthreads();
     }
-    int run = s[threadIdx.x] - sum;
-    for (int c = lo; c < hi; ++c) {
-        D.cell_start[c] = run;
-        run += D.cell_cnt[c];
-        D.cell_cnt[c] = 0;
-    }
-    if (threadIdx.x == 1023) D.cell_start[n] = s[1023];
+    if (threadIdx.x == 0) D.cell_start[n] = s_carry;
 }
 
 __global__ void k_cell_fill(Dev D, GlobP g, const int2 *litems, int n_litems) {
@@ -322,19 +345,38 @@ __global__ void k_cell_fill(Dev D, GlobP g, const int2 *litems, int n_litems) {
     }
 }
 
-// sorts every cell's beads by index so that list order is deterministic
-__global__ void k_cell_sort(Dev D) {
+// sorts every cell's beads by index so that list order is deterministic:
+// one warp per cell ranks up to 256 beads in shared memory (rank = number of
+// smaller indices; indices are distinct); larger cells are insertion-sorted
+__global__ void __launch_bounds__(256) k_cell_sort(Dev D) {
     if (*(volatile int *)D.any == 0) return;
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < D.n_cells; c += gridDim.x * blockDim.x) {
-        const int a = D.cell_start[c], b = D.cell_start[c + 1];
-        for (int k = a + 1; k < b; ++k) {
-            const int v = D.cell_beads[k];
-            int m = k - 1;
-            while (m >= a && D.cell_beads[m] > v) {
-                D.cell_beads[m + 1] = D.cell_beads[m];
-                --m;
+    constexpr int kCap = 256;
+    __shared__ int sb[8][kCap];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * 8;
+    for (int c = blockIdx.x * 8 + warp; c < D.n_cells; c += nwarps) {
+        const int a = D.cell_start[c], b = D.cell_start[c + 1], m = b - a;
+        if (m <= 1) continue;
+        if (m <= kCap) {
+            for (int k = lane; k < m; k += 32) sb[warp][k] = D.cell_beads[a + k];
+            __syncwarp();
+            for (int k = lane; k < m; k += 32) {
+                const int v = sb[warp][k];
+                int r = 0;
+                for (int q = 0; q < m; ++q) r += sb[warp][q] < v;
+                D.cell_beads[a + r] = v;
             }
-            D.cell_beads[m + 1] = v;
+            __syncwarp();
+        } else if (lane == 0) {
+            for (int k = a + 1; k < b; ++k) {
+                const int v = D.cell_beads[k];
+                int q = k - 1;
+                while (q >= a && D.cell_beads[q] > v) {
+                    D.cell_beads[q + 1] = D.cell_beads[q];
+                    --q;
+                }
+                D.cell_beads[q + 1] = v;
+            }
         }
     }
 }
@@ -358,22 +400,45 @@ __global__ void __launch_bounds__(256) k_cell_search(Dev D, GlobP g, int cur, co
             const uint4 mi = D.mir[cur][gi];
             const int c0 = D.bead_cell[gi] - ip.cell_base;
             const int cx = c0 % ip.nc[0], cy = (c0 / ip.nc[0]) % ip.nc[1], cz = c0 / (ip.nc[0] * ip.nc[1]);
-            int count = 0;
-            for (int nbc = 0; nbc < 27; ++nbc) {
-                int qx = cx + nbc % 3 - 1, qy = cy + (nbc / 3) % 3 - 1, qz = cz + nbc / 9 - 1;
+            // lane q < 27 owns neighbour cell q; a warp prefix over their
+            // counts flattens the 27 ranges into one candidate sequence that
+            // every pass consumes 32 at a time (cell order, then bead order)
+            int cstart = 0, ccnt = 0;
+            if (lane < 27) {
+                int qx = cx + lane % 3 - 1, qy = cy + (lane / 3) % 3 - 1, qz = cz + lane / 9 - 1;
                 qx = qx < 0 ? qx + ip.nc[0] : (qx >= ip.nc[0] ? qx - ip.nc[0] : qx);
                 qy = qy < 0 ? qy + ip.nc[1] : (qy >= ip.nc[1] ? qy - ip.nc[1] : qy);
                 qz = qz < 0 ? qz + ip.nc[2] : (qz >= ip.nc[2] ? qz - ip.nc[2] : qz);
                 const int c = ip.cell_base + (qz * ip.nc[1] + qy) * ip.nc[0] + qx;
-                const int a = D.cell_start[c], b = D.cell_start[c + 1];
-                for (int k = a; k < b; k += 32) {
-                    int f = 0, gj = -1;
-                    if (k + lane < b) {
-                        gj = D.cell_beads[k + lane];
-                        if (gj != gi) f = test_pair(D, g, ip, cur, gi, bii, mi, xi_w, gj, maxcut2f, inst);
-                    }
-                    warp_append(D, g, gi, lane, f, gj, count);
+                cstart = D.cell_start[c];
+                ccnt = D.cell_start[c + 1] - cstart;
+            }
+            int incl = ccnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int excl = incl - ccnt;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            int count = 0;
+            for (int k0 = 0; k0 < total; k0 += 32) {
+                const int k = k0 + lane, kk = min(k, total - 1);
+                // owning cell of candidate kk: the last q <= 26 with excl[q] <= kk
+                // (that cell is non-empty); every lane runs the same shuffles
+                int lo = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int e = __shfl_sync(0xffffffffu, excl, min(lo + step, 26));
+                    if (lo + step <= 26 && e <= kk) lo += step;
                 }
+                const int cs = __shfl_sync(0xffffffffu, cstart, lo), ce = __shfl_sync(0xffffffffu, excl, lo);
+                int f = 0, gj = -1;
+                if (k < total) {
+                    gj = D.cell_beads[cs + (k - ce)];
+                    if (gj != gi) f = test_pair(D, g, ip, cur, gi, bii, mi, xi_w, gj, maxcut2f, inst);
+                }
+                warp_append(D, g, gi, lane, f, gj, count);
             }
             bead_end(D, g, gi, lane, count);
         }
