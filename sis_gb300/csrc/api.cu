@@ -60,7 +60,7 @@ struct sis_ctx {
     GlobP g{};
     sis_params p{};
     int n = 0, n_inst = 0, cur = 0, G = 8;
-    int bpb = 2 * 152; // base-pair blocks of k_pre (tuned)
+    int bpb = 2 * 152; // base-pair blocks of k_pre: two per SM (set from the device at creation)
     std::vector<InstP> ip;
     std::vector<int4> binfo;
     std::vector<int> seq;
@@ -430,28 +430,6 @@ int autotune(sis_ctx *ctx) {
         }
     }
     ctx->G = bestG;
-    // base-pair blocks: fewer, longer-lived blocks fill their evaluation
-    // queues more often; more blocks hide more gather latency
-    if (ctx->g.bp_model > 0) {
-        const int bcand[4] = {152, 304, 608, 1216};
-        best = 1e30f;
-        for (int c = 0; c < 4; ++c) {
-            CK(launch_pre(ctx->D, ctx->g, ctx->cur, 0, 1, bcand[c], ctx->st));
-            CK(cudaEventRecord(e0, ctx->st));
-            for (int r = 0; r < 3; ++r) CK(launch_pre(ctx->D, ctx->g, ctx->cur, 0, 1, bcand[c], ctx->st));
-            CK(cudaEventRecord(e1, ctx->st));
-            CK(cudaEventSynchronize(e1));
-            float ms;
-            CK(cudaEventElapsedTime(&ms, e0, e1));
-            ctx->launches += 4;
-            if (ms < best) {
-                best = ms;
-                ctx->bpb = bcand[c];
-            }
-        }
-        // the trial launches scattered base-pair forces: clear them
-        CK(cudaMemsetAsync(ctx->D.fbp, 0, sizeof(double4) * ctx->n, ctx->st));
-    }
     ctx->tuned = true;
     return SIS_OK;
 }
@@ -612,6 +590,12 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
         return SIS_ERR_CUDA;
     }
     for (int e = 0; e < kEvents; ++e) cudaEventCreate(&ctx->ev[e]);
+    {
+        int dev = 0, sms = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            sms > 0)
+            ctx->bpb = 2 * sms;
+    }
     Dev &D = ctx->D;
     const int n = ctx->n, ni = ctx->n_inst;
     int rc = 0;

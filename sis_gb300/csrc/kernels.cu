@@ -76,8 +76,8 @@ __device__ __forceinline__ V3<double> v3(const double4 &a) { return mk<double>(a
 //    in slot[s][0..7]: bond force on s+1; angle forces on s, s+1, s+2;
 //    dihedral forces on s..s+3.  Absent terms store zeros.
 //  * blocks from nbond_blocks on: base-pair records (force_bp*.F90), grid
-//    stride; mode 0 scatters forces into fbp and caches ene_bp/bp_status,
-//    mode 1 computes energies only (energy_bp*.F90) at temperature tK_in.
+//    stride; they scatter forces into fbp and cache ene_bp/bp_status
+//    (k_bp_energy computes the energies of energy_bp*.F90).
 // The global record index is mapped to (instance, slot) by binary search
 // over the per-instance prefix counts written by the last list rebuild.
 __device__ __forceinline__ bool bp_record(const Dev &D, int r, int total, int n_inst, int &slot) {
@@ -320,7 +320,7 @@ template <typename R> __device__ __forceinline__ void bp_eval(const Dev &D, cons
 
 template <typename R>
 __global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_blocks, int do_bp) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31;
     if ((int)blockIdx.x < nbond_blocks) {
         // bonded terms, one start bead per thread; flagged terms are queued in
         // shared memory and re-evaluated in FP64 on packed warps
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_
     if (threadIdx.x == 0) qn_s = 0;
     __syncthreads();
     const int total = *D.bp_total;
-    const int nbp = gridDim.x - nbond_blocks;
+    const int nbp = (int)gridDim.x - nbond_blocks;
     for (int base = ((int)blockIdx.x - nbond_blocks) * 256; base < total; base += nbp * 256) {
         int slot = -1;
         bool pass = false;
@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, doub
 // MODE 1 computes forces only (terms selected by mask) into fout.
 
 template <typename R, int G, int MODE>
-__global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
+__global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
                                               double *__restrict__ fout, int mask) {
     constexpr int BPB = 256 / G;
     __shared__ R sA[3][BPB], sB[3][BPB];
@@ -595,21 +595,29 @@ __global__ void __launch_bounds__(256) k_step(Dev D, GlobP g, int cur, const dou
         const int c = t / BPB, bb = t - c * BPB;
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
-        double fb = 0.0;
-        if (mask & 8) {
-            double *fp = reinterpret_cast<double *>(D.fbp + ii) + c;
-            fb = *fp;
-            *fp = 0.0;
-            if constexpr (sizeof(R) == 4) fb = fx_value(fb);
-        }
         double Fc;
-        if constexpr (sizeof(R) == 4) Fc = (double)(sA[c][bb] + sB[c][bb]) + fb;
-        else Fc = sA[c][bb] + sB[c][bb] + fb;
+        double *fp = reinterpret_cast<double *>(D.fbp + ii) + c;
+        if constexpr (sizeof(R) == 4) {
+            // FP32 lane sums plus the fixed-point base-pair force, one conversion to FP64
+            float fb = 0.f;
+            if (mask & 8) {
+                fb = (float)__double_as_longlong(*fp) * (float)FX_UNIT;
+                *fp = 0.0;
+            }
+            Fc = (double)(sA[c][bb] + sB[c][bb] + fb);
+        } else {
+            double fb = 0.0;
+            if (mask & 8) {
+                fb = *fp;
+                *fp = 0.0;
+            }
+            Fc = sA[c][bb] + sB[c][bb] + fb;
+        }
         if (MODE == 1) {
             fout[3 * (size_t)ii + c] = Fc;
             continue;
         }
-        Fc = Fc * (double)sScale[bb];
+        if (sScale[bb] != 1.f) Fc = Fc * (double)sScale[bb];
         const int4 bj = D.binfo[ii];
         const InstP &jp = D.ip[bj.x];
         const double4 m = D.mdc[ii];
