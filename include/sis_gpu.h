@@ -224,6 +224,27 @@ int64_t sis_gpu_kernel_launches(const sis_ctx *ctx);
  * base-pair, step and rebuild kernels.  For roofline measurements. */
 int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3);
 
+/* Temperature replica exchange on the device (src/replica_exchange.F90,
+ * src/energy_replica.F90, src/var_replica.F90:105-259; the reference runs one
+ * replica per MPI rank, here every replica is an instance of the context).
+ * sis_gpu_remd_init: temps[n_inst] is the ladder by label, strictly
+ * ascending; the instances must be replicas of one topology, salt and box,
+ * each at a distinct rung (it starts on that label).
+ * sis_gpu_remd_exchange: one exchange attempt between the pairs of labels
+ * (0,1), (2,3), ... (parity 0, the reference's odd pattern 1-2, 3-4, ...) or
+ * (1,2), (3,4), ... (parity 1), on the current coordinates: total potential
+ * energies at the own and at the partner temperature (set_ele at the
+ * partner's temperature, base-pair energies recomputed), Sugita's criterion
+ * delta = ((E_j(T_m) - E_i(T_m))/T_m - (E_j(T_n) - E_i(T_n))/T_n)/k_B, accept
+ * if delta < 0 or u <= exp(-delta); an accepted pair swaps labels and
+ * temperatures, its velocities are scaled by sqrt(T_n/T_m) (scale_velo) and
+ * its noise coefficients follow the new temperature.  uniforms: one per pair
+ * in label order (n_inst/2 + 1 values; the reference's random0), or NULL for
+ * device Philox uniforms.  rep2lab (out, may be NULL): the label of every
+ * instance afterwards; n_accepted (out, may be NULL). */
+int sis_gpu_remd_init(sis_ctx *ctx, const double *temps);
+int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, int32_t *rep2lab, int32_t *n_accepted);
+
 /* No counterpart in the reference.  sis_gpu_step with host noise (same
  * layout: nsteps x nmp x 3 doubles, step-major), but allocating nothing: it
  * stages one step's noise at a time through a fixed static device buffer

@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OBJ = ROOT / "_build"
 LIB = PKG / "_lib" / "libsisgpu.so"
-SOURCES = ["kernels.cu", "lists.cu", "api.cu"]
+SOURCES = ["kernels.cu", "lists.cu", "remd.cu", "api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-Wno-deprecated-declarations,-ffp-contract=off", "-diag-suppress", "1444"]
 

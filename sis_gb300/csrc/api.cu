@@ -95,6 +95,11 @@ struct sis_ctx {
     GlobP graph_g{};
     unsigned long long graph_passes = 0; // D.rebuilds[1] already counted in launches
     bool use_graphs = true;
+    // temperature replica exchange (remd.cu)
+    bool remd_on = false;
+    RemdDev remd{};
+    double *remd_u = nullptr; // [n_inst / 2 + 1] caller's uniforms
+    unsigned long long remd_ctr = 0;
     int n_vel_init = 0;
     bool tuned = false;
 };
@@ -122,8 +127,7 @@ template <typename T> int dalloc(sis_ctx *ctx, T **p, size_t count) {
 }
 
 // set_ele.F90:45-99 (default constants) for instance k
-void set_ele(sis_ctx *ctx, int k) {
-    InstP &I = ctx->ip[k];
+void set_ele_fields(const sis_ctx *ctx, InstP &I, double ionic) {
     const sis_params &p = ctx->p;
     const double MM_A = 87.740, MM_B = -0.40008, MM_C = 9.398e-4, MM_D = -1.410e-6;
     const double T = I.tempK;
@@ -141,7 +145,7 @@ void set_ele(sis_ctx *ctx, int k) {
     const double Zp = p.length_per_charge / lb;
     double coef = JOUL2KCAL_MOL * 1.0e10 * (ELE * ELE) / (4.0 * PI * EPS0 * diele);
     coef = coef * (Zp * Zp);
-    const double lambdaD = 1.0e10 * sqrt((1.0e-3 * EPS0 * diele * BOLTZ_J) / (2.0 * N_AVO * (ELE * ELE))) * sqrt(T / ctx->ionic[k]);
+    const double lambdaD = 1.0e10 * sqrt((1.0e-3 * EPS0 * diele * BOLTZ_J) / (2.0 * N_AVO * (ELE * ELE))) * sqrt(T / ionic);
     I.ele_coef = coef;
     I.rcdist = 1.0 / lambdaD;
     I.ele_cut = (p.ele_cutoff_type == 2) ? p.ele_cutoff_inp * lambdaD : p.ele_cutoff_inp;
@@ -152,6 +156,7 @@ void set_ele(sis_ctx *ctx, int k) {
     const double m = p.nl_margin;
     I.ele_nl_cut2 = p.flg_ele ? (I.ele_cut + m) * (I.ele_cut + m) : -1.0;
 }
+void set_ele(sis_ctx *ctx, int k) { set_ele_fields(ctx, ctx->ip[k], ctx->ionic[k]); }
 
 double diele_of(const sis_ctx *ctx, int k) {
     const double MM_A = 87.740, MM_B = -0.40008, MM_C = 9.398e-4, MM_D = -1.410e-6;
@@ -160,12 +165,25 @@ double diele_of(const sis_ctx *ctx, int k) {
 }
 
 // job_md.F90:94-133 friction and masses, set_md_coef job_md.F90:700-767
-void md_coefs(sis_ctx *ctx, std::vector<double4> &mdc) {
-    const sis_params &p = ctx->p;
+double friction_of(const sis_params &p) {
     const double radius = 10.0;
     const double v = (p.integrator == SIS_INTGRT_GJF2GJ) ? p.viscosity_Pas * sqrt(1.0e3 / KCAL2JOUL) * N_AVO * 1.0e-20
                                                           : (JOUL2KCAL_MOL * 1.0e-18) * p.viscosity_Pas;
-    const double fric = 6.0 * PI * v * radius;
+    return 6.0 * PI * v * radius;
+}
+// md_coef(4): the noise amplitude, the one coefficient that depends on T
+double noise_coef(const sis_params &p, double fric, double m, double T) {
+    const double dt = p.dt;
+    if (p.integrator == SIS_INTGRT_GJF2GJ) {
+        const double c1 = 0.5 * dt * fric / m;
+        const double c2 = sqrt(1.0 / (1.0 + c1));
+        return 0.5 * c2 / m * sqrt(2.0 * fric * BOLTZ_KCAL_MOL * T * dt);
+    }
+    return sqrt(2.0 * BOLTZ_KCAL_MOL * T * dt / fric);
+}
+void md_coefs(sis_ctx *ctx, std::vector<double4> &mdc) {
+    const sis_params &p = ctx->p;
+    const double fric = friction_of(p);
     mdc.resize(ctx->n);
     ctx->mass.resize(ctx->n);
     for (int i = 0; i < ctx->n; ++i) {
@@ -183,10 +201,9 @@ void md_coefs(sis_ctx *ctx, std::vector<double4> &mdc) {
         if (p.integrator == SIS_INTGRT_GJF2GJ) {
             const double c1 = 0.5 * dt * fric / m;
             const double c2 = sqrt(1.0 / (1.0 + c1));
-            mdc[i] = make_double4((1.0 - c1) / (1.0 + c1), c2 * dt / m, c2 * dt,
-                                  0.5 * c2 / m * sqrt(2.0 * fric * BOLTZ_KCAL_MOL * T * dt));
+            mdc[i] = make_double4((1.0 - c1) / (1.0 + c1), c2 * dt / m, c2 * dt, noise_coef(p, fric, m, T));
         } else {
-            mdc[i] = make_double4(dt / fric, 0.0, 0.0, sqrt(2.0 * BOLTZ_KCAL_MOL * T * dt / fric));
+            mdc[i] = make_double4(dt / fric, 0.0, 0.0, noise_coef(p, fric, m, T));
         }
     }
 }
@@ -250,9 +267,7 @@ int upload_ip(sis_ctx *ctx) {
 // dG = dH - T dS is rounded once per operation (as the FP64 kernels and the
 // FP64 restatement evaluate it), and the FP32 copy keeps the sign of the FP64
 // value, so the dG < 0 test of the mixed path decides as the FP64 path does.
-int upload_dgf(sis_ctx *ctx, int k) {
-    const double T = ctx->ip[k].tempK;
-    float *row = ctx->dgf.data() + (size_t)k * 469;
+void dgf_row(const sis_ctx *ctx, double T, float *row) {
     for (int h = 0; h < 469; ++h) {
         const double p = T * ctx->bp3_dS[h];
         const double v = ctx->bp3_dH[h] - p;
@@ -261,6 +276,10 @@ int upload_dgf(sis_ctx *ctx, int k) {
         if (!(v < 0.0) && !(f >= 0.f)) f = 0.f;
         row[h] = f;
     }
+}
+int upload_dgf(sis_ctx *ctx, int k) {
+    float *row = ctx->dgf.data() + (size_t)k * 469;
+    dgf_row(ctx, ctx->ip[k].tempK, row);
     CK(cudaMemcpyAsync(ctx->dgf_d + (size_t)k * 469, row, sizeof(float) * 469, cudaMemcpyHostToDevice, ctx->st));
     return SIS_OK;
 }
@@ -1228,5 +1247,131 @@ extern "C" int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const dou
     ctx->steps += nsteps;
     ctx->bp_cache = true;
     CK(cudaStreamSynchronize(ctx->st));
+    return check_err(ctx);
+}
+
+// ========================================================= replica exchange
+extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
+    if (!ctx || !temps || ctx->n_inst < 2) return SIS_ERR_ARG;
+    const int ni = ctx->n_inst;
+    for (int l = 1; l < ni; ++l)
+        if (!(temps[l] > temps[l - 1])) return fail(ctx, SIS_ERR_ARG, "remd: the temperature ladder must be strictly ascending");
+    // replicas of one topology, salt and box
+    const InstP &I0 = ctx->ip[0];
+    const int nl = I0.n;
+    for (int k = 1; k < ni; ++k) {
+        const InstP &I = ctx->ip[k];
+        bool same = I.n == nl && ctx->ionic[k] == ctx->ionic[0] && I.pbc == I0.pbc;
+        for (int d = 0; d < 3 && same; ++d) same = I.box[d] == I0.box[d];
+        for (int i = 0; i < nl && same; ++i) {
+            const int4 a = ctx->binfo[I0.bead_off + i], b = ctx->binfo[I.bead_off + i];
+            same = ctx->seq[I0.bead_off + i] == ctx->seq[I.bead_off + i] && a.y - I0.bead_off == b.y - I.bead_off && a.z == b.z &&
+                   a.w == b.w;
+        }
+        if (!same) return fail(ctx, SIS_ERR_ARG, "remd: instances must be replicas of one topology, salt and box");
+    }
+    // each replica starts on the label of its temperature
+    std::vector<int> rep2lab(ni, -1), lab2rep(ni, -1);
+    for (int k = 0; k < ni; ++k) {
+        for (int l = 0; l < ni; ++l)
+            if (temps[l] == ctx->ip[k].tempK && lab2rep[l] < 0) {
+                rep2lab[k] = l;
+                lab2rep[l] = k;
+                break;
+            }
+        if (rep2lab[k] < 0) return fail(ctx, SIS_ERR_ARG, "remd: every instance's temperature must be a distinct rung of the ladder");
+    }
+    // per-label tables: temperature fields, noise coefficient per local bead, FP32 triplet free energies
+    std::vector<InstP> lab_ip(ni, I0);
+    std::vector<double> lab_w((size_t)ni * nl);
+    std::vector<float> lab_dgf((size_t)ni * 469);
+    const double fric = friction_of(ctx->p);
+    for (int l = 0; l < ni; ++l) {
+        lab_ip[l].tempK = temps[l];
+        set_ele_fields(ctx, lab_ip[l], ctx->ionic[0]);
+        if (I0.large) {
+            const double c2 = std::max(std::max(lab_ip[l].wca_nl_cut2, lab_ip[l].ele_nl_cut2), lab_ip[l].bp_nl_cut2);
+            for (int d = 0; d < 3; ++d)
+                if (I0.cell_len[d] < sqrt(c2) * 1.0005)
+                    return fail(ctx, SIS_ERR_ARG, "remd: a rung's electrostatic cutoff exceeds the cell grid of the box");
+        }
+        for (int i = 0; i < nl; ++i) lab_w[(size_t)l * nl + i] = noise_coef(ctx->p, fric, ctx->mass[I0.bead_off + i], temps[l]);
+        dgf_row(ctx, temps[l], lab_dgf.data() + (size_t)l * 469);
+    }
+    RemdDev &R = ctx->remd;
+    if (!ctx->remd_on) {
+        int rc = 0;
+        InstP *lab_ip_d = nullptr;
+        double *lab_w_d = nullptr;
+        float *lab_dgf_d = nullptr;
+        rc |= dalloc(ctx, &R.ip2, ni);
+        rc |= dalloc(ctx, &lab_ip_d, ni);
+        rc |= dalloc(ctx, &R.ene2, (size_t)12 * ni);
+        rc |= dalloc(ctx, &R.rep2lab, ni);
+        rc |= dalloc(ctx, &R.lab2rep, ni);
+        rc |= dalloc(ctx, &R.changed, ni);
+        rc |= dalloc(ctx, &R.vscale, ni);
+        rc |= dalloc(ctx, &R.n_acc, 1);
+        rc |= dalloc(ctx, &lab_w_d, (size_t)ni * nl);
+        rc |= dalloc(ctx, &lab_dgf_d, (size_t)ni * 469);
+        rc |= dalloc(ctx, &ctx->remd_u, ni / 2 + 1);
+        if (rc) return SIS_ERR_NOMEM;
+        R.lab_ip = lab_ip_d;
+        R.lab_w = lab_w_d;
+        R.lab_dgf = lab_dgf_d;
+        R.ip = ctx->ip_d;
+        R.dgf = ctx->dgf_d;
+    }
+    R.n_local = nl;
+    CK(cudaMemcpyAsync((void *)R.lab_ip, lab_ip.data(), sizeof(InstP) * ni, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync((void *)R.lab_w, lab_w.data(), sizeof(double) * lab_w.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync((void *)R.lab_dgf, lab_dgf.data(), sizeof(float) * lab_dgf.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(R.rep2lab, rep2lab.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(R.lab2rep, lab2rep.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->remd_on = true;
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, int32_t *rep2lab, int32_t *n_accepted) {
+    if (!ctx || (parity != 0 && parity != 1)) return SIS_ERR_ARG;
+    if (!ctx->remd_on) return fail(ctx, SIS_ERR_STATE, "remd: sis_gpu_remd_init has not been called");
+    int rc = ensure_lists(ctx);
+    if (rc) return rc;
+    const int ni = ctx->n_inst;
+    const RemdDev &R = ctx->remd;
+    // energies at the replicas' own temperatures (energy_replica.F90:54-58)
+    if (ctx->g.bp_model > 0) CK(launch_bp_energy(ctx->D, ctx->g, ctx->cur, -1.0, bp_blocks(ctx), ctx->st));
+    CK(cudaMemsetAsync(ctx->D.ene, 0, sizeof(double) * 12 * ni, ctx->st));
+    CK(launch_energy(ctx->D, ctx->g, ctx->cur, ctx->st));
+    // and at their partners' temperatures (energy_replica.F90:72-121)
+    CK(launch_remd_partner_ip(ctx->D, R, ni, parity, ctx->st));
+    Dev D2 = ctx->D;
+    D2.ip = R.ip2;
+    D2.ene = R.ene2;
+    if (ctx->g.bp_model > 0) CK(launch_bp_energy(D2, ctx->g, ctx->cur, -1.0, bp_blocks(ctx), ctx->st));
+    CK(cudaMemsetAsync(R.ene2, 0, sizeof(double) * 12 * ni, ctx->st));
+    CK(launch_energy(D2, ctx->g, ctx->cur, ctx->st));
+    const double *u = nullptr;
+    if (uniforms) {
+        CK(cudaMemcpyAsync(ctx->remd_u, uniforms, sizeof(double) * (ni / 2 + 1), cudaMemcpyHostToDevice, ctx->st));
+        u = ctx->remd_u;
+    }
+    CK(launch_remd_decide(ctx->D, R, ctx->g, parity, u, BOLTZ_KCAL_MOL, ctx->remd_ctr++, ctx->st));
+    ctx->launches += 2 * (2 + (ctx->g.bp_model > 0)) + 3;
+    // lists of replicas whose electrostatic cutoff moved with the Debye length
+    if ((rc = run_rebuild(ctx, 0))) return rc;
+    int nacc = 0;
+    std::vector<int> r2l(ni);
+    CK(cudaMemcpyAsync(r2l.data(), R.rep2lab, sizeof(int) * ni, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(&nacc, R.n_acc, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(ctx->ip.data(), ctx->ip_d, sizeof(InstP) * ni, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int k = 0; k < ni; ++k) {
+        if (rep2lab) rep2lab[k] = r2l[k];
+        if (ctx->g.bp_model == 4 || ctx->g.bp_model == 5) dgf_row(ctx, ctx->ip[k].tempK, ctx->dgf.data() + (size_t)k * 469);
+    }
+    if (n_accepted) *n_accepted = nacc;
+    ctx->bp_cache = false;
     return check_err(ctx);
 }

@@ -12,6 +12,22 @@ struct RebuildPlan {
     int n_large_items, large_grid;
 };
 
+// device tables of a replica-exchange run (remd.cu)
+struct RemdDev {
+    InstP *ip;            // the context's instance records (written on a swap)
+    InstP *ip2;           // [n_inst] the same records at the partner label's temperature
+    const InstP *lab_ip;  // [n_labels] records whose temperature fields are each label's
+    double *ene2;         // [n_inst][12] energies at the partner temperature
+    int *rep2lab, *lab2rep;
+    int *changed;         // [n_inst] 0 kept, 1 velocities times vscale, 2 velocities over vscale
+    double *vscale;       // [n_inst]
+    int *n_acc;           // [1] accepted swaps of the last exchange
+    const double *lab_w;  // [n_labels][n_local] noise coefficient per label and local bead
+    int n_local;          // beads per replica
+    float *dgf;           // the context's FP32 triplet table [n_inst][469]
+    const float *lab_dgf; // [n_labels][469]
+};
+
 cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long noise_step, cudaStream_t st);
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
 cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st);
@@ -19,6 +35,9 @@ cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, i
 cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st,
                            const cudaGraphConditionalHandle *cond = nullptr);
 int step_blocks(int G, int n);
+cudaError_t launch_remd_partner_ip(const Dev &D, const RemdDev &R, int n_inst, int parity, cudaStream_t st);
+cudaError_t launch_remd_decide(const Dev &D, const RemdDev &R, const GlobP &g, int parity, const double *u, double kB,
+                               unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);

@@ -164,6 +164,25 @@ class Engine:
         """Run steady-state steps as CUDA graphs (default) or launch by launch."""
         self._ck(self.L.sis_gpu_set_graphs(self.h, int(bool(enable))))
 
+    def remd_init(self, temps):
+        """Temperature replica exchange over the instances; temps: the ladder by label."""
+        t = np.ascontiguousarray(temps, dtype=np.float64)
+        if t.size != self.n_inst:
+            raise ValueError("one temperature per instance")
+        self._ck(self.L.sis_gpu_remd_init(self.h, ptr(t)))
+
+    def remd_exchange(self, parity: int, uniforms: Optional[np.ndarray] = None):
+        """One exchange attempt; returns (label of every instance, accepted pairs)."""
+        u = None
+        if uniforms is not None:
+            u = np.zeros(self.n_inst // 2 + 1)
+            uu = np.asarray(uniforms, dtype=np.float64).ravel()
+            u[:min(u.size, uu.size)] = uu[:u.size]
+        r2l = np.zeros(self.n_inst, dtype=np.int32)
+        acc = C.c_int32()
+        self._ck(self.L.sis_gpu_remd_exchange(self.h, int(parity), ptr(u), r2l.ctypes.data_as(C.c_void_p), C.byref(acc)))
+        return r2l, int(acc.value)
+
     def get_step(self) -> int:
         v = C.c_uint64()
         self._ck(self.L.sis_gpu_get_step(self.h, C.byref(v)))
