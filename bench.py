@@ -173,21 +173,40 @@ def run_gpu(args):
     # the model (force_dih_cos.F90) diverges as a bond angle reaches 180 degrees;
     # a per-bead cap far above thermal forces keeps such events finite
     eng.set_force_cap(args.force_cap)
+    # replica exchange (BASELINE config c3): an attempt every exchange_interval
+    # MD steps, odd and even patterns alternating, inside the timed region
+    remd = args.workload == "remd"
+    rx = {"since": 0, "attempts": 0, "accepted": 0}
+    if remd:
+        eng.remd_init([inst.tempK for inst in sysm.instances])
+
+    def advance():
+        eng.step(S)
+        if remd:
+            rx["since"] += S
+            if rx["since"] >= args.exchange_interval:
+                _, acc = eng.remd_exchange(rx["attempts"] % 2)
+                rx["attempts"] += 1
+                rx["accepted"] += acc
+                rx["since"] = 0
+
     for _ in range(args.warmup):
         eng.flush_l2()
-        eng.step(S)
+        advance()
     launches0 = eng.kernel_launches()
     st0 = eng.stats()
     cap0 = st0["capped"]
+    rx0 = dict(rx)
     times = []
     barrier(world)
     with Clocks(local) as clk:
         for _ in range(args.steps):
             eng.flush_l2()
             eng.event(0)
-            eng.step(S)
+            advance()
             eng.event(1)
             times.append(eng.elapsed_ms(0, 1))
+    rx_timed = {"attempts": rx["attempts"] - rx0["attempts"], "accepted": rx["accepted"] - rx0["accepted"]}
     launches = eng.kernel_launches() - launches0
     st1 = eng.stats()
     total_ms = max_over_ranks(sum(times), world)
@@ -237,7 +256,7 @@ def run_gpu(args):
         eng.synchronize()
         t0 = time.perf_counter()
         eng.set_state(-1, x, v, a)
-        eng.step(S)
+        advance()
         x, v, a = eng.get_state(-1)
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(sum(e2e_t), world)
@@ -250,6 +269,8 @@ def run_gpu(args):
            "relax_steps": {"force_capped": args.relax, "free": args.relax},
            "force_cap": args.force_cap, "capped_bead_steps": st1["capped"] - cap0,
            "launches_before_timed": int(launches0), "step_graphs": not args.no_graphs,
+           **({"exchange_interval": args.exchange_interval, "exchange_attempts_timed": rx_timed["attempts"],
+               "exchange_pairs_accepted_timed": rx_timed["accepted"]} if remd else {}),
            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -362,6 +383,7 @@ def main():
     ap.add_argument("--force-cap", type=float, default=1000.0)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per bead of the step kernel (0: autotune)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel from the host instead of step graphs")
+    ap.add_argument("--exchange-interval", type=int, default=1000, help="MD steps between replica-exchange attempts (remd)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
