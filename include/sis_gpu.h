@@ -167,6 +167,9 @@ int sis_gpu_force_term(sis_ctx *ctx, int32_t inst, int32_t term, double *forces)
  * The base-pair slot uses the energies cached by the last force evaluation
  * while that cache is valid, as src/energy_bp.F90 does. */
 int sis_gpu_energy_sumup(sis_ctx *ctx, int32_t inst, double tempK, double *energies11);
+/* energy_rg (src/energy_rg.F90:17-26): unweighted radius of gyration of the
+ * current coordinates, for one instance or (inst = -1) every instance. */
+int sis_gpu_rg(sis_ctx *ctx, int32_t inst, double *rg);
 /* energy_kinetic (src/energy_kinetic.F90) */
 int sis_gpu_energy_kinetic(sis_ctx *ctx, int32_t inst, double *ekin);
 /* invalidates the base-pair energy cache (flg_bp_energy = .False.) */

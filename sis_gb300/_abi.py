@@ -82,6 +82,7 @@ EXPORTS = {
     "sis_gpu_force_term": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
     "sis_gpu_energy_sumup": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_void_p]),
     "sis_gpu_energy_kinetic": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    "sis_gpu_rg": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "sis_gpu_invalidate_bp_cache": (C.c_int, [C.c_void_p]),
     "sis_gpu_step": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "sis_gpu_set_condition": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),

@@ -945,6 +945,17 @@ extern "C" int sis_gpu_force_term(sis_ctx *ctx, int32_t inst, int32_t term, doub
     return force_common(ctx, inst, 1 << (term - 1), forces);
 }
 
+extern "C" int sis_gpu_rg(sis_ctx *ctx, int32_t inst, double *rg) {
+    if (!ctx || !rg || inst < -1 || inst >= ctx->n_inst) return SIS_ERR_ARG;
+    if (!ctx->state_set) return fail(ctx, SIS_ERR_STATE, "coordinates have not been set");
+    CK(launch_rg(ctx->D, ctx->g, ctx->cur, ctx->fout_d, ctx->st));
+    ctx->launches++;
+    const int off = inst < 0 ? 0 : inst, cnt = inst < 0 ? ctx->n_inst : 1;
+    CK(cudaMemcpyAsync(rg, ctx->fout_d + off, sizeof(double) * cnt, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
 extern "C" int sis_gpu_invalidate_bp_cache(sis_ctx *ctx) {
     if (!ctx) return SIS_ERR_ARG;
     ctx->bp_cache = false;

@@ -906,6 +906,47 @@ cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st
     return cudaGetLastError();
 }
 
+// energy_rg.F90:17-26: unweighted radius of gyration of each instance's
+// coordinates (two passes: centre, then mean squared distance), one block
+// per instance with a fixed-order reduction
+__device__ __forceinline__ double block_sum(double v, double *s) {
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double r = s[0];
+    __syncthreads();
+    return r;
+}
+__global__ void __launch_bounds__(256) k_rg(Dev D, int cur, double *out) {
+    __shared__ double s[256];
+    const InstP &ip = D.ip[blockIdx.x];
+    const double4 *x = D.x[cur] + ip.bead_off;
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    for (int i = threadIdx.x; i < ip.n; i += blockDim.x) {
+        cx += x[i].x;
+        cy += x[i].y;
+        cz += x[i].z;
+    }
+    cx = block_sum(cx, s) / ip.n;
+    cy = block_sum(cy, s) / ip.n;
+    cz = block_sum(cz, s) / ip.n;
+    double s2 = 0.0;
+    for (int i = threadIdx.x; i < ip.n; i += blockDim.x) {
+        const double vx = x[i].x - cx, vy = x[i].y - cy, vz = x[i].z - cz;
+        s2 += vx * vx + vy * vy + vz * vz;
+    }
+    s2 = block_sum(s2, s);
+    if (threadIdx.x == 0) out[blockIdx.x] = sqrt(s2 / ip.n);
+}
+
+cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaStream_t st) {
+    k_rg<<<g.n_inst, 256, 0, st>>>(D, cur, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st) {
     k_init_velocities<double><<<(g.n + 255) / 256, 256, 0, st>>>(D, g, ctr);
     return cudaGetLastError();

@@ -39,6 +39,7 @@ cudaError_t launch_remd_partner_ip(const Dev &D, const RemdDev &R, int n_inst, i
 cudaError_t launch_remd_decide(const Dev &D, const RemdDev &R, const GlobP &g, int parity, const double *u, double kB,
                                unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
+cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaStream_t st);
 cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 // after_step: the rebuild follows a step (k_trigger decides the flags);

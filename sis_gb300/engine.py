@@ -164,6 +164,12 @@ class Engine:
         """Run steady-state steps as CUDA graphs (default) or launch by launch."""
         self._ck(self.L.sis_gpu_set_graphs(self.h, int(bool(enable))))
 
+    def rg(self, inst: int = -1) -> np.ndarray:
+        """Radius of gyration of one instance or (inst = -1) of every instance."""
+        out = np.zeros(self.n_inst if inst < 0 else 1)
+        self._ck(self.L.sis_gpu_rg(self.h, int(inst), ptr(out)))
+        return out
+
     def remd_init(self, temps):
         """Temperature replica exchange over the instances; temps: the ladder by label."""
         t = np.ascontiguousarray(temps, dtype=np.float64)

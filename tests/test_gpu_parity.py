@@ -174,6 +174,21 @@ def test_base_pair_near_collinear_angle(sin_theta, sis_ff):
         assert max_rel(got, ref) < tol, (prec, max_rel(got, ref))
 
 
+def test_radius_of_gyration_matches_oracle(sis_ff):
+    """energy_rg.F90:17-26 for every instance of an uneven batch, after steps."""
+    sysm = uneven_batch(sis_ff, n_inst=8, lmin=20, lmax=120, seed=78)
+    eng = Engine(sysm, precision=FP64, seed=4)
+    eng.step(30)
+    x = eng.get_state(-1)[0]
+    off = sysm.offsets()
+    rg = eng.rg()
+    for k in range(len(sysm.instances)):
+        orc = Oracle.from_instance(sysm, k)
+        orc.set_xyz(0, x[off[k]:off[k + 1]])
+        assert abs(rg[k] - orc.rg(0)) <= 1e-12 * orc.rg(0), k
+        assert eng.rg(k)[0] == rg[k]
+
+
 def test_batched_instances_match_their_own_oracles(sis_ff):
     sysm = uneven_batch(sis_ff, n_inst=8, lmin=20, lmax=120, seed=77)
     eng = Engine(sysm, precision=FP64)
