@@ -248,6 +248,22 @@ int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3);
 int sis_gpu_remd_init(sis_ctx *ctx, const double *temps);
 int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, int32_t *rep2lab, int32_t *n_accepted);
 
+/* Serving slots (no counterpart in the reference, whose jobs are separate
+ * runs).  Replaces the topology, conditions and state of instance inst by a
+ * job of n_chains chains (chain_len, chain_moltype, seq and has_charge as in
+ * sis_topology, for the job's beads only) that fits in the instance's bead
+ * count; the instance's remaining beads become inert fillers (single-bead
+ * chains of sequence D, uncharged, frozen), which no list, bonded or
+ * base-pair term includes.  n_chains = 0 empties the slot.  The job's noise
+ * stream is `stream` and its step counter starts at the current step, so
+ * the job follows the same trajectory as alone in a context of its own with
+ * the same seed and stream; init_velocities != 0 draws its velocities as
+ * that context's first sis_gpu_init_velocities would, else they are zero.
+ * The slot's lists are rebuilt before returning. */
+int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, const int32_t *chain_len, const int32_t *chain_moltype,
+                      const int32_t *seq, const uint8_t *has_charge, double tempK, double ionic_strength, uint32_t stream,
+                      const double *xyz, int32_t init_velocities);
+
 /* No counterpart in the reference.  sis_gpu_step with host noise (same
  * layout: nsteps x nmp x 3 doubles, step-major), but allocating nothing: it
  * stages one step's noise at a time through a fixed static device buffer

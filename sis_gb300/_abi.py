@@ -103,6 +103,8 @@ EXPORTS = {
     "sis_gpu_step_profiled": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "sis_gpu_step_noise_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "sis_gpu_remd_init": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sis_gpu_load_slot": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                    C.c_double, C.c_uint32, C.c_void_p, C.c_int32]),
     "sis_gpu_remd_exchange": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
 }
 

@@ -1386,3 +1386,80 @@ extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double 
     ctx->bp_cache = false;
     return check_err(ctx);
 }
+
+// ===================================================== serving slots
+extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, const int32_t *chain_len,
+                                 const int32_t *chain_moltype, const int32_t *seq, const uint8_t *has_charge, double tempK,
+                                 double ionic, uint32_t stream, const double *xyz, int32_t init_velocities) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || n_chains < 0 || !(tempK > 0.0) || !(ionic > 0.0)) return SIS_ERR_ARG;
+    InstP &I = ctx->ip[inst];
+    const int off = I.bead_off, n = I.n;
+    int L = 0;
+    for (int c = 0; c < n_chains; ++c) {
+        if (!chain_len || chain_len[c] < 1) return SIS_ERR_ARG;
+        L += chain_len[c];
+    }
+    if (L > n) return fail(ctx, SIS_ERR_ARG, "load_slot: the job has more beads than the slot");
+    if (L > 0 && (!seq || !xyz)) return SIS_ERR_ARG;
+    // topology: the job's chains, then inert single-bead fillers (sequence D,
+    // uncharged: no list, bonded or base-pair term takes them; frozen below)
+    int b = off;
+    for (int c = 0; c < n_chains; ++c) {
+        const int len = chain_len[c];
+        const bool circ = chain_moltype && chain_moltype[c] == 2;
+        for (int l = 0; l < len; ++l, ++b) {
+            const int s = seq[b - off], q = has_charge ? (has_charge[b - off] ? 1 : 0) : 1;
+            if (s < 0 || s > 4) return SIS_ERR_ARG;
+            ctx->binfo[b] = make_int4(inst, off + (b - off - l), len | (circ ? (int)0x80000000u : 0), l | (s << 24) | (q << 28));
+            ctx->seq[b] = s;
+        }
+    }
+    for (; b < off + n; ++b) {
+        ctx->binfo[b] = make_int4(inst, b, 1, 4 << 24);
+        ctx->seq[b] = 4;
+    }
+    // conditions; the noise counter of the job starts at the current step
+    I.tempK = tempK;
+    ctx->ionic[inst] = ionic;
+    set_ele(ctx, inst);
+    I.stream = stream;
+    unsigned long long sc = 0;
+    CK(cudaMemcpy(&sc, ctx->D.step_ctr, sizeof(sc), cudaMemcpyDeviceToHost));
+    I.step0 = sc;
+    std::vector<double4> mdc;
+    md_coefs(ctx, mdc);
+    for (int i = off + L; i < off + n; ++i) mdc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+    CK(cudaMemcpyAsync(ctx->D.binfo + off, ctx->binfo.data() + off, sizeof(int4) * n, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->D.mass + off, ctx->mass.data() + off, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->D.mdc + off, mdc.data() + off, sizeof(double4) * n, cudaMemcpyHostToDevice, ctx->st));
+    int rc = upload_ip(ctx);
+    if (!rc) rc = upload_dgf(ctx, inst);
+    if (rc) return rc;
+    // state: the job's coordinates (fillers on its first bead), zero velocities
+    if (!ctx->pin) CK(cudaMallocHost((void **)&ctx->pin, sizeof(double4) * ctx->n));
+    CK(cudaStreamSynchronize(ctx->st));
+    double4 *h = ctx->pin;
+    for (int i = 0; i < n; ++i) {
+        const int j = i < L ? i : 0;
+        h[i] = L > 0 ? make_double4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 0.0) : make_double4(0.0, 0.0, 0.0, 0.0);
+    }
+    CK(cudaMemcpyAsync(ctx->D.x[ctx->cur] + off, h, sizeof(double4) * n, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctx->D.v + off, 0, sizeof(double4) * n, ctx->st));
+    CK(cudaMemsetAsync(ctx->D.beta + off, 0, sizeof(double4) * n, ctx->st));
+    CK(cudaMemsetAsync(ctx->D.move + off, 0, sizeof(double4) * n, ctx->st));
+    CK(launch_mirror(ctx->D, ctx->g, ctx->cur, ctx->st));
+    ctx->launches++;
+    // velocities as the first sis_gpu_init_velocities of a context would draw them
+    if (init_velocities) {
+        CK(launch_init_velocities(ctx->D, ctx->g, 1ull << 62, ctx->st, inst));
+        ctx->launches++;
+    }
+    // the slot's lists, now (with every coordinate set)
+    if (ctx->state_set) {
+        if ((rc = flag_all(ctx, inst))) return rc;
+        if ((rc = run_rebuild(ctx, 0))) return rc;
+    }
+    ctx->bp_cache = false;
+    CK(cudaStreamSynchronize(ctx->st));
+    return check_err(ctx);
+}

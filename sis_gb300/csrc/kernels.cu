@@ -807,10 +807,13 @@ __global__ void k_energy_finish(Dev D, GlobP g) {
 }
 
 // initial velocities and accels from Philox (job_md.F90:214-238)
-template <typename R> __global__ void k_init_velocities(Dev D, GlobP g, unsigned long long ctr) {
+// only_inst >= 0: that instance alone.  Frozen beads (all coefficients zero,
+// e.g. the inert filler of a serving slot) get zero velocity.
+template <typename R> __global__ void k_init_velocities(Dev D, GlobP g, unsigned long long ctr, int only_inst) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
     const int4 bi = D.binfo[i];
+    if (only_inst >= 0 && bi.x != only_inst) return;
     const double T = D.ip[bi.x].tempK;
     const double kB = 1.380649e-23 * (1.0 / 4184.0 * 6.02214076e23);
     const double c1 = sqrt(T * kB / D.mass[i]);
@@ -826,6 +829,7 @@ template <typename R> __global__ void k_init_velocities(Dev D, GlobP g, unsigned
     b.y = m.w * gauss3<double>(g.seed, li, ctr + 1, 1, ip.stream);
     b.z = m.w * gauss3<double>(g.seed, li, ctr + 1, 2, ip.stream);
     b.w = 0.0;
+    if (m.x == 0.0 && m.y == 0.0 && m.z == 0.0 && m.w == 0.0) v = make_double4(0.0, 0.0, 0.0, 0.0);
     D.v[i] = v;
     D.beta[i] = b;
 }
@@ -947,8 +951,8 @@ cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaSt
     return cudaGetLastError();
 }
 
-cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st) {
-    k_init_velocities<double><<<(g.n + 255) / 256, 256, 0, st>>>(D, g, ctr);
+cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st, int only_inst) {
+    k_init_velocities<double><<<(g.n + 255) / 256, 256, 0, st>>>(D, g, ctr, only_inst);
     return cudaGetLastError();
 }
 

@@ -40,7 +40,7 @@ cudaError_t launch_remd_decide(const Dev &D, const RemdDev &R, const GlobP &g, i
                                unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaStream_t st);
-cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st);
+cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st, int only_inst = -1);
 cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 // after_step: the rebuild follows a step (k_trigger decides the flags);
 // otherwise the flags were set by the host and k_rebuild_begin starts it

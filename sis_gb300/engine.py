@@ -170,6 +170,18 @@ class Engine:
         self._ck(self.L.sis_gpu_rg(self.h, int(inst), ptr(out)))
         return out
 
+    def load_slot(self, inst: int, chains, tempK: float, ionic_strength: float, stream: int, xyz,
+                  init_velocities: bool = False):
+        """Replace instance `inst` by a job (list of Chain) that fits its bead count."""
+        lens = np.array([len(c) for c in chains], dtype=np.int32)
+        molt = np.array([c.moltype for c in chains], dtype=np.int32)
+        seq = np.ascontiguousarray(np.concatenate([c.seq for c in chains]) if len(chains) else np.zeros(0), dtype=np.int32)
+        x = np.ascontiguousarray(xyz, dtype=np.float64) if len(chains) else np.zeros((0, 3))
+        vp = C.c_void_p
+        self._ck(self.L.sis_gpu_load_slot(self.h, int(inst), len(chains), lens.ctypes.data_as(vp), molt.ctypes.data_as(vp),
+                                          seq.ctypes.data_as(vp), None, float(tempK), float(ionic_strength), int(stream),
+                                          x.ctypes.data_as(vp), int(bool(init_velocities))))
+
     def remd_init(self, temps):
         """Temperature replica exchange over the instances; temps: the ladder by label."""
         t = np.ascontiguousarray(temps, dtype=np.float64)
