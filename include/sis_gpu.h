@@ -91,6 +91,8 @@ typedef struct sis_params {
     double tempK_ref;
     int32_t integrator;              /* SIS_INTGRT_* */
     double dt, viscosity_Pas, nl_margin;
+    int32_t nstep_bp_mc;             /* [Basepair] nstep_MC: Monte Carlo removal every n steps (0: none) */
+    int32_t max_bp_per_nt;           /* [Basepair] max_bp_per_nt */
     /* engine options (no counterpart in the reference) */
     int32_t precision;               /* SIS_PREC_* */
     uint64_t seed;                   /* Philox key for the Langevin noise */
@@ -247,6 +249,21 @@ int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3);
  * instance afterwards; n_accepted (out, may be NULL). */
 int sis_gpu_remd_init(sis_ctx *ctx, const double *temps);
 int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, int32_t *rep2lab, int32_t *n_accepted);
+
+/* Base-pair Monte Carlo removal (src/force_bp_limit_triplet.F90,
+ * job_md.F90:364-401), active when sis_params.nstep_bp_mc > 0: every
+ * nstep_bp_mc steps and after every list rebuild of an instance, its
+ * base-pair evaluation keeps each record's forces, removes pairs until no
+ * nucleotide carries more than max_bp_per_nt (the reference's selection,
+ * shuffle and Metropolis walk, on device Philox uniforms), scatters the
+ * survivors and masks the others until the next pass.  sis_gpu_bp_mc
+ * requests a pass at the next force or step evaluation of one instance (or
+ * all, inst = -1); draws, if given, are the uniforms it consumes in the
+ * reference's order (genrand_double3/double1 values), for exact parity.
+ * sis_gpu_get_bp_status: the status of every base-pair record, in the order
+ * of sis_gpu_get_list(..., SIS_LIST_BP, ...). */
+int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, int32_t n_draws);
+int sis_gpu_get_bp_status(sis_ctx *ctx, int32_t inst, uint8_t *out, int32_t cap, int32_t *n_out);
 
 /* Serving slots (no counterpart in the reference, whose jobs are separate
  * runs).  Replaces the topology, conditions and state of instance inst by a

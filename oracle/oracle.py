@@ -38,6 +38,7 @@ class or_params(C.Structure):
         ("ele_excl_bond", C.c_int32), ("ele_excl_angle", C.c_int32),
         ("temp_independent", C.c_int32), ("tempK_ref", C.c_double),
         ("integrator", C.c_int32), ("dt", C.c_double), ("viscosity_Pas", C.c_double), ("nl_margin", C.c_double),
+        ("nstep_bp_mc", C.c_int32), ("max_bp_per_nt", C.c_int32),
     ]
 
 
@@ -77,6 +78,9 @@ def lib() -> C.CDLL:
             "or_get_list": (i32, [vp, i32, i32, vp, i32]),
             "or_get_bp_coef": (i32, [vp, i32, vp, i32]),
             "or_force": (None, [vp, i32, vp]),
+            "or_force_mc": (None, [vp, i32, vp]),
+            "or_get_mc_draws": (i32, [vp, vp, i32]),
+            "or_get_bp_status": (i32, [vp, i32, vp, i32]),
             "or_force_term": (None, [vp, i32, i32, vp]),
             "or_energy_sumup": (None, [vp, i32, d, vp]),
             "or_energy_kinetic": (d, [vp, i32]),
@@ -132,6 +136,7 @@ def pack(ff, o) -> or_params:
     p.ele_excl_bond, p.ele_excl_angle = int(o.ele_excl_bond), int(o.ele_excl_angle)
     p.temp_independent, p.tempK_ref = o.temp_independent, o.tempK_ref
     p.integrator, p.dt, p.viscosity_Pas, p.nl_margin = o.integrator, o.dt, o.viscosity_Pas, o.nl_margin
+    p.nstep_bp_mc, p.max_bp_per_nt = o.nstep_bp_mc, o.max_bp_per_nt
     return p
 
 
@@ -213,6 +218,24 @@ class Oracle:
         f = np.empty((self.nmp, 3))
         self.L.or_force(self.h, r, _p(f))
         return f
+
+    def force_mc(self, r=0):
+        """Forces with the base-pair Monte Carlo removal (force_bp_limit_triplet)."""
+        f = np.zeros((self.nmp, 3))
+        self.L.or_force_mc(self.h, r, _p(f))
+        return f
+
+    def mc_draws(self):
+        n = self.L.or_get_mc_draws(self.h, None, 0)
+        out = np.zeros(n)
+        self.L.or_get_mc_draws(self.h, _p(out), n)
+        return out
+
+    def bp_status(self, r=0):
+        n = self.L.or_get_bp_status(self.h, r, None, 0)
+        out = np.zeros(n, dtype=np.uint8)
+        self.L.or_get_bp_status(self.h, r, out.ctypes.data_as(C.c_void_p), n)
+        return out
 
     def force_term(self, r, term):
         f = np.empty((self.nmp, 3))

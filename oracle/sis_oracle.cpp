@@ -114,6 +114,9 @@ struct or_system {
     std::vector<Rep> rep;
     bool flg_bp_energy;
     int64_t nrebuild;
+    int64_t istep = 0;            /* MD steps taken (job_md.F90 istep) */
+    bool mc_now = false;          /* the next force evaluation runs the base-pair MC */
+    std::vector<double> mc_draws; /* draws consumed by the last base-pair MC */
     std::vector<or_mt> mts;
     or_mt *spare_owner; /* the spare of rnd_boxmuller is shared by all replicas */
     bool spare_stored;
@@ -820,7 +823,7 @@ void force_ele(const or_system *s, int irep, double *F, int lo, int hi) {
 
 /* force_bp.F90:44-204 (model 1/3) and force_bp_triplet.F90:62-240 (model 4/5):
  * one record.  Returns true when the pair is formed (ene <= cutoff). */
-bool bp_one(const or_system *s, int irep, int ibp, double tK, double *F, double *ene_out) {
+bool bp_one(const or_system *s, int irep, int ibp, double tK, double *F, double *ene_out, double (*fout)[3] = nullptr) {
     const Rep &R = s->rep[irep];
     const int *rec = &R.bp_mp[7 * ibp];
     const int i1 = rec[0], i2 = rec[1], i3 = rec[2], i4 = rec[3], i5 = rec[4], i6 = rec[5];
@@ -939,16 +942,83 @@ bool bp_one(const or_system *s, int irep, int ibp, double tK, double *F, double 
     double ene = triplet ? b.U0 * dG * exp(-u) : b.U0 * exp(-u);
     if (ene <= s->p.bp_cutoff_energy) {
         *ene_out = ene;
-        if (F) {
-            const int ids[6] = {i1, i2, i3, i4, i5, i6};
-            for (int q = 0; q < 6; ++q) {
-                double f[3] = {ene * fb[q][0], ene * fb[q][1], ene * fb[q][2]};
-                addf(F, ids[q], f, 1.0);
-            }
+        const int ids[6] = {i1, i2, i3, i4, i5, i6};
+        for (int q = 0; q < 6; ++q) {
+            double f[3] = {ene * fb[q][0], ene * fb[q][1], ene * fb[q][2]};
+            if (F) addf(F, ids[q], f, 1.0);
+            if (fout)
+                for (int k = 0; k < 3; ++k) fout[q][k] = f[k];
         }
         return true;
     }
     return false;
+}
+
+/* force_bp_limit_triplet.F90:66-372: every record evaluated (records off the
+ * window or above the energy cut stay off), then, while any nucleotide
+ * carries more than max_bp_per_nt pairs: pick one of those nucleotides
+ * uniformly (genrand_double3), shuffle its pairs (one genrand_double3 swap
+ * per position), walk them keeping the candidate with probability
+ * exp((E_j - E_keep) / kT) (genrand_double1), and delete the survivor.  The
+ * remaining pairs' forces are added to F; their status is the mask of the
+ * steps until the next Monte Carlo pass (job_md.F90:399-401).  Models 1 and 3
+ * use the same removal on their energies: the reference's force_bp_limit.F90
+ * reads the pair type from bp_mp(3,.) (a bead index) and is not restated. */
+void bp_mc(or_system *s, int irep, double tK, double *F) {
+    Rep &R = s->rep[irep];
+    const int nbp = (int)R.bp_mp.size() / 7;
+    std::vector<double> fr((size_t)nbp * 18, 0.0);
+    std::vector<int> excess(s->nmp, -s->p.max_bp_per_nt);
+    R.bp_status.assign(nbp, 0);
+    R.ene_bp.assign(nbp, 0.0);
+    for (int ibp = 0; ibp < nbp; ++ibp) {
+        double e;
+        if (bp_one(s, irep, ibp, tK, nullptr, &e, (double(*)[3]) & fr[(size_t)18 * ibp])) {
+            R.bp_status[ibp] = 1;
+            R.ene_bp[ibp] = e;
+            excess[R.bp_mp[7 * ibp] - 1]++;
+            excess[R.bp_mp[7 * ibp + 1] - 1]++;
+        }
+    }
+    const double beta = 1.0 / (BOLTZ_KCAL_MOL * tK);
+    or_mt *mt = &s->mts[irep];
+    s->mc_draws.clear();
+    std::vector<int> list, seq;
+    for (;;) {
+        list.clear();
+        for (int i = 0; i < s->nmp; ++i)
+            if (excess[i] > 0) list.push_back(i + 1);
+        if (list.empty()) break;
+        double rnd = or_mt_double3(mt);
+        s->mc_draws.push_back(rnd);
+        const int nt = list[(int)ceil(rnd * (double)list.size()) - 1];
+        seq.clear();
+        for (int ibp = 0; ibp < nbp; ++ibp)
+            if (R.bp_status[ibp] && (R.bp_mp[7 * ibp] == nt || R.bp_mp[7 * ibp + 1] == nt)) seq.push_back(ibp);
+        const int m = (int)seq.size();
+        for (int i = 0; i < m; ++i) {
+            rnd = or_mt_double3(mt);
+            s->mc_draws.push_back(rnd);
+            std::swap(seq[i], seq[(int)ceil(rnd * (double)m) - 1]);
+        }
+        int del = seq[0];
+        for (int i = 1; i < m; ++i) {
+            const int j = seq[i];
+            const double ratio = exp((R.ene_bp[j] - R.ene_bp[del]) * beta);
+            rnd = or_mt_double1(mt);
+            s->mc_draws.push_back(rnd);
+            if (rnd < ratio) del = j;
+        }
+        R.bp_status[del] = 0;
+        R.ene_bp[del] = 0.0;
+        excess[R.bp_mp[7 * del] - 1]--;
+        excess[R.bp_mp[7 * del + 1] - 1]--;
+    }
+    for (int ibp = 0; ibp < nbp; ++ibp) {
+        if (!R.bp_status[ibp]) continue;
+        for (int q = 0; q < 6; ++q) addf(F, R.bp_mp[7 * ibp + q], &fr[(size_t)18 * ibp + 3 * q], 1.0);
+    }
+    R.bp_status_MC = R.bp_status;
 }
 
 int nthreads() {
@@ -995,7 +1065,7 @@ static void force_impl(or_system *s, int irep, double *forces, int only_term) {
             else force_angl(s, irep, F, lo, hi);
         }
         if ((only_term == 0 || only_term == 3) && s->p.dih_type != 0) { range(ndih, lo, hi); force_dih(s, irep, F, lo, hi); }
-        if (only_term == 0 || only_term == 4) {
+        if ((only_term == 0 || only_term == 4) && !s->mc_now) {
             range(nbp, lo, hi);
             for (int k = lo; k < hi; ++k) {
                 if (!R.bp_status_MC[k]) continue;
@@ -1015,10 +1085,27 @@ static void force_impl(or_system *s, int irep, double *forces, int only_term) {
         for (int t = 1; t < nt; ++t) a += ft[(size_t)t * 3 * n + i];
         forces[i] = a;
     }
+    if ((only_term == 0 || only_term == 4) && s->mc_now) bp_mc(s, irep, tK, forces);
     if (only_term == 0 || only_term == 4) s->flg_bp_energy = true;
 }
 
 extern "C" void or_force(or_system *s, int32_t irep, double *forces) { force_impl(s, irep, forces, 0); }
+extern "C" void or_force_mc(or_system *s, int32_t irep, double *forces) {
+    s->mc_now = true;
+    force_impl(s, irep, forces, 0);
+    s->mc_now = false;
+}
+extern "C" int32_t or_get_mc_draws(const or_system *s, double *out, int32_t cap) {
+    const int n = (int)s->mc_draws.size();
+    for (int i = 0; i < std::min(n, cap); ++i) out[i] = s->mc_draws[i];
+    return n;
+}
+extern "C" int32_t or_get_bp_status(const or_system *s, int32_t irep, uint8_t *out, int32_t cap) {
+    const Rep &R = s->rep[irep];
+    const int n = (int)R.bp_status.size();
+    for (int i = 0; i < std::min(n, cap); ++i) out[i] = R.bp_status[i];
+    return n;
+}
 extern "C" void or_force_term(or_system *s, int32_t irep, int32_t term, double *forces) {
     force_impl(s, irep, forces, term);
 }
@@ -1280,11 +1367,16 @@ extern "C" void or_seed(or_system *s, int32_t seed) {
 
 /* ------------------------------------------------------------- time loop */
 extern "C" void or_md_init(or_system *s) {
+    std::vector<double> f(3 * (size_t)s->nmp);
     for (int r = 0; r < s->nrep; ++r) {
         or_neighbor_list(s, r);
         std::fill(s->rep[r].xyz_move.begin(), s->rep[r].xyz_move.end(), 0.0);
+        /* job_md.F90:270-273,344-345: the set-up evaluation runs the base-pair
+           Monte Carlo and its survivors are the first mask */
+        if (s->p.nstep_bp_mc > 0) or_force_mc(s, r, f.data());
     }
     s->nrebuild = 0;
+    s->istep = 0;
 }
 
 /* job_md.F90:214-238 initial velocities and accelerations */
@@ -1309,8 +1401,13 @@ extern "C" int64_t or_run(or_system *s, int64_t nsteps, const double *noise) {
     std::vector<double> forces(3 * n), rnd(3 * n);
     int64_t before = s->nrebuild;
     for (int64_t istep = 0; istep < nsteps; ++istep) {
+        /* job_md.F90:364-367: Monte Carlo every nstep_bp_mc steps (1-based step
+           count), and after every neighbour-list rebuild (:392-394) */
+        const int nmc = s->p.nstep_bp_mc;
+        const bool mc_step = nmc > 0 && (s->istep + 1) % nmc == 0;
         for (int r = 0; r < s->nrep; ++r) {
             Rep &R = s->rep[r];
+            s->mc_now = mc_step;
             double d2max = 0.0, d2max_2nd = 0.0;
             for (int i = 0; i < n; ++i) {
                 double d2 = dot(&R.xyz_move[3 * i], &R.xyz_move[3 * i]);
@@ -1324,8 +1421,10 @@ extern "C" int64_t or_run(or_system *s, int64_t nsteps, const double *noise) {
             if (sqrt(d2max) + sqrt(d2max_2nd) > s->p.nl_margin) {
                 or_neighbor_list(s, r);
                 std::fill(R.xyz_move.begin(), R.xyz_move.end(), 0.0);
+                if (nmc > 0) s->mc_now = true;
             }
             force_impl(s, r, forces.data(), 0);
+            s->mc_now = false;
             if (noise) {
                 memcpy(rnd.data(), noise + ((size_t)istep * s->nrep + r) * 3 * n, sizeof(double) * 3 * n);
             } else {
@@ -1355,6 +1454,7 @@ extern "C" int64_t or_run(or_system *s, int64_t nsteps, const double *noise) {
                 }
             }
         }
+        s->istep++;
     }
     return s->nrebuild - before;
 }

@@ -57,6 +57,8 @@ typedef struct or_params {
     /* [MD] */
     int32_t integrator; /* 1: GJF-2GJ, 2: Ermak-McCammon */
     double dt, viscosity_Pas, nl_margin;
+    /* [Basepair] nstep_MC (0: no Monte Carlo removal), max_bp_per_nt */
+    int32_t nstep_bp_mc, max_bp_per_nt;
 } or_params;
 
 typedef struct or_system or_system;
@@ -134,6 +136,15 @@ void or_seed(or_system *s, int32_t seed);
 
 /* physical constants (const_phys.F90) for cross-checks */
 double or_const(int32_t which);
+
+/* force_bp_limit_triplet.F90: forces with the base-pair Monte Carlo removal
+ * (every record evaluated, then pairs deleted until no nucleotide carries
+ * more than max_bp_per_nt); the draws it consumed from the replica's MT
+ * stream are kept in order (or_get_mc_draws).  or_get_bp_status: the status
+ * of every record of the last force evaluation. */
+void or_force_mc(or_system *s, int32_t irep, double *forces);
+int32_t or_get_mc_draws(const or_system *s, double *out, int32_t cap);
+int32_t or_get_bp_status(const or_system *s, int32_t irep, uint8_t *out, int32_t cap);
 
 #ifdef __cplusplus
 }

@@ -44,6 +44,7 @@ class sis_params(C.Structure):
         ("ele_excl_bond", C.c_int32), ("ele_excl_angle", C.c_int32),
         ("temp_independent", C.c_int32), ("tempK_ref", C.c_double),
         ("integrator", C.c_int32), ("dt", C.c_double), ("viscosity_Pas", C.c_double), ("nl_margin", C.c_double),
+        ("nstep_bp_mc", C.c_int32), ("max_bp_per_nt", C.c_int32),
         ("precision", C.c_int32), ("seed", C.c_uint64), ("nbr_cap", C.c_int32), ("bp_cap", C.c_int32),
     ]
 
@@ -103,6 +104,8 @@ EXPORTS = {
     "sis_gpu_step_profiled": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "sis_gpu_step_noise_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "sis_gpu_remd_init": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sis_gpu_bp_mc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]),
+    "sis_gpu_get_bp_status": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "sis_gpu_load_slot": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                     C.c_double, C.c_uint32, C.c_void_p, C.c_int32]),
     "sis_gpu_remd_exchange": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
@@ -151,6 +154,7 @@ def pack_params(system: System, precision: int, seed: int = 12345, nbr_cap: int 
     p.ele_excl_bond, p.ele_excl_angle = int(o.ele_excl_bond), int(o.ele_excl_angle)
     p.temp_independent, p.tempK_ref = o.temp_independent, o.tempK_ref
     p.integrator, p.dt, p.viscosity_Pas, p.nl_margin = o.integrator, o.dt, o.viscosity_Pas, o.nl_margin
+    p.nstep_bp_mc, p.max_bp_per_nt = o.nstep_bp_mc, o.max_bp_per_nt
     p.precision, p.seed, p.nbr_cap, p.bp_cap = precision, seed, nbr_cap, bp_cap
     return p
 

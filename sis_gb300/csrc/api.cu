@@ -95,6 +95,9 @@ struct sis_ctx {
     GlobP graph_g{};
     unsigned long long graph_passes = 0; // D.rebuilds[1] already counted in launches
     bool use_graphs = true;
+    double *mc_draws_d = nullptr; // caller-supplied Monte Carlo uniforms
+    int mc_draws_cap = 0;
+    bool mc_pending = false;      // they apply to the next force or step call
     // temperature replica exchange (remd.cu)
     bool remd_on = false;
     RemdDev remd{};
@@ -337,6 +340,10 @@ int bp_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? ctx->bpb : 0; }
 int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
     CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st));
     ctx->launches++;
+    if (ctx->g.nstep_mc > 0) {
+        CK(launch_bp_mc(ctx->D, ctx->g, ctx->st));
+        ctx->launches++;
+    }
     CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, noise, ns, ctx->st));
     ctx->launches++;
     ctx->cur ^= 1;
@@ -392,6 +399,7 @@ int build_step_graph(sis_ctx *ctx) {
         int cur = ctx->cur;
         for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k) {
             e = launch_pre(ctx->D, ctx->g, cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st);
+            if (e == cudaSuccess) e = launch_bp_mc(ctx->D, ctx->g, ctx->st);
             if (e == cudaSuccess) e = launch_step(ctx->G, ctx->D, ctx->g, cur, nullptr, 0, ctx->st);
             cur ^= 1;
             if (e == cudaSuccess) e = launch_trigger(ctx->D, ctx->g, step_blocks(ctx->G, ctx->n), ctx->st, &cond[k]);
@@ -596,6 +604,8 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     g.wca_coef = 12.0 * p.wca_eps / g.wca_sig2;
     g.bp_cutoff_energy = p.bp_cutoff_energy;
     g.f_bp_cutoff_energy = (float)p.bp_cutoff_energy;
+    g.nstep_mc = (p.bp_model > 0 && p.nstep_bp_mc > 0) ? p.nstep_bp_mc : 0;
+    g.max_bp_per_nt = p.max_bp_per_nt > 0 ? p.max_bp_per_nt : 1;
     g.nl_margin = p.nl_margin;
     g.f_bond_k = (float)g.bond_k; g.f_bond_r0 = (float)g.bond_r0;
     g.f_angl_k = (float)g.angl_k; g.f_angl_t0 = (float)g.angl_t0; g.f_cos_t0 = (float)g.cos_t0;
@@ -635,6 +645,16 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.nnbr, n);
     rc |= dalloc(ctx, &D.bps, bp_total_cap);
     rc |= dalloc(ctx, &D.bps_n, bp_total_cap);
+    if (g.nstep_mc > 0) {
+        rc |= dalloc(ctx, &D.bp_mask, bp_total_cap);
+        rc |= dalloc(ctx, &D.bp_frec, (size_t)18 * bp_total_cap);
+        rc |= dalloc(ctx, &D.mc_due, ni);
+        rc |= dalloc(ctx, &D.mc_excess, n);
+        rc |= dalloc(ctx, &D.mc_list, n);
+        rc |= dalloc(ctx, &D.mc_seq, bp_total_cap);
+        rc |= dalloc(ctx, &D.mc_calls, ni);
+        rc |= dalloc(ctx, &D.mc_draw_pos, 1);
+    }
     rc |= dalloc(ctx, &D.bp_cnt, 2 * ni);
     rc |= dalloc(ctx, &D.bp_total, 1);
     rc |= dalloc(ctx, &D.ene_bp, bp_total_cap);
@@ -748,6 +768,11 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     ctx->dgf.assign((size_t)469 * ni, 0.f);
     for (int k = 0; k < ni && ok; ++k) ok &= upload_dgf(ctx, k) == SIS_OK;
     ok &= cudaStreamSynchronize(ctx->st) == cudaSuccess;
+    if (ctx->g.nstep_mc > 0) {
+        // job_md.F90:270-273: the first evaluation runs the base-pair Monte Carlo pass
+        std::vector<int> due(ni, 1);
+        ok &= cudaMemcpy(D.mc_due, due.data(), sizeof(int) * ni, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
     ok &= cudaMemcpy(ctx->items_d, items.data(), sizeof(int2) * std::max<size_t>(1, items.size()), cudaMemcpyHostToDevice) ==
           cudaSuccess;
     if (!ok) {
@@ -772,6 +797,7 @@ extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
         if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
+    if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
     delete ctx;
 }
 
@@ -927,11 +953,19 @@ static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
     const int do_bp = (mask & 8) && ctx->g.bp_model > 0;
     CK(launch_pre(ctx->D, ctx->g, ctx->cur, (mask & 7) != 0, do_bp, bp_blocks(ctx), ctx->st));
     ctx->launches++;
+    if (do_bp && ctx->g.nstep_mc > 0) {
+        CK(launch_bp_mc(ctx->D, ctx->g, ctx->st));
+        ctx->launches++;
+    }
     if (do_bp) ctx->bp_cache = true;
     CK(launch_force(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->fout_d, mask, ctx->st));
     ctx->launches++;
     if (forces) CK(cudaMemcpyAsync(forces, ctx->fout_d + 3 * (size_t)off, sizeof(double) * 3 * cnt, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    if (do_bp) {
+        ctx->D.mc_draws = nullptr;
+        ctx->mc_pending = false;
+    }
     return check_err(ctx);
 }
 
@@ -1014,10 +1048,10 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     }
     int64_t s = 0;
     bool graphs = false;
-    if (!noise && ctx->use_graphs && nsteps >= kGraphSteps) {
+    if (!noise && ctx->use_graphs && !ctx->mc_pending && nsteps >= kGraphSteps) {
         if ((rc = ensure_step_graph(ctx))) return rc;
         for (; s + kGraphSteps <= nsteps; s += kGraphSteps) CK(cudaGraphLaunch(ctx->gexec, ctx->st));
-        ctx->launches += 3 * s;
+        ctx->launches += (3 + (ctx->g.nstep_mc > 0)) * s;
         graphs = true;
     }
     for (; s < nsteps; ++s) {
@@ -1027,6 +1061,8 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     ctx->steps += nsteps;
     ctx->bp_cache = true;
     CK(cudaStreamSynchronize(ctx->st));
+    ctx->D.mc_draws = nullptr;
+    ctx->mc_pending = false;
     if (graphs) {
         // rebuild bodies the graphs actually ran
         unsigned long long passes = 0;
@@ -1462,4 +1498,42 @@ extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, c
     ctx->bp_cache = false;
     CK(cudaStreamSynchronize(ctx->st));
     return check_err(ctx);
+}
+
+// ============================================== base-pair Monte Carlo pass
+extern "C" int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, int32_t n_draws) {
+    if (!ctx || inst < -1 || inst >= ctx->n_inst || n_draws < 0 || (n_draws > 0 && !draws)) return SIS_ERR_ARG;
+    if (ctx->g.nstep_mc <= 0) return fail(ctx, SIS_ERR_STATE, "bp_mc: the context has no base-pair Monte Carlo (nstep_bp_mc = 0)");
+    const int one = 1;
+    for (int k = inst < 0 ? 0 : inst; k < (inst < 0 ? ctx->n_inst : inst + 1); ++k)
+        CK(cudaMemcpy(ctx->D.mc_due + k, &one, sizeof(int), cudaMemcpyHostToDevice));
+    if (n_draws > 0) {
+        if (n_draws > ctx->mc_draws_cap) {
+            if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
+            ctx->mc_draws_d = nullptr;
+            if (cudaMalloc(&ctx->mc_draws_d, sizeof(double) * n_draws) != cudaSuccess) return fail(ctx, SIS_ERR_NOMEM, "bp_mc draws");
+            ctx->mc_draws_cap = n_draws;
+        }
+        CK(cudaMemcpy(ctx->mc_draws_d, draws, sizeof(double) * n_draws, cudaMemcpyHostToDevice));
+        CK(cudaMemset(ctx->D.mc_draw_pos, 0, sizeof(int)));
+        ctx->D.mc_draws = ctx->mc_draws_d;
+        ctx->D.mc_n_draws = n_draws;
+        ctx->mc_pending = true;
+    }
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_get_bp_status(sis_ctx *ctx, int32_t inst, uint8_t *out, int32_t cap, int32_t *n_out) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || !n_out) return SIS_ERR_ARG;
+    const InstP &I = ctx->ip[inst];
+    int c = 0;
+    CK(cudaMemcpyAsync(&c, ctx->D.bp_cnt + inst, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    c = std::min(c, I.bp_cap);
+    *n_out = c;
+    if (out && cap > 0) {
+        CK(cudaMemcpyAsync(out, ctx->D.bp_status + I.bp_off, std::min(c, cap), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    return SIS_OK;
 }

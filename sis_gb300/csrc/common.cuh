@@ -92,6 +92,7 @@ struct GlobP {
     float f_wca_sig2, f_wca_coef, f_wca_sigma, f_wca_eps;
     unsigned long long seed;
     double fcap; // > 0: per-bead force magnitude cap (equilibration only)
+    int nstep_mc, max_bp_per_nt; // base-pair Monte Carlo removal (0: none)
 };
 
 // base-pair parameter record (var_potential.F90 basepair_parameters), index 1..6
@@ -150,6 +151,17 @@ struct Dev {
     int n_cells;
     // energies [n_inst][12] (slots 0..10 + kinetic)
     double *ene;
+    // base-pair Monte Carlo removal (force_bp_limit_triplet.F90)
+    unsigned char *bp_mask; // per staging slot: survived the last Monte Carlo pass (bp_status_MC)
+    long long *bp_frec;     // [slot][18] energy-scaled forces of the 6 beads (fixed point, or FP64 bits)
+    int *mc_due;            // [n_inst] the next base-pair evaluation runs the Monte Carlo pass
+    int *mc_excess;         // [n] pairs per nucleotide minus max_bp_per_nt
+    int *mc_list;           // [n] scratch: nucleotides with excess
+    int *mc_seq;            // [staging slots] scratch: pairs of the chosen nucleotide
+    unsigned long long *mc_calls; // [n_inst] Monte Carlo passes (Philox counter)
+    const double *mc_draws; // caller-supplied uniforms for the next pass, or NULL (Philox)
+    int *mc_draw_pos;       // [1] next caller-supplied uniform
+    int mc_n_draws;
 };
 
 // ----------------------------------------------------------------- vectors

@@ -164,7 +164,10 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
     const int type = rec.z & 0xff;
     const InstP &ip = D.ip[rec.w];
     bool pass;
-    if constexpr (sizeof(R) == 4) {
+    if (g.nstep_mc > 0 && !D.mc_due[rec.w] && !D.bp_mask[slot]) {
+        // removed by the last Monte Carlo pass (force_bp_triplet.F90:64-66)
+        pass = false;
+    } else if constexpr (sizeof(R) == 4) {
         const BPPf &bf = D.bppf[type];
         const V3<float> v = dvec32(D.mir[cur][rec.x], D.mir[cur][rec.y], ip);
         const float d2 = fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z));
@@ -212,7 +215,25 @@ __device__ __forceinline__ void bp_finish(const Dev &D, const GlobP &g, int slot
         if (e <= g.bp_cutoff_energy) {
             ene = e;
             st = 1;
-            if (scatter_all || ud <= 20.0) {
+            if (g.nstep_mc > 0 && D.mc_due[rec.w]) {
+                // Monte Carlo pass: keep the record's forces until k_bp_mc decides
+                long long *fr = D.bp_frec + (size_t)slot * 18;
+                for (int q = 0; q < 6; ++q) {
+                    const V3<double> c = e * fd[q];
+                    const double cc[3] = {c.x, c.y, c.z};
+                    for (int k = 0; k < 3; ++k) {
+                        long long w;
+                        if (g.prec == 0) w = __double_as_longlong(cc[k]);
+                        else if (!(scatter_all || ud <= 20.0)) w = 0;
+                        else if (fabs(cc[k]) < FX_LIMIT) w = fx_of(cc[k]);
+                        else {
+                            atomicOr(D.err, ERR_NONFINITE);
+                            w = 0;
+                        }
+                        fr[3 * q + k] = w;
+                    }
+                }
+            } else if (scatter_all || ud <= 20.0) {
                 const int ids[6] = {rec.x, rec.y, nb.x, nb.y, nb.z, nb.w};
 #pragma unroll
                 for (int q = 0; q < 6; ++q) {
@@ -292,6 +313,20 @@ __device__ __noinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, in
         st = e <= g.f_bp_cutoff_energy;
         if (!st) {
             e = 0.f;
+        } else if (g.nstep_mc > 0 && D.mc_due[rec.w]) {
+            // Monte Carlo pass: keep the record's forces until k_bp_mc decides
+            long long *fr = D.bp_frec + (size_t)slot * 18;
+            for (int q = 0; q < 6; ++q) {
+                const float c[3] = {e * f[q].x, e * f[q].y, e * f[q].z};
+                for (int k = 0; k < 3; ++k) {
+                    long long w = 0;
+                    if (u <= 20.f) {
+                        if (fabsf(c[k]) < FX_LIMIT) w = fx_of(c[k]);
+                        else atomicOr(D.err, ERR_NONFINITE);
+                    }
+                    fr[3 * q + k] = w;
+                }
+            }
         } else if (u <= 20.f) {
             const int ids[6] = {rec.x, rec.y, nb.x, nb.y, nb.z, nb.w};
 #pragma unroll
@@ -377,6 +412,156 @@ __global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_
     if ((int)threadIdx.x < qn_s) bp_eval<R>(D, g, cur, q[threadIdx.x]);
 }
 
+// ------------------------------------------------ base-pair Monte Carlo
+// Uniforms of the Monte Carlo pass: the caller's sequence, or Philox blocks
+// keyed by (draw, pass counter, tag bit, instance stream), turned into (0,1)
+// and [0,1] doubles the way genrand_double3 and genrand_double1 build theirs
+// from two 32-bit words (mt_stream.F90:708-769).
+__device__ double mc_uniform(const Dev &D, const GlobP &g, const InstP &ip, unsigned long long call, unsigned idx, bool closed) {
+    if (D.mc_draws) {
+        const int p = atomicAdd(D.mc_draw_pos, 1);
+        if (p < D.mc_n_draws) return D.mc_draws[p];
+        atomicOr(D.err, ERR_NONFINITE);
+        return 0.5;
+    }
+    const uint4 r = philox4x32_10(make_uint4(idx, (unsigned)call, (unsigned)(call >> 32) | 0x80000000u, ip.stream),
+                                  make_uint2((unsigned)g.seed, (unsigned)(g.seed >> 32)));
+    if (closed) return ((double)(r.x >> 5) * 67108864.0 + (double)(r.y >> 6)) * (1.0 / 9007199254740991.0);
+    return ((double)(r.x >> 6) * 67108864.0 + (double)(r.y >> 6) + 0.5) * (1.0 / 4503599627370496.0);
+}
+
+// force_bp_limit_triplet.F90:181-233 for every instance whose pass is due,
+// one block per instance: count the pairs of every nucleotide; while some
+// nucleotide carries more than max_bp_per_nt, pick one of them uniformly
+// (in index order), gather its pairs in the reference's record order (i, j),
+// shuffle them with one (0,1) draw per position, walk them keeping the
+// candidate with probability exp((E_j - E_keep)/kT) ([0,1] draws) and remove
+// the survivor; then scatter the remaining pairs' forces and store the mask.
+template <typename R> __global__ void __launch_bounds__(256) k_bp_mc(Dev D, GlobP g) {
+    const int k = blockIdx.x;
+    if (!D.mc_due[k]) return;
+    __shared__ int s_cnt, s_nt, s_m;
+    __shared__ int s_warp[8];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const InstP &ip = D.ip[k];
+    const int b0 = ip.bead_off, nb = ip.n;
+    const int seg = ip.bp_off, cnt = min(D.bp_cnt[k], ip.bp_cap);
+    for (int i = tid; i < nb; i += 256) D.mc_excess[b0 + i] = -g.max_bp_per_nt;
+    __syncthreads();
+    for (int q = tid; q < cnt; q += 256)
+        if (D.bp_status[seg + q]) {
+            const int4 rec = D.bps[seg + q];
+            atomicAdd(&D.mc_excess[rec.x], 1);
+            atomicAdd(&D.mc_excess[rec.y], 1);
+        }
+    __syncthreads();
+    const double kB = 1.380649e-23 * ((1.0 / 4184.0) * 6.02214076e23);
+    const double beta = 1.0 / (kB * ip.tempK);
+    const unsigned long long call = D.mc_calls[k];
+    unsigned draw = 0;
+    for (;;) {
+        // nucleotides with excess pairs, in index order
+        if (tid == 0) s_cnt = 0;
+        __syncthreads();
+        for (int base = 0; base < nb; base += 256) {
+            const int i = base + tid;
+            const bool f = i < nb && D.mc_excess[b0 + i] > 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, f);
+            if (lane == 0) s_warp[warp] = __popc(bal);
+            __syncthreads();
+            int before = s_cnt;
+            for (int w = 0; w < warp; ++w) before += s_warp[w];
+            if (f) D.mc_list[b0 + before + __popc(bal & ((1u << lane) - 1u))] = b0 + i;
+            __syncthreads();
+            if (tid == 0)
+                for (int w = 0; w < 8; ++w) s_cnt += s_warp[w];
+            __syncthreads();
+        }
+        const int nex = s_cnt;
+        if (nex == 0) break;
+        if (tid == 0) {
+            const double rnd = mc_uniform(D, g, ip, call, draw++, false);
+            s_nt = D.mc_list[b0 + (int)ceil(rnd * (double)nex) - 1];
+            s_m = 0;
+        }
+        __syncthreads();
+        const int nt = s_nt;
+        for (int q = tid; q < cnt; q += 256) {
+            const int slot = seg + q;
+            if (!D.bp_status[slot]) continue;
+            const int4 rec = D.bps[slot];
+            if (rec.x == nt || rec.y == nt) D.mc_seq[seg + atomicAdd(&s_m, 1)] = slot;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const int m = s_m;
+            int *sq = D.mc_seq + seg;
+            for (int a = 1; a < m; ++a) {
+                const int v = sq[a];
+                const int4 rv = D.bps[v];
+                int b = a - 1;
+                while (b >= 0) {
+                    const int4 rb = D.bps[sq[b]];
+                    if (rb.x < rv.x || (rb.x == rv.x && rb.y < rv.y)) break;
+                    sq[b + 1] = sq[b];
+                    --b;
+                }
+                sq[b + 1] = v;
+            }
+            for (int a = 0; a < m; ++a) {
+                const double rnd = mc_uniform(D, g, ip, call, draw++, false);
+                const int b = (int)ceil(rnd * (double)m) - 1;
+                const int t = sq[a];
+                sq[a] = sq[b];
+                sq[b] = t;
+            }
+            int del = sq[0];
+            for (int a = 1; a < m; ++a) {
+                const int j = sq[a];
+                const double ratio = exp((D.ene_bp[j] - D.ene_bp[del]) * beta);
+                const double rnd = mc_uniform(D, g, ip, call, draw++, true);
+                if (rnd < ratio) del = j;
+            }
+            D.bp_status[del] = 0;
+            D.ene_bp[del] = 0.0;
+            const int4 rd = D.bps[del];
+            D.mc_excess[rd.x] -= 1;
+            D.mc_excess[rd.y] -= 1;
+        }
+        __syncthreads();
+    }
+    // the survivors: mask of the following steps, and their forces
+    for (int q = tid; q < cnt; q += 256) {
+        const int slot = seg + q;
+        const unsigned char st = D.bp_status[slot];
+        D.bp_mask[slot] = st;
+        if (!st) continue;
+        const int4 rec = D.bps[slot], nb4 = D.bps_n[slot];
+        const int ids[6] = {rec.x, rec.y, nb4.x, nb4.y, nb4.z, nb4.w};
+        const long long *fr = D.bp_frec + (size_t)slot * 18;
+        for (int b = 0; b < 6; ++b) {
+            if constexpr (sizeof(R) == 4) {
+                fx_scatter(D, ids[b], fr[3 * b], fr[3 * b + 1], fr[3 * b + 2]);
+            } else {
+                atomicAdd(&D.fbp[ids[b]].x, __longlong_as_double(fr[3 * b]));
+                atomicAdd(&D.fbp[ids[b]].y, __longlong_as_double(fr[3 * b + 1]));
+                atomicAdd(&D.fbp[ids[b]].z, __longlong_as_double(fr[3 * b + 2]));
+            }
+        }
+    }
+    if (tid == 0) {
+        D.mc_due[k] = 0;
+        D.mc_calls[k] = call + 1;
+    }
+}
+
+cudaError_t launch_bp_mc(const Dev &D, const GlobP &g, cudaStream_t st) {
+    if (g.nstep_mc <= 0) return cudaSuccess;
+    if (g.prec == 0) k_bp_mc<double><<<g.n_inst, 256, 0, st>>>(D, g);
+    else k_bp_mc<float><<<g.n_inst, 256, 0, st>>>(D, g);
+    return cudaGetLastError();
+}
+
 // energy_bp.F90 / energy_bp_triplet.F90 for every record at temperature tK
 // (tK < 0: each instance's own): clamped angles, FP64 from the FP64 positions.
 __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, double tK_in) {
@@ -393,8 +578,9 @@ __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, doub
         const bool triplet = g.bp_model == 4 || g.bp_model == 5;
         double ene = 0.0, dG = 1.0;
         unsigned char st = 0;
-        bool skip = false;
-        if (triplet) {
+        // records removed by the last Monte Carlo pass (energy_bp_triplet.F90:40)
+        bool skip = g.nstep_mc > 0 && !D.bp_mask[slot];
+        if (triplet && !skip) {
             double tK = tK_in < 0 ? ip.tempK : tK_in;
             if (g.temp_indep) tK = 0.0;
             dG = __dsub_rn(D.bp3_dH[h], __dmul_rn(tK, D.bp3_dS[h]));
@@ -749,6 +935,10 @@ __global__ void __launch_bounds__(256) k_trigger(Dev D, GlobP g, int nparts, cud
         }
     }
     if (any) atomicOr(D.any, 1);
+    // job_md.F90:364-367: the next step (1-based count step_ctr + 2) runs the
+    // base-pair Monte Carlo pass every nstep_mc steps
+    if (g.nstep_mc > 0 && (D.step_ctr[0] + 2ull) % (unsigned long long)g.nstep_mc == 0ull)
+        for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) D.mc_due[k] = 1;
     __syncthreads();
     if (threadIdx.x == 0) {
         D.ticket[0] = 0u;

@@ -32,6 +32,8 @@ cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const doub
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
 cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st);
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st);
+// base-pair Monte Carlo removal of every instance whose pass is due (no-op without it)
+cudaError_t launch_bp_mc(const Dev &D, const GlobP &g, cudaStream_t st);
 cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st,
                            const cudaGraphConditionalHandle *cond = nullptr);
 int step_blocks(int G, int n);

@@ -472,6 +472,8 @@ __global__ void __launch_bounds__(1024) k_rebuild_finish(Dev D, GlobP g, int in_
     for (int k = lo; k < hi; ++k) {
         D.bp_cnt[n + k] = run;
         run += min(D.bp_cnt[k], D.ip[k].bp_cap);
+        // new records: the next evaluation runs the Monte Carlo pass (job_md.F90:392-394)
+        if (D.flag[k] && g.nstep_mc > 0) D.mc_due[k] = 1;
         D.flag[k] = 0;
     }
     if (threadIdx.x == 1023) *D.bp_total = s[1023];

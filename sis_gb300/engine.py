@@ -182,6 +182,18 @@ class Engine:
                                           seq.ctypes.data_as(vp), None, float(tempK), float(ionic_strength), int(stream),
                                           x.ctypes.data_as(vp), int(bool(init_velocities))))
 
+    def bp_mc(self, inst: int = -1, draws: Optional[np.ndarray] = None):
+        """Request a base-pair Monte Carlo pass at the next force or step evaluation."""
+        d = None if draws is None else np.ascontiguousarray(draws, dtype=np.float64)
+        self._ck(self.L.sis_gpu_bp_mc(self.h, int(inst), ptr(d), 0 if d is None else d.size))
+
+    def get_bp_status(self, inst: int) -> np.ndarray:
+        n = C.c_int32()
+        self._ck(self.L.sis_gpu_get_bp_status(self.h, inst, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.uint8)
+        self._ck(self.L.sis_gpu_get_bp_status(self.h, inst, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n)))
+        return out
+
     def remd_init(self, temps):
         """Temperature replica exchange over the instances; temps: the ladder by label."""
         t = np.ascontiguousarray(temps, dtype=np.float64)

@@ -93,6 +93,10 @@ class Options:
     dt: float = 0.05
     viscosity_Pas: float = 1e-5
     nl_margin: float = 10.0
+    # [Basepair] nstep_MC, max_bp_per_nt: base-pair Monte Carlo removal every
+    # nstep_bp_mc steps (0: none), at most max_bp_per_nt pairs per nucleotide
+    nstep_bp_mc: int = 0
+    max_bp_per_nt: int = 1
 
 
 @dataclass
