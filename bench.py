@@ -167,6 +167,8 @@ def run_gpu(args):
         eng.set_lanes(args.lanes)
     if args.no_graphs:  # every kernel launched from the host (what per-kernel profilers can see)
         eng.set_graphs(False)
+    if args.overlap >= 0:
+        eng.set_overlap(bool(args.overlap))
     eng.init_velocities()
     # equilibrate before timing (force-capped, then free dynamics; neither is
     # timed): the coil start has no WCA overlap but is far from equilibrium
@@ -426,6 +428,7 @@ def main():
     ap.add_argument("--force-cap", type=float, default=1000.0)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per bead of the step kernel (0: autotune)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel from the host instead of step graphs")
+    ap.add_argument("--overlap", type=int, default=-1, help="1/0: pair-force kernel beside the bonded pass or not (-1: default)")
     ap.add_argument("--exchange-interval", type=int, default=1000, help="MD steps between replica-exchange attempts (remd)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="job arrivals per second (serve)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window in seconds (serve)")

@@ -211,6 +211,11 @@ int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes);
  * every kernel is launched from the host.  Results are identical; per-kernel
  * profilers see only the second form. */
 int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable);
+/* 1: a step's pair forces (WCA, Debye-Hueckel) are computed by a kernel of
+ * their own on a second stream, concurrently with the bonded and base-pair
+ * pass, and the step kernel takes them from a per-bead buffer; 0 (default):
+ * one step kernel computes them.  Results are identical. */
+int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable);
 
 int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *st);
 /* Human-readable description of the last error on this context. */

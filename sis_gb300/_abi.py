@@ -94,6 +94,7 @@ EXPORTS = {
     "sis_gpu_get_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64)]),
     "sis_gpu_set_lanes": (C.c_int, [C.c_void_p, C.c_int32]),
     "sis_gpu_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sis_gpu_set_overlap": (C.c_int, [C.c_void_p, C.c_int32]),
     "sis_gpu_set_step": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sis_gpu_last_error": (C.c_char_p, [C.c_void_p]),
     "sis_gpu_event_record": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -92,9 +92,17 @@ struct sis_ctx {
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t st2 = nullptr; // captures the conditional rebuild bodies
     int graph_cur = -1, graph_G = 0, graph_bpb = 0;
+    bool graph_overlap = false;
     GlobP graph_g{};
     unsigned long long graph_passes = 0; // D.rebuilds[1] already counted in launches
     bool use_graphs = true;
+    // overlap: the step's pair forces (k_pairs) run on st3 concurrently with
+    // the bonded and base-pair pass; fork/join events.  Off by default: with
+    // k_pairs holding the register file at five blocks per SM the two passes
+    // barely overlap, and the split costs 1-3% on every workload measured.
+    bool overlap = false;
+    cudaStream_t st3 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double *mc_draws_d = nullptr; // caller-supplied Monte Carlo uniforms
     int mc_draws_cap = 0;
     bool mc_pending = false;      // they apply to the next force or step call
@@ -337,15 +345,28 @@ int inst_range(const sis_ctx *ctx, int inst, int &off, int &cnt) {
 
 int bp_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? ctx->bpb : 0; }
 
-int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
-    CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st));
-    ctx->launches++;
-    if (ctx->g.nstep_mc > 0) {
-        CK(launch_bp_mc(ctx->D, ctx->g, ctx->st));
-        ctx->launches++;
+// The forces and update of one step at buffer parity `cur` on ctx->st:
+// k_pre (+ k_bp_mc), then k_step; with overlap, k_pairs runs on st3 beside
+// k_pre and k_step takes its pair forces from fpair.
+cudaError_t enqueue_forces_update(sis_ctx *ctx, int cur, const double *noise, long long ns) {
+    cudaError_t e;
+    if (ctx->overlap) {
+        if ((e = cudaEventRecord(ctx->ev_fork, ctx->st)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(ctx->st3, ctx->ev_fork, 0)) != cudaSuccess) return e;
+        if ((e = launch_pairs(ctx->G, ctx->D, ctx->g, cur, ctx->st3)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(ctx->ev_join, ctx->st3)) != cudaSuccess) return e;
     }
-    CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, noise, ns, ctx->st));
-    ctx->launches++;
+    if ((e = launch_pre(ctx->D, ctx->g, cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st)) != cudaSuccess) return e;
+    if ((e = launch_bp_mc(ctx->D, ctx->g, ctx->st)) != cudaSuccess) return e;
+    if (!ctx->overlap) return launch_step(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
+    if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
+    return launch_step_split(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
+}
+int step_kernels(const sis_ctx *ctx) { return 2 + (ctx->g.nstep_mc > 0) + (ctx->overlap ? 1 : 0); }
+
+int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
+    CK(enqueue_forces_update(ctx, ctx->cur, noise, ns));
+    ctx->launches += step_kernels(ctx);
     ctx->cur ^= 1;
     return run_rebuild(ctx, 1);
 }
@@ -398,9 +419,7 @@ int build_step_graph(sis_ctx *ctx) {
     if (e == cudaSuccess) {
         int cur = ctx->cur;
         for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k) {
-            e = launch_pre(ctx->D, ctx->g, cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st);
-            if (e == cudaSuccess) e = launch_bp_mc(ctx->D, ctx->g, ctx->st);
-            if (e == cudaSuccess) e = launch_step(ctx->G, ctx->D, ctx->g, cur, nullptr, 0, ctx->st);
+            e = enqueue_forces_update(ctx, cur, nullptr, 0);
             cur ^= 1;
             if (e == cudaSuccess) e = launch_trigger(ctx->D, ctx->g, step_blocks(ctx->G, ctx->n), ctx->st, &cond[k]);
             if (e == cudaSuccess) e = add_rebuild_node(ctx, cond[k], cur);
@@ -420,13 +439,14 @@ int build_step_graph(sis_ctx *ctx) {
     ctx->graph_G = ctx->G;
     ctx->graph_bpb = ctx->bpb;
     ctx->graph_g = ctx->g;
+    ctx->graph_overlap = ctx->overlap;
     return SIS_OK;
 }
 
 // the step graph for the current parameters, captured again when they changed
 int ensure_step_graph(sis_ctx *ctx) {
     if (ctx->gexec && ctx->graph_cur == ctx->cur && ctx->graph_G == ctx->G && ctx->graph_bpb == ctx->bpb &&
-        memcmp(&ctx->graph_g, &ctx->g, sizeof(GlobP)) == 0)
+        ctx->graph_overlap == ctx->overlap && memcmp(&ctx->graph_g, &ctx->g, sizeof(GlobP)) == 0)
         return SIS_OK;
     return build_step_graph(ctx);
 }
@@ -697,6 +717,15 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.cell_beads, n);
     rc |= dalloc(ctx, &D.ene, (size_t)12 * ni);
     rc |= dalloc(ctx, &ctx->fout_d, (size_t)3 * n);
+    {
+        double4 *fp = nullptr;
+        rc |= dalloc(ctx, &fp, n);
+        D.fpair = fp;
+    }
+    if (cudaStreamCreateWithFlags(&ctx->st3, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        rc |= 1;
     if (rc) {
         sis_gpu_destroy(ctx);
         return SIS_ERR_NOMEM;
@@ -797,6 +826,9 @@ extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
         if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
+    if (ctx->st3) cudaStreamDestroy(ctx->st3);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
     delete ctx;
 }
@@ -1051,7 +1083,7 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     if (!noise && ctx->use_graphs && !ctx->mc_pending && nsteps >= kGraphSteps) {
         if ((rc = ensure_step_graph(ctx))) return rc;
         for (; s + kGraphSteps <= nsteps; s += kGraphSteps) CK(cudaGraphLaunch(ctx->gexec, ctx->st));
-        ctx->launches += (3 + (ctx->g.nstep_mc > 0)) * s;
+        ctx->launches += (step_kernels(ctx) + 1) * s;
         graphs = true;
     }
     for (; s < nsteps; ++s) {
@@ -1149,6 +1181,12 @@ extern "C" int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable) {
     return SIS_OK;
 }
 
+extern "C" int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable) {
+    if (!ctx || (enable != 0 && enable != 1)) return SIS_ERR_ARG;
+    ctx->overlap = enable != 0;
+    return SIS_OK;
+}
+
 extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
     if (!ctx || !s) return SIS_ERR_ARG;
     memset(s, 0, sizeof(*s));
@@ -1212,12 +1250,20 @@ extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
     double acc[3] = {0.0, 0.0, 0.0};
     cudaEvent_t *e = ctx->ev + 8; // events 8..11
     for (int64_t s = 0; s < nsteps; ++s) {
+        // the kernels one after the other on ctx->st, so that each is timed alone
         CK(cudaEventRecord(e[0], ctx->st));
         CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st));
-        ctx->launches++;
+        CK(launch_bp_mc(ctx->D, ctx->g, ctx->st));
+        ctx->launches += 1 + (ctx->g.nstep_mc > 0);
         CK(cudaEventRecord(e[1], ctx->st));
-        CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
-        ctx->launches++;
+        if (ctx->overlap) {
+            CK(launch_pairs(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->st));
+            CK(launch_step_split(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
+            ctx->launches += 2;
+        } else {
+            CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
+            ctx->launches++;
+        }
         ctx->cur ^= 1;
         CK(cudaEventRecord(e[2], ctx->st));
         rc = run_rebuild(ctx, 1);

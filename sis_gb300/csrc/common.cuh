@@ -129,6 +129,7 @@ struct Dev {
     const BPP *bpp;         // [7]
     const BPPf *bppf;       // [7]
     void *slot;             // [n][8] bonded forces per term start (float4 or double4)
+    void *fpair;            // [n] pair forces of the current step (float4 or double4)
     const short *bp3_hash;  // [4097]
     const double *bp3_dH, *bp3_dS; // [469]
     const float *bp_dgf;    // [n_inst][469] FP32 dH - T dS at each instance's

@@ -632,6 +632,81 @@ __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, doub
 // every instance (job_md.F90:376-395).
 // MODE 1 computes forces only (terms selected by mask) into fout.
 
+// Phase A of a step: WCA and Debye-Hueckel forces on bead i from its merged
+// pair list, lane `lane` of G taking every G-th entry (force_wca.F90:34-67,
+// force_ele_DH.F90:39-82); mask bit 16 WCA, bit 32 ele
+template <typename R, int G>
+__device__ __forceinline__ V3<R> pair_sum(const Dev &D, const GlobP &g, int cur, int i, int lane, const InstP &ip, int mask) {
+    V3<R> an = mk<R>(0, 0, 0);
+    const int cnt = min(D.nnbr[i], g.cap);
+    const int *__restrict__ nb = D.nbr + (size_t)i * g.cap;
+    if constexpr (sizeof(R) == 4) {
+        const uint4 mi = D.mir[cur][i];
+        const uint4 *__restrict__ mir = D.mir[cur];
+        const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
+        const float sig2 = g.f_wca_sig2, wcoef = g.f_wca_coef;
+        const float ecoef = ip.ele_coef_f, rc = ip.rcdist_f;
+        const float cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+#pragma unroll 4
+        for (int k = lane; k < cnt; k += G) {
+            const int e = __ldg(nb + k);
+            const uint4 mj = __ldg(mir + (e & IDX_MASK));
+            const float vx = (float)(int)(mi.x - mj.x) * f0;
+            const float vy = (float)(int)(mi.y - mj.y) * f1;
+            const float vz = (float)(int)(mi.z - mj.z) * f2;
+            const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+            float c = 0.f;
+            if ((e & WCA_BIT) && (mask & 16) && d2 < sig2) {
+                const float sq = __fdiv_rn(sig2, d2);
+                const float s2 = sq * sq, s4 = s2 * s2;
+                c += wcoef * (s4 * s2 * sq - s4);
+            }
+            if ((e & ELE_BIT) && (mask & 32) && d2 <= cut2) {
+                float ri = rsqrtf(d2);
+                ri = ri * fmaf(-0.5f * d2 * ri, ri, 1.5f);
+                const float r = d2 * ri;
+                c += ecoef * ri * ri * (ri + rc) * __expf(-r * rc);
+            }
+            an.x = fmaf(c, vx, an.x);
+            an.y = fmaf(c, vy, an.y);
+            an.z = fmaf(c, vz, an.z);
+        }
+    } else {
+        const R sig2 = g.wca_sig2, wcoef = g.wca_coef;
+        const R ecoef = ip.ele_coef, rc = ip.rcdist;
+        const R cut2 = g.flg_ele ? ip.ele_cut2 : R(-1);
+        const Pos<R> P = pos_of<R>(D, cur);
+        for (int k = lane; k < cnt; k += G) {
+            const int e = __ldg(nb + k);
+            const V3<R> v = P.d(i, e & IDX_MASK, ip);
+            const R c = pair_coef<R>(e, dot3(v, v), sig2, wcoef, ecoef, rc, cut2, mask);
+            an = an + c * v;
+        }
+    }
+    return an;
+}
+
+// Pair forces of every bead into fpair (float4 / double4), the step kernel's
+// phase A run by itself, so that it can overlap the bonded and base-pair pass
+template <typename R, int G> __global__ void __launch_bounds__(256, 5) k_pairs(Dev D, GlobP g, int cur) {
+    constexpr int BPB = 256 / G;
+    const int b = threadIdx.x / G, lane = threadIdx.x % G;
+    const int i_raw = blockIdx.x * BPB + b;
+    const int i = i_raw < g.n ? i_raw : g.n - 1;
+    const InstP &ip = D.ip[D.binfo[i].x];
+    V3<R> an = pair_sum<R, G>(D, g, cur, i, lane, ip, 48);
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+        an.x += __shfl_xor_sync(0xffffffffu, an.x, o, G);
+        an.y += __shfl_xor_sync(0xffffffffu, an.y, o, G);
+        an.z += __shfl_xor_sync(0xffffffffu, an.z, o, G);
+    }
+    if (lane == 0 && i_raw < g.n) {
+        using V4 = typename Vec4<R>::type;
+        reinterpret_cast<V4 *>(D.fpair)[i] = Vec4<R>::make(an);
+    }
+}
+
 template <typename R, int G, int MODE>
 __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
                                               double *__restrict__ fout, int mask) {
@@ -662,53 +737,15 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     const InstP &ip = D.ip[bi.x];
 
     // -------------------------------------------------------------- phase A
+    // (mask bit 64: the pair forces were computed by k_pairs)
     V3<R> an = mk<R>(0, 0, 0);
-    if (mask & 48) {
-        const int cnt = min(D.nnbr[i], g.cap);
-        const int *__restrict__ nb = D.nbr + (size_t)i * g.cap;
-        if constexpr (sizeof(R) == 4) {
-            const uint4 mi = D.mir[cur][i];
-            const uint4 *__restrict__ mir = D.mir[cur];
-            const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
-            const float sig2 = g.f_wca_sig2, wcoef = g.f_wca_coef;
-            const float ecoef = ip.ele_coef_f, rc = ip.rcdist_f;
-            const float cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
-#pragma unroll 4
-            for (int k = lane; k < cnt; k += G) {
-                const int e = __ldg(nb + k);
-                const uint4 mj = __ldg(mir + (e & IDX_MASK));
-                const float vx = (float)(int)(mi.x - mj.x) * f0;
-                const float vy = (float)(int)(mi.y - mj.y) * f1;
-                const float vz = (float)(int)(mi.z - mj.z) * f2;
-                const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
-                float c = 0.f;
-                if ((e & WCA_BIT) && (mask & 16) && d2 < sig2) {
-                    const float sq = __fdiv_rn(sig2, d2);
-                    const float s2 = sq * sq, s4 = s2 * s2;
-                    c += wcoef * (s4 * s2 * sq - s4);
-                }
-                if ((e & ELE_BIT) && (mask & 32) && d2 <= cut2) {
-                    float ri = rsqrtf(d2);
-                    ri = ri * fmaf(-0.5f * d2 * ri, ri, 1.5f);
-                    const float r = d2 * ri;
-                    c += ecoef * ri * ri * (ri + rc) * __expf(-r * rc);
-                }
-                an.x = fmaf(c, vx, an.x);
-                an.y = fmaf(c, vy, an.y);
-                an.z = fmaf(c, vz, an.z);
-            }
-        } else {
-            const R sig2 = g.wca_sig2, wcoef = g.wca_coef;
-            const R ecoef = ip.ele_coef, rc = ip.rcdist;
-            const R cut2 = g.flg_ele ? ip.ele_cut2 : R(-1);
-            const Pos<R> P = pos_of<R>(D, cur);
-            for (int k = lane; k < cnt; k += G) {
-                const int e = __ldg(nb + k);
-                const V3<R> v = P.d(i, e & IDX_MASK, ip);
-                const R c = pair_coef<R>(e, dot3(v, v), sig2, wcoef, ecoef, rc, cut2, mask);
-                an = an + c * v;
-            }
+    if (mask & 64) {
+        if (lane == 0) {
+            using V4 = typename Vec4<R>::type;
+            an = v3(reinterpret_cast<const V4 *>(D.fpair)[i]);
         }
+    } else if (mask & 48) {
+        an = pair_sum<R, G>(D, g, cur, i, lane, ip, mask);
     }
     // bonded: gather of slot forces, 9 contributions spread over the lanes
     V3<R> ab = mk<R>(0, 0, 0);
@@ -1061,6 +1098,33 @@ static cudaError_t launch_step_r(int G, const Dev &D, const GlobP &g, int cur, c
 cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st) {
     if (g.prec == 0) return launch_step_r<double, 0>(G, D, g, cur, noise, ns, nullptr, 63, st);
     return launch_step_r<float, 0>(G, D, g, cur, noise, ns, nullptr, 63, st);
+}
+
+// the step with its pair forces taken from fpair (k_pairs ran before it, with
+// the same G, so that every sum is formed in the same order as in one kernel)
+cudaError_t launch_step_split(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st) {
+    if (g.prec == 0) return launch_step_r<double, 0>(G, D, g, cur, noise, ns, nullptr, 63 | 64, st);
+    return launch_step_r<float, 0>(G, D, g, cur, noise, ns, nullptr, 63 | 64, st);
+}
+
+template <typename R, int G> static cudaError_t launch_pairs_g(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
+    constexpr int bpb = 256 / G;
+    k_pairs<R, G><<<(g.n + bpb - 1) / bpb, 256, 0, st>>>(D, g, cur);
+    return cudaGetLastError();
+}
+template <typename R> static cudaError_t launch_pairs_r(int G, const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
+    switch (G) {
+    case 1: return launch_pairs_g<R, 1>(D, g, cur, st);
+    case 2: return launch_pairs_g<R, 2>(D, g, cur, st);
+    case 4: return launch_pairs_g<R, 4>(D, g, cur, st);
+    case 8: return launch_pairs_g<R, 8>(D, g, cur, st);
+    case 16: return launch_pairs_g<R, 16>(D, g, cur, st);
+    default: return launch_pairs_g<R, 32>(D, g, cur, st);
+    }
+}
+cudaError_t launch_pairs(int G, const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
+    if (g.prec == 0) return launch_pairs_r<double>(G, D, g, cur, st);
+    return launch_pairs_r<float>(G, D, g, cur, st);
 }
 
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st) {

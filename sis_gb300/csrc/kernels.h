@@ -30,6 +30,9 @@ struct RemdDev {
 
 cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long noise_step, cudaStream_t st);
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
+// the step split in two: pair forces of every bead into fpair, then the step proper
+cudaError_t launch_pairs(int G, const Dev &D, const GlobP &g, int cur, cudaStream_t st);
+cudaError_t launch_step_split(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st);
 cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st);
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st);
 // base-pair Monte Carlo removal of every instance whose pass is due (no-op without it)

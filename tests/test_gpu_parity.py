@@ -332,6 +332,25 @@ def test_step_graph_equals_single_steps(name, prec, systems, sis_ff):
     assert a.get_step() == b.get_step() == nsteps
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+def test_overlapped_step_equals_fused_step(graphs, sis_ff):
+    """Pair forces in their own kernel on a second stream (default) or inside
+    the step kernel: the same trajectory bit for bit."""
+    sysm = crowded_box(sis_ff, n_chains=12, n=500, molar=0.05, seed=23, rmin=4.0)
+    a = Engine(sysm, precision=MIXED, seed=6)
+    b = Engine(sysm, precision=MIXED, seed=6)
+    b.set_overlap(False)
+    for e in (a, b):
+        e.set_lanes(8)
+        e.set_graphs(graphs)
+        e.set_force_cap(1000.0)
+        e.init_velocities()
+        e.step(80)
+    for u, w in zip(a.get_state(-1), b.get_state(-1)):
+        assert np.array_equal(u, w)
+    assert a.stats()["rebuilds"] == b.stats()["rebuilds"] > 1
+
+
 def test_instance_alone_equals_instance_in_batch(sis_ff):
     big = uneven_batch(sis_ff, n_inst=6, lmin=30, lmax=80, seed=5)
     alone = System(big.ff, big.opts, [big.instances[3]])
