@@ -334,11 +334,12 @@ def test_step_graph_equals_single_steps(name, prec, systems, sis_ff):
 
 @pytest.mark.parametrize("graphs", [True, False])
 def test_overlapped_step_equals_fused_step(graphs, sis_ff):
-    """Pair forces in their own kernel on a second stream (default) or inside
-    the step kernel: the same trajectory bit for bit."""
+    """Pair forces in their own kernel on a second stream or inside the step
+    kernel (default): the same trajectory bit for bit."""
     sysm = crowded_box(sis_ff, n_chains=12, n=500, molar=0.05, seed=23, rmin=4.0)
     a = Engine(sysm, precision=MIXED, seed=6)
     b = Engine(sysm, precision=MIXED, seed=6)
+    a.set_overlap(True)
     b.set_overlap(False)
     for e in (a, b):
         e.set_lanes(8)
