@@ -424,7 +424,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="crowded", choices=list(WORKLOADS))
     ap.add_argument("--md-steps", type=int, default=100)
-    ap.add_argument("--relax", type=int, default=1000)
+    ap.add_argument("--relax", type=int, default=3000)
     ap.add_argument("--force-cap", type=float, default=1000.0)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per bead of the step kernel (0: autotune)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel from the host instead of step graphs")
