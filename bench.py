@@ -81,9 +81,14 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the region starts once the sampler is producing samples
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.n0 = len(self.lines)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -103,7 +108,8 @@ class Clocks:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
+        # samples taken during the region (the last one before it as well, if the region was shorter than a period)
+        for l in self.lines[max(0, getattr(self, "n0", 0) - 1):]:
             f = [x.strip() for x in l.split(",")]
             if len(f) < 9:
                 continue
