@@ -289,7 +289,7 @@ def run_gpu(args):
            "gpu_launches": int(launches),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_step", "kernel_ms": step_ms,
-                        "bp_kernel_ms": ms3[0] / prof_steps, "rebuild_kernels_ms": ms3[2] / prof_steps,
+                        "bonded_bp_ms": ms3[0] / prof_steps, "trigger_rebuild_ms": ms3[2] / prof_steps,
                         "bytes_per_bead_step": bytes_per_bead},
            "clocks": clk.summary()}
     if rank == 0:

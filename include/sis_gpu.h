@@ -229,9 +229,11 @@ int sis_gpu_synchronize(sis_ctx *ctx);
 int sis_gpu_flush_l2(sis_ctx *ctx);
 /* Number of kernels this context has launched so far. */
 int64_t sis_gpu_kernel_launches(const sis_ctx *ctx);
-/* Like sis_gpu_step (Philox noise) with CUDA events around every kernel
- * group on the context's stream; ms[0..2] receive the summed durations of the
- * base-pair, step and rebuild kernels.  For roofline measurements. */
+/* Like sis_gpu_step (Philox noise), launched kernel by kernel with CUDA
+ * events around every kernel group on the context's stream; ms[0..2] receive
+ * the summed durations of the bonded and base-pair pass, the step kernel, and
+ * the trigger and rebuild kernels (launched every step, early exit when no
+ * rebuild is due).  For roofline measurements. */
 int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3);
 
 /* Temperature replica exchange on the device (src/replica_exchange.F90,

@@ -60,7 +60,8 @@ struct sis_ctx {
     GlobP g{};
     sis_params p{};
     int n = 0, n_inst = 0, cur = 0, G = 8;
-    int bpb = 2 * 152; // base-pair blocks of k_pre: two per SM (set from the device at creation)
+    int bpb = 2 * 152; // blocks of k_bp_eval and k_bp_energy: two per SM (set from the device at creation)
+    int bpt = 8 * 152; // blocks of k_bp_test: the staging capacity, at most eight per SM
     std::vector<InstP> ip;
     std::vector<int4> binfo;
     std::vector<int> seq;
@@ -103,6 +104,9 @@ struct sis_ctx {
     bool overlap = false;
     cudaStream_t st3 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // k_bonded runs on st4 beside the base-pair kernels on st; ev_bond joins it
+    cudaStream_t st4 = nullptr;
+    cudaEvent_t ev_bond = nullptr;
     double *mc_draws_d = nullptr; // caller-supplied Monte Carlo uniforms
     int mc_draws_cap = 0;
     bool mc_pending = false;      // they apply to the next force or step call
@@ -344,25 +348,41 @@ int inst_range(const sis_ctx *ctx, int inst, int &off, int &cnt) {
 }
 
 int bp_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? ctx->bpb : 0; }
+int bp_test_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? ctx->bpt : 0; }
+
+// The bonded and base-pair pass of one step at buffer parity `cur`: k_bonded
+// on st4 beside k_bp_test, k_bp_eval (+ k_bp_mc) on ctx->st,
+// joined on ctx->st.
+// The fork event ev_fork is recorded on ctx->st by the caller.
+cudaError_t enqueue_pre(sis_ctx *ctx, int cur) {
+    cudaError_t e;
+    if (ctx->g.bp_model == 0) return launch_bonded(ctx->D, ctx->g, cur, ctx->st);
+    if ((e = cudaStreamWaitEvent(ctx->st4, ctx->ev_fork, 0)) != cudaSuccess) return e;
+    if ((e = launch_bonded(ctx->D, ctx->g, cur, ctx->st4)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(ctx->ev_bond, ctx->st4)) != cudaSuccess) return e;
+    if ((e = launch_bp(ctx->D, ctx->g, cur, bp_test_blocks(ctx), bp_blocks(ctx), ctx->st)) != cudaSuccess) return e;
+    if ((e = launch_bp_mc(ctx->D, ctx->g, ctx->st)) != cudaSuccess) return e;
+    return cudaStreamWaitEvent(ctx->st, ctx->ev_bond, 0);
+}
+int pre_step_kernels(const sis_ctx *ctx) { return 1 + bp_kernels(ctx->g) + (ctx->g.nstep_mc > 0); }
 
 // The forces and update of one step at buffer parity `cur` on ctx->st:
-// k_pre (+ k_bp_mc), then k_step; with overlap, k_pairs runs on st3 beside
-// k_pre and k_step takes its pair forces from fpair.
+// the bonded and base-pair pass, then k_step; with overlap, k_pairs runs on
+// st3 beside that pass and k_step takes its pair forces from fpair.
 cudaError_t enqueue_forces_update(sis_ctx *ctx, int cur, const double *noise, long long ns) {
     cudaError_t e;
+    if ((e = cudaEventRecord(ctx->ev_fork, ctx->st)) != cudaSuccess) return e;
     if (ctx->overlap) {
-        if ((e = cudaEventRecord(ctx->ev_fork, ctx->st)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(ctx->st3, ctx->ev_fork, 0)) != cudaSuccess) return e;
         if ((e = launch_pairs(ctx->G, ctx->D, ctx->g, cur, ctx->st3)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(ctx->ev_join, ctx->st3)) != cudaSuccess) return e;
     }
-    if ((e = launch_pre(ctx->D, ctx->g, cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st)) != cudaSuccess) return e;
-    if ((e = launch_bp_mc(ctx->D, ctx->g, ctx->st)) != cudaSuccess) return e;
+    if ((e = enqueue_pre(ctx, cur)) != cudaSuccess) return e;
     if (!ctx->overlap) return launch_step(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
     if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
     return launch_step_split(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
 }
-int step_kernels(const sis_ctx *ctx) { return 2 + (ctx->g.nstep_mc > 0) + (ctx->overlap ? 1 : 0); }
+int step_kernels(const sis_ctx *ctx) { return pre_step_kernels(ctx) + 1 + (ctx->overlap ? 1 : 0); }
 
 int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
     CK(enqueue_forces_update(ctx, ctx->cur, noise, ns));
@@ -372,8 +392,8 @@ int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
 }
 
 // ----------------------------------------------------------- step graphs
-// kGraphSteps MD steps captured as one graph: per step k_pre, k_step,
-// k_trigger and a conditional (IF) node whose body is the rebuild; k_trigger
+// kGraphSteps MD steps captured as one graph: per step k_bonded beside the
+// base-pair kernels, k_step, k_trigger and a conditional (IF) node whose body is the rebuild; k_trigger
 // sets the node's condition on the device, so a step without a rebuild runs
 // three kernels and no early-exit launches.  An even step count leaves the
 // position buffer parity unchanged, so one graph serves every launch.
@@ -460,7 +480,7 @@ int autotune(sis_ctx *ctx) {
     float best = 1e30f;
     int bestG = ctx->G;
     cudaEvent_t e0 = ctx->ev[12], e1 = ctx->ev[13];
-    CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, 0, 0, ctx->st));
+    CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, 0, 0, 0, ctx->st));
     ctx->launches++;
     for (int c = 0; c < 4; ++c) {
         CK(launch_force(cand[c], ctx->D, ctx->g, ctx->cur, ctx->fout_d, 55, ctx->st)); // warm-up (mask without base pairs)
@@ -644,6 +664,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
         if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
             sms > 0)
             ctx->bpb = 2 * sms;
+        ctx->bpt = std::max(1, std::min((bp_total_cap + 255) / 256, 8 * (sms > 0 ? sms : 152)));
     }
     Dev &D = ctx->D;
     const int n = ctx->n, ni = ctx->n_inst;
@@ -665,6 +686,10 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.nnbr, n);
     rc |= dalloc(ctx, &D.bps, bp_total_cap);
     rc |= dalloc(ctx, &D.bps_n, bp_total_cap);
+    rc |= dalloc(ctx, &D.bp_win, bp_total_cap);
+    rc |= dalloc(ctx, &D.bp_nwin, 1);
+    rc |= dalloc(ctx, &D.bp_fixq, bp_total_cap);
+    rc |= dalloc(ctx, &D.bp_fixn, 1);
     if (g.nstep_mc > 0) {
         rc |= dalloc(ctx, &D.bp_mask, bp_total_cap);
         rc |= dalloc(ctx, &D.bp_frec, (size_t)18 * bp_total_cap);
@@ -703,7 +728,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.m2, ni);
     rc |= dalloc(ctx, &D.flag, ni);
     rc |= dalloc(ctx, &D.any, 1);
-    rc |= dalloc(ctx, &D.ticket, 2);
+    rc |= dalloc(ctx, &D.ticket, 3);
     rc |= dalloc(ctx, &D.part_inst, (size_t)2 * step_blocks(32, n));
     rc |= dalloc(ctx, &D.part_m, (size_t)4 * step_blocks(32, n));
     rc |= dalloc(ctx, &D.step_ctr, 1);
@@ -723,8 +748,10 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
         D.fpair = fp;
     }
     if (cudaStreamCreateWithFlags(&ctx->st3, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->st4, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_bond, cudaEventDisableTiming) != cudaSuccess)
         rc |= 1;
     if (rc) {
         sis_gpu_destroy(ctx);
@@ -827,6 +854,8 @@ extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
     if (ctx->st) cudaStreamDestroy(ctx->st);
     if (ctx->st2) cudaStreamDestroy(ctx->st2);
     if (ctx->st3) cudaStreamDestroy(ctx->st3);
+    if (ctx->st4) cudaStreamDestroy(ctx->st4);
+    if (ctx->ev_bond) cudaEventDestroy(ctx->ev_bond);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
@@ -983,8 +1012,8 @@ static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
     int rc = ensure_lists(ctx);
     if (rc) return rc;
     const int do_bp = (mask & 8) && ctx->g.bp_model > 0;
-    CK(launch_pre(ctx->D, ctx->g, ctx->cur, (mask & 7) != 0, do_bp, bp_blocks(ctx), ctx->st));
-    ctx->launches++;
+    CK(launch_pre(ctx->D, ctx->g, ctx->cur, (mask & 7) != 0, do_bp, bp_test_blocks(ctx), bp_blocks(ctx), ctx->st));
+    ctx->launches += pre_kernels(ctx->g, (mask & 7) != 0, do_bp);
     if (do_bp && ctx->g.nstep_mc > 0) {
         CK(launch_bp_mc(ctx->D, ctx->g, ctx->st));
         ctx->launches++;
@@ -1250,11 +1279,11 @@ extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
     double acc[3] = {0.0, 0.0, 0.0};
     cudaEvent_t *e = ctx->ev + 8; // events 8..11
     for (int64_t s = 0; s < nsteps; ++s) {
-        // the kernels one after the other on ctx->st, so that each is timed alone
+        // the passes one after the other on ctx->st, so that each is timed alone
         CK(cudaEventRecord(e[0], ctx->st));
-        CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, ctx->g.bp_model > 0, bp_blocks(ctx), ctx->st));
-        CK(launch_bp_mc(ctx->D, ctx->g, ctx->st));
-        ctx->launches += 1 + (ctx->g.nstep_mc > 0);
+        CK(cudaEventRecord(ctx->ev_fork, ctx->st));
+        CK(enqueue_pre(ctx, ctx->cur));
+        ctx->launches += pre_step_kernels(ctx);
         CK(cudaEventRecord(e[1], ctx->st));
         if (ctx->overlap) {
             CK(launch_pairs(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->st));

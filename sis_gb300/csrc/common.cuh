@@ -126,9 +126,13 @@ struct Dev {
     int *bp_total;          // [1] records over all instances
     double *ene_bp;         // per staging slot
     unsigned char *bp_status;
+    int *bp_win;            // [staging slots] records inside the distance window this step
+    int *bp_nwin;           // [1] their count
+    int *bp_fixq;           // [staging slots] records the FP32 pass left to the FP64 one
+    int *bp_fixn;           // [1] their count
     const BPP *bpp;         // [7]
     const BPPf *bppf;       // [7]
-    void *slot;             // [n][8] bonded forces per term start (float4 or double4)
+    void *slot;             // [8][n] bonded forces per term start (float4 or double4)
     void *fpair;            // [n] pair forces of the current step (float4 or double4)
     const short *bp3_hash;  // [4097]
     const double *bp3_dH, *bp3_dS; // [469]
@@ -139,7 +143,7 @@ struct Dev {
     unsigned long long *m1, *m2; // [n_inst] top-2 displacement^2 (bit patterns)
     int *flag;              // [n_inst] rebuild requested
     int *any;               // [1] any flag set
-    unsigned int *ticket;   // [2] last-block tickets (trigger, rebuild)
+    unsigned int *ticket;   // [3] last-block tickets (trigger, rebuild, base-pair evaluation)
     int *part_inst;         // [2 * step blocks] per-block trigger partials: instance
     unsigned long long *part_m; // [4 * step blocks] and its top-two displacement^2
     unsigned long long *step_ctr; // [1] Philox step counter

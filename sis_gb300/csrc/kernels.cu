@@ -1,17 +1,20 @@
 // Step, force, base-pair and energy kernels of libsisgpu.
 //
-// One MD step (job_md.F90:360-460) is two kernels plus the list check:
-//   k_pre   bonded terms, one thread per term start bead, written to per-term
-//           force slots (no atomics); and the base-pair 6-bead terms over the
-//           candidate list (force_bp*.F90), compacted per warp to the records
-//           inside the distance window and scattered into fbp (FP64 atomics
-//           in the FP64 path, exact int64 fixed-point atomics in the mixed
-//           path);
-//   k_step  one group of G lanes per bead: gathers the WCA and Debye-Hueckel
-//           pair forces over the bead's full pair list and the bonded slots
-//           touching the bead, adds fbp, and applies the GJF-2GJ (or
-//           Ermak-McCammon) update in FP64; per-block partials of the
-//           displacement trigger (job_md.F90:376-395) are merged by k_trigger.
+// One MD step (job_md.F90:360-460) is these kernels plus the list check:
+//   k_bonded  bonded terms, one thread per term start bead, written to
+//             per-term force slots (no atomics);
+//   k_bp_test, k_bp_eval
+//             the base-pair 6-bead terms over the candidate list
+//             (force_bp*.F90): one thread per record for the distance
+//             window, then one per windowed record, scattered into fbp (FP64
+//             atomics in the FP64 path, exact int64 fixed-point atomics in
+//             the mixed path); they run beside k_bonded;
+//   k_step    one group of G lanes per bead: gathers the WCA and
+//             Debye-Hueckel pair forces over the bead's full pair list and
+//             the bonded slots touching the bead, adds fbp, and applies the
+//             GJF-2GJ (or Ermak-McCammon) update in FP64; per-block partials
+//             of the displacement trigger (job_md.F90:376-395) are merged by
+//             k_trigger.
 // The list rebuild (lists.cu) follows and exits at once when no instance
 // asked for one.
 #include "common.cuh"
@@ -68,16 +71,16 @@ template <typename V> __device__ __forceinline__ V3<float> v3of(const float4 &a)
 __device__ __forceinline__ V3<float> v3(const float4 &a) { return mk<float>(a.x, a.y, a.z); }
 __device__ __forceinline__ V3<double> v3(const double4 &a) { return mk<double>(a.x, a.y, a.z); }
 
-// --------------------------------------------------------------- k_pre
-// Term-parallel pass before the step kernel.
-//  * blocks [0, nbond_blocks): thread s evaluates the bond (s,s+1), the angle
-//    (s,s+1,s+2) and the dihedral (s..s+3) of list_local.F90 (all three term
-//    types in every thread, so warps do not diverge) and stores their forces
-//    in slot[s][0..7]: bond force on s+1; angle forces on s, s+1, s+2;
+// ------------------------------------------------------- k_bonded, k_bp
+// Term-parallel passes before the step kernel.
+//  * k_bonded: thread s evaluates the bond (s,s+1), the angle (s,s+1,s+2)
+//    and the dihedral (s..s+3) of list_local.F90 (all three term types in
+//    every thread, so warps do not diverge) and stores their forces in
+//    slot[0..7][s]: bond force on s+1; angle forces on s, s+1, s+2;
 //    dihedral forces on s..s+3.  Absent terms store zeros.
-//  * blocks from nbond_blocks on: base-pair records (force_bp*.F90), grid
-//    stride; they scatter forces into fbp and cache ene_bp/bp_status
-//    (k_bp_energy computes the energies of energy_bp*.F90).
+//  * k_bp_test, k_bp_eval: base-pair records (force_bp*.F90), grid stride;
+//    they scatter forces into fbp and cache ene_bp/bp_status (k_bp_energy
+//    computes the energies of energy_bp*.F90).
 // The global record index is mapped to (instance, slot) by binary search
 // over the per-instance prefix counts written by the last list rebuild.
 __device__ __forceinline__ bool bp_record(const Dev &D, int r, int total, int n_inst, int &slot) {
@@ -92,52 +95,94 @@ __device__ __forceinline__ bool bp_record(const Dev &D, int r, int total, int n_
     return true;
 }
 
-// Bonded terms starting at bead s (list_local.F90 order).  The FP32 path
-// flags angle terms with |cos| > NEAR_ONE and dihedrals whose flanking angle
-// is that close to 180 degrees; the caller re-evaluates those in FP64.
+// Positions of the bonded pass: the mirror (FP32 path) or the FP64 state.
+template <typename R> struct PosLd;
+template <> struct PosLd<float> {
+    using T = uint4;
+    __device__ static T ld(const Dev &D, int cur, int i) { return __ldg(D.mir[cur] + i); }
+    __device__ static V3<float> sep(const T &a, const T &b, const InstP &ip) { return dvec32(a, b, ip); }
+};
+template <> struct PosLd<double> {
+    using T = double4;
+    __device__ static T ld(const Dev &D, int cur, int i) { return D.x[cur][i]; }
+    __device__ static V3<double> sep(const T &a, const T &b, const InstP &ip) { return dvec64(a, b, ip); }
+};
+
+// Bonded terms starting at bead s (list_local.F90 order).  The four positions
+// are loaded once and the three separations formed from them (the angle's
+// x(q1) - x(s) is the exact negation of the bond's x(s) - x(q1) in both
+// precisions).  Forces go to the slot planes slot[k][s], k = 0..7, so that a
+// warp's stores are contiguous.  In the FP32 path, an angle term with
+// |cos| > NEAR_ONE_STRICT, or a dihedral with a flanking angle that close to
+// 0 or 180 degrees, is evaluated again from cross products formed exactly
+// from the fixed-point mirror and its residuals (cross_fx); only a sine below
+// 1e-6 leaves it flagged for the caller's FP64 evaluation.
 template <typename R>
 __device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int cur, int s, bool *angle_near, bool *dih_near) {
     using V4 = typename Vec4<R>::type;
-    V4 *S = (V4 *)D.slot + (size_t)s * 8;
+    using L = PosLd<R>;
+    V4 *S = (V4 *)D.slot + s;
+    const size_t pl = (size_t)g.n;
     const int4 bi = D.binfo[s];
     const InstP &ip = D.ip[bi.x];
-    const Pos<R> P = pos_of<R>(D, cur);
     const int l = bi_lidx(bi), n = bi_clen(bi);
     const bool circ = bi_circ(bi);
     const int q1 = chain_bead(bi, l + 1), q2 = chain_bead(bi, l + 2), q3 = chain_bead(bi, l + 3);
+    const bool has_b = q1 >= 0 && (!circ || n >= 2);
+    const bool has_a = q2 >= 0 && (!circ || n >= 3);
+    const bool has_d = g.dih_type != 0 && q3 >= 0 && (!circ || n >= 4);
+    const typename L::T p0 = L::ld(D, cur, s), p1 = L::ld(D, cur, q1 >= 0 ? q1 : s), p2 = L::ld(D, cur, q2 >= 0 ? q2 : s),
+                        p3 = L::ld(D, cur, q3 >= 0 ? q3 : s);
+    const V3<R> v01 = L::sep(p0, p1, ip), v21 = L::sep(p2, p1, ip), v23 = L::sep(p2, p3, ip);
     const V3<R> z = mk<R>(0, 0, 0);
     *angle_near = *dih_near = false;
     // bond (s, s+1)
-    V3<R> fb = z;
-    if (q1 >= 0 && (!circ || n >= 2)) fb = bond_f<R>(P.d(s, q1, ip), g);
-    S[0] = Vec4<R>::make(fb);
+    const V3<R> fb = has_b ? bond_f<R>(v01, g) : z;
     // angle (s, s+1, s+2)
     V3<R> Fa[3] = {z, z, z};
-    if (q2 >= 0 && (!circ || n >= 3)) {
+    if (has_a) {
         R c;
-        angle_forces<R>(P.d(q1, s, ip), P.d(q2, q1, ip), g, Fa, &c);
+        angle_forces<R>(-v01, v21, g, Fa, &c);
         if (sizeof(R) == 4) *angle_near = fm::fabs(c) > R(NEAR_ONE_STRICT);
     }
-    S[1] = Vec4<R>::make(Fa[0]);
-    S[2] = Vec4<R>::make(Fa[1]);
-    S[3] = Vec4<R>::make(Fa[2]);
     // dihedral (s, s+1, s+2, s+3)
     V3<R> Fd[4] = {z, z, z, z};
-    if (g.dih_type != 0 && q3 >= 0 && (!circ || n >= 4)) {
+    if (has_d) {
         bool nr;
-        dih_forces<R>(P.d(s, q1, ip), P.d(q2, q1, ip), P.d(q2, q3, ip), g, Fd, &nr);
+        dih_forces<R>(v01, v21, v23, g, Fd, &nr);
         if (sizeof(R) == 4) *dih_near = nr;
     }
-    S[4] = Vec4<R>::make(Fd[0]);
-    S[5] = Vec4<R>::make(Fd[1]);
-    S[6] = Vec4<R>::make(Fd[2]);
-    S[7] = Vec4<R>::make(Fd[3]);
+    if constexpr (sizeof(R) == 4) {
+        if (*angle_near || *dih_near) {
+            const uint4 *mr = D.mir[cur];
+            const float4 *rr = D.res[cur];
+            const FxV a01 = fxv(mr, rr, s, q1), a21 = fxv(mr, rr, q2, q1);
+            float s2;
+            if (*angle_near) {
+                angle_forces_cr(-v01, v21, cross_fx(a21, a01, ip), g, Fa, &s2);
+                *angle_near = s2 < 1e-12f;
+            }
+            if (*dih_near) {
+                dih_forces_mn(v01, v21, v23, cross_fx(a01, a21, ip), cross_fx(a21, fxv(mr, rr, q2, q3), ip), g, Fd, &s2);
+                *dih_near = s2 < 1e-12f;
+            }
+        }
+    }
+    S[0] = Vec4<R>::make(fb);
+    S[pl] = Vec4<R>::make(Fa[0]);
+    S[2 * pl] = Vec4<R>::make(Fa[1]);
+    S[3 * pl] = Vec4<R>::make(Fa[2]);
+    S[4 * pl] = Vec4<R>::make(Fd[0]);
+    S[5 * pl] = Vec4<R>::make(Fd[1]);
+    S[6 * pl] = Vec4<R>::make(Fd[2]);
+    S[7 * pl] = Vec4<R>::make(Fd[3]);
 }
 
 // FP64 re-evaluation of a flagged angle (kind 0) or dihedral (kind 1) term
 // starting at bead s; overwrites its FP32 slot forces.
 __device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, int s, int kind) {
-    float4 *S = (float4 *)D.slot + (size_t)s * 8;
+    float4 *S = (float4 *)D.slot + s;
+    const size_t pl = (size_t)g.n;
     const int4 bi = D.binfo[s];
     const InstP &ip = D.ip[bi.x];
     const double4 *__restrict__ x64 = D.x[cur];
@@ -147,12 +192,12 @@ __device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, 
         V3<double> F[3];
         double c;
         angle_forces<double>(dvec64(x64[q1], x64[s], ip), dvec64(x64[q2], x64[q1], ip), g, F, &c);
-        for (int k = 0; k < 3; ++k) S[1 + k] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
+        for (int k = 0; k < 3; ++k) S[(1 + k) * pl] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
     } else {
         V3<double> F[4];
         bool nr;
         dih_forces<double>(dvec64(x64[s], x64[q1], ip), dvec64(x64[q2], x64[q1], ip), dvec64(x64[q2], x64[q3], ip), g, F, &nr);
-        for (int k = 0; k < 4; ++k) S[4 + k] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
+        for (int k = 0; k < 4; ++k) S[(4 + k) * pl] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
     }
 }
 
@@ -283,7 +328,7 @@ __device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, in
 // mirror differences and residuals (cross_fx); only if an angle is within
 // 1e-6 rad does it return true (writing nothing), so that the caller redoes
 // the record in FP64.
-__device__ __noinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, int slot) {
+__device__ __forceinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, int slot) {
     const uint4 *__restrict__ m = D.mir[cur];
     const int4 rec = D.bps[slot];
     const int4 nb = D.bps_n[slot];
@@ -345,71 +390,81 @@ __device__ __noinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, in
     return false;
 }
 
+// --------------------------------------------------- bonded and base pairs
+// Bonded terms, one start bead per thread; flagged terms are queued in shared
+// memory and re-evaluated in FP64 on packed warps.
+template <typename R> __global__ void __launch_bounds__(256) k_bonded(Dev D, GlobP g, int cur) {
+    __shared__ int qa[256], qd[256];
+    __shared__ int na, nd;
+    if (threadIdx.x == 0) na = nd = 0;
+    __syncthreads();
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < g.n) {
+        bool an, dn;
+        bonded_terms<R>(D, g, cur, s, &an, &dn);
+        if (an) qa[atomicAdd(&na, 1)] = s;
+        if (dn) qd[atomicAdd(&nd, 1)] = s;
+    }
+    __syncthreads();
+    if constexpr (sizeof(R) == 4) {
+        for (int k = threadIdx.x; k < na; k += blockDim.x) bonded_fp64(D, g, cur, qa[k], 0);
+        for (int k = threadIdx.x; k < nd; k += blockDim.x) bonded_fp64(D, g, cur, qd[k], 1);
+    }
+}
+
+// Base-pair records in two passes.  k_bp_test gives every record one thread
+// (few registers, so the whole list is resident at once) and appends the
+// records inside the distance window to bp_win, about one in ten; k_bp_eval
+// then evaluates one windowed record per thread, so the 6-bead term runs on
+// full warps.  The FP32 evaluation defers the records with a bond angle
+// within 1e-6 rad of 0 or 180 degrees (there are none in ordinary dynamics);
+// the last block of k_bp_eval to finish evaluates them in FP64 and resets the
+// counts for the next pass.  The order of bp_win does not matter: each record
+// writes its own energy and status, and forces add exactly (fixed point) in
+// the mixed path.
 template <typename R> __device__ __forceinline__ void bp_eval(const Dev &D, const GlobP &g, int cur, int slot) {
     if constexpr (sizeof(R) == 4) {
-        if (bp_eval_f(D, g, cur, slot)) bp_eval_d(D, g, cur, slot);
+        if (bp_eval_f(D, g, cur, slot)) D.bp_fixq[atomicAdd(D.bp_fixn, 1)] = slot;
     } else {
         bp_eval_d(D, g, cur, slot);
     }
 }
 
-template <typename R>
-__global__ void __launch_bounds__(256) k_pre(Dev D, GlobP g, int cur, int nbond_blocks, int do_bp) {
+template <typename R> __global__ void __launch_bounds__(256) k_bp_test(Dev D, GlobP g, int cur) {
     const int lane = threadIdx.x & 31;
-    if ((int)blockIdx.x < nbond_blocks) {
-        // bonded terms, one start bead per thread; flagged terms are queued in
-        // shared memory and re-evaluated in FP64 on packed warps
-        __shared__ int qa[256], qd[256];
-        __shared__ int na, nd;
-        if (threadIdx.x == 0) na = nd = 0;
-        __syncthreads();
-        const int s = blockIdx.x * blockDim.x + threadIdx.x;
-        if (s < g.n) {
-            bool an, dn;
-            bonded_terms<R>(D, g, cur, s, &an, &dn);
-            if (an) qa[atomicAdd(&na, 1)] = s;
-            if (dn) qd[atomicAdd(&nd, 1)] = s;
-        }
-        __syncthreads();
-        if constexpr (sizeof(R) == 4) {
-            for (int k = threadIdx.x; k < na; k += blockDim.x) bonded_fp64(D, g, cur, qa[k], 0);
-            for (int k = threadIdx.x; k < nd; k += blockDim.x) bonded_fp64(D, g, cur, qd[k], 1);
-        }
-        return;
-    }
-    if (!do_bp) return;
-    // Base-pair records: the block tests 256 records at a time and appends the
-    // ones inside the distance window to a shared queue; whenever the queue
-    // holds 256, every thread evaluates one, so the 6-bead term runs on full
-    // warps (about one candidate in ten passes the window, too few to fill a
-    // warp from a single test round).  In the FP32 path, a record with a bond
-    // angle within 0.03 rad of 0 or 180 degrees (~0.3%) is redone in FP64 at once.
-    __shared__ int q[512];
-    __shared__ int qn_s;
-    if (threadIdx.x == 0) qn_s = 0;
-    __syncthreads();
     const int total = *D.bp_total;
-    const int nbp = (int)gridDim.x - nbond_blocks;
-    for (int base = ((int)blockIdx.x - nbond_blocks) * 256; base < total; base += nbp * 256) {
+    for (int base = (int)blockIdx.x * 256; base < total; base += (int)gridDim.x * 256) {
         int slot = -1;
         bool pass = false;
         if (bp_record(D, base + (int)threadIdx.x, total, g.n_inst, slot)) pass = bp_test<R>(D, g, cur, slot);
         const unsigned bal = __ballot_sync(0xffffffffu, pass);
         int wb = 0;
-        if (lane == 0 && bal) wb = atomicAdd(&qn_s, __popc(bal));
+        if (lane == 0 && bal) wb = atomicAdd(D.bp_nwin, __popc(bal));
         wb = __shfl_sync(0xffffffffu, wb, 0);
-        if (pass) q[wb + __popc(bal & ((1u << lane) - 1u))] = slot;
-        __syncthreads();
-        const int qn = qn_s;
-        if (qn >= 256) {
-            bp_eval<R>(D, g, cur, q[threadIdx.x]);
-            __syncthreads();
-            if ((int)threadIdx.x < qn - 256) q[threadIdx.x] = q[threadIdx.x + 256];
-            if (threadIdx.x == 0) qn_s = qn - 256;
-        }
+        if (pass) D.bp_win[wb + __popc(bal & ((1u << lane) - 1u))] = slot;
+    }
+}
+
+template <typename R> __global__ void __launch_bounds__(256) k_bp_eval(Dev D, GlobP g, int cur) {
+    __shared__ int s_last;
+    const int n = *(volatile int *)D.bp_nwin;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) bp_eval<R>(D, g, cur, D.bp_win[k]);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&D.ticket[2], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if constexpr (sizeof(R) == 4) {
+        const int nf = *(volatile int *)D.bp_fixn;
+        for (int k = threadIdx.x; k < nf; k += blockDim.x) bp_eval_d(D, g, cur, D.bp_fixq[k]);
         __syncthreads();
     }
-    if ((int)threadIdx.x < qn_s) bp_eval<R>(D, g, cur, q[threadIdx.x]);
+    if (threadIdx.x == 0) {
+        *D.bp_fixn = 0;
+        *D.bp_nwin = 0;
+        D.ticket[2] = 0u;
+    }
 }
 
 // ------------------------------------------------ base-pair Monte Carlo
@@ -772,7 +827,7 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
                 k = 4 + (3 - (t - 5));
             }
             const int q = chain_bead(bi, start);
-            if ((mask & cls) && q >= 0) ab = ab + sgn * v3(S[(size_t)q * 8 + k]);
+            if ((mask & cls) && q >= 0) ab = ab + sgn * v3(S[(size_t)k * g.n + q]);
         }
     }
 #pragma unroll
@@ -1133,14 +1188,36 @@ cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *f
 }
 
 // bonded terms (if do_bonded) and base-pair forces (if do_bp) of one step
-cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st) {
-    const int nb = do_bonded ? (g.n + 255) / 256 : 0;
-    const int grid = nb + (do_bp ? bp_blocks : 0);
-    if (grid == 0) return cudaSuccess;
-    if (g.prec == 0) k_pre<double><<<grid, 256, 0, st>>>(D, g, cur, nb, do_bp);
-    else k_pre<float><<<grid, 256, 0, st>>>(D, g, cur, nb, do_bp);
+cudaError_t launch_bonded(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
+    if (g.prec == 0) k_bonded<double><<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur);
+    else k_bonded<float><<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur);
     return cudaGetLastError();
 }
+
+// test_blocks covers the staging capacity (grid stride beyond it), eval_blocks
+// the windowed records of an ordinary step
+cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int test_blocks, int eval_blocks, cudaStream_t st) {
+    if (g.prec == 0) {
+        k_bp_test<double><<<test_blocks, 256, 0, st>>>(D, g, cur);
+        k_bp_eval<double><<<eval_blocks, 256, 0, st>>>(D, g, cur);
+    } else {
+        k_bp_test<float><<<test_blocks, 256, 0, st>>>(D, g, cur);
+        k_bp_eval<float><<<eval_blocks, 256, 0, st>>>(D, g, cur);
+    }
+    return cudaGetLastError();
+}
+int bp_kernels(const GlobP &g) { return g.bp_model > 0 ? 2 : 0; }
+
+// bonded terms (if do_bonded) and base-pair forces (if do_bp), one after the
+// other on st
+cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int test_blocks, int eval_blocks,
+                       cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    if (do_bonded) e = launch_bonded(D, g, cur, st);
+    if (e == cudaSuccess && do_bp && g.bp_model > 0) e = launch_bp(D, g, cur, test_blocks, eval_blocks, st);
+    return e;
+}
+int pre_kernels(const GlobP &g, int do_bonded, int do_bp) { return (do_bonded ? 1 : 0) + (do_bp ? bp_kernels(g) : 0); }
 
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st) {
     k_bp_energy<<<bp_blocks, 256, 0, st>>>(D, g, cur, tK);

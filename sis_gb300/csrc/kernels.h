@@ -33,7 +33,13 @@ cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *f
 // the step split in two: pair forces of every bead into fpair, then the step proper
 cudaError_t launch_pairs(int G, const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_step_split(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st);
-cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int bp_blocks, cudaStream_t st);
+cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int test_blocks, int eval_blocks,
+                       cudaStream_t st);
+int pre_kernels(const GlobP &g, int do_bonded, int do_bp);
+cudaError_t launch_bonded(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
+// k_bp_test and k_bp_eval
+cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int test_blocks, int eval_blocks, cudaStream_t st);
+int bp_kernels(const GlobP &g);
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st);
 // base-pair Monte Carlo removal of every instance whose pass is due (no-op without it)
 cudaError_t launch_bp_mc(const Dev &D, const GlobP &g, cudaStream_t st);

@@ -208,6 +208,39 @@ __device__ __forceinline__ void angle_forces(const V3<T> &x21, const V3<T> &x32,
     }
 }
 
+// FP32 angle term near 0 or 180 degrees from its cross product
+// cr = x21 x x32 accurate to FP32 ulps (cross_fx).  The perpendicular
+// vectors of both forms are vector triple products,
+//   (d2132/d21) x21 - x32 = (x21 x cr)/d21,  (d2132/d32) x32 - x21 = -(x32 x cr)/d32,
+// which cancel nothing, so the forces keep FP32 relative accuracy however
+// small the sine.  *sin2 receives |cr|^2 / (d21 d32).
+__device__ __forceinline__ void angle_forces_cr(const V3<float> &x21, const V3<float> &x32, const V3<float> &cr, const GlobP &g,
+                                                V3<float> F[3], float *sin2) {
+    const float d21 = dot3(x21, x21), d32 = dot3(x32, x32), d2132 = dot3(x32, x21);
+    float t = dot3(cr, cr);
+    *sin2 = t / (d21 * d32);
+    const V3<float> p21 = (1.f / d21) * cross3(x21, cr), p32 = (-1.f / d32) * cross3(x32, cr);
+    if (!g.angl_reb) {
+        const float delta = atan2f(sqrtf(t), -d2132) - g.f_angl_t0;
+        if (t <= 1.f) t = 1.f;
+        const float f = g.f_angl_k * delta / sqrtf(t);
+        const V3<float> f21 = f * p21, f32 = f * p32;
+        F[0] = -f21;
+        F[1] = f21 - f32;
+        F[2] = f32;
+    } else {
+        const float k = g.f_angl_k, co0 = g.f_cos_t0;
+        const float a1232 = sqrtf(d21 * d32);
+        const float cs = -d2132 / a1232;
+        const float omc = t / (d21 * d32);
+        const float f = -k * (cs - co0) * (1.f - cs * co0) / (omc * omc);
+        const V3<float> f1 = (-f / a1232) * p21, f3 = (f / a1232) * p32;
+        F[0] = f1;
+        F[1] = -(f1 + f3);
+        F[2] = f3;
+    }
+}
+
 // energy_angl.F90:18-41 / energy_angl_ReB.F90 with v12 = x1 - x2, v32 = x3 - x2
 template <typename T> __device__ __forceinline__ T angle_energy_core(const V3<T> &v12, const V3<T> &v32, const GlobP &g, T *cos_out) {
     T t = dot3(v32, v12) / fm::sqrt(dot3(v12, v12) * dot3(v32, v32));
@@ -280,6 +313,37 @@ __device__ __forceinline__ void dih_forces(const V3<T> &vij, const V3<T> &vkj, c
     F[0] = fi;
     F[1] = (T(-1) + a) * fi + (-b) * fl;
     F[2] = (-a) * fi + (T(-1) + b) * fl;
+    F[3] = fl;
+}
+
+// FP32 dihedral for a flanking bond angle near 0 or 180 degrees, from
+// m = vij x vkj and n = vkj x vkl accurate to FP32 ulps (cross_fx).  The
+// sine argument vij.n equals the triple product vkl.m; it is formed with the
+// cross product of the straighter flanking angle, since a plain separation
+// nearly parallel to vkj would carry its rounding into the other form.
+// *sin2 receives the smaller squared sine of the two flanking angles.
+__device__ __forceinline__ void dih_forces_mn(const V3<float> &vij, const V3<float> &vkj, const V3<float> &vkl, const V3<float> &m,
+                                              const V3<float> &n, const GlobP &g, V3<float> F[4], float *sin2) {
+    const float akj2 = dot3(vkj, vkj), akj = sqrtf(akj2);
+    const float mm = dot3(m, m), nn = dot3(n, n);
+    const float sm = mm / (dot3(vij, vij) * akj2), sn = nn / (akj2 * dot3(vkl, vkl));
+    *sin2 = fminf(sm, sn);
+    const float y = sm < sn ? dot3(vkl, m) : dot3(vij, n);
+    const float dih = atan2f(akj * y, dot3(m, n));
+    float pre;
+    if (g.dih_type == 1) {
+        pre = -g.f_dih_k * sinf(dih + g.f_dih_p0) * akj;
+    } else {
+        const float w = g.f_dih_w;
+        const float dd = dih - g.f_dih_p0;
+        pre = (g.f_dih_k * w) * dd * expf((-0.5f * w) * (dd * dd)) * akj;
+    }
+    const V3<float> fi = (-pre / mm) * m;
+    const V3<float> fl = (pre / nn) * n;
+    const float a = dot3(vij, vkj) / akj2, b = dot3(vkl, vkj) / akj2;
+    F[0] = fi;
+    F[1] = (-1.f + a) * fi + (-b) * fl;
+    F[2] = (-a) * fi + (-1.f + b) * fl;
     F[3] = fl;
 }
 

@@ -51,6 +51,29 @@ def near_collinear_bp_system(ff, sin_theta):
     return System(ff, Options(bp_model=1), [inst])
 
 
+def near_straight_chain_system(ff, sin_theta):
+    """Five beads whose middle bond angle 1-2-3 has sine sin_theta (nearly
+    180 deg): it is the angle term's own angle and a flanking angle of both
+    dihedrals; the outer angles sit near 150 deg, out of plane."""
+    ex, ey = np.array([1.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0])
+    phi = np.arcsin(sin_theta)
+    x2 = np.zeros(3)
+    x1 = x2 - 5.84 * ex
+    x3 = x2 + 5.84 * (np.cos(phi) * ex + np.sin(phi) * ey)
+
+    def arm(a, b, e):
+        u = (b - a) / np.linalg.norm(b - a)
+        e = np.asarray(e, float) - (np.asarray(e, float) @ u) * u
+        e /= np.linalg.norm(e)
+        t = np.pi - 2.6
+        return b + 5.84 * (np.cos(t) * u + np.sin(t) * e)
+
+    x0 = arm(x2, x1, [0.0, 0.6, 0.8])
+    x4 = arm(x2, x3, [0.0, -0.3, 0.95])
+    inst = Instance([Chain.from_string("AAAAA")], tempK=300.0, ionic_strength=0.15, xyz=np.stack([x0, x1, x2, x3, x4]))
+    return System(ff, Options(bp_model=1), [inst])
+
+
 def circ_system(ff):
     rng = np.random.default_rng(9)
     seq = rng.integers(0, 4, 48).astype(np.int32)
@@ -152,6 +175,25 @@ def test_mixed_precision_force_error(name, systems):
     eng.invalidate_bp_cache()
     e = eng.energy_sumup(0)
     assert abs(e[0] - eref[0]) <= 1e-5 * np.abs(eref[1:7]).sum()
+
+
+@pytest.mark.parametrize("sin_theta", [0.02, 1e-2, 1e-3, 1e-4, 1e-5])
+def test_bonded_near_straight_angle(sin_theta, sis_ff):
+    """A bond angle within 0.8 deg of 180 deg: the mixed path evaluates the
+    angle term and the two dihedrals it flanks again from cross products
+    formed exactly from the fixed-point mirror (cross_fx) and keeps the 1e-5
+    bar down to sin = 1e-5 without FP64.  The dihedral forces grow as
+    1/sin there.  The FP64 tolerance follows the eps / sin^2 conditioning of
+    the reference's formulas, as for the base-pair angles."""
+    sysm = near_straight_chain_system(sis_ff, sin_theta)
+    orc = oracle_for(sysm)
+    tol64 = max(FORCE_TOL_FP64, 2.2e-16 / sin_theta ** 2)
+    for term in (2, 3):
+        ref = orc.force_term(0, term)
+        assert np.abs(ref).max() > 1e-3
+        for prec, tol in ((FP64, tol64), (MIXED, FORCE_RMS_TOL_MIXED)):
+            got = Engine(sysm, precision=prec).force_term(0, term)
+            assert max_rel(got, ref) < tol, (term, prec, max_rel(got, ref))
 
 
 @pytest.mark.parametrize("sin_theta", [0.1, 0.031, 0.029, 1e-3, 3e-5])
