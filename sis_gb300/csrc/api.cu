@@ -62,6 +62,7 @@ struct sis_ctx {
     int n = 0, n_inst = 0, cur = 0, G = 8;
     int bpb = 2 * 152; // blocks of k_bp_eval and k_bp_energy: two per SM (set from the device at creation)
     int bpt = 8 * 152; // blocks of k_bp_test: the staging capacity, at most eight per SM
+    int coop_grid = 0;  // blocks of the cooperative trigger/rebuild kernel (set at creation)
     std::vector<InstP> ip;
     std::vector<int4> binfo;
     std::vector<int> seq;
@@ -91,11 +92,9 @@ struct sis_ctx {
     // steady-state step graph (kGraphSteps steps, rebuild bodies behind
     // conditional nodes) and the parameters it was captured with
     cudaGraphExec_t gexec = nullptr;
-    cudaStream_t st2 = nullptr; // captures the conditional rebuild bodies
     int graph_cur = -1, graph_G = 0, graph_bpb = 0;
     bool graph_overlap = false;
     GlobP graph_g{};
-    unsigned long long graph_passes = 0; // D.rebuilds[1] already counted in launches
     bool use_graphs = true;
     // overlap: the step's pair forces (k_pairs) run on st3 concurrently with
     // the bonded and base-pair pass; fork/join events.  Off by default: with
@@ -302,8 +301,8 @@ int upload_dgf(sis_ctx *ctx, int k) {
 int ensure_lists(sis_ctx *ctx);
 
 int run_rebuild(sis_ctx *ctx, int after_step = 0) {
-    ctx->launches += 2 + (ctx->plan.n_small_items > 0) + 5 * (ctx->plan.n_large_items > 0);
-    CK(launch_rebuild(ctx->D, ctx->g, ctx->cur, ctx->plan, after_step, step_blocks(ctx->G, ctx->n), ctx->st));
+    ctx->launches++;
+    CK(launch_rebuild(ctx->D, ctx->g, ctx->cur, ctx->plan, after_step, step_blocks(ctx->G, ctx->n), ctx->coop_grid, ctx->st));
     return SIS_OK;
 }
 
@@ -337,6 +336,11 @@ int check_err(sis_ctx *ctx) {
     if (e & ERR_PAIR_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "pair list capacity exceeded");
     if (e & ERR_BP_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "base-pair list capacity exceeded");
     if (e & ERR_NONFINITE) return fail(ctx, SIS_ERR_NONFINITE, "non-finite displacement");
+    if (e & ERR_TIMEOUT) {
+        // a block left the trigger/rebuild kernel early: start its barrier afresh
+        CK(cudaMemsetAsync(ctx->D.gbar, 0, 2 * sizeof(unsigned int), ctx->st));
+        return fail(ctx, SIS_ERR_CUDA, "grid barrier of the trigger/rebuild kernel timed out");
+    }
     return SIS_OK;
 }
 
@@ -393,56 +397,25 @@ int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
 
 // ----------------------------------------------------------- step graphs
 // kGraphSteps MD steps captured as one graph: per step k_bonded beside the
-// base-pair kernels, k_step, k_trigger and a conditional (IF) node whose body is the rebuild; k_trigger
-// sets the node's condition on the device, so a step without a rebuild runs
-// three kernels and no early-exit launches.  An even step count leaves the
-// position buffer parity unchanged, so one graph serves every launch.
+// base-pair kernels, k_step and k_trigger_rebuild, which ends at once when no
+// instance's trigger fired, so a step without a rebuild runs five kernels and
+// nothing else.  An even step count leaves the position buffer parity
+// unchanged, so one graph serves every launch.
 constexpr int kGraphSteps = 20;
-
-cudaError_t add_rebuild_node(sis_ctx *ctx, cudaGraphConditionalHandle cond, int cur) {
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t cg = nullptr;
-    const cudaGraphNode_t *deps = nullptr;
-    size_t nd = 0;
-    cudaError_t e = cudaStreamGetCaptureInfo(ctx->st, &cs, nullptr, &cg, &deps, nullptr, &nd);
-    if (e != cudaSuccess) return e;
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = cond;
-    np.conditional.type = cudaGraphCondTypeIf;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
-    if (e != cudaSuccess) return e;
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    e = cudaStreamBeginCaptureToGraph(ctx->st2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-    if (e != cudaSuccess) return e;
-    cudaError_t eb = launch_rebuild_body(ctx->D, ctx->g, cur, ctx->plan, 1, ctx->st2);
-    cudaGraph_t got = nullptr;
-    e = cudaStreamEndCapture(ctx->st2, &got);
-    if (eb != cudaSuccess) return eb;
-    if (e != cudaSuccess) return e;
-    return cudaStreamUpdateCaptureDependencies(ctx->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
-}
 
 int build_step_graph(sis_ctx *ctx) {
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     ctx->gexec = nullptr;
-    if (!ctx->st2) CK(cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking));
     cudaGraph_t graph = nullptr;
     CK(cudaGraphCreate(&graph, 0));
-    cudaError_t e = cudaSuccess;
-    cudaGraphConditionalHandle cond[kGraphSteps];
-    for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k)
-        e = cudaGraphConditionalHandleCreate(&cond[k], graph, 0, cudaGraphCondAssignDefault);
-    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(ctx->st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    cudaError_t e = cudaStreamBeginCaptureToGraph(ctx->st, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
     if (e == cudaSuccess) {
         int cur = ctx->cur;
         for (int k = 0; k < kGraphSteps && e == cudaSuccess; ++k) {
             e = enqueue_forces_update(ctx, cur, nullptr, 0);
             cur ^= 1;
-            if (e == cudaSuccess) e = launch_trigger(ctx->D, ctx->g, step_blocks(ctx->G, ctx->n), ctx->st, &cond[k]);
-            if (e == cudaSuccess) e = add_rebuild_node(ctx, cond[k], cur);
+            if (e == cudaSuccess)
+                e = launch_rebuild(ctx->D, ctx->g, cur, ctx->plan, 1, step_blocks(ctx->G, ctx->n), ctx->coop_grid, ctx->st);
         }
         cudaGraph_t got = nullptr;
         const cudaError_t ee = cudaStreamEndCapture(ctx->st, &got);
@@ -665,6 +638,10 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
             sms > 0)
             ctx->bpb = 2 * sms;
         ctx->bpt = std::max(1, std::min((bp_total_cap + 255) / 256, 8 * (sms > 0 ? sms : 152)));
+        // the trigger/rebuild kernel: two blocks per SM (fewer if they do not fit)
+        const int per = std::min(2, coop_blocks_per_sm());
+        ctx->coop_grid = std::min(kMaxCoopBlocks, std::max(1, per) * (sms > 0 ? sms : 152));
+        if (per < 1) ctx->coop_grid = 0;
     }
     Dev &D = ctx->D;
     const int n = ctx->n, ni = ctx->n_inst;
@@ -724,8 +701,10 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &dS_d, 469);
     rc |= dalloc(ctx, &ctx->dgf_d, (size_t)469 * ni);
     rc |= dalloc(ctx, &ctx->ip_d, ni);
-    rc |= dalloc(ctx, &D.m1, ni);
-    rc |= dalloc(ctx, &D.m2, ni);
+    rc |= dalloc(ctx, &D.m1, 2 * (size_t)ni);
+    rc |= dalloc(ctx, &D.m2, 2 * (size_t)ni);
+    rc |= dalloc(ctx, &D.gbar, 2);
+    rc |= dalloc(ctx, &D.gsum, kMaxCoopBlocks);
     rc |= dalloc(ctx, &D.flag, ni);
     rc |= dalloc(ctx, &D.any, 1);
     rc |= dalloc(ctx, &D.ticket, 3);
@@ -734,7 +713,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.step_ctr, 1);
     rc |= dalloc(ctx, &D.err, 1);
     rc |= dalloc(ctx, &D.max_need, 2);
-    rc |= dalloc(ctx, &D.rebuilds, 2); // [0] instance rebuilds, [1] rebuild passes run by step graphs
+    rc |= dalloc(ctx, &D.rebuilds, 2); // [0] instance rebuilds, [1] unused
     rc |= dalloc(ctx, &D.capped, 1);
     rc |= dalloc(ctx, &D.bead_cell, n);
     rc |= dalloc(ctx, &D.cell_cnt, ncells);
@@ -756,6 +735,10 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     if (rc) {
         sis_gpu_destroy(ctx);
         return SIS_ERR_NOMEM;
+    }
+    if (ctx->coop_grid < 1) {
+        sis_gpu_destroy(ctx);
+        return SIS_ERR_CUDA;
     }
     D.n_cells = ncells;
     D.bpp = bpp_d;
@@ -852,7 +835,6 @@ extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
     for (int e = 0; e < kEvents; ++e)
         if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
     if (ctx->st) cudaStreamDestroy(ctx->st);
-    if (ctx->st2) cudaStreamDestroy(ctx->st2);
     if (ctx->st3) cudaStreamDestroy(ctx->st3);
     if (ctx->st4) cudaStreamDestroy(ctx->st4);
     if (ctx->ev_bond) cudaEventDestroy(ctx->ev_bond);
@@ -1124,13 +1106,7 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     CK(cudaStreamSynchronize(ctx->st));
     ctx->D.mc_draws = nullptr;
     ctx->mc_pending = false;
-    if (graphs) {
-        // rebuild bodies the graphs actually ran
-        unsigned long long passes = 0;
-        CK(cudaMemcpy(&passes, ctx->D.rebuilds + 1, sizeof(passes), cudaMemcpyDeviceToHost));
-        ctx->launches += (long long)(passes - ctx->graph_passes) * rebuild_body_kernels(ctx->plan);
-        ctx->graph_passes = passes;
-    }
+    (void)graphs;
     return check_err(ctx);
 }
 

@@ -41,6 +41,8 @@ constexpr int MAX_BP_TYPES = 7;
 constexpr int ERR_PAIR_OVERFLOW = 1;
 constexpr int ERR_BP_OVERFLOW = 2;
 constexpr int ERR_NONFINITE = 4;
+constexpr int ERR_TIMEOUT = 8; // a grid barrier wait of k_trigger_rebuild ran out
+constexpr int kMaxCoopBlocks = 4096;
 
 // Fixed-point base-pair force accumulation of the mixed path: one unit is
 // 2^-32 kcal/mol/A; contributions of magnitude 2^30 or more are reported as
@@ -140,10 +142,12 @@ struct Dev {
                             // temperature; its sign equals that of the FP64 value
     const InstP *ip;
     // rebuild trigger
-    unsigned long long *m1, *m2; // [n_inst] top-2 displacement^2 (bit patterns)
+    unsigned long long *m1, *m2; // [2][n_inst] top-2 displacement^2 (bit patterns), by step parity
     int *flag;              // [n_inst] rebuild requested
     int *any;               // [1] any flag set
-    unsigned int *ticket;   // [3] last-block tickets (trigger, rebuild, base-pair evaluation)
+    unsigned int *ticket;   // [3] last-block tickets (unused, unused, base-pair evaluation)
+    unsigned int *gbar;     // [2] grid barrier of k_trigger_rebuild: arrivals, generation
+    int *gsum;              // [kMaxCoopBlocks] per-block sums of the cell scan
     int *part_inst;         // [2 * step blocks] per-block trigger partials: instance
     unsigned long long *part_m; // [4 * step blocks] and its top-two displacement^2
     unsigned long long *step_ctr; // [1] Philox step counter

@@ -13,10 +13,9 @@
 //             Debye-Hueckel pair forces over the bead's full pair list and
 //             the bonded slots touching the bead, adds fbp, and applies the
 //             GJF-2GJ (or Ermak-McCammon) update in FP64; per-block partials
-//             of the displacement trigger (job_md.F90:376-395) are merged by
-//             k_trigger.
-// The list rebuild (lists.cu) follows and exits at once when no instance
-// asked for one.
+//             of the displacement trigger (job_md.F90:376-395) go to
+//             k_trigger_rebuild (lists.cu), which merges them and rebuilds
+//             the lists of the instances that fired.
 #include "common.cuh"
 #include "kernels.h"
 #include "terms.cuh"
@@ -929,7 +928,9 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
 
     // -------------------------------------------------------------- phase C
     // displacement^2 per bead and its top two per instance (shared memory);
-    // the block's result goes to its partial record, reduced by k_trigger
+    // the block's result goes to its partial record, merged by the trigger
+    // (k_trigger_rebuild) into m1/m2 of this step's parity
+    const size_t mo = (size_t)(step & 1ull) * g.n_inst;
     for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
@@ -943,8 +944,8 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
             const unsigned long long old = atomicMax(&s_m1[k], bits);
             atomicMax(&s_m2[k], old < bits ? old : bits);
         } else {
-            const unsigned long long old = atomicMax(&D.m1[inst], bits);
-            atomicMax(&D.m2[inst], old < bits ? old : bits);
+            const unsigned long long old = atomicMax(&D.m1[mo + inst], bits);
+            atomicMax(&D.m2[mo + inst], old < bits ? old : bits);
         }
     }
     __syncthreads();
@@ -958,84 +959,9 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     if (s_cnt > 2 && s_cnt <= 32 && (int)threadIdx.x < s_cnt) {
         const unsigned long long b1 = s_m1[threadIdx.x], b2 = s_m2[threadIdx.x];
         const int inst = s_lo + threadIdx.x;
-        const unsigned long long old = atomicMax(&D.m1[inst], b1);
+        const unsigned long long old = atomicMax(&D.m1[mo + inst], b1);
         const unsigned long long c2 = old < b1 ? old : b1;
-        atomicMax(&D.m2[inst], c2 > b2 ? c2 : b2);
-    }
-}
-
-// Rebuild trigger (job_md.F90:376-395): reduces the step kernel's per-block
-// top-two displacements per instance, then the last block sets the rebuild
-// flag of every instance with sqrt(d2max) + sqrt(d2max_2nd) > margin, clears
-// the base-pair staging count of flagged instances and advances the Philox
-// step counter.
-__device__ __forceinline__ void top2_merge(unsigned long long &a1, unsigned long long &a2, unsigned long long b1,
-                                           unsigned long long b2) {
-    const unsigned long long lo = a1 < b1 ? a1 : b1;
-    a1 = a1 > b1 ? a1 : b1;
-    const unsigned long long m = a2 > b2 ? a2 : b2;
-    a2 = lo > m ? lo : m;
-}
-
-// The last block also sets the graph conditional cond (use_cond: launched as
-// a node of a captured step graph) to whether any instance asked for a
-// rebuild, so that the graph runs its rebuild body only then.
-__global__ void __launch_bounds__(256) k_trigger(Dev D, GlobP g, int nparts, cudaGraphConditionalHandle cond, int use_cond) {
-    __shared__ int s_last;
-    const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x; base < 2 * nparts; base += gridDim.x * blockDim.x) {
-        const int r = base + threadIdx.x;
-        int inst = r < 2 * nparts ? D.part_inst[r] : -1;
-        unsigned long long a1 = 0ull, a2 = 0ull;
-        if (inst >= 0) {
-            a1 = D.part_m[2 * r];
-            a2 = D.part_m[2 * r + 1];
-        }
-        const int i0 = __shfl_sync(0xffffffffu, inst, 0);
-        const bool uniform = __all_sync(0xffffffffu, inst == i0 || inst < 0) && i0 >= 0;
-        if (uniform) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long b1 = __shfl_xor_sync(0xffffffffu, a1, o), b2 = __shfl_xor_sync(0xffffffffu, a2, o);
-                top2_merge(a1, a2, b1, b2);
-            }
-            if (lane == 0) {
-                const unsigned long long old = atomicMax(&D.m1[i0], a1);
-                const unsigned long long c2 = old < a1 ? old : a1;
-                atomicMax(&D.m2[i0], c2 > a2 ? c2 : a2);
-            }
-        } else if (inst >= 0) {
-            const unsigned long long old = atomicMax(&D.m1[inst], a1);
-            const unsigned long long c2 = old < a1 ? old : a1;
-            atomicMax(&D.m2[inst], c2 > a2 ? c2 : a2);
-        }
-    }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = (atomicAdd(&D.ticket[0], 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    int any = 0;
-    for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) {
-        const double a = __longlong_as_double((long long)atomicExch(&D.m1[k], 0ull));
-        const double b = __longlong_as_double((long long)atomicExch(&D.m2[k], 0ull));
-        if (sqrt(a) + sqrt(b) > g.nl_margin) {
-            D.flag[k] = 1;
-            D.bp_cnt[k] = 0;
-            any = 1;
-        }
-    }
-    if (any) atomicOr(D.any, 1);
-    // job_md.F90:364-367: the next step (1-based count step_ctr + 2) runs the
-    // base-pair Monte Carlo pass every nstep_mc steps
-    if (g.nstep_mc > 0 && (D.step_ctr[0] + 2ull) % (unsigned long long)g.nstep_mc == 0ull)
-        for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) D.mc_due[k] = 1;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        D.ticket[0] = 0u;
-        D.step_ctr[0] += 1ull;
-        if (use_cond) cudaGraphSetConditional(cond, *(volatile int *)D.any ? 1u : 0u);
+        atomicMax(&D.m2[mo + inst], c2 > b2 ? c2 : b2);
     }
 }
 
@@ -1221,12 +1147,6 @@ int pre_kernels(const GlobP &g, int do_bonded, int do_bp) { return (do_bonded ? 
 
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st) {
     k_bp_energy<<<bp_blocks, 256, 0, st>>>(D, g, cur, tK);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st, const cudaGraphConditionalHandle *cond) {
-    const int grid = std::max(1, std::min(64, (2 * nparts + 255) / 256));
-    k_trigger<<<grid, 256, 0, st>>>(D, g, nparts, cond ? *cond : cudaGraphConditionalHandle{}, cond != nullptr);
     return cudaGetLastError();
 }
 

@@ -43,8 +43,6 @@ int bp_kernels(const GlobP &g);
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st);
 // base-pair Monte Carlo removal of every instance whose pass is due (no-op without it)
 cudaError_t launch_bp_mc(const Dev &D, const GlobP &g, cudaStream_t st);
-cudaError_t launch_trigger(const Dev &D, const GlobP &g, int nparts, cudaStream_t st,
-                           const cudaGraphConditionalHandle *cond = nullptr);
 int step_blocks(int G, int n);
 cudaError_t launch_remd_partner_ip(const Dev &D, const RemdDev &R, int n_inst, int parity, cudaStream_t st);
 cudaError_t launch_remd_decide(const Dev &D, const RemdDev &R, const GlobP &g, int parity, const double *u, double kB,
@@ -53,14 +51,13 @@ cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st
 cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaStream_t st);
 cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st, int only_inst = -1);
 cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
-// after_step: the rebuild follows a step (k_trigger decides the flags);
-// otherwise the flags were set by the host and k_rebuild_begin starts it
-cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, cudaStream_t st);
-// the rebuild proper (every kernel after k_trigger / k_rebuild_begin); in_graph:
-// it is the body of a step graph's conditional node, whose passes are counted
-// in D.rebuilds[1]
-cudaError_t launch_rebuild_body(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int in_graph, cudaStream_t st);
-// kernels launch_rebuild_body enqueues
-int rebuild_body_kernels(const RebuildPlan &pl);
+// k_trigger_rebuild, one cooperative launch of `grid` blocks (at most
+// coop_blocks_per_sm() per SM, and at most kMaxCoopBlocks): after_step, the
+// displacement trigger of the step just taken (nparts: the step kernel's
+// blocks) and the rebuild of the instances that fired; otherwise the rebuild
+// of the instances the host flagged.
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, int grid,
+                           cudaStream_t st);
+int coop_blocks_per_sm();
 
 } // namespace sisg

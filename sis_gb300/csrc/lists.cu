@@ -1,7 +1,7 @@
-// Neighbour-list rebuild of libsisgpu: neighbor_list.F90:1-233 and
-// pbc_wrap (pbc.F90:196-226) for the instances whose displacement trigger
-// fired (flag[inst] != 0).  Every kernel returns at once when no instance is
-// flagged, so the rebuild can be enqueued after every step.
+// Displacement trigger and neighbour-list rebuild of libsisgpu:
+// job_md.F90:376-395, neighbor_list.F90:1-233 and pbc_wrap (pbc.F90:196-226)
+// for the instances whose trigger fired (flag[inst] != 0), in one cooperative
+// kernel launched after every step; it ends at once when no instance fired.
 //
 // Membership is decided exactly as the reference decides it: the squared
 // distance of the pair (lower global index first, pbc_vec_d single shift) is
@@ -222,15 +222,95 @@ __device__ __forceinline__ void bead_end(const Dev &D, const GlobP &g, int gi, i
     }
 }
 
+// ------------------------------------------------------- grid barrier
+// Every block of the cooperative launch is resident at once, so a wait ends
+// when the last block arrives.  The wait is bounded all the same: after
+// about a second the block records ERR_TIMEOUT and leaves the kernel.
+__device__ bool grid_sync(const Dev &D) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int *cnt = D.gbar, *gen = D.gbar + 1;
+        const unsigned int g0 = *(volatile unsigned int *)gen;
+        __threadfence();
+        int ok = 0;
+        if (atomicAdd(cnt, 1u) == gridDim.x - 1) {
+            *cnt = 0u;
+            __threadfence();
+            atomicAdd(gen, 1u);
+            ok = 1;
+        } else {
+            for (int it = 0; it < (1 << 24); ++it) {
+                if (*(volatile unsigned int *)gen != g0) {
+                    ok = 1;
+                    break;
+                }
+                __nanosleep(32);
+            }
+            if (!ok) atomicOr(D.err, ERR_TIMEOUT);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// ------------------------------------------------------------ trigger
+// job_md.F90:376-395: the step kernel leaves per-block top-two squared
+// displacements (partials, or atomics into m1/m2 for blocks spanning many
+// instances); they are merged per instance into m1/m2 of the step's parity.
+__device__ __forceinline__ void top2_merge(unsigned long long &a1, unsigned long long &a2, unsigned long long b1,
+                                           unsigned long long b2) {
+    const unsigned long long lo = a1 < b1 ? a1 : b1;
+    a1 = a1 > b1 ? a1 : b1;
+    const unsigned long long m = a2 > b2 ? a2 : b2;
+    a2 = lo > m ? lo : m;
+}
+__device__ void trigger_reduce(const Dev &D, int nparts, unsigned long long *m1, unsigned long long *m2) {
+    const int lane = threadIdx.x & 31;
+    for (int base = blockIdx.x * blockDim.x; base < 2 * nparts; base += gridDim.x * blockDim.x) {
+        const int r = base + threadIdx.x;
+        const int inst = r < 2 * nparts ? D.part_inst[r] : -1;
+        unsigned long long a1 = 0ull, a2 = 0ull;
+        if (inst >= 0) {
+            a1 = D.part_m[2 * r];
+            a2 = D.part_m[2 * r + 1];
+        }
+        const int i0 = __shfl_sync(0xffffffffu, inst, 0);
+        const bool uniform = __all_sync(0xffffffffu, inst == i0 || inst < 0) && i0 >= 0;
+        if (uniform) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long b1 = __shfl_xor_sync(0xffffffffu, a1, o), b2 = __shfl_xor_sync(0xffffffffu, a2, o);
+                top2_merge(a1, a2, b1, b2);
+            }
+            if (lane == 0) {
+                const unsigned long long old = atomicMax(&m1[i0], a1);
+                const unsigned long long c2 = old < a1 ? old : a1;
+                atomicMax(&m2[i0], c2 > a2 ? c2 : a2);
+            }
+        } else if (inst >= 0) {
+            const unsigned long long old = atomicMax(&m1[inst], a1);
+            const unsigned long long c2 = old < a1 ? old : a1;
+            atomicMax(&m2[inst], c2 > a2 ? c2 : a2);
+        }
+    }
+}
+__device__ __forceinline__ bool trigger_fires(const GlobP &g, const unsigned long long *m1, const unsigned long long *m2, int k) {
+    const double a = __longlong_as_double((long long)__ldcg(m1 + k));
+    const double b = __longlong_as_double((long long)__ldcg(m2 + k));
+    return sqrt(a) + sqrt(b) > g.nl_margin;
+}
+
 // --------------------------------------------------- all-pairs (small)
 // items: (instance, first local bead); 32 beads per item, one warp per bead.
-__global__ void __launch_bounds__(256) k_rebuild_small(Dev D, GlobP g, int cur, const int2 *items, int n_items, float slack) {
-    if (*(volatile int *)D.any == 0) return;
+__device__ void rebuild_small(const Dev &D, const GlobP &g, int cur, const int2 *items, int n_items, float slack) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
         const int2 item = items[it];
         const int inst = item.x;
-        if (D.flag[inst] == 0) continue;
+        if (__ldcg(D.flag + inst) == 0) continue;
         const InstP &ip = D.ip[inst];
         const float maxcut2f = (float)fmax(fmax(ip.wca_nl_cut2, ip.ele_nl_cut2), ip.bp_nl_cut2) * slack;
         for (int li = item.y + warp; li < min(item.y + 32, ip.n); li += 8) {
@@ -253,6 +333,8 @@ __global__ void __launch_bounds__(256) k_rebuild_small(Dev D, GlobP g, int cur, 
 }
 
 // ------------------------------------------------------- cell list (large)
+// Data that other blocks of the same launch wrote are read with __ldcg (L2),
+// never from a possibly stale L1 line.
 __device__ __forceinline__ int cell_of(const double4 &xw, const InstP &ip) {
     int c[3];
     const double xs[3] = {xw.x, xw.y, xw.z};
@@ -265,11 +347,10 @@ __device__ __forceinline__ int cell_of(const double4 &xw, const InstP &ip) {
 }
 
 // bead ranges of large instances: litems = (instance, first local bead), 256 beads each
-__global__ void k_cell_bin(Dev D, GlobP g, int cur, const int2 *litems, int n_litems) {
-    if (*(volatile int *)D.any == 0) return;
+__device__ void cell_bin(const Dev &D, int cur, const int2 *litems, int n_litems) {
     for (int it = blockIdx.x; it < n_litems; it += gridDim.x) {
         const int2 item = litems[it];
-        if (D.flag[item.x] == 0) continue;
+        if (__ldcg(D.flag + item.x) == 0) continue;
         const InstP &ip = D.ip[item.x];
         const int li = item.y + threadIdx.x;
         if (li >= ip.n) continue;
@@ -281,22 +362,53 @@ __global__ void k_cell_bin(Dev D, GlobP g, int cur, const int2 *litems, int n_li
     }
 }
 
-// exclusive scan of cell counts (one block, coalesced tiles of 4096 cells);
-// counts are reset to serve as fill cursors
-__global__ void __launch_bounds__(1024) k_cell_scan(Dev D) {
-    if (*(volatile int *)D.any == 0) return;
-    __shared__ int s_warp[32];
-    __shared__ int s_carry;
-    const int n = D.n_cells;
+// Exclusive scan of the cell counts over the whole grid: block b owns a
+// contiguous chunk of cells; first its sum (gsum[b]), then, after a grid
+// barrier, its offset (the sum of gsum over lower blocks) and a block scan of
+// its chunk in tiles of 4 cells per thread.  Counts are reset to serve as
+// fill cursors.
+__device__ __forceinline__ int block_sum(int v, int *s_red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
-    for (int base = 0; base < n; base += 4096) {
-        const int c0 = base + 4 * threadIdx.x;
-        int v[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = c0 + q < n ? D.cell_cnt[c0 + q] : 0;
-        const int tsum = v[0] + v[1] + v[2] + v[3];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_red[w];
+    return t;
+}
+__device__ __forceinline__ void scan_chunk(const Dev &D, int &lo, int &hi) {
+    const int n = D.n_cells;
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    lo = min(n, (int)blockIdx.x * chunk);
+    hi = min(n, lo + chunk);
+}
+__device__ void cell_scan_sums(const Dev &D, int *s_red) {
+    int lo, hi;
+    scan_chunk(D, lo, hi);
+    int v = 0;
+    for (int c = lo + threadIdx.x; c < hi; c += blockDim.x) v += __ldcg(D.cell_cnt + c);
+    const int t = block_sum(v, s_red);
+    if (threadIdx.x == 0) D.gsum[blockIdx.x] = t;
+}
+__device__ void cell_scan_write(const Dev &D, int *s_red) {
+    __shared__ int s_warp[8];
+    __shared__ int s_carry;
+    int lo, hi;
+    scan_chunk(D, lo, hi);
+    int v = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) v += __ldcg(D.gsum + b);
+    const int offset = block_sum(v, s_red);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_carry = offset;
+    __syncthreads();
+    for (int base = lo; base < hi; base += 4 * (int)blockDim.x) {
+        const int c0 = base + 4 * threadIdx.x;
+        int x[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) x[q] = c0 + q < hi ? __ldcg(D.cell_cnt + c0 + q) : 0;
+        const int tsum = x[0] + x[1] + x[2] + x[3];
         int incl = tsum;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -305,42 +417,37 @@ __global__ void __launch_bounds__(1024) k_cell_scan(Dev D) {
         }
         if (lane == 31) s_warp[warp] = incl;
         __syncthreads();
-        if (warp == 0) {
-            int w = s_warp[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += y;
-            }
-            s_warp[lane] = w;
-        }
-        __syncthreads();
-        int run = s_carry + (warp ? s_warp[warp - 1] : 0) + incl - tsum;
+        int wpre = 0;
+        for (int w = 0; w < warp; ++w) wpre += s_warp[w];
+        int run = s_carry + wpre + incl - tsum;
 #pragma unroll
         for (int q = 0; q < 4; ++q)
-            if (c0 + q < n) {
+            if (c0 + q < hi) {
                 D.cell_start[c0 + q] = run;
                 D.cell_cnt[c0 + q] = 0;
-                run += v[q];
+                run += x[q];
             }
         __syncthreads();
-        if (threadIdx.x == 1023) s_carry += s_warp[31];
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_warp[w];
+            s_carry += t;
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) D.cell_start[n] = s_carry;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) D.cell_start[D.n_cells] = s_carry;
 }
 
-__global__ void k_cell_fill(Dev D, GlobP g, const int2 *litems, int n_litems) {
-    if (*(volatile int *)D.any == 0) return;
+__device__ void cell_fill(const Dev &D, const int2 *litems, int n_litems) {
     for (int it = blockIdx.x; it < n_litems; it += gridDim.x) {
         const int2 item = litems[it];
-        if (D.flag[item.x] == 0) continue;
+        if (__ldcg(D.flag + item.x) == 0) continue;
         const InstP &ip = D.ip[item.x];
         const int li = item.y + threadIdx.x;
         if (li >= ip.n) continue;
         const int gi = ip.bead_off + li;
-        const int c = D.bead_cell[gi];
-        const int pos = D.cell_start[c] + atomicAdd(&D.cell_cnt[c], 1);
+        const int c = __ldcg(D.bead_cell + gi);
+        const int pos = __ldcg(D.cell_start + c) + atomicAdd(&D.cell_cnt[c], 1);
         D.cell_beads[pos] = gi;
     }
 }
@@ -348,17 +455,16 @@ __global__ void k_cell_fill(Dev D, GlobP g, const int2 *litems, int n_litems) {
 // sorts every cell's beads by index so that list order is deterministic:
 // one warp per cell ranks up to 256 beads in shared memory (rank = number of
 // smaller indices; indices are distinct); larger cells are insertion-sorted
-__global__ void __launch_bounds__(256) k_cell_sort(Dev D) {
-    if (*(volatile int *)D.any == 0) return;
+__device__ void cell_sort(const Dev &D) {
     constexpr int kCap = 256;
     __shared__ int sb[8][kCap];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = gridDim.x * 8;
     for (int c = blockIdx.x * 8 + warp; c < D.n_cells; c += nwarps) {
-        const int a = D.cell_start[c], b = D.cell_start[c + 1], m = b - a;
+        const int a = __ldcg(D.cell_start + c), b = __ldcg(D.cell_start + c + 1), m = b - a;
         if (m <= 1) continue;
         if (m <= kCap) {
-            for (int k = lane; k < m; k += 32) sb[warp][k] = D.cell_beads[a + k];
+            for (int k = lane; k < m; k += 32) sb[warp][k] = __ldcg(D.cell_beads + a + k);
             __syncwarp();
             for (int k = lane; k < m; k += 32) {
                 const int v = sb[warp][k];
@@ -369,10 +475,10 @@ __global__ void __launch_bounds__(256) k_cell_sort(Dev D) {
             __syncwarp();
         } else if (lane == 0) {
             for (int k = a + 1; k < b; ++k) {
-                const int v = D.cell_beads[k];
+                const int v = __ldcg(D.cell_beads + k);
                 int q = k - 1;
-                while (q >= a && D.cell_beads[q] > v) {
-                    D.cell_beads[q + 1] = D.cell_beads[q];
+                while (q >= a && __ldcg(D.cell_beads + q) > v) {
+                    D.cell_beads[q + 1] = __ldcg(D.cell_beads + q);
                     --q;
                 }
                 D.cell_beads[q + 1] = v;
@@ -382,14 +488,13 @@ __global__ void __launch_bounds__(256) k_cell_sort(Dev D) {
 }
 
 // one warp per bead: the 27 neighbouring cells' beads as candidates
-__global__ void __launch_bounds__(256) k_cell_search(Dev D, GlobP g, int cur, const int2 *litems, int n_litems, float slack) {
-    if (*(volatile int *)D.any == 0) return;
+__device__ void cell_search(const Dev &D, const GlobP &g, int cur, const int2 *litems, int n_litems, float slack) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // each litem covers 256 beads; 8 warps stride over them
     for (int it = blockIdx.x; it < n_litems; it += gridDim.x) {
         const int2 item = litems[it];
         const int inst = item.x;
-        if (D.flag[inst] == 0) continue;
+        if (__ldcg(D.flag + inst) == 0) continue;
         const InstP &ip = D.ip[inst];
         const float maxcut2f = (float)fmax(fmax(ip.wca_nl_cut2, ip.ele_nl_cut2), ip.bp_nl_cut2) * slack;
         for (int li = item.y + warp; li < min(item.y + 256, ip.n); li += 8) {
@@ -398,7 +503,7 @@ __global__ void __launch_bounds__(256) k_cell_search(Dev D, GlobP g, int cur, co
             bead_begin(D, cur, gi, ip, lane, xi_w);
             const int4 bii = D.binfo[gi];
             const uint4 mi = D.mir[cur][gi];
-            const int c0 = D.bead_cell[gi] - ip.cell_base;
+            const int c0 = __ldcg(D.bead_cell + gi) - ip.cell_base;
             const int cx = c0 % ip.nc[0], cy = (c0 / ip.nc[0]) % ip.nc[1], cz = c0 / (ip.nc[0] * ip.nc[1]);
             // lane q < 27 owns neighbour cell q; a warp prefix over their
             // counts flattens the 27 ranges into one candidate sequence that
@@ -410,8 +515,8 @@ __global__ void __launch_bounds__(256) k_cell_search(Dev D, GlobP g, int cur, co
                 qy = qy < 0 ? qy + ip.nc[1] : (qy >= ip.nc[1] ? qy - ip.nc[1] : qy);
                 qz = qz < 0 ? qz + ip.nc[2] : (qz >= ip.nc[2] ? qz - ip.nc[2] : qz);
                 const int c = ip.cell_base + (qz * ip.nc[1] + qy) * ip.nc[0] + qx;
-                cstart = D.cell_start[c];
-                ccnt = D.cell_start[c + 1] - cstart;
+                cstart = __ldcg(D.cell_start + c);
+                ccnt = __ldcg(D.cell_start + c + 1) - cstart;
             }
             int incl = ccnt;
 #pragma unroll
@@ -435,7 +540,7 @@ __global__ void __launch_bounds__(256) k_cell_search(Dev D, GlobP g, int cur, co
                 const int cs = __shfl_sync(0xffffffffu, cstart, lo), ce = __shfl_sync(0xffffffffu, excl, lo);
                 int f = 0, gj = -1;
                 if (k < total) {
-                    gj = D.cell_beads[cs + (k - ce)];
+                    gj = __ldcg(D.cell_beads + cs + (k - ce));
                     if (gj != gi) f = test_pair(D, g, ip, cur, gi, bii, mi, xi_w, gj, maxcut2f, inst);
                 }
                 warp_append(D, g, gi, lane, f, gj, count);
@@ -446,23 +551,24 @@ __global__ void __launch_bounds__(256) k_cell_search(Dev D, GlobP g, int cur, co
 }
 
 // ------------------------------------------------------------ finish
-// One block: base-pair prefix counts, rebuild bookkeeping, reset of flags
-// and cell counters.
-__global__ void __launch_bounds__(1024) k_rebuild_finish(Dev D, GlobP g, int in_graph) {
-    if (*(volatile int *)D.any == 0) return;
-    __shared__ int s[1024];
+// Block 0: base-pair prefix counts over the instances and rebuild
+// bookkeeping; every block: reset of its share of the cell counters.
+__device__ void rebuild_finish(const Dev &D, const GlobP &g) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < D.n_cells; c += gridDim.x * blockDim.x) D.cell_cnt[c] = 0;
+    if (blockIdx.x != 0) return;
+    __shared__ int s[256];
     const int n = g.n_inst;
-    const int per = (n + 1023) / 1024;
+    const int per = (n + 255) / 256;
     const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
     int sum = 0, nflag = 0;
     for (int k = lo; k < hi; ++k) {
-        const int c = min(D.bp_cnt[k], D.ip[k].bp_cap);
+        const int c = min(__ldcg(D.bp_cnt + k), D.ip[k].bp_cap);
         sum += c;
-        nflag += D.flag[k] != 0;
+        nflag += __ldcg(D.flag + k) != 0;
     }
     s[threadIdx.x] = sum;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
+    for (int o = 1; o < 256; o <<= 1) {
         const int v = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0;
         __syncthreads();
         s[threadIdx.x] += v;
@@ -471,53 +577,106 @@ __global__ void __launch_bounds__(1024) k_rebuild_finish(Dev D, GlobP g, int in_
     int run = s[threadIdx.x] - sum;
     for (int k = lo; k < hi; ++k) {
         D.bp_cnt[n + k] = run;
-        run += min(D.bp_cnt[k], D.ip[k].bp_cap);
+        run += min(__ldcg(D.bp_cnt + k), D.ip[k].bp_cap);
         // new records: the next evaluation runs the Monte Carlo pass (job_md.F90:392-394)
-        if (D.flag[k] && g.nstep_mc > 0) D.mc_due[k] = 1;
+        if (__ldcg(D.flag + k) && g.nstep_mc > 0) D.mc_due[k] = 1;
         D.flag[k] = 0;
     }
-    if (threadIdx.x == 1023) *D.bp_total = s[1023];
+    if (threadIdx.x == 255) *D.bp_total = s[255];
     if (nflag) atomicAdd((unsigned long long *)D.rebuilds, (unsigned long long)nflag);
-    for (int c = threadIdx.x; c < D.n_cells; c += blockDim.x) D.cell_cnt[c] = 0;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        *D.any = 0;
-        if (in_graph) atomicAdd((unsigned long long *)(D.rebuilds + 1), 1ull);
-    }
+    if (threadIdx.x == 0) *D.any = 0;
 }
 
-// Clears the base-pair staging count of flagged instances; first kernel of a rebuild.
-__global__ void k_rebuild_begin(Dev D, GlobP g) {
-    if (*(volatile int *)D.any == 0) return;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.n_inst; k += gridDim.x * blockDim.x)
-        if (D.flag[k]) D.bp_cnt[k] = 0;
-}
-
-cudaError_t launch_rebuild_body(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int in_graph, cudaStream_t st) {
+// --------------------------------------------- trigger and rebuild kernel
+// One cooperative launch after every step (after_step) or on request.
+//  * after_step: the trigger.  Partials merge into m1/m2 of the step's parity
+//    (step counter & 1); after a grid barrier every block reads the merged
+//    values and decides alone whether any instance fired, so a step without a
+//    rebuild ends there.  Block 0 flags the instances that fired (clearing
+//    their base-pair staging counts), schedules the Monte Carlo pass
+//    (job_md.F90:364-367), clears m1/m2 of the other parity for the next
+//    step and advances the Philox step counter.
+//  * otherwise the host flagged the instances (flag, any); block 0 clears
+//    their staging counts.
+// The rebuild of the flagged instances follows, its phases separated by grid
+// barriers: wrap and cell binning; cell scan; fill; sort; the 27-cell search
+// and the all-pairs scan of small instances; finish.
+__global__ void __launch_bounds__(256) k_trigger_rebuild(Dev D, GlobP g, int cur, RebuildPlan pl, int nparts, int after_step) {
+    __shared__ int s_red[8];
     const float slack = 1.001f;
-    if (pl.n_small_items > 0) k_rebuild_small<<<pl.small_grid, 256, 0, st>>>(D, g, cur, pl.small_items, pl.n_small_items, slack);
-    if (pl.n_large_items > 0) {
-        k_cell_bin<<<pl.large_grid, 256, 0, st>>>(D, g, cur, pl.large_items, pl.n_large_items);
-        k_cell_scan<<<1, 1024, 0, st>>>(D);
-        k_cell_fill<<<pl.large_grid, 256, 0, st>>>(D, g, pl.large_items, pl.n_large_items);
-        k_cell_sort<<<(D.n_cells + 255) / 256, 256, 0, st>>>(D);
-        k_cell_search<<<pl.large_grid, 256, 0, st>>>(D, g, cur, pl.large_items, pl.n_large_items, slack);
+    if (after_step) {
+        const unsigned long long ctr = *(volatile unsigned long long *)D.step_ctr;
+        const int p = (int)(ctr & 1ull);
+        unsigned long long *m1 = D.m1 + (size_t)p * g.n_inst, *m2 = D.m2 + (size_t)p * g.n_inst;
+        trigger_reduce(D, nparts, m1, m2);
+        if (!grid_sync(D)) return;
+        int fired = 0;
+        for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) fired |= trigger_fires(g, m1, m2, k);
+        const int any = __syncthreads_or(fired);
+        if (blockIdx.x == 0) {
+            unsigned long long *o1 = D.m1 + (size_t)(p ^ 1) * g.n_inst, *o2 = D.m2 + (size_t)(p ^ 1) * g.n_inst;
+            const bool mc = g.nstep_mc > 0 && (ctr + 2ull) % (unsigned long long)g.nstep_mc == 0ull;
+            for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) {
+                if (any && trigger_fires(g, m1, m2, k)) {
+                    D.flag[k] = 1;
+                    D.bp_cnt[k] = 0;
+                }
+                o1[k] = 0ull;
+                o2[k] = 0ull;
+                if (mc) D.mc_due[k] = 1;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (any) *D.any = 1;
+                *D.step_ctr = ctr + 1ull;
+            }
+        }
+        if (!any) return;
+    } else {
+        if (*(volatile int *)D.any == 0) return;
+        if (blockIdx.x == 0)
+            for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x)
+                if (D.flag[k]) D.bp_cnt[k] = 0;
     }
-    k_rebuild_finish<<<1, 1024, 0, st>>>(D, g, in_graph);
-    return cudaGetLastError();
+    if (!grid_sync(D)) return;
+    if (pl.n_large_items > 0) {
+        cell_bin(D, cur, pl.large_items, pl.n_large_items);
+        if (!grid_sync(D)) return;
+        cell_scan_sums(D, s_red);
+        if (!grid_sync(D)) return;
+        cell_scan_write(D, s_red);
+        if (!grid_sync(D)) return;
+        cell_fill(D, pl.large_items, pl.n_large_items);
+        if (!grid_sync(D)) return;
+        cell_sort(D);
+        if (!grid_sync(D)) return;
+        cell_search(D, g, cur, pl.large_items, pl.n_large_items, slack);
+    }
+    if (pl.n_small_items > 0) rebuild_small(D, g, cur, pl.small_items, pl.n_small_items, slack);
+    if (!grid_sync(D)) return;
+    rebuild_finish(D, g);
 }
 
-int rebuild_body_kernels(const RebuildPlan &pl) { return (pl.n_small_items > 0) + 5 * (pl.n_large_items > 0) + 1; }
+int coop_blocks_per_sm() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_trigger_rebuild, 256, 0) != cudaSuccess) return 0;
+    return nb;
+}
 
-cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts,
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, int grid,
                            cudaStream_t st) {
-    if (after_step) {
-        cudaError_t e = launch_trigger(D, g, nparts, st);
-        if (e != cudaSuccess) return e;
-    } else {
-        k_rebuild_begin<<<(g.n_inst + 255) / 256, 256, 0, st>>>(D, g);
-    }
-    return launch_rebuild_body(D, g, cur, pl, 0, st);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_trigger_rebuild, D, g, cur, pl, nparts, after_step);
 }
 
 } // namespace sisg
