@@ -123,13 +123,13 @@ typedef struct sis_stats {
     int64_t wca_pairs;      /* current half-list WCA pairs */
     int64_t ele_pairs;      /* current half-list ele pairs */
     int64_t bp_pairs;       /* current base-pair candidates */
-    int32_t error_flags;    /* bit 0 pair overflow, bit 1 bp overflow, bit 2 nonfinite */
+    int32_t error_flags;    /* bit 0 pair overflow, bit 1 bp overflow, bit 2 nonfinite, bit 3 barrier timeout */
     int32_t n_beads;
     int32_t n_inst;
-    int32_t lanes_per_bead; /* autotuned group width of the step kernel */
+    int32_t lanes_per_bead; /* group width of the step kernel (sis_gpu_set_lanes) */
     int64_t capped;         /* bead-steps at which sis_gpu_set_force_cap's cap bound */
-    int32_t bp_blocks;      /* autotuned block count of the base-pair pass */
-    int32_t reserved;
+    int32_t bp_blocks;      /* block count of the base-pair evaluation */
+    int32_t overlap;        /* 1: pair forces in their own kernel (sis_gpu_set_overlap) */
 } sis_stats;
 
 /* Creates a context and uploads topology and parameters.  Replaces the
@@ -203,18 +203,18 @@ int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *out4);
 int sis_gpu_get_step(sis_ctx *ctx, uint64_t *step);
 int sis_gpu_set_step(sis_ctx *ctx, uint64_t step);
 
-/* Lanes per bead of the step kernel (1, 2, 4, 8, 16 or 32); 0 re-enables
- * the autotuner that picks it on the first long run. */
+/* Lanes per bead of the step kernel (1, 2, 4, 8, 16 or 32); 0 (default)
+ * lets the autotuner pick it on the first long run (64 steps or more). */
 int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes);
 /* 1 (default): sis_gpu_step runs steady-state steps as captured CUDA graphs
- * (20 steps each, the rebuild behind a device-set conditional node); 0:
- * every kernel is launched from the host.  Results are identical; per-kernel
- * profilers see only the second form. */
+ * (20 steps each); 0: every kernel is launched from the host.  Results are
+ * identical; per-kernel profilers see only the second form. */
 int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable);
 /* 1: a step's pair forces (WCA, Debye-Hueckel) are computed by a kernel of
- * their own on a second stream, concurrently with the bonded and base-pair
- * pass, and the step kernel takes them from a per-bead buffer; 0 (default):
- * one step kernel computes them.  Results are identical. */
+ * their own on another stream, concurrently with the bonded and base-pair
+ * pass, and the step kernel takes them from a per-bead buffer; 0: the step
+ * kernel computes them; -1 (default): the autotuner chooses, with the lanes
+ * per bead, on the first long run.  Results are identical. */
 int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable);
 
 int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *st);

@@ -65,7 +65,7 @@ class sis_stats(C.Structure):
         ("steps", C.c_int64), ("rebuilds", C.c_int64), ("pair_entries", C.c_int64), ("wca_pairs", C.c_int64),
         ("ele_pairs", C.c_int64), ("bp_pairs", C.c_int64), ("error_flags", C.c_int32), ("n_beads", C.c_int32),
         ("n_inst", C.c_int32), ("lanes_per_bead", C.c_int32), ("capped", C.c_int64),
-        ("bp_blocks", C.c_int32), ("reserved", C.c_int32),
+        ("bp_blocks", C.c_int32), ("overlap", C.c_int32),
     ]
 
 

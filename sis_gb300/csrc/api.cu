@@ -97,10 +97,11 @@ struct sis_ctx {
     GlobP graph_g{};
     bool use_graphs = true;
     // overlap: the step's pair forces (k_pairs) run on st3 concurrently with
-    // the bonded and base-pair pass; fork/join events.  Off by default: with
-    // k_pairs holding the register file at five blocks per SM the two passes
-    // barely overlap, and the split costs 1-3% on every workload measured.
+    // the bonded and base-pair pass; fork/join events.  overlap_mode -1: the
+    // autotuner chooses it with the lanes (until then off); 0 or 1: fixed.
     bool overlap = false;
+    int overlap_mode = -1;
+    bool lanes_fixed = false;
     cudaStream_t st3 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // k_bonded runs on st4 beside the base-pair kernels on st; ev_bond joins it
@@ -444,32 +445,114 @@ int ensure_step_graph(sis_ctx *ctx) {
     return build_step_graph(ctx);
 }
 
-// Picks the lanes-per-bead width G of the step kernel by timing force-only
-// launches (no state changes: they read positions and write a scratch force
-// array; the base-pair buffer they consume is zero between steps).
+// Picks the lanes-per-bead width G of the step kernel, and whether its pair
+// forces run in k_pairs beside the bonded and base-pair pass (overlap), by
+// timing the step kernels of every candidate: four steps captured as a graph
+// (without the trigger and rebuild), launched once to warm up and once
+// timed.  The step kernels update v, beta and move in place, the
+// displacement maxima of blocks that span many instances and the force-cap
+// counter; those are saved before and restored after, and the rest of what
+// they write (the other position buffer and its mirror, the per-block
+// partials, the base-pair forces they consume) is rewritten by the next real
+// step.  With the Monte Carlo removal on, the base-pair kernels are left out
+// of the timing, since they would consume the pass that is due.
 int autotune(sis_ctx *ctx) {
     if (ctx->tuned) return SIS_OK;
-    const int cand[4] = {2, 4, 8, 16};
-    float best = 1e30f;
-    int bestG = ctx->G;
-    cudaEvent_t e0 = ctx->ev[12], e1 = ctx->ev[13];
-    CK(launch_pre(ctx->D, ctx->g, ctx->cur, 1, 0, 0, 0, ctx->st));
-    ctx->launches++;
-    for (int c = 0; c < 4; ++c) {
-        CK(launch_force(cand[c], ctx->D, ctx->g, ctx->cur, ctx->fout_d, 55, ctx->st)); // warm-up (mask without base pairs)
-        CK(cudaEventRecord(e0, ctx->st));
-        for (int r = 0; r < 3; ++r) CK(launch_force(cand[c], ctx->D, ctx->g, ctx->cur, ctx->fout_d, 55, ctx->st));
-        CK(cudaEventRecord(e1, ctx->st));
-        CK(cudaEventSynchronize(e1));
-        float ms;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
-        ctx->launches += 4;
-        if (ms < best) {
-            best = ms;
-            bestG = cand[c];
+    std::vector<int> gs = ctx->lanes_fixed ? std::vector<int>{ctx->G} : std::vector<int>{2, 4, 8, 16};
+    std::vector<int> ovs = ctx->overlap_mode >= 0 ? std::vector<int>{ctx->overlap_mode} : std::vector<int>{0, 1};
+    if (gs.size() * ovs.size() == 1) {
+        ctx->G = gs[0];
+        ctx->overlap = ovs[0] != 0;
+        ctx->tuned = true;
+        return SIS_OK;
+    }
+    const bool with_bp = ctx->g.bp_model > 0 && ctx->g.nstep_mc == 0;
+    const size_t n = ctx->n, ni = ctx->n_inst;
+    Dev &D = ctx->D;
+    double4 *save = nullptr;
+    unsigned long long *msave = nullptr;
+    if (cudaMalloc(&save, sizeof(double4) * 3 * n) != cudaSuccess ||
+        cudaMalloc(&msave, sizeof(unsigned long long) * (4 * ni + 1)) != cudaSuccess) {
+        cudaFree(save);
+        cudaGetLastError();
+        return fail(ctx, SIS_ERR_NOMEM, "autotune scratch");
+    }
+    auto copy = [&](bool back) -> cudaError_t {
+        const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+        double4 *st[3] = {D.v, D.beta, D.move};
+        unsigned long long *ms[3] = {D.m1, D.m2, D.capped};
+        const size_t mc[3] = {2 * ni, 2 * ni, 1}, mo[3] = {0, 2 * ni, 4 * ni};
+        cudaError_t e = cudaSuccess;
+        for (int f = 0; f < 3 && e == cudaSuccess; ++f)
+            e = back ? cudaMemcpyAsync(st[f], save + f * n, sizeof(double4) * n, k, ctx->st)
+                     : cudaMemcpyAsync(save + f * n, st[f], sizeof(double4) * n, k, ctx->st);
+        for (int f = 0; f < 3 && e == cudaSuccess; ++f)
+            e = back ? cudaMemcpyAsync(ms[f], msave + mo[f], sizeof(unsigned long long) * mc[f], k, ctx->st)
+                     : cudaMemcpyAsync(msave + mo[f], ms[f], sizeof(unsigned long long) * mc[f], k, ctx->st);
+        return e;
+    };
+    auto pass = [&](int G, int ov) -> cudaError_t {
+        cudaError_t e;
+        if ((e = cudaEventRecord(ctx->ev_fork, ctx->st)) != cudaSuccess) return e;
+        if (ov) {
+            if ((e = cudaStreamWaitEvent(ctx->st3, ctx->ev_fork, 0)) != cudaSuccess) return e;
+            if ((e = launch_pairs(G, D, ctx->g, ctx->cur, ctx->st3)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(ctx->ev_join, ctx->st3)) != cudaSuccess) return e;
         }
+        if (with_bp) {
+            if ((e = cudaStreamWaitEvent(ctx->st4, ctx->ev_fork, 0)) != cudaSuccess) return e;
+            if ((e = launch_bonded(D, ctx->g, ctx->cur, ctx->st4)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(ctx->ev_bond, ctx->st4)) != cudaSuccess) return e;
+            if ((e = launch_bp(D, ctx->g, ctx->cur, bp_test_blocks(ctx), bp_blocks(ctx), ctx->st)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_bond, 0)) != cudaSuccess) return e;
+        } else if ((e = launch_bonded(D, ctx->g, ctx->cur, ctx->st)) != cudaSuccess) {
+            return e;
+        }
+        if (ov) {
+            if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
+            return launch_step_split(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st);
+        }
+        return launch_step(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st);
+    };
+    cudaError_t e = copy(false);
+    float best = 1e30f;
+    int bestG = gs[0], bestOv = ovs[0];
+    for (int G : gs)
+        for (int ov : ovs) {
+            if (e != cudaSuccess) break;
+            cudaGraph_t gr = nullptr;
+            cudaGraphExec_t ge = nullptr;
+            e = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeRelaxed);
+            for (int r = 0; r < 4 && e == cudaSuccess; ++r) e = pass(G, ov);
+            const cudaError_t ee = cudaStreamEndCapture(ctx->st, &gr);
+            if (e == cudaSuccess) e = ee;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, gr, 0);
+            if (gr) cudaGraphDestroy(gr);
+            float ms = 1e30f;
+            if (e == cudaSuccess) e = cudaGraphLaunch(ge, ctx->st);
+            if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[12], ctx->st);
+            if (e == cudaSuccess) e = cudaGraphLaunch(ge, ctx->st);
+            if (e == cudaSuccess) e = cudaEventRecord(ctx->ev[13], ctx->st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev[13]);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->ev[12], ctx->ev[13]);
+            if (ge) cudaGraphExecDestroy(ge);
+            ctx->launches += 8 * (2 + (ov ? 1 : 0) + (with_bp ? bp_kernels(ctx->g) : 0));
+            if (e == cudaSuccess && ms < best) {
+                best = ms;
+                bestG = G;
+                bestOv = ov;
+            }
+        }
+    if (e == cudaSuccess) e = copy(true);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    cudaFree(save);
+    cudaFree(msave);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, SIS_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
     }
     ctx->G = bestG;
+    ctx->overlap = bestOv != 0;
     ctx->tuned = true;
     return SIS_OK;
 }
@@ -1171,12 +1254,10 @@ extern "C" int sis_gpu_set_step(sis_ctx *ctx, uint64_t step) {
 extern "C" int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes) {
     if (!ctx || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32))
         return SIS_ERR_ARG;
-    if (lanes == 0) {
-        ctx->tuned = false;
-    } else {
-        ctx->G = lanes;
-        ctx->tuned = true;
-    }
+    ctx->lanes_fixed = lanes != 0;
+    if (lanes != 0) ctx->G = lanes;
+    // the overlap is still the autotuner's to choose unless it was fixed too
+    ctx->tuned = ctx->lanes_fixed && ctx->overlap_mode >= 0;
     return SIS_OK;
 }
 
@@ -1187,8 +1268,10 @@ extern "C" int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable) {
 }
 
 extern "C" int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable) {
-    if (!ctx || (enable != 0 && enable != 1)) return SIS_ERR_ARG;
-    ctx->overlap = enable != 0;
+    if (!ctx || (enable != 0 && enable != 1 && enable != -1)) return SIS_ERR_ARG;
+    ctx->overlap_mode = enable;
+    if (enable >= 0) ctx->overlap = enable != 0;
+    ctx->tuned = ctx->lanes_fixed && ctx->overlap_mode >= 0;
     return SIS_OK;
 }
 
@@ -1200,6 +1283,7 @@ extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
     s->n_inst = ctx->n_inst;
     s->lanes_per_bead = ctx->G;
     s->bp_blocks = bp_blocks(ctx);
+    s->overlap = ctx->overlap ? 1 : 0;
     long long rb = 0;
     unsigned long long cp = 0;
     int e = 0;

@@ -213,9 +213,10 @@ class Engine:
         self._ck(self.L.sis_gpu_remd_exchange(self.h, int(parity), ptr(u), r2l.ctypes.data_as(C.c_void_p), C.byref(acc)))
         return r2l, int(acc.value)
 
-    def set_overlap(self, enable: bool):
-        """Pair forces in their own kernel beside the bonded/base-pair pass (default) or in the step kernel."""
-        self._ck(self.L.sis_gpu_set_overlap(self.h, int(bool(enable))))
+    def set_overlap(self, enable):
+        """Pair forces in their own kernel beside the bonded/base-pair pass
+        (True) or in the step kernel (False); None lets the autotuner choose."""
+        self._ck(self.L.sis_gpu_set_overlap(self.h, -1 if enable is None else int(bool(enable))))
 
     def get_step(self) -> int:
         v = C.c_uint64()

@@ -376,8 +376,8 @@ def test_step_graph_equals_single_steps(name, prec, systems, sis_ff):
 
 @pytest.mark.parametrize("graphs", [True, False])
 def test_overlapped_step_equals_fused_step(graphs, sis_ff):
-    """Pair forces in their own kernel on a second stream or inside the step
-    kernel (default): the same trajectory bit for bit."""
+    """Pair forces in their own kernel on another stream or inside the step
+    kernel: the same trajectory bit for bit."""
     sysm = crowded_box(sis_ff, n_chains=12, n=500, molar=0.05, seed=23, rmin=4.0)
     a = Engine(sysm, precision=MIXED, seed=6)
     b = Engine(sysm, precision=MIXED, seed=6)
@@ -392,6 +392,35 @@ def test_overlapped_step_equals_fused_step(graphs, sis_ff):
     for u, w in zip(a.get_state(-1), b.get_state(-1)):
         assert np.array_equal(u, w)
     assert a.stats()["rebuilds"] == b.stats()["rebuilds"] > 1
+
+
+@pytest.mark.parametrize("name", ["uneven", "cells"])
+def test_autotune_leaves_the_state_as_it_was(name, sis_ff):
+    """The autotuner times the real step kernels of every candidate (lanes
+    per bead, pair kernel beside the bonded pass or not) and restores what
+    they update in place.  A run that tuned first equals, bit for bit, a run
+    fixed at the configuration it chose.  The uneven batch has blocks that
+    span many instances, whose displacement maxima go straight to the
+    per-instance words the tuning also restores."""
+    if name == "uneven":
+        sysm = uneven_batch(sis_ff, n_inst=24, lmin=8, lmax=120, seed=5)
+    else:
+        sysm = crowded_box(sis_ff, n_chains=12, n=500, molar=0.05, seed=23, rmin=4.0)
+    a = Engine(sysm, precision=MIXED, seed=9)
+    a.set_force_cap(1000.0)
+    a.init_velocities()
+    a.step(80)
+    st = a.stats()
+    b = Engine(sysm, precision=MIXED, seed=9)
+    b.set_lanes(st["lanes_per_bead"])
+    b.set_overlap(bool(st["overlap"]))
+    b.set_force_cap(1000.0)
+    b.init_velocities()
+    b.step(80)
+    for u, w in zip(a.get_state(-1), b.get_state(-1)):
+        assert np.array_equal(u, w)
+    assert a.stats()["rebuilds"] == b.stats()["rebuilds"]
+    assert a.stats()["capped"] == b.stats()["capped"]
 
 
 def test_instance_alone_equals_instance_in_batch(sis_ff):
