@@ -38,6 +38,7 @@ extern "C" {
 #define SIS_ERR_NONFINITE -4    /* NaN/Inf detected in coordinates or forces */
 #define SIS_ERR_NOMEM -5        /* device allocation failed */
 #define SIS_ERR_STATE -6        /* call out of order (e.g. force before set_state) */
+#define SIS_ERR_TIMEOUT -7      /* a bounded device wait ran out (the grid barrier of the trigger/rebuild kernel) */
 
 /* arithmetic of the force terms */
 #define SIS_PREC_FP64 0  /* all terms and the integration in FP64 (plain path) */
@@ -218,6 +219,12 @@ int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable);
 int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable);
 
 int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *st);
+/* Failure-detection self-test (no counterpart in the reference): one block of
+ * a cooperative launch never reaches the grid barrier that the
+ * trigger/rebuild kernel uses, so the other blocks' bounded waits run out
+ * (about a second).  Returns SIS_ERR_TIMEOUT when the kernel reported the
+ * timeout; the barrier is then reset, and the context works on. */
+int sis_gpu_probe_barrier_timeout(sis_ctx *ctx);
 /* Human-readable description of the last error on this context. */
 const char *sis_gpu_last_error(const sis_ctx *ctx);
 

@@ -18,7 +18,8 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libsisgpu.so"
 
 SIS_OK = 0
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "list overflow", -4: "non-finite values", -5: "out of device memory",
-          -6: "call out of order"}
+          -6: "call out of order", -7: "device wait timed out"}
+SIS_ERR_TIMEOUT = -7
 
 
 class SisError(RuntimeError):
@@ -101,6 +102,7 @@ EXPORTS = {
     "sis_gpu_event_elapsed": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_float)]),
     "sis_gpu_synchronize": (C.c_int, [C.c_void_p]),
     "sis_gpu_flush_l2": (C.c_int, [C.c_void_p]),
+    "sis_gpu_probe_barrier_timeout": (C.c_int, [C.c_void_p]),
     "sis_gpu_kernel_launches": (C.c_int64, [C.c_void_p]),
     "sis_gpu_step_profiled": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "sis_gpu_step_noise_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),

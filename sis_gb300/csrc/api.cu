@@ -340,7 +340,8 @@ int check_err(sis_ctx *ctx) {
     if (e & ERR_TIMEOUT) {
         // a block left the trigger/rebuild kernel early: start its barrier afresh
         CK(cudaMemsetAsync(ctx->D.gbar, 0, 2 * sizeof(unsigned int), ctx->st));
-        return fail(ctx, SIS_ERR_CUDA, "grid barrier of the trigger/rebuild kernel timed out");
+        CK(cudaStreamSynchronize(ctx->st));
+        return fail(ctx, SIS_ERR_TIMEOUT, "grid barrier of the trigger/rebuild kernel timed out");
     }
     return SIS_OK;
 }
@@ -1273,6 +1274,13 @@ extern "C" int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable) {
     if (enable >= 0) ctx->overlap = enable != 0;
     ctx->tuned = ctx->lanes_fixed && ctx->overlap_mode >= 0;
     return SIS_OK;
+}
+
+extern "C" int sis_gpu_probe_barrier_timeout(sis_ctx *ctx) {
+    if (!ctx) return SIS_ERR_ARG;
+    CK(launch_barrier_probe(ctx->D, ctx->coop_grid, ctx->coop_grid - 1, ctx->st));
+    ctx->launches++;
+    return check_err(ctx);
 }
 
 extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {

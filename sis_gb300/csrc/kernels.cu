@@ -740,6 +740,70 @@ __device__ __forceinline__ V3<R> pair_sum(const Dev &D, const GlobP &g, int cur,
     return an;
 }
 
+// pair_sum for k_pairs, whose register budget leaves room for the batch
+template <typename R, int G>
+__device__ __forceinline__ V3<R> pair_sum_b(const Dev &D, const GlobP &g, int cur, int i, int lane, const InstP &ip, int mask) {
+    V3<R> an = mk<R>(0, 0, 0);
+    const int cnt = min(D.nnbr[i], g.cap);
+    const int *__restrict__ nb = D.nbr + (size_t)i * g.cap;
+    if constexpr (sizeof(R) == 4) {
+        const uint4 mi = D.mir[cur][i];
+        const uint4 *__restrict__ mir = D.mir[cur];
+        const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
+        const float sig2 = g.f_wca_sig2, wcoef = g.f_wca_coef;
+        const float ecoef = ip.ele_coef_f, rc = ip.rcdist_f;
+        const float cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+        // batches of B entries per lane: the B list words, then the B mirror
+        // gathers, are all issued before any is used, so each lane keeps B
+        // gathers in flight; the entries still add in list order, as in
+        // pair_sum, so the split step equals the fused one bit for bit
+        constexpr int B = 4;
+        for (int k0 = lane; k0 < cnt; k0 += B * G) {
+            int e[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) e[u] = k0 + u * G < cnt ? __ldg(nb + k0 + u * G) : 0;
+            uint4 mj[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u) mj[u] = k0 + u * G < cnt ? __ldg(mir + (e[u] & IDX_MASK)) : mi;
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                if (k0 + u * G >= cnt) break;
+                const float vx = (float)(int)(mi.x - mj[u].x) * f0;
+                const float vy = (float)(int)(mi.y - mj[u].y) * f1;
+                const float vz = (float)(int)(mi.z - mj[u].z) * f2;
+                const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+                float c = 0.f;
+                if ((e[u] & WCA_BIT) && (mask & 16) && d2 < sig2) {
+                    const float sq = __fdiv_rn(sig2, d2);
+                    const float s2 = sq * sq, s4 = s2 * s2;
+                    c += wcoef * (s4 * s2 * sq - s4);
+                }
+                if ((e[u] & ELE_BIT) && (mask & 32) && d2 <= cut2) {
+                    float ri = rsqrtf(d2);
+                    ri = ri * fmaf(-0.5f * d2 * ri, ri, 1.5f);
+                    const float r = d2 * ri;
+                    c += ecoef * ri * ri * (ri + rc) * __expf(-r * rc);
+                }
+                an.x = fmaf(c, vx, an.x);
+                an.y = fmaf(c, vy, an.y);
+                an.z = fmaf(c, vz, an.z);
+            }
+        }
+    } else {
+        const R sig2 = g.wca_sig2, wcoef = g.wca_coef;
+        const R ecoef = ip.ele_coef, rc = ip.rcdist;
+        const R cut2 = g.flg_ele ? ip.ele_cut2 : R(-1);
+        const Pos<R> P = pos_of<R>(D, cur);
+        for (int k = lane; k < cnt; k += G) {
+            const int e = __ldg(nb + k);
+            const V3<R> v = P.d(i, e & IDX_MASK, ip);
+            const R c = pair_coef<R>(e, dot3(v, v), sig2, wcoef, ecoef, rc, cut2, mask);
+            an = an + c * v;
+        }
+    }
+    return an;
+}
+
 // Pair forces of every bead into fpair (float4 / double4), the step kernel's
 // phase A run by itself, so that it can overlap the bonded and base-pair pass
 template <typename R, int G> __global__ void __launch_bounds__(256, 5) k_pairs(Dev D, GlobP g, int cur) {
@@ -748,7 +812,7 @@ template <typename R, int G> __global__ void __launch_bounds__(256, 5) k_pairs(D
     const int i_raw = blockIdx.x * BPB + b;
     const int i = i_raw < g.n ? i_raw : g.n - 1;
     const InstP &ip = D.ip[D.binfo[i].x];
-    V3<R> an = pair_sum<R, G>(D, g, cur, i, lane, ip, 48);
+    V3<R> an = pair_sum_b<R, G>(D, g, cur, i, lane, ip, 48);
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
         an.x += __shfl_xor_sync(0xffffffffu, an.x, o, G);

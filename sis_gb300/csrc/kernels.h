@@ -59,5 +59,7 @@ cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st
 cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, int grid,
                            cudaStream_t st);
 int coop_blocks_per_sm();
+// the grid barrier with block `absent` missing (a self-test of its timeout)
+cudaError_t launch_barrier_probe(const Dev &D, int grid, int absent, cudaStream_t st);
 
 } // namespace sisg

@@ -224,8 +224,14 @@ __device__ __forceinline__ void bead_end(const Dev &D, const GlobP &g, int gi, i
 
 // ------------------------------------------------------- grid barrier
 // Every block of the cooperative launch is resident at once, so a wait ends
-// when the last block arrives.  The wait is bounded all the same: after
-// about a second the block records ERR_TIMEOUT and leaves the kernel.
+// when the last block arrives.  The wait is bounded all the same: after one
+// second of the global timer (or 2^26 polls) the block records ERR_TIMEOUT
+// and leaves the kernel.
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 __device__ bool grid_sync(const Dev &D) {
     __shared__ int s_ok;
     __syncthreads();
@@ -240,11 +246,13 @@ __device__ bool grid_sync(const Dev &D) {
             atomicAdd(gen, 1u);
             ok = 1;
         } else {
-            for (int it = 0; it < (1 << 24); ++it) {
+            const unsigned long long t0 = global_ns();
+            for (int it = 0; it < (1 << 26); ++it) {
                 if (*(volatile unsigned int *)gen != g0) {
                     ok = 1;
                     break;
                 }
+                if ((it & 255) == 255 && global_ns() - t0 > 1000000000ull) break;
                 __nanosleep(32);
             }
             if (!ok) atomicOr(D.err, ERR_TIMEOUT);
@@ -656,6 +664,26 @@ __global__ void __launch_bounds__(256) k_trigger_rebuild(Dev D, GlobP g, int cur
     if (pl.n_small_items > 0) rebuild_small(D, g, cur, pl.small_items, pl.n_small_items, slack);
     if (!grid_sync(D)) return;
     rebuild_finish(D, g);
+}
+
+// Self-test of the barrier's bounded wait: block `absent` leaves at once, so
+// the wait of every other block runs out, records ERR_TIMEOUT and returns.
+__global__ void __launch_bounds__(256) k_barrier_probe(Dev D, int absent) {
+    if ((int)blockIdx.x == absent) return;
+    grid_sync(D);
+}
+
+cudaError_t launch_barrier_probe(const Dev &D, int grid, int absent, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_barrier_probe, D, absent);
 }
 
 int coop_blocks_per_sm() {
