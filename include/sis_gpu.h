@@ -278,6 +278,11 @@ int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, 
  * of sis_gpu_get_list(..., SIS_LIST_BP, ...). */
 int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, int32_t n_draws);
 int sis_gpu_get_bp_status(sis_ctx *ctx, int32_t inst, uint8_t *out, int32_t cap, int32_t *n_out);
+/* The energy of every base-pair record cached by the last force or energy
+ * evaluation (ene_bp of var_state.F90, zero for records outside the window
+ * or above the energy cut), in the order of sis_gpu_get_list(...,
+ * SIS_LIST_BP, ...): what write_bp.F90 writes to the .bp/.bpall/.bpe files. */
+int sis_gpu_get_bp_energies(sis_ctx *ctx, int32_t inst, double *out, int32_t cap, int32_t *n_out);
 
 /* Serving slots (no counterpart in the reference, whose jobs are separate
  * runs).  Replaces the topology, conditions and state of instance inst by a

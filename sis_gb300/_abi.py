@@ -109,6 +109,7 @@ EXPORTS = {
     "sis_gpu_remd_init": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sis_gpu_bp_mc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]),
     "sis_gpu_get_bp_status": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "sis_gpu_get_bp_energies": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "sis_gpu_load_slot": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                     C.c_double, C.c_uint32, C.c_void_p, C.c_int32]),
     "sis_gpu_remd_exchange": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),

@@ -89,8 +89,8 @@ struct sis_ctx {
     size_t flush_bytes = 0;
     std::vector<void *> allocs;
     double4 *pin = nullptr; // pinned staging buffer for state transfers (n double4)
-    // steady-state step graph (kGraphSteps steps, rebuild bodies behind
-    // conditional nodes) and the parameters it was captured with
+    // steady-state step graph (kGraphSteps steps, each ending with the
+    // cooperative trigger/rebuild kernel) and the parameters it was captured with
     cudaGraphExec_t gexec = nullptr;
     int graph_cur = -1, graph_G = 0, graph_bpb = 0;
     bool graph_overlap = false;
@@ -1248,6 +1248,9 @@ extern "C" int sis_gpu_set_step(sis_ctx *ctx, uint64_t step) {
     if (!ctx) return SIS_ERR_ARG;
     unsigned long long v = step;
     CK(cudaMemcpyAsync(ctx->D.step_ctr, &v, sizeof(v), cudaMemcpyHostToDevice, ctx->st));
+    // the displacement maxima are kept by step parity: start both afresh
+    CK(cudaMemsetAsync(ctx->D.m1, 0, sizeof(unsigned long long) * 2 * ctx->n_inst, ctx->st));
+    CK(cudaMemsetAsync(ctx->D.m2, 0, sizeof(unsigned long long) * 2 * ctx->n_inst, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return SIS_OK;
 }
@@ -1662,6 +1665,21 @@ extern "C" int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, in
         ctx->D.mc_draws = ctx->mc_draws_d;
         ctx->D.mc_n_draws = n_draws;
         ctx->mc_pending = true;
+    }
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_get_bp_energies(sis_ctx *ctx, int32_t inst, double *out, int32_t cap, int32_t *n_out) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || !n_out) return SIS_ERR_ARG;
+    const InstP &I = ctx->ip[inst];
+    int c = 0;
+    CK(cudaMemcpyAsync(&c, ctx->D.bp_cnt + inst, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    c = std::min(c, I.bp_cap);
+    *n_out = c;
+    if (out && cap > 0) {
+        CK(cudaMemcpyAsync(out, ctx->D.ene_bp + I.bp_off, sizeof(double) * std::min(c, cap), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
     }
     return SIS_OK;
 }

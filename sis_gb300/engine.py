@@ -187,6 +187,14 @@ class Engine:
         d = None if draws is None else np.ascontiguousarray(draws, dtype=np.float64)
         self._ck(self.L.sis_gpu_bp_mc(self.h, int(inst), ptr(d), 0 if d is None else d.size))
 
+    def get_bp_energies(self, inst: int) -> np.ndarray:
+        """Cached energy of every base-pair record (order of get_list(inst, 2))."""
+        n = C.c_int32()
+        self._ck(self.L.sis_gpu_get_bp_energies(self.h, inst, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.float64)
+        self._ck(self.L.sis_gpu_get_bp_energies(self.h, inst, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n)))
+        return out
+
     def get_bp_status(self, inst: int) -> np.ndarray:
         n = C.c_int32()
         self._ck(self.L.sis_gpu_get_bp_status(self.h, inst, None, 0, C.byref(n)))

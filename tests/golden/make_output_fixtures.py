@@ -1,0 +1,89 @@
+"""Generates tests/golden/outputs.json: files written by sis_gb300.outputs
+for a fixed table of frames, and what the reference's own readers
+(utils/sisout.py, utils/sisbp.py of the reference tree) make of them.
+
+Run in a container that holds the reference tree:
+    python tests/golden/make_output_fixtures.py /path/to/reference
+The reference's sisbp.py imports an error class from a package that is not
+part of the tree; a stand-in module with that class is installed first.
+"""
+import json
+import sys
+import tempfile
+import types
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from sis_gb300.outputs import BpFile, OutFile  # noqa: E402
+
+# frames: step, T, Ekin, energies[0..10]; values chosen to exercise every
+# branch of G editing (F forms with 6..0 decimals, E forms, zero, negatives)
+FRAMES = [
+    (0, 300.0, 41.868614648997, [29.1441412318505, 0.003363370866894, 4.398169526634435, 0.0, -11.058858430180448,
+                                 0.0, 35.8, 0, 0, 0, 0]),
+    (100, 300.0, 1234.5678, [-0.05, 99999.9, 999999.4, 1.0e-7, -2.5e8, 0.1, -0.0999999, 0, 0, 0, 0]),
+    (123456789, 310.15, 7.0, [1.0, -1.0, 12.345678, 123.4567, 1234.567, 12345.67, 123456.7, 0, 0, 0, 0]),
+]
+# base-pair records (i, j), status and energies of two frames at 300 K
+BP_FRAMES = [
+    ([(5, 20), (6, 19), (7, 18), (30, 44)], [1, 1, 0, 1], [-3.2, -0.4, -5.0, -1.5]),
+    ([(5, 20), (6, 19)], [1, 1], [-0.2, -2.75]),
+]
+
+
+def main(ref: Path):
+    sys.path.insert(0, str(ref / "utils"))
+    lop = types.ModuleType("lop")
+    elements = types.ModuleType("lop.elements")
+    error = types.ModuleType("lop.elements.error")
+
+    class MyError(Exception):
+        pass
+
+    error.MyError = MyError
+    sys.modules.update({"lop": lop, "lop.elements": elements, "lop.elements.error": error})
+    import sisbp  # noqa: E402
+    import sisout  # noqa: E402
+
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for replica in (False, True):
+            p = Path(d) / f"run{int(replica)}.out"
+            w = OutFile(p, replica=replica, ele=True)
+            for k, (step, T, ekin, e) in enumerate(FRAMES):
+                w.write(step, T, ekin, e, rep_label=k + 1 if replica else None)
+            w.close()
+            text = p.read_text()
+            f = sisout.SisoutFile(str(p))
+            f.open_to_read()
+            f.read_header()
+            cols = {k: v for k, v in vars(f.head_col).items() if v is not None}
+            rows = []
+            while f.has_more_data():
+                rows.append([float(v) for v in f.read_onestep()[0][0]])
+            f.close()
+            out[f"out_replica{int(replica)}"] = {"text": text, "columns": cols, "rows": rows}
+        p = Path(d) / "run.bp"
+        w = BpFile(p)
+        for pairs, st, ene in BP_FRAMES:
+            w.write_frame(np.array(pairs), np.array(st), np.array(ene), 300.0)
+        w.close()
+        f = sisbp.SisbpFile(str(p))
+        f.open_to_read()
+        frames = []
+        while f.has_more_data():
+            pairs, energies = f.read_onestep()
+            frames.append({"pairs": [list(q) for q in pairs], "energies": [float(e) for e in energies]})
+        f.close()
+        out["bp"] = {"bytes_hex": p.read_bytes().hex(), "frames": frames}
+    out["frames"] = FRAMES
+    out["bp_frames"] = BP_FRAMES
+    (Path(__file__).parent / "outputs.json").write_text(json.dumps(out, indent=1))
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
