@@ -334,15 +334,20 @@ int check_err(sis_ctx *ctx) {
     CK(cudaMemcpyAsync(&e, ctx->D.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     if (e) CK(cudaMemsetAsync(ctx->D.err, 0, sizeof(int), ctx->st));
+    if (e & ERR_TIMEOUT) {
+        // blocks left the trigger/rebuild kernel early: start its barrier
+        // afresh, clear the cell counters a binning phase may have left
+        // partly filled, and rebuild every list at the next call (a rebuild
+        // may have stopped half way)
+        CK(cudaMemsetAsync(ctx->D.gbar, 0, 2 * sizeof(unsigned int), ctx->st));
+        if (ctx->D.n_cells > 0) CK(cudaMemsetAsync(ctx->D.cell_cnt, 0, sizeof(int) * ctx->D.n_cells, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        ctx->lists_valid = false;
+    }
     if (e & ERR_PAIR_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "pair list capacity exceeded");
     if (e & ERR_BP_OVERFLOW) return fail(ctx, SIS_ERR_LIST_OVERFLOW, "base-pair list capacity exceeded");
     if (e & ERR_NONFINITE) return fail(ctx, SIS_ERR_NONFINITE, "non-finite displacement");
-    if (e & ERR_TIMEOUT) {
-        // a block left the trigger/rebuild kernel early: start its barrier afresh
-        CK(cudaMemsetAsync(ctx->D.gbar, 0, 2 * sizeof(unsigned int), ctx->st));
-        CK(cudaStreamSynchronize(ctx->st));
-        return fail(ctx, SIS_ERR_TIMEOUT, "grid barrier of the trigger/rebuild kernel timed out");
-    }
+    if (e & ERR_TIMEOUT) return fail(ctx, SIS_ERR_TIMEOUT, "grid barrier of the trigger/rebuild kernel timed out");
     return SIS_OK;
 }
 
