@@ -193,6 +193,27 @@ int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic
  * structures with overlapping beads; it has no counterpart in the reference
  * and is off unless set. */
 int sis_gpu_set_force_cap(sis_ctx *ctx, double fmax);
+
+/* Optional terms of force.F90:62-75 and energy_sumup.F90:47-52, evaluated in
+ * FP64 in both precisions: force term 7 of sis_gpu_force_term, energy slots
+ * 7 (stage), 8 (tweezers), 9 (Rg bias) and 10 (restraints).
+ * sis_gpu_set_stage: the wall at z = 0 of force_stage.F90 / energy_stage.F90
+ * (stage_sigma, stage_eps); sigma = 0 turns it off.
+ * sis_gpu_set_rg_bias: the bias on the radius of gyration of force_rg.F90 /
+ * energy_rg.F90 for one instance (inst = -1: all); pott 0 off, 1 harmonic,
+ * 2 flat-bottomed (no force while Rg <= rg0).
+ * sis_gpu_set_bias_items: the sigmoid restraints (force_restraint.F90) and
+ * tweezers trap pairs (force_tweezers.F90) of one instance, replacing those
+ * set before: kind_ij[n][3] = kind, i, j (1-based beads of the instance);
+ * par[n][14].  kind 1 restraint on both beads, 2 restraint on bead i only
+ * (Sigmoid-to-bead), par eps, d, s, rcut; kind 3 constant-force trap pair,
+ * par the force on bead i (its negative on bead j); kind 4 force-ramp trap
+ * pair, par k_i, k_j, trap starts (i xyz, j xyz), trap velocities per step
+ * (i xyz, j xyz): the traps sit at start + velocity * istep, istep counting
+ * the step being taken (job_md.F90:362), or the steps taken outside one. */
+int sis_gpu_set_stage(sis_ctx *ctx, double sigma, double eps);
+int sis_gpu_set_rg_bias(sis_ctx *ctx, int32_t inst, int32_t pott, double k, double rg0);
+int sis_gpu_set_bias_items(sis_ctx *ctx, int32_t inst, int32_t n, const int32_t *kind_ij, const double *par);
 /* per-bead integrator coefficients of instance inst, 4 per bead: GJF-2GJ
  * md_coef(1:3) and md_coef_rep(1) (src/job_md.F90:700-767) */
 int sis_gpu_get_md_coef(sis_ctx *ctx, int32_t inst, double *out4);

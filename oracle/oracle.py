@@ -101,6 +101,10 @@ def lib() -> C.CDLL:
             "or_mt_boxmuller": (d, [vp]),
             "or_seed": (None, [vp, i32]),
             "or_const": (d, [i32]),
+            "or_set_stage": (None, [vp, d, d]),
+            "or_set_rg_bias": (None, [vp, i32, d, vp]),
+            "or_set_restraints": (None, [vp, i32, vp, vp]),
+            "or_set_tweezers": (None, [vp, i32, vp, vp, i32, vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -236,6 +240,33 @@ class Oracle:
         out = np.zeros(n, dtype=np.uint8)
         self.L.or_get_bp_status(self.h, r, out.ctypes.data_as(C.c_void_p), n)
         return out
+
+    # optional terms (force.F90:62-75): force term 7, energy slots 7-10
+    def set_stage(self, sigma, eps):
+        self.L.or_set_stage(self.h, float(sigma), float(eps))
+
+    def set_rg_bias(self, k, rg0, flat=False, off=False):
+        r0 = np.broadcast_to(np.asarray(rg0, dtype=np.float64), (self.nrep,)).copy()
+        self._rg0 = r0
+        self.L.or_set_rg_bias(self.h, 0 if off else (2 if flat else 1), float(k), _p(r0))
+
+    def set_restraints(self, restraints):
+        ids = np.array([[q.i, q.j, 2 if q.to_bead else 1] for q in restraints], dtype=np.int32).reshape(-1, 3)
+        par = np.array([[q.eps, q.d, q.s, q.rcut] for q in restraints], dtype=np.float64).reshape(-1, 4)
+        self._rest = (ids, par)
+        self.L.or_set_restraints(self.h, len(restraints), _p(ids), _p(par))
+
+    def set_tweezers(self, dcf=(), fr=()):
+        """dcf: ConstantForcePair (same force in every replica); fr: ForceRampPair."""
+        dp = np.array([[q.i, q.j] for q in dcf], dtype=np.int32).reshape(-1, 2)
+        df = np.ascontiguousarray(np.broadcast_to(np.array([q.force for q in dcf], dtype=np.float64).reshape(-1, 3),
+                                                  (self.nrep, len(dcf), 3)))
+        fp = np.array([[q.i, q.j] for q in fr], dtype=np.int32).reshape(-1, 2)
+        fk = np.array([q.k for q in fr], dtype=np.float64).reshape(-1, 2)
+        fi = np.array([q.init for q in fr], dtype=np.float64).reshape(-1, 2, 3)
+        fv = np.array([q.velo for q in fr], dtype=np.float64).reshape(-1, 2, 3)
+        self._twz = (dp, df, fp, fk, fi, fv)
+        self.L.or_set_tweezers(self.h, len(dcf), _p(dp), _p(df), len(fr), _p(fp), _p(fk), _p(fi), _p(fv))
 
     def force_term(self, r, term):
         f = np.empty((self.nmp, 3))

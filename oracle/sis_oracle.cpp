@@ -14,6 +14,7 @@
  */
 #include "sis_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -121,6 +122,19 @@ struct or_system {
     or_mt *spare_owner; /* the spare of rnd_boxmuller is shared by all replicas */
     bool spare_stored;
     double spare_value;
+    /* optional terms, force.F90:62-75 / energy_sumup.F90:47-52 */
+    bool stage = false;
+    double stage_sigma = 0.0, stage_eps = 0.0;
+    int rg_pott = 0;               /* 0 off, 1 harmonic, 2 flat-bottomed (const_idx.F90 POTT) */
+    double rg_k = 0.0;
+    std::vector<double> rg0;       /* per replica (bias_rg_0) */
+    std::vector<int> rest_id;      /* [n][3]: imp, jmp (1-based), type 1 both beads, 2 subject only */
+    std::vector<double> rest_para; /* [n][4]: eps, d, s, rcut (rest_sigb_para, rest_sigb_rcut) */
+    std::vector<int> dcf_pairs;    /* [n][2] twz_DCF_pairs */
+    std::vector<double> dcf_f;     /* [nrep][n][3] twz_DCF_forces */
+    std::vector<int> fr_pairs;     /* [n][2] twz_FR_pairs */
+    std::vector<double> fr_k;      /* [n][2] twz_FR_k */
+    std::vector<double> fr_init, fr_velo; /* [n][2][3] twz_FR_init, twz_FR_velo */
 };
 
 namespace {
@@ -1031,9 +1045,78 @@ int nthreads() {
 
 } // namespace
 
+/* The optional terms of force.F90:62-75 (term 7 here): force_stage.F90,
+ * force_tweezers.F90 (istep: the step being taken, job_md.F90:362),
+ * force_rg.F90 and force_restraint.F90. */
+static void force_bias(or_system *s, int irep, double *forces, int64_t istep) {
+    const Rep &R = s->rep[irep];
+    const int n = s->nmp;
+    if (s->stage) {
+        const double coef = 24.0 * s->stage_eps / s->stage_sigma;
+        const double small = DBL_EPSILON; /* const_phys.F90 SMALL_VALUE = epsilon(PI) */
+        for (int i = 0; i < n; ++i) {
+            double z = R.xyz[3 * i + 2];
+            if (z < small) z = small;
+            z = s->stage_sigma / z;
+            const double z2 = z * z, z6 = z2 * z2 * z2, z7 = z6 * z, z13 = z6 * z7;
+            forces[3 * i + 2] = forces[3 * i + 2] + coef * (2.0 * z13 - z7);
+        }
+    }
+    const int ndcf = (int)s->dcf_pairs.size() / 2;
+    for (int q = 0; q < ndcf; ++q) {
+        const int i1 = s->dcf_pairs[2 * q] - 1, i2 = s->dcf_pairs[2 * q + 1] - 1;
+        const double *F = &s->dcf_f[((size_t)irep * ndcf + q) * 3];
+        for (int k = 0; k < 3; ++k) {
+            forces[3 * i1 + k] = forces[3 * i1 + k] + F[k];
+            forces[3 * i2 + k] = forces[3 * i2 + k] - F[k];
+        }
+    }
+    for (int q = 0; q < (int)s->fr_pairs.size() / 2; ++q) {
+        for (int t = 0; t < 2; ++t) {
+            const int i = s->fr_pairs[2 * q + t] - 1;
+            double p[3], v[3];
+            for (int k = 0; k < 3; ++k) p[k] = s->fr_init[6 * q + 3 * t + k] + s->fr_velo[6 * q + 3 * t + k] * (double)istep;
+            pbc_vec_d(s, p, &R.xyz[3 * i], v);
+            for (int k = 0; k < 3; ++k) forces[3 * i + k] = forces[3 * i + k] + s->fr_k[2 * q + t] * v[k];
+        }
+    }
+    if (s->rg_pott > 0) {
+        double cm[3] = {0.0, 0.0, 0.0}, s2 = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < 3; ++k) cm[k] += R.xyz[3 * i + k];
+        for (int k = 0; k < 3; ++k) cm[k] /= (double)n;
+        for (int i = 0; i < n; ++i) {
+            double v[3] = {R.xyz[3 * i] - cm[0], R.xyz[3 * i + 1] - cm[1], R.xyz[3 * i + 2] - cm[2]};
+            s2 += dot(v, v);
+        }
+        const double rg = sqrt(s2 / (double)n), r0 = s->rg0[irep];
+        if (!(s->rg_pott == 2 && rg <= r0)) {
+            const double factor = -s->rg_k * (rg - r0) / (rg * n);
+            for (int i = 0; i < n; ++i)
+                for (int k = 0; k < 3; ++k) forces[3 * i + k] = forces[3 * i + k] + factor * (R.xyz[3 * i + k] - cm[k]);
+        }
+    }
+    for (int q = 0; q < (int)s->rest_id.size() / 3; ++q) {
+        const int i = s->rest_id[3 * q] - 1, j = s->rest_id[3 * q + 1] - 1, type = s->rest_id[3 * q + 2];
+        double v[3];
+        pbc_vec_d(s, &R.xyz[3 * i], &R.xyz[3 * j], v);
+        const double r = norm2(v);
+        const double *pp = &s->rest_para[4 * q];
+        if (r >= pp[3]) continue;
+        const double th = tanh((r - pp[1]) / pp[2]);
+        const double coef = 0.5 * pp[0] / pp[2] * (1.0 - th * th) / r;
+        for (int k = 0; k < 3; ++k) {
+            forces[3 * i + k] = forces[3 * i + k] - coef * v[k];
+            if (type == 1) forces[3 * j + k] = forces[3 * j + k] + coef * v[k];
+        }
+    }
+}
+
 /* force.F90:1-77 : all terms.  Per-thread private buffers summed at the end as
- * force.F90:66-69 does. */
-static void force_impl(or_system *s, int irep, double *forces, int only_term) {
+ * force.F90:66-69 does.  istep: the reference's step number for the
+ * time-dependent traps (the step being taken, or the steps taken outside
+ * the MD loop). */
+static void force_impl(or_system *s, int irep, double *forces, int only_term, int64_t istep) {
     Rep &R = s->rep[irep];
     const int n = s->nmp;
     const int nt = nthreads();
@@ -1087,12 +1170,13 @@ static void force_impl(or_system *s, int irep, double *forces, int only_term) {
     }
     if ((only_term == 0 || only_term == 4) && s->mc_now) bp_mc(s, irep, tK, forces);
     if (only_term == 0 || only_term == 4) s->flg_bp_energy = true;
+    if (only_term == 0 || only_term == 7) force_bias(s, irep, forces, istep);
 }
 
-extern "C" void or_force(or_system *s, int32_t irep, double *forces) { force_impl(s, irep, forces, 0); }
+extern "C" void or_force(or_system *s, int32_t irep, double *forces) { force_impl(s, irep, forces, 0, s->istep); }
 extern "C" void or_force_mc(or_system *s, int32_t irep, double *forces) {
     s->mc_now = true;
-    force_impl(s, irep, forces, 0);
+    force_impl(s, irep, forces, 0, s->istep);
     s->mc_now = false;
 }
 extern "C" int32_t or_get_mc_draws(const or_system *s, double *out, int32_t cap) {
@@ -1107,7 +1191,7 @@ extern "C" int32_t or_get_bp_status(const or_system *s, int32_t irep, uint8_t *o
     return n;
 }
 extern "C" void or_force_term(or_system *s, int32_t irep, int32_t term, double *forces) {
-    force_impl(s, irep, forces, term);
+    force_impl(s, irep, forces, term, s->istep);
 }
 
 /* ---------------------------------------------------------------- energies */
@@ -1248,9 +1332,60 @@ extern "C" void or_energy_sumup(or_system *s, int32_t irep, double tempK_in, dou
             }
         }
     }
+    /* energy_stage.F90, energy_tweezers.F90, energy_rg.F90, energy_restraint.F90 */
+    if (s->stage) {
+        const double eps4 = 4 * s->stage_eps;
+        for (int i = 0; i < s->nmp; ++i) {
+            const double z = s->stage_sigma / R.xyz[3 * i + 2];
+            const double z2 = z * z, z6 = z2 * z2 * z2;
+            E[7] = E[7] + eps4 * (z6 * z6 - z6);
+        }
+    }
+    const int ndcf = (int)s->dcf_pairs.size() / 2;
+    for (int q = 0; q < ndcf; ++q) {
+        double v[3];
+        pbc_vec_d(s, X(s, irep, s->dcf_pairs[2 * q]), X(s, irep, s->dcf_pairs[2 * q + 1]), v);
+        E[8] = E[8] - dot(v, &s->dcf_f[((size_t)irep * ndcf + q) * 3]);
+    }
+    if (s->rg_pott > 0) {
+        const double rg = or_rg(s, irep), r0 = s->rg0[irep];
+        E[9] = (s->rg_pott == 2 && rg <= r0) ? 0.0 : 0.5 * s->rg_k * (rg - r0) * (rg - r0);
+    }
+    for (int q = 0; q < (int)s->rest_id.size() / 3; ++q) {
+        double v[3];
+        pbc_vec_d(s, X(s, irep, s->rest_id[3 * q]), X(s, irep, s->rest_id[3 * q + 1]), v);
+        const double r = norm2(v);
+        const double *pp = &s->rest_para[4 * q];
+        if (r >= pp[3]) continue;
+        E[10] = E[10] - 0.5 * pp[0] * (1.0 - tanh((r - pp[1]) / pp[2]));
+    }
     double tot = 0.0;
     for (int k = 1; k <= 10; ++k) tot += E[k];
     E[0] = tot;
+}
+
+extern "C" void or_set_stage(or_system *s, double sigma, double eps) {
+    s->stage = sigma > 0.0;
+    s->stage_sigma = sigma;
+    s->stage_eps = eps;
+}
+extern "C" void or_set_rg_bias(or_system *s, int32_t pott, double k, const double *rg0) {
+    s->rg_pott = pott;
+    s->rg_k = k;
+    s->rg0.assign(rg0, rg0 + s->nrep);
+}
+extern "C" void or_set_restraints(or_system *s, int32_t n, const int32_t *ids3, const double *para4) {
+    s->rest_id.assign(ids3, ids3 + 3 * n);
+    s->rest_para.assign(para4, para4 + 4 * n);
+}
+extern "C" void or_set_tweezers(or_system *s, int32_t ndcf, const int32_t *dcf_pairs, const double *dcf_f, int32_t nfr,
+                                const int32_t *fr_pairs, const double *fr_k, const double *fr_init, const double *fr_velo) {
+    s->dcf_pairs.assign(dcf_pairs, dcf_pairs + 2 * ndcf);
+    s->dcf_f.assign(dcf_f, dcf_f + (size_t)3 * ndcf * s->nrep);
+    s->fr_pairs.assign(fr_pairs, fr_pairs + 2 * nfr);
+    s->fr_k.assign(fr_k, fr_k + 2 * nfr);
+    s->fr_init.assign(fr_init, fr_init + 6 * nfr);
+    s->fr_velo.assign(fr_velo, fr_velo + 6 * nfr);
 }
 
 extern "C" void or_set_bp_energy_flag(or_system *s, int32_t f) { s->flg_bp_energy = f != 0; }
@@ -1423,7 +1558,7 @@ extern "C" int64_t or_run(or_system *s, int64_t nsteps, const double *noise) {
                 std::fill(R.xyz_move.begin(), R.xyz_move.end(), 0.0);
                 if (nmc > 0) s->mc_now = true;
             }
-            force_impl(s, r, forces.data(), 0);
+            force_impl(s, r, forces.data(), 0, s->istep + 1);
             s->mc_now = false;
             if (noise) {
                 memcpy(rnd.data(), noise + ((size_t)istep * s->nrep + r) * 3 * n, sizeof(double) * 3 * n);

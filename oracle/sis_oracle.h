@@ -146,6 +146,20 @@ void or_force_mc(or_system *s, int32_t irep, double *forces);
 int32_t or_get_mc_draws(const or_system *s, double *out, int32_t cap);
 int32_t or_get_bp_status(const or_system *s, int32_t irep, uint8_t *out, int32_t cap);
 
+/* Optional terms (force.F90:62-75, energy_sumup.F90:47-52), force term 7 and
+ * energy slots 7-10.  Stage wall (force_stage.F90): sigma <= 0 turns it off.
+ * Rg bias (force_rg.F90): pott 0 off, 1 harmonic, 2 flat-bottomed; rg0 per
+ * replica.  Sigmoid restraints (force_restraint.F90): ids3 [n][3] = imp, jmp
+ * (1-based), type (1 both beads, 2 subject only); para4 [n][4] = eps, d, s,
+ * rcut.  Tweezers (force_tweezers.F90): dual-trap constant force pairs with
+ * forces [nrep][ndcf][3], force-ramp pairs with k [nfr][2], trap starts and
+ * velocities [nfr][2][3]; the ramps move with the step being taken. */
+void or_set_stage(or_system *s, double sigma, double eps);
+void or_set_rg_bias(or_system *s, int32_t pott, double k, const double *rg0);
+void or_set_restraints(or_system *s, int32_t n, const int32_t *ids3, const double *para4);
+void or_set_tweezers(or_system *s, int32_t ndcf, const int32_t *dcf_pairs, const double *dcf_f, int32_t nfr,
+                     const int32_t *fr_pairs, const double *fr_k, const double *fr_init, const double *fr_velo);
+
 #ifdef __cplusplus
 }
 #endif

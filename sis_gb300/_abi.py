@@ -103,6 +103,9 @@ EXPORTS = {
     "sis_gpu_synchronize": (C.c_int, [C.c_void_p]),
     "sis_gpu_flush_l2": (C.c_int, [C.c_void_p]),
     "sis_gpu_probe_barrier_timeout": (C.c_int, [C.c_void_p]),
+    "sis_gpu_set_stage": (C.c_int, [C.c_void_p, C.c_double, C.c_double]),
+    "sis_gpu_set_rg_bias": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_double]),
+    "sis_gpu_set_bias_items": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "sis_gpu_kernel_launches": (C.c_int64, [C.c_void_p]),
     "sis_gpu_step_profiled": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "sis_gpu_step_noise_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),

@@ -107,6 +107,11 @@ struct sis_ctx {
     // k_bonded runs on st4 beside the base-pair kernels on st; ev_bond joins it
     cudaStream_t st4 = nullptr;
     cudaEvent_t ev_bond = nullptr;
+    // optional terms: restraint and trap items of every instance (global bead
+    // indices), uploaded flat to bias_d
+    std::vector<std::vector<BiasItem>> bias_items;
+    BiasItem *bias_d = nullptr;
+    size_t bias_cap = 0;
     double *mc_draws_d = nullptr; // caller-supplied Monte Carlo uniforms
     int mc_draws_cap = 0;
     bool mc_pending = false;      // they apply to the next force or step call
@@ -389,11 +394,12 @@ cudaError_t enqueue_forces_update(sis_ctx *ctx, int cur, const double *noise, lo
         if ((e = cudaEventRecord(ctx->ev_join, ctx->st3)) != cudaSuccess) return e;
     }
     if ((e = enqueue_pre(ctx, cur)) != cudaSuccess) return e;
+    if ((e = launch_bias(ctx->D, ctx->g, cur, 1, ctx->st)) != cudaSuccess) return e;
     if (!ctx->overlap) return launch_step(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
     if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
     return launch_step_split(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
 }
-int step_kernels(const sis_ctx *ctx) { return pre_step_kernels(ctx) + 1 + (ctx->overlap ? 1 : 0); }
+int step_kernels(const sis_ctx *ctx) { return pre_step_kernels(ctx) + bias_kernels(ctx->g) + 1 + (ctx->overlap ? 1 : 0); }
 
 int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
     CK(enqueue_forces_update(ctx, ctx->cur, noise, ns));
@@ -793,6 +799,8 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.m1, 2 * (size_t)ni);
     rc |= dalloc(ctx, &D.m2, 2 * (size_t)ni);
     rc |= dalloc(ctx, &D.gbar, 2);
+    rc |= dalloc(ctx, &D.rgb, ni);
+    rc |= dalloc(ctx, &D.rgv, ni);
     rc |= dalloc(ctx, &D.gsum, kMaxCoopBlocks);
     rc |= dalloc(ctx, &D.flag, ni);
     rc |= dalloc(ctx, &D.any, 1);
@@ -930,6 +938,7 @@ extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
+    if (ctx->bias_d) cudaFree(ctx->bias_d);
     delete ctx;
 }
 
@@ -1090,6 +1099,10 @@ static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
         ctx->launches++;
     }
     if (do_bp) ctx->bp_cache = true;
+    if (mask & 128) {
+        CK(launch_bias(ctx->D, ctx->g, ctx->cur, 0, ctx->st));
+        ctx->launches += bias_kernels(ctx->g);
+    }
     CK(launch_force(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->fout_d, mask, ctx->st));
     ctx->launches++;
     if (forces) CK(cudaMemcpyAsync(forces, ctx->fout_d + 3 * (size_t)off, sizeof(double) * 3 * cnt, cudaMemcpyDeviceToHost, ctx->st));
@@ -1103,12 +1116,12 @@ static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
 
 extern "C" int sis_gpu_force(sis_ctx *ctx, int32_t inst, double *forces) {
     if (!ctx) return SIS_ERR_ARG;
-    return force_common(ctx, inst, 63, forces);
+    return force_common(ctx, inst, 63 | 128, forces);
 }
 
 extern "C" int sis_gpu_force_term(sis_ctx *ctx, int32_t inst, int32_t term, double *forces) {
-    if (!ctx || term < 1 || term > 6) return SIS_ERR_ARG;
-    return force_common(ctx, inst, 1 << (term - 1), forces);
+    if (!ctx || term < 1 || term > 7) return SIS_ERR_ARG;
+    return force_common(ctx, inst, term == 7 ? 128 : 1 << (term - 1), forces);
 }
 
 extern "C" int sis_gpu_rg(sis_ctx *ctx, int32_t inst, double *rg) {
@@ -1138,7 +1151,8 @@ extern "C" int sis_gpu_energy_sumup(sis_ctx *ctx, int32_t inst, double tempK, do
     }
     CK(cudaMemsetAsync(ctx->D.ene, 0, sizeof(double) * 12 * ctx->n_inst, ctx->st));
     CK(launch_energy(ctx->D, ctx->g, ctx->cur, ctx->st));
-    ctx->launches += 2;
+    CK(launch_bias_energy(ctx->D, ctx->g, ctx->cur, ctx->st));
+    ctx->launches += 2 + (ctx->g.flg_bias ? 1 + ctx->g.flg_rg : 0);
     double h[12];
     CK(cudaMemcpyAsync(h, ctx->D.ene + 12 * (size_t)inst, sizeof(double) * 12, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -1212,6 +1226,77 @@ extern "C" int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, d
     if (!rc) rc = upload_dgf(ctx, inst);
     if (rc) return rc;
     CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
+// ------------------------------------------------------- optional terms
+namespace {
+void bias_flags(sis_ctx *ctx) {
+    GlobP &g = ctx->g;
+    g.flg_rg = 0;
+    for (const InstP &I : ctx->ip) g.flg_rg |= I.rg_pott != 0;
+    size_t n = 0;
+    for (const auto &v : ctx->bias_items) n += v.size();
+    g.n_bias = (int)n;
+    g.flg_bias = g.flg_stage || g.flg_rg || g.n_bias > 0;
+}
+} // namespace
+
+extern "C" int sis_gpu_set_stage(sis_ctx *ctx, double sigma, double eps) {
+    if (!ctx || !(sigma >= 0.0)) return SIS_ERR_ARG;
+    ctx->g.flg_stage = sigma > 0.0;
+    ctx->g.stage_sigma = sigma;
+    ctx->g.stage_eps = eps;
+    bias_flags(ctx);
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_set_rg_bias(sis_ctx *ctx, int32_t inst, int32_t pott, double k, double rg0) {
+    if (!ctx || inst < -1 || inst >= ctx->n_inst || pott < 0 || pott > 2) return SIS_ERR_ARG;
+    for (int q = 0; q < ctx->n_inst; ++q) {
+        if (inst >= 0 && q != inst) continue;
+        ctx->ip[q].rg_pott = pott;
+        ctx->ip[q].rg_k = k;
+        ctx->ip[q].rg0 = rg0;
+    }
+    int rc = upload_ip(ctx);
+    if (rc) return rc;
+    bias_flags(ctx);
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_set_bias_items(sis_ctx *ctx, int32_t inst, int32_t n, const int32_t *kind_ij, const double *par) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || n < 0 || (n > 0 && (!kind_ij || !par))) return SIS_ERR_ARG;
+    if (ctx->bias_items.empty()) ctx->bias_items.resize(ctx->n_inst);
+    const InstP &I = ctx->ip[inst];
+    std::vector<BiasItem> items((size_t)n);
+    for (int q = 0; q < n; ++q) {
+        BiasItem &b = items[q];
+        b.kind = kind_ij[3 * q];
+        const int i = kind_ij[3 * q + 1], j = kind_ij[3 * q + 2];
+        if (b.kind < 1 || b.kind > 4 || i < 1 || i > I.n || j < 1 || j > I.n) return fail(ctx, SIS_ERR_ARG, "bad restraint or trap item");
+        b.i = I.bead_off + i - 1;
+        b.j = I.bead_off + j - 1;
+        b.inst = inst;
+        for (int k = 0; k < 14; ++k) b.p[k] = par[14 * (size_t)q + k];
+        if (b.kind <= 2 && !(b.p[2] != 0.0)) return fail(ctx, SIS_ERR_ARG, "restraint width s must be nonzero");
+    }
+    ctx->bias_items[inst] = std::move(items);
+    std::vector<BiasItem> flat;
+    for (const auto &v : ctx->bias_items) flat.insert(flat.end(), v.begin(), v.end());
+    if (flat.size() > ctx->bias_cap) {
+        if (ctx->bias_d) cudaFree(ctx->bias_d);
+        ctx->bias_d = nullptr;
+        ctx->bias_cap = 0;
+        if (cudaMalloc(&ctx->bias_d, sizeof(BiasItem) * flat.size()) != cudaSuccess) return fail(ctx, SIS_ERR_NOMEM, "bias items");
+        ctx->bias_cap = flat.size();
+    }
+    if (!flat.empty()) {
+        CK(cudaMemcpyAsync(ctx->bias_d, flat.data(), sizeof(BiasItem) * flat.size(), cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    ctx->D.bias = ctx->bias_d;
+    bias_flags(ctx);
     return SIS_OK;
 }
 
@@ -1359,7 +1444,8 @@ extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
         CK(cudaEventRecord(e[0], ctx->st));
         CK(cudaEventRecord(ctx->ev_fork, ctx->st));
         CK(enqueue_pre(ctx, ctx->cur));
-        ctx->launches += pre_step_kernels(ctx);
+        CK(launch_bias(ctx->D, ctx->g, ctx->cur, 1, ctx->st));
+        ctx->launches += pre_step_kernels(ctx) + bias_kernels(ctx->g);
         CK(cudaEventRecord(e[1], ctx->st));
         if (ctx->overlap) {
             CK(launch_pairs(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->st));
@@ -1542,6 +1628,7 @@ extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double 
     if (ctx->g.bp_model > 0) CK(launch_bp_energy(ctx->D, ctx->g, ctx->cur, -1.0, bp_blocks(ctx), ctx->st));
     CK(cudaMemsetAsync(ctx->D.ene, 0, sizeof(double) * 12 * ni, ctx->st));
     CK(launch_energy(ctx->D, ctx->g, ctx->cur, ctx->st));
+    CK(launch_bias_energy(ctx->D, ctx->g, ctx->cur, ctx->st));
     // and at their partners' temperatures (energy_replica.F90:72-121)
     CK(launch_remd_partner_ip(ctx->D, R, ni, parity, ctx->st));
     Dev D2 = ctx->D;
@@ -1550,13 +1637,14 @@ extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double 
     if (ctx->g.bp_model > 0) CK(launch_bp_energy(D2, ctx->g, ctx->cur, -1.0, bp_blocks(ctx), ctx->st));
     CK(cudaMemsetAsync(R.ene2, 0, sizeof(double) * 12 * ni, ctx->st));
     CK(launch_energy(D2, ctx->g, ctx->cur, ctx->st));
+    CK(launch_bias_energy(D2, ctx->g, ctx->cur, ctx->st));
     const double *u = nullptr;
     if (uniforms) {
         CK(cudaMemcpyAsync(ctx->remd_u, uniforms, sizeof(double) * (ni / 2 + 1), cudaMemcpyHostToDevice, ctx->st));
         u = ctx->remd_u;
     }
     CK(launch_remd_decide(ctx->D, R, ctx->g, parity, u, BOLTZ_KCAL_MOL, ctx->remd_ctr++, ctx->st));
-    ctx->launches += 2 * (2 + (ctx->g.bp_model > 0)) + 3;
+    ctx->launches += 2 * (2 + (ctx->g.bp_model > 0) + (ctx->g.flg_bias ? 1 + ctx->g.flg_rg : 0)) + 3;
     // lists of replicas whose electrostatic cutoff moved with the Debye length
     if ((rc = run_rebuild(ctx, 0))) return rc;
     int nacc = 0;

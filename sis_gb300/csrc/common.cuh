@@ -80,6 +80,9 @@ struct InstP {
     // noise stream of the instance: Philox counter (local bead, step - step0, stream)
     unsigned int stream;
     unsigned long long step0;
+    // Rg bias (force_rg.F90): rg_pott 0 off, 1 harmonic, 2 flat-bottomed
+    int rg_pott;
+    double rg_k, rg0;
 };
 
 struct GlobP {
@@ -95,6 +98,21 @@ struct GlobP {
     unsigned long long seed;
     double fcap; // > 0: per-bead force magnitude cap (equilibration only)
     int nstep_mc, max_bp_per_nt; // base-pair Monte Carlo removal (0: none)
+    // optional terms (force.F90:62-75): any of them on; stage wall; an Rg
+    // bias on some instance; restraint and trap items
+    int flg_bias, flg_stage, flg_rg, n_bias;
+    double stage_sigma, stage_eps;
+};
+
+// One sigmoid restraint or tweezers trap pair (force_restraint.F90,
+// force_tweezers.F90).  kind 1: restraint on both beads; 2: restraint on bead
+// i only (the reference's Sigmoid-to-bead); 3: constant-force trap pair;
+// 4: force-ramp trap pair.  p: 1, 2 eps, d, s, rcut; 3 the force on bead i
+// (x, y, z); 4 k_i, k_j, trap starts (i x y z, j x y z), trap velocities
+// (i x y z, j x y z).
+struct BiasItem {
+    int kind, i, j, inst; // global bead indices
+    double p[14];
 };
 
 // base-pair parameter record (var_potential.F90 basepair_parameters), index 1..6
@@ -120,6 +138,11 @@ struct Dev {
     float4 *res[2];         // mirror residuals x*S - q (units), w unused
     double4 *v, *beta, *move, *mdc, *fbp;
     int4 *binfo;
+    // optional terms: restraint and trap items; per instance the Rg bias
+    // centre and force factor, and its energy
+    const BiasItem *bias;
+    double4 *rgb;
+    double *rgv;
     double *mass;
     int *nbr, *nnbr;
     // base-pair lists

@@ -941,14 +941,14 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
         if constexpr (sizeof(R) == 4) {
             // FP32 lane sums plus the fixed-point base-pair force, one conversion to FP64
             float fb = 0.f;
-            if (mask & 8) {
+            if (mask & 136) {
                 fb = (float)__double_as_longlong(*fp) * (float)FX_UNIT;
                 *fp = 0.0;
             }
             Fc = (double)(sA[c][bb] + sB[c][bb] + fb);
         } else {
             double fb = 0.0;
-            if (mask & 8) {
+            if (mask & 136) {
                 fb = *fp;
                 *fp = 0.0;
             }
@@ -1259,6 +1259,162 @@ __global__ void __launch_bounds__(256) k_rg(Dev D, int cur, double *out) {
     }
     s2 = block_sum(s2, s);
     if (threadIdx.x == 0) out[blockIdx.x] = sqrt(s2 / ip.n);
+}
+
+// ------------------------------------------------------- optional terms
+// force.F90:62-75 and energy_sumup.F90:47-52: stage wall (force_stage.F90),
+// tweezers (force_tweezers.F90), Rg bias (force_rg.F90) and sigmoid
+// restraints (force_restraint.F90), in FP64 from the FP64 positions in both
+// paths (they are O(n) or a handful of pairs).  Forces go to fbp, as the
+// base-pair forces do: FP64 atomics in the FP64 path, exact fixed point in
+// the mixed path; the step kernel consumes fbp under mask bit 8 or 128.
+constexpr double kSmallValue = 2.220446049250313e-16; // const_phys.F90 SMALL_VALUE = epsilon(PI)
+
+__device__ __forceinline__ void bias_scatter(const Dev &D, const GlobP &g, int i, double fx, double fy, double fz) {
+    if (g.prec == 0) {
+        atomicAdd(&D.fbp[i].x, fx);
+        atomicAdd(&D.fbp[i].y, fy);
+        atomicAdd(&D.fbp[i].z, fz);
+        return;
+    }
+    if (!(fabs(fx) < FX_LIMIT && fabs(fy) < FX_LIMIT && fabs(fz) < FX_LIMIT)) {
+        atomicOr(D.err, ERR_NONFINITE);
+        return;
+    }
+    fx_scatter(D, i, fx_of(fx), fx_of(fy), fx_of(fz));
+}
+
+// force_rg.F90:17-31 / energy_rg.F90: the centre and radius of gyration of
+// every instance with an Rg bias (one block each, fixed-order sums), its
+// force factor -k (rg - rg0) / (rg n) and its energy
+__global__ void __launch_bounds__(256) k_bias_rg(Dev D, GlobP g, int cur) {
+    __shared__ double s[256];
+    const InstP &ip = D.ip[blockIdx.x];
+    if (ip.rg_pott == 0) return;
+    const double4 *x = D.x[cur] + ip.bead_off;
+    double cx = 0.0, cy = 0.0, cz = 0.0;
+    for (int i = threadIdx.x; i < ip.n; i += blockDim.x) {
+        cx += x[i].x;
+        cy += x[i].y;
+        cz += x[i].z;
+    }
+    cx = block_sum(cx, s) / ip.n;
+    cy = block_sum(cy, s) / ip.n;
+    cz = block_sum(cz, s) / ip.n;
+    double s2 = 0.0;
+    for (int i = threadIdx.x; i < ip.n; i += blockDim.x) {
+        const double vx = x[i].x - cx, vy = x[i].y - cy, vz = x[i].z - cz;
+        s2 += vx * vx + vy * vy + vz * vz;
+    }
+    s2 = block_sum(s2, s);
+    if (threadIdx.x == 0) {
+        const double rg = sqrt(s2 / ip.n);
+        const bool off = ip.rg_pott == 2 && rg <= ip.rg0;
+        D.rgb[blockIdx.x] = make_double4(cx, cy, cz, off ? 0.0 : -ip.rg_k * (rg - ip.rg0) / (rg * ip.n));
+        D.rgv[blockIdx.x] = off ? 0.0 : 0.5 * ip.rg_k * (rg - ip.rg0) * (rg - ip.rg0);
+    }
+}
+
+// Threads [0, n): the stage wall and the Rg bias of one bead; then one
+// thread per item.  in_step: force ramps place their traps at the
+// reference's istep, which counts the step being taken (job_md.F90:362):
+// the steps taken plus 1 inside a step, plus 0 outside the MD loop.
+__global__ void __launch_bounds__(256) k_bias(Dev D, GlobP g, int cur, int in_step) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const double4 *x = D.x[cur];
+    if (t < g.n) {
+        const int inst = D.binfo[t].x;
+        const double4 xi = x[t];
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        if (g.flg_stage) {
+            double z = xi.z;
+            if (z < kSmallValue) z = kSmallValue;
+            z = g.stage_sigma / z;
+            const double z2 = z * z, z6 = z2 * z2 * z2, z7 = z6 * z, z13 = z6 * z7;
+            fz += 24.0 * g.stage_eps / g.stage_sigma * (2.0 * z13 - z7);
+        }
+        if (g.flg_rg && D.ip[inst].rg_pott != 0) {
+            const double4 r = D.rgb[inst];
+            fx += r.w * (xi.x - r.x);
+            fy += r.w * (xi.y - r.y);
+            fz += r.w * (xi.z - r.z);
+        }
+        if (fx != 0.0 || fy != 0.0 || fz != 0.0) bias_scatter(D, g, t, fx, fy, fz);
+        return;
+    }
+    const int q = t - g.n;
+    if (q >= g.n_bias) return;
+    const BiasItem b = D.bias[q];
+    const InstP &ip = D.ip[b.inst];
+    if (b.kind <= 2) {
+        const V3<double> v = dvec64(x[b.i], x[b.j], ip);
+        const double r = sqrt(dot3(v, v));
+        if (r >= b.p[3]) return;
+        const double th = tanh((r - b.p[1]) / b.p[2]);
+        const double coef = 0.5 * b.p[0] / b.p[2] * (1.0 - th * th) / r;
+        bias_scatter(D, g, b.i, -coef * v.x, -coef * v.y, -coef * v.z);
+        if (b.kind == 1) bias_scatter(D, g, b.j, coef * v.x, coef * v.y, coef * v.z);
+    } else if (b.kind == 3) {
+        bias_scatter(D, g, b.i, b.p[0], b.p[1], b.p[2]);
+        bias_scatter(D, g, b.j, -b.p[0], -b.p[1], -b.p[2]);
+    } else {
+        const double istep = (double)(*D.step_ctr + (unsigned long long)in_step);
+        for (int tt = 0; tt < 2; ++tt) {
+            const int i = tt ? b.j : b.i;
+            const double4 trap = make_double4(b.p[2 + 3 * tt] + b.p[8 + 3 * tt] * istep, b.p[3 + 3 * tt] + b.p[9 + 3 * tt] * istep,
+                                              b.p[4 + 3 * tt] + b.p[10 + 3 * tt] * istep, 0.0);
+            const V3<double> v = dvec64(trap, x[i], ip);
+            bias_scatter(D, g, i, b.p[tt] * v.x, b.p[tt] * v.y, b.p[tt] * v.z);
+        }
+    }
+}
+
+// energy_stage.F90, energy_tweezers.F90, energy_rg.F90, energy_restraint.F90
+// into the energy slots 7-10 (k_bias_rg ran first)
+__global__ void __launch_bounds__(256) k_bias_energy(Dev D, GlobP g, int cur) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const double4 *x = D.x[cur];
+    if (t < g.n) {
+        if (!g.flg_stage) return;
+        const int inst = D.binfo[t].x;
+        const double z = g.stage_sigma / x[t].z;
+        const double z2 = z * z, z6 = z2 * z2 * z2;
+        atomicAdd(D.ene + (size_t)inst * 12 + 7, 4.0 * g.stage_eps * (z6 * z6 - z6));
+        return;
+    }
+    int q = t - g.n;
+    if (q < g.n_inst) {
+        if (g.flg_rg && D.ip[q].rg_pott != 0) atomicAdd(D.ene + (size_t)q * 12 + 9, D.rgv[q]);
+        return;
+    }
+    q -= g.n_inst;
+    if (q >= g.n_bias) return;
+    const BiasItem b = D.bias[q];
+    const InstP &ip = D.ip[b.inst];
+    double *E = D.ene + (size_t)b.inst * 12;
+    if (b.kind <= 2) {
+        const V3<double> v = dvec64(x[b.i], x[b.j], ip);
+        const double r = sqrt(dot3(v, v));
+        if (r < b.p[3]) atomicAdd(E + 10, -0.5 * b.p[0] * (1.0 - tanh((r - b.p[1]) / b.p[2])));
+    } else if (b.kind == 3) {
+        const V3<double> v = dvec64(x[b.i], x[b.j], ip);
+        atomicAdd(E + 8, -(v.x * b.p[0] + v.y * b.p[1] + v.z * b.p[2]));
+    }
+}
+
+cudaError_t launch_bias(const Dev &D, const GlobP &g, int cur, int in_step, cudaStream_t st) {
+    if (!g.flg_bias) return cudaSuccess;
+    if (g.flg_rg) k_bias_rg<<<g.n_inst, 256, 0, st>>>(D, g, cur);
+    k_bias<<<(g.n + g.n_bias + 255) / 256, 256, 0, st>>>(D, g, cur, in_step);
+    return cudaGetLastError();
+}
+int bias_kernels(const GlobP &g) { return g.flg_bias ? 1 + (g.flg_rg ? 1 : 0) : 0; }
+
+cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
+    if (!g.flg_bias) return cudaSuccess;
+    if (g.flg_rg) k_bias_rg<<<g.n_inst, 256, 0, st>>>(D, g, cur);
+    k_bias_energy<<<(g.n + g.n_inst + g.n_bias + 255) / 256, 256, 0, st>>>(D, g, cur);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaStream_t st) {

@@ -49,6 +49,11 @@ cudaError_t launch_remd_decide(const Dev &D, const RemdDev &R, const GlobP &g, i
                                unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaStream_t st);
+// the optional terms' forces into fbp (in_step 1 inside a step, 0 outside)
+// and their energies into slots 7-10; nothing when none is on
+cudaError_t launch_bias(const Dev &D, const GlobP &g, int cur, int in_step, cudaStream_t st);
+int bias_kernels(const GlobP &g);
+cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long long ctr, cudaStream_t st, int only_inst = -1);
 cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 // k_trigger_rebuild, one cooperative launch of `grid` blocks (at most

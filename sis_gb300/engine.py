@@ -187,6 +187,49 @@ class Engine:
         d = None if draws is None else np.ascontiguousarray(draws, dtype=np.float64)
         self._ck(self.L.sis_gpu_bp_mc(self.h, int(inst), ptr(d), 0 if d is None else d.size))
 
+    # optional terms (force.F90:62-75): force term 7, energy slots 7-10
+    def set_stage(self, sigma: float, eps: float):
+        """Stage wall at z = 0 (force_stage.F90); sigma = 0 turns it off."""
+        self._ck(self.L.sis_gpu_set_stage(self.h, float(sigma), float(eps)))
+
+    def set_rg_bias(self, inst: int, k: float, rg0: float, flat: bool = False, off: bool = False):
+        """Bias on the radius of gyration (force_rg.F90); inst -1: all."""
+        self._ck(self.L.sis_gpu_set_rg_bias(self.h, int(inst), 0 if off else (2 if flat else 1), float(k), float(rg0)))
+
+    def set_restraints(self, inst: int, restraints):
+        """Sigmoid restraints (sis_gb300.model.Restraint) of one instance."""
+        self._bias_items(inst)["rest"] = list(restraints)
+        self._upload_bias(inst)
+
+    def set_tweezers(self, inst: int, dcf=(), fr=()):
+        """Trap pairs of one instance: ConstantForcePair and ForceRampPair."""
+        self._bias_items(inst)["twz"] = (list(dcf), list(fr))
+        self._upload_bias(inst)
+
+    def _bias_items(self, inst):
+        if not hasattr(self, "_bias"):
+            self._bias = {}
+        return self._bias.setdefault(inst, {"rest": [], "twz": ([], [])})
+
+    def _upload_bias(self, inst):
+        b = self._bias_items(inst)
+        kij, par = [], []
+        for q in b["rest"]:
+            kij.append((2 if q.to_bead else 1, q.i, q.j))
+            par.append([q.eps, q.d, q.s, q.rcut] + [0.0] * 10)
+        dcf, fr = b["twz"]
+        for q in dcf:
+            kij.append((3, q.i, q.j))
+            par.append(list(np.asarray(q.force, dtype=np.float64).reshape(3)) + [0.0] * 11)
+        for q in fr:
+            kij.append((4, q.i, q.j))
+            par.append(list(np.asarray(q.k, dtype=np.float64).reshape(2)) + list(np.asarray(q.init, dtype=np.float64).reshape(6))
+                       + list(np.asarray(q.velo, dtype=np.float64).reshape(6)))
+        kij = np.ascontiguousarray(np.array(kij, dtype=np.int32).reshape(-1, 3))
+        par = np.ascontiguousarray(np.array(par, dtype=np.float64).reshape(-1, 14))
+        self._ck(self.L.sis_gpu_set_bias_items(self.h, int(inst), kij.shape[0], kij.ctypes.data_as(C.c_void_p),
+                                               par.ctypes.data_as(C.c_void_p)))
+
     def get_bp_energies(self, inst: int) -> np.ndarray:
         """Cached energy of every base-pair record (order of get_list(inst, 2))."""
         n = C.c_int32()

@@ -99,6 +99,45 @@ class Options:
     max_bp_per_nt: int = 1
 
 
+# ------------------------------------------------------- optional terms
+# force.F90:62-75 (force_restraint.F90, force_tweezers.F90); bead indices
+# are 1-based within the instance, as in the reference's input files.
+@dataclass
+class Restraint:
+    """Sigmoid restraint between beads i and j (force_restraint.F90,
+    energy_restraint.F90): E = -eps/2 (1 - tanh((r - d)/s)) for r < rcut.
+    to_bead: the reference's Sigmoid-to-bead type, whose force acts on bead
+    i only (bead j is the reference point)."""
+    i: int
+    j: int
+    eps: float
+    d: float
+    s: float
+    rcut: float
+    to_bead: bool = False
+
+
+@dataclass
+class ConstantForcePair:
+    """Dual-trap tweezers at constant force (force_tweezers.F90:29-36):
+    +force on bead i, -force on bead j (kcal/mol/A); E = -(x_i - x_j).force."""
+    i: int
+    j: int
+    force: Sequence[float]
+
+
+@dataclass
+class ForceRampPair:
+    """Dual-trap tweezers with moving harmonic traps (force_tweezers.F90:38-60):
+    trap t of bead (i, j)[t] sits at init[t] + velo[t] * istep, istep being the
+    step taken, and pulls its bead with k[t] times the separation."""
+    i: int
+    j: int
+    k: Sequence[float]
+    init: Sequence[Sequence[float]]
+    velo: Sequence[Sequence[float]]
+
+
 @dataclass
 class Chain:
     seq: np.ndarray  # int32 SEQT codes

@@ -91,6 +91,49 @@ def test_force_is_minus_energy_gradient_model5_reb_expdih(nn_ff):
     assert _fd_check(orc, range(27)) < 2e-5
 
 
+def _biased_chain(sis_ff):
+    """A 20-nt chain lifted above a stage wall at z = 0, with an Rg bias, two
+    sigmoid restraints (one on both beads, one to a reference bead) and a
+    constant-force trap pair."""
+    from sis_gb300.model import ConstantForcePair, Restraint
+
+    sysm = single_chain(sis_ff, n=20, seed=3)
+    x = sysm.instances[0].xyz.copy()
+    x[:, 2] += 9.0 - x[:, 2].min()
+    sysm.instances[0].xyz = x
+    orc = Oracle.from_instance(sysm, 0)
+    orc.neighbor_list(0)
+    orc.set_stage(5.0, 1.2)
+    orc.set_rg_bias(2.0, 0.6 * orc.rg(0))
+    orc.set_restraints([Restraint(1, 20, 3.0, 15.0, 2.0, 60.0), Restraint(3, 12, 2.0, 20.0, 3.0, 100.0, to_bead=True)])
+    orc.set_tweezers(dcf=[ConstantForcePair(1, 20, (0.5, -0.3, 0.2))])
+    return orc
+
+
+def test_optional_terms_are_minus_energy_gradient(sis_ff):
+    """Stage wall, Rg bias, sigmoid restraints and constant-force traps
+    (force_stage/rg/restraint/tweezers.F90 against their energy routines).
+    The reference bead of a to-bead restraint (bead 12) feels no force by
+    design (force_restraint.F90:36-39), so its energy gradient is left out."""
+    orc = _biased_chain(sis_ff)
+    f7 = orc.force_term(0, 7)
+    assert np.abs(f7).max() > 0.1
+    e = orc.energy_sumup(0)
+    assert all(abs(e[k]) > 1e-6 for k in (7, 8, 9, 10))
+    assert _fd_check(orc, [b for b in range(20) if b != 11]) < 2e-5
+
+
+def test_flat_bottomed_rg_bias_is_off_inside(sis_ff):
+    orc = _biased_chain(sis_ff)
+    orc.set_stage(0.0, 0.0)
+    orc.set_restraints([])
+    orc.set_tweezers()
+    orc.set_rg_bias(2.0, 1.5 * orc.rg(0), flat=True)
+    assert np.abs(orc.force_term(0, 7)).max() == 0.0 and orc.energy_sumup(0)[9] == 0.0
+    orc.set_rg_bias(2.0, 0.5 * orc.rg(0), flat=True)
+    assert np.abs(orc.force_term(0, 7)).max() > 0.0 and orc.energy_sumup(0)[9] > 0.0
+
+
 def test_force_is_minus_energy_gradient_with_pairs(sis_ff):
     """A compact structure so that WCA, DH and base pairs all contribute."""
     rng = np.random.default_rng(5)
