@@ -10,7 +10,6 @@ and after repeated failures the chain backs off a few beads.
 from __future__ import annotations
 
 import math
-from dataclasses import dataclass
 from typing import List, Optional, Tuple
 
 import numpy as np
@@ -169,34 +168,3 @@ def uneven_batch(ff: ForceField, n_inst: int = 256, lmin: int = 20, lmax: int = 
         T = float(rng.uniform(280.0, 340.0))
         insts.append(Instance([Chain(seq)], tempK=T, ionic_strength=salt, xyz=random_coil(rng, n)))
     return System(ff, sis_options(), insts)
-
-
-@dataclass
-class Job:
-    arrival_s: float
-    n: int
-    steps: int
-    tempK: float
-    salt: float
-    seed: int
-
-
-def serving_stream(n_jobs: int, rate: float = 50.0, seed: int = 1005, lmin: int = 20, lmax: int = 2000,
-                   smin: float = 1e4, smax: float = 1e6) -> List[Job]:
-    """Poisson arrivals; length log-U[lmin,lmax]; steps log-U[smin,smax];
-    T U[280,360] K; salt U[20,500] mM."""
-    rng = np.random.default_rng(seed)
-    t = 0.0
-    jobs = []
-    for k in range(n_jobs):
-        t += rng.exponential(1.0 / rate)
-        n = int(round(math.exp(rng.uniform(math.log(lmin), math.log(lmax)))))
-        s = int(round(math.exp(rng.uniform(math.log(smin), math.log(smax)))))
-        jobs.append(Job(t, n, s, float(rng.uniform(280.0, 360.0)), float(rng.uniform(0.02, 0.5)), seed * 100000 + k))
-    return jobs
-
-
-def job_instance(job: Job) -> Instance:
-    rng = np.random.default_rng(job.seed)
-    seq = random_sequence(rng, job.n)
-    return Instance([Chain(seq)], tempK=job.tempK, ionic_strength=job.salt, xyz=random_coil(rng, job.n))
