@@ -188,6 +188,12 @@ int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise);
 /* set_ele + set_md_coef for one instance at a new temperature / salt
  * (src/set_ele.F90, src/job_md.F90:700-767). */
 int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic_strength);
+/* The simulated-annealing update of job_md.F90:597-611 for one instance (or
+ * all, inst = -1): the temperature of the noise coefficients (set_md_coef)
+ * and of the base-pair free energies dG = dH - T dS moves to tempK; the
+ * Debye-Hueckel parameters keep the temperature they were set at, as the
+ * reference calls no set_ele there. */
+int sis_gpu_set_temperature(sis_ctx *ctx, int32_t inst, double tempK);
 /* Caps the magnitude of every bead's total force at fmax (kcal/mol/A) in
  * sis_gpu_step; 0 removes the cap.  An equilibration aid for starting
  * structures with overlapping beads; it has no counterpart in the reference

@@ -1229,6 +1229,27 @@ extern "C" int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, d
     return SIS_OK;
 }
 
+extern "C" int sis_gpu_set_temperature(sis_ctx *ctx, int32_t inst, double tempK) {
+    if (!ctx || inst < -1 || inst >= ctx->n_inst || !(tempK > 0.0)) return SIS_ERR_ARG;
+    // the temperature ladder of replica exchange owns the temperatures
+    if (ctx->remd_on) return fail(ctx, SIS_ERR_ARG, "set_temperature: replica exchange is on");
+    const int k0 = inst < 0 ? 0 : inst, k1 = inst < 0 ? ctx->n_inst : inst + 1;
+    for (int k = k0; k < k1; ++k) ctx->ip[k].tempK = tempK;
+    std::vector<double4> mdc;
+    md_coefs(ctx, mdc);
+    for (int k = k0; k < k1; ++k) {
+        const InstP &I = ctx->ip[k];
+        CK(cudaMemcpyAsync(ctx->D.mdc + I.bead_off, mdc.data() + I.bead_off, sizeof(double4) * I.n, cudaMemcpyHostToDevice,
+                           ctx->st));
+    }
+    int rc = upload_ip(ctx);
+    for (int k = k0; k < k1 && !rc; ++k) rc = upload_dgf(ctx, k);
+    if (rc) return rc;
+    ctx->bp_cache = false;
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
 // ------------------------------------------------------- optional terms
 namespace {
 void bias_flags(sis_ctx *ctx) {

@@ -24,8 +24,14 @@ def write_header(f, natom: int, unitcell: bool) -> None:
     f.write(struct.pack("<iii", 4, natom, 4))
 
 
-def write_frame(f, xyz: np.ndarray, box: Optional[Tuple[float, float, float]] = None) -> None:
+def write_frame(f, xyz: np.ndarray, box: Optional[Tuple[float, float, float]] = None,
+                fix_com_origin: bool = False) -> None:
+    """One frame; with fix_com_origin the coordinates are written relative to
+    their centroid, summed bead by bead in FP64 (dcd.F90:576-581)."""
     xyz = np.asarray(xyz, dtype=np.float64)
+    if fix_com_origin and xyz.shape[0] > 0:
+        com = np.array([np.cumsum(xyz[:, k])[-1] for k in range(3)]) / float(xyz.shape[0])
+        xyz = xyz - com
     if box is not None:
         f.write(struct.pack("<i", 48) + struct.pack("<6d", box[0], 0.0, box[1], 0.0, 0.0, box[2]) + struct.pack("<i", 48))
     n = xyz.shape[0]

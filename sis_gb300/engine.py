@@ -134,6 +134,14 @@ class Engine:
         self.system.instances[inst].tempK = tempK
         self.system.instances[inst].ionic_strength = ionic_strength
 
+    def set_temperature(self, inst: int, tempK: float):
+        """The annealing update (job_md.F90:597-611): noise coefficients and
+        base-pair free energies at tempK, Debye-Hueckel left as it was set;
+        inst = -1 for every instance."""
+        self._ck(self.L.sis_gpu_set_temperature(self.h, int(inst), float(tempK)))
+        for k in (range(self.n_inst) if inst < 0 else [inst]):
+            self.system.instances[k].tempK = tempK
+
     def set_force_cap(self, fmax: float):
         """Equilibration aid: caps each bead's force magnitude (0 = off)."""
         self._ck(self.L.sis_gpu_set_force_cap(self.h, float(fmax)))
@@ -191,10 +199,32 @@ class Engine:
     def set_stage(self, sigma: float, eps: float):
         """Stage wall at z = 0 (force_stage.F90); sigma = 0 turns it off."""
         self._ck(self.L.sis_gpu_set_stage(self.h, float(sigma), float(eps)))
+        self._stage = float(sigma) > 0.0
 
     def set_rg_bias(self, inst: int, k: float, rg0: float, flat: bool = False, off: bool = False):
         """Bias on the radius of gyration (force_rg.F90); inst -1: all."""
         self._ck(self.L.sis_gpu_set_rg_bias(self.h, int(inst), 0 if off else (2 if flat else 1), float(k), float(rg0)))
+        if not hasattr(self, "_rg"):
+            self._rg = {}
+        for q in (range(self.n_inst) if inst < 0 else [inst]):
+            self._rg[q] = None if off else (float(k), float(rg0), bool(flat))
+
+    def rg_bias(self, inst: int):
+        """(k, rg0, flat) of an instance's Rg bias, or None when it is off."""
+        return getattr(self, "_rg", {}).get(inst)
+
+    def tweezers(self, inst: int):
+        """(ConstantForcePair list, ForceRampPair list) of an instance."""
+        return getattr(self, "_bias", {}).get(inst, {"twz": ([], [])})["twz"]
+
+    def optional_terms(self) -> dict:
+        """Which optional terms are on in any instance (the flg_stage,
+        flg_twz, flg_bias_rg and flg_restraint of var_potential.F90)."""
+        b = getattr(self, "_bias", {})
+        return {"stage": getattr(self, "_stage", False),
+                "twz": any(len(v["twz"][0]) + len(v["twz"][1]) > 0 for v in b.values()),
+                "rg": any(v is not None for v in getattr(self, "_rg", {}).values()),
+                "rest": any(len(v["rest"]) > 0 for v in b.values())}
 
     def set_restraints(self, inst: int, restraints):
         """Sigmoid restraints (sis_gb300.model.Restraint) of one instance."""
