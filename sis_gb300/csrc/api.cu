@@ -167,6 +167,7 @@ void set_ele_fields(const sis_ctx *ctx, InstP &I, double ionic) {
     coef = coef * (Zp * Zp);
     const double lambdaD = 1.0e10 * sqrt((1.0e-3 * EPS0 * diele * BOLTZ_J) / (2.0 * N_AVO * (ELE * ELE))) * sqrt(T / ionic);
     I.ele_coef = coef;
+    I.diele = diele;
     I.rcdist = 1.0 / lambdaD;
     I.ele_cut = (p.ele_cutoff_type == 2) ? p.ele_cutoff_inp * lambdaD : p.ele_cutoff_inp;
     I.ele_cut2 = I.ele_cut * I.ele_cut;
@@ -177,12 +178,6 @@ void set_ele_fields(const sis_ctx *ctx, InstP &I, double ionic) {
     I.ele_nl_cut2 = p.flg_ele ? (I.ele_cut + m) * (I.ele_cut + m) : -1.0;
 }
 void set_ele(sis_ctx *ctx, int k) { set_ele_fields(ctx, ctx->ip[k], ctx->ionic[k]); }
-
-double diele_of(const sis_ctx *ctx, int k) {
-    const double MM_A = 87.740, MM_B = -0.40008, MM_C = 9.398e-4, MM_D = -1.410e-6;
-    const double Tc = (ctx->p.temp_independent == 0 ? ctx->ip[k].tempK : ctx->p.tempK_ref) - 273.15;
-    return MM_A + MM_B * Tc + MM_C * Tc * Tc + MM_D * Tc * Tc * Tc;
-}
 
 // job_md.F90:94-133 friction and masses, set_md_coef job_md.F90:700-767
 double friction_of(const sis_params &p) {
@@ -1342,7 +1337,7 @@ extern "C" int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *o) {
     o[0] = I.ele_coef;
     o[1] = 1.0 / I.rcdist;
     o[2] = I.ele_cut;
-    o[3] = diele_of(ctx, inst);
+    o[3] = I.diele;
     return SIS_OK;
 }
 

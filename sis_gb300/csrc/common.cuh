@@ -72,6 +72,7 @@ struct InstP {
     int bp_off, bp_cap;// base-pair staging segment
     double tempK;
     double ele_coef, rcdist, ele_cut, ele_cut2, diele_dTcoef;
+    double diele;      // dielectric constant the electrostatic fields were set with
     float ele_coef_f, rcdist_f, ele_cut2_f;
     double wca_nl_cut2, ele_nl_cut2, bp_nl_cut2;
     // cell grid of large PBC instances (large == 0: all-pairs scan)

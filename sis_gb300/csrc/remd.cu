@@ -22,6 +22,7 @@ __device__ __forceinline__ void copy_temperature_fields(InstP &d, const InstP &s
     d.ele_cut = s.ele_cut;
     d.ele_cut2 = s.ele_cut2;
     d.diele_dTcoef = s.diele_dTcoef;
+    d.diele = s.diele;
     d.ele_coef_f = s.ele_coef_f;
     d.rcdist_f = s.rcdist_f;
     d.ele_cut2_f = s.ele_cut2_f;

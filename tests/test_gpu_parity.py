@@ -239,7 +239,7 @@ def test_batched_instances_match_their_own_oracles(sis_ff):
         for kind in (0, 1, 2):
             assert as_set(eng.get_list(k, kind)) == as_set(orc.get_list(0, kind))
         assert max_rel(eng.force(k), orc.force(0)) < FORCE_TOL_FP64
-        assert np.allclose(eng.get_ele(k)[:3], orc.get_ele(0)[:3], rtol=1e-15, atol=0)
+        assert np.allclose(eng.get_ele(k), orc.get_ele(0), rtol=1e-15, atol=0)
 
 
 @pytest.mark.parametrize("name", ["chain64", "pbc564", "t2s2hp_model5", "compact_bp"])

@@ -507,8 +507,11 @@ def test_set_temperature_moves_the_noise_and_leaves_electrostatics(sis_ff):
 
 @pytest.mark.gpu
 def test_job_on_the_engine(sis_ff, tmp_path):
-    """A short annealed job with a restart: the files hold what the engine
-    computed, and the restarted job ends where the uninterrupted one does."""
+    """A short annealed job: the files hold what the engine computed, and a
+    job stopped by a STOP_SIS file at step 50 and restarted from its .rst
+    ends bit for bit where a job that reloads its own state at step 50 does
+    (a loaded state rebuilds the lists, and list order enters the sums; the
+    lanes and the overlap are fixed so that both engines sum alike)."""
     from sis_gb300 import FP64
     from sis_gb300.coil import single_chain
     from sis_gb300.dcd import read_dcd
@@ -516,33 +519,48 @@ def test_job_on_the_engine(sis_ff, tmp_path):
 
     sysm = single_chain(sis_ff, n=24, seed=2)
     anneal = [(0, 320.0), (60, 300.0)]
-    a = Engine(sysm, precision=FP64, seed=4)
-    a.set_force_cap(1000.0)
+
+    def engine():
+        e = Engine(sysm, precision=FP64, seed=4)
+        e.set_lanes(2)
+        e.set_overlap(False)
+        e.set_force_cap(1000.0)
+        return e
+
+    quiet = dict(log=lambda s: None)
+    a = engine()
     a.init_velocities()
     x0 = a.get_state(0)
+    a.set_state(0, *x0)
+    c50 = MdControl(nstep=50, nstep_save=20, nstep_save_rst=50, anneal=anneal)
+    assert MdJob(a, str(tmp_path / "a"), c50, **quiet).run() == "end"
+    ra = read_rst(tmp_path / "a.rst")
+    assert ra.step == 50 and ra.ianneal == 1
+    a.set_state(0, *a.get_state(0))
     c = MdControl(nstep=100, nstep_save=20, nstep_save_rst=50, anneal=anneal)
-    assert MdJob(a, str(tmp_path / "a"), c, log=lambda s: None).run() == "end"
-    cols = read_out(tmp_path / "a.out")
-    assert list(cols["nframe"]) == [0, 20, 40, 60, 80, 100]
-    assert list(cols["T"]) == [320.0, 320.0, 320.0, 300.0, 300.0, 300.0]
-    frames, _ = read_dcd(tmp_path / "a.dcd")
-    assert frames.shape == (6, 24, 3)
+    assert MdJob(a, str(tmp_path / "a2"), c, restart=ra, **quiet).run() == "end"
+    assert list(read_out(tmp_path / "a.out")["nframe"]) == [0, 20, 40]
+    cols = read_out(tmp_path / "a2.out")
+    assert list(cols["nframe"]) == [60, 80, 100]
+    assert list(cols["T"]) == [300.0, 300.0, 300.0]
+    assert list(read_out(tmp_path / "a.out")["T"]) == [320.0, 320.0, 320.0]
+    frames, _ = read_dcd(tmp_path / "a2.dcd")
+    assert frames.shape == (3, 24, 3)
     assert np.allclose(frames[-1], a.get_state(0)[0], atol=1e-4)
-    # interrupted at 50 by a STOP_SIS file, then restarted
-    b = Engine(sysm, precision=FP64, seed=4)
-    b.set_force_cap(1000.0)
-    b.set_state(0, *x0)
+    # stopped at 50 by a STOP_SIS file, then restarted in a fresh context
     (tmp_path / "b").mkdir()
+    b = engine()
+    b.set_state(0, *x0)
     (tmp_path / "b" / "STOP_SIS").write_text("")
     cb = MdControl(nstep=100, nstep_save=20, nstep_save_rst=50, nstep_check_stop=50, anneal=anneal)
-    assert MdJob(b, str(tmp_path / "b" / "b"), cb, log=lambda s: None).run() == "stop_file"
+    assert MdJob(b, str(tmp_path / "b" / "b"), cb, **quiet).run() == "stop_file"
     os.remove(tmp_path / "b" / "STOP_SIS")
     r = read_rst(tmp_path / "b" / "b.rst")
     assert r.step == 50 and r.ianneal == 1
-    b2 = Engine(sysm, precision=FP64, seed=4)
-    b2.set_force_cap(1000.0)
+    assert np.array_equal(r.xyz[1], ra.xyz[1]) and np.array_equal(r.velos[1], ra.velos[1])
+    b2 = engine()
     restart_engine(b2, tmp_path / "b" / "b.rst")
-    assert MdJob(b2, str(tmp_path / "b" / "b2"), cb, restart=r, log=lambda s: None).run() == "end"
+    assert MdJob(b2, str(tmp_path / "b" / "b2"), cb, restart=r, **quiet).run() == "end"
     assert list(read_out(Path(tmp_path / "b" / "b2.out"))["nframe"]) == [60, 80, 100]
     for u, w in zip(a.get_state(0), b2.get_state(0)):
-        assert np.allclose(u, w, rtol=0, atol=1e-9 * max(1.0, np.abs(u).max()))
+        assert np.array_equal(u, w)
