@@ -217,6 +217,18 @@ class MdJob:
                 self.twz.write(step, x[o[k]:o[k + 1]], fr, self._box(k))
 
     # ---------------------------------------------------------- schedules
+    def _setup_condition(self):
+        """main.F90:97: with an annealing schedule the run is set up at the
+        first stage's temperature, electrostatics (set_ele) included; the
+        later stages move only the noise and base-pair temperatures."""
+        sch = self.c.anneal
+        if sch is None:
+            return
+        if self.replica:
+            raise ValueError("an annealing schedule does not work with replica exchange")
+        for k, inst in enumerate(self.eng.system.instances):
+            self.eng.set_condition(k, sch[0][1], inst.ionic_strength)
+
     def _setup_anneal(self):
         """job_md.F90:206-230: the stage the run starts in."""
         sch = self.c.anneal
@@ -287,6 +299,9 @@ class MdJob:
         """Steps to control.nstep or until a stop condition; returns
         ``"end"``, ``"stop_file"`` or ``"wall_time"``."""
         c, eng = self.c, self.eng
+        self._setup_condition()
+        # job_md.F90:195-199: every replica's lists are built as the job starts
+        eng.neighbor_list(-1)
         self._setup_anneal()
         self._setup_timed_rg()
         self._open()

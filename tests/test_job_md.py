@@ -106,7 +106,12 @@ class FakeEngine:
         return np.array([-2.5])
 
     def set_condition(self, k, tK, ionic):
+        if self.labels is None:
+            self.log.append(("cond", self.s, k, tK))
         self.system.instances[k].tempK = tK
+
+    def neighbor_list(self, inst=-1):
+        self.log.append(("nl", self.s))
 
     def set_temperature(self, inst, tK):
         self.log.append(("temp", self.s, tK))
@@ -146,9 +151,11 @@ def reference_events(c, istep, restarted=False, nrep=0, twz=False, stop_at=None,
     """Events of job_md.F90:360-680 taken one step at a time.  stop_at(step)
     says whether the stop check of that step finds a reason to stop;
     ianneal0 is the annealing stage a restart file holds."""
-    ev = []
+    ev = [("nl", istep)]
     anneal_on, ianneal, next_anneal = c.anneal is not None, 1, None
     if c.anneal is not None:
+        # main.F90:97: set up at the first stage's temperature
+        ev.append(("cond", istep, 0, c.anneal[0][1]))
         n = len(c.anneal)
         if istep >= c.anneal[-1][0]:
             ianneal, anneal_on = n, False
@@ -222,7 +229,7 @@ def _run(tmp_path, monkeypatch, c, eng, **kw):
 
 
 def _order(ev):
-    kind = {"temp": 0, "rg": 0, "twz": 1, "save": 2, "rep": 3, "exch": 4, "rst": 5}
+    kind = {"cond": 0, "nl": 0, "temp": 0, "rg": 0, "twz": 1, "save": 2, "rep": 3, "exch": 4, "rst": 5}
     return sorted(ev, key=lambda e: (e[1], kind[e[0]], e[2:]))
 
 
