@@ -5,6 +5,7 @@ and, after each, checks a row of intervals: frames to .out/.bp/.bpall/.bpe/
 .dcd every ``nstep_save`` (:462-507), the replica label table every
 ``nstep_rep_save`` and an exchange every ``nstep_rep_exchange`` (:509-560),
 the next annealing stage (:597-611) and timed Rg-bias stage (:613-627), a
+progress line every ``[Progress] step`` (:629-635, progress.F90), a
 ``STOP_SIS`` file beside the output prefix and the wall-clock limit every
 ``nstep_check_stop`` (:637-654), and a restart file every ``nstep_save_rst``
 or when it stops (:659-676).  :class:`MdJob` does the same checks, but runs
@@ -24,7 +25,8 @@ from dataclasses import dataclass
 from typing import Callable, Optional, Sequence, Tuple
 
 from . import dcd
-from .outputs import BpeFile, BpFile, OutFile, RepFile, Restart, TwzFile, write_rst
+from .outputs import (BpeFile, BpFile, OutFile, RepFile, Restart, TwzFile, fortran_f, fortran_g, fortran_i,
+                      write_rst)
 
 # const.F90 FILENAME_DIGIT_REPLICA
 FILENAME_DIGIT_REPLICA = 4
@@ -51,6 +53,7 @@ class MdControl:
     out_rst: bool = True
     out_twz: bool = False
     fix_com_origin: bool = False
+    step_progress: int = 0  # [Progress] step; 0: no progress lines
 
     def __post_init__(self):
         if self.nstep < 0 or self.nstep_save <= 0 or self.nstep_check_stop <= 0:
@@ -59,6 +62,8 @@ class MdControl:
             self.nstep_save_rst = self.nstep_save
         if self.nstep_save_rst <= 0:
             raise ValueError("nstep_save_rst must be positive")
+        if self.step_progress < 0:
+            raise ValueError("step_progress must be >= 0")
         if self.anneal is not None:
             if len(self.anneal) == 0:
                 raise ValueError("an annealing schedule needs at least one row")
@@ -77,7 +82,8 @@ def _next_multiple(istep: int, n: int) -> int:
 
 class MdJob:
     """Runs ``control.nstep`` steps of every instance of an Engine and
-    writes the reference's output files under ``prefix``.
+    writes the reference's output files under ``prefix``; messages and
+    progress lines go to ``log``.
 
     ``replica_temps``: the temperature ladder of replica exchange (one rung
     per instance, by label; ``Engine.remd_init`` is called with it).
@@ -216,6 +222,31 @@ class MdJob:
             if fr:
                 self.twz.write(step, x[o[k]:o[k + 1]], fr, self._box(k))
 
+    # ----------------------------------------------------------- progress
+    def _progress_init(self):
+        """progress.F90 progress_init: the header of the progress lines."""
+        for line in ("# PROGRESS", "#1: step", "#2: million steps / day (latest cycle)",
+                     "#3: million steps / day (averaged)", "#4: remaining time / hours"):
+            self.log(line)
+        self._p_ini = self._p_pre = (self.istep, self.clock())
+
+    def _progress_update(self):
+        """progress.F90 progress_update: ``(i12,1x,g13.6,1x,g13.6,1x,f6.1)``
+        of the step, million steps per day since the previous line and since
+        the start, and the hours left at the average rate."""
+        now = self.clock()
+        day = 86400.0
+
+        def rate(ref):
+            dt = (now - ref[1]) / day
+            return (self.istep - ref[0]) / 1.0e6 / dt if dt > 0 else float("inf")
+
+        r_pre, r_ini = rate(self._p_pre), rate(self._p_ini)
+        left = (self.c.nstep - self.istep) / 1.0e6 / r_ini * 24.0 if r_ini > 0 else float("inf")
+        self.log(fortran_i(self.istep, 12) + " " + fortran_g(r_pre) + " " + fortran_g(r_ini) + " "
+                 + fortran_f(left, 6, 1))
+        self._p_pre = (self.istep, now)
+
     # ---------------------------------------------------------- schedules
     def _setup_condition(self):
         """main.F90:97: with an annealing schedule the run is set up at the
@@ -279,6 +310,8 @@ class MdJob:
         if self.twz is not None:
             # the step before a save step, for the .twz record of that step
             cand.append(_next_multiple(i + 1, c.nstep_save) - 1)
+        if c.step_progress > 0:
+            cand.append(_next_multiple(i, c.step_progress))
         if self.replica and c.nstep_rep_exchange > 0:
             cand.append(_next_multiple(i, c.nstep_rep_exchange))
             if c.nstep_rep_save > 0:
@@ -309,6 +342,8 @@ class MdJob:
             if self.restart is None:
                 # job_md.F90:332-338: the frame of step 0
                 self.save_frames()
+            if c.step_progress > 0:
+                self._progress_init()
             why = STOP_END
             while self.istep < c.nstep:
                 if self.twz is not None and (self.istep + 1) % c.nstep_save == 0:
@@ -340,6 +375,8 @@ class MdJob:
                     _, k, r0 = c.timed_bias_rg[self.itrg - 1]
                     eng.set_rg_bias(-1, k, r0, flat=self.rg_flat)
                     self.next_trg = c.timed_bias_rg[self.itrg][0] if self.itrg < len(c.timed_bias_rg) else None
+                if c.step_progress > 0 and i % c.step_progress == 0:
+                    self._progress_update()
                 stop = self._check_stop() if i % c.nstep_check_stop == 0 else None
                 if c.out_rst and (i % c.nstep_save_rst == 0 or stop):
                     self.write_restart()

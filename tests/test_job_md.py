@@ -254,6 +254,43 @@ def test_events_match_the_one_step_loop(c, tmp_path, monkeypatch):
     assert len(eng.steps) <= c.nstep // c.nstep_save + len(got) + 1
 
 
+def test_random_schedules_match_the_one_step_loop(tmp_path, monkeypatch):
+    """40 seeded random controls, with and without annealing, timed Rg
+    bias, tweezers records, replicas and a STOP_SIS file."""
+    rng = np.random.default_rng(11)
+    fr = [ForceRampPair(0, 4, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (0.0, 0.0, 0.0)))]
+    for case in range(40):
+        d = tmp_path / f"c{case}"
+        d.mkdir()
+        nstep = int(rng.integers(1, 400))
+        kw = dict(nstep=nstep, nstep_save=int(rng.integers(1, 60)), nstep_save_rst=int(rng.integers(1, 200)),
+                  nstep_check_stop=int(rng.integers(1, 150)), step_progress=int(rng.integers(0, 50)))
+        nrep = 0
+        if rng.random() < 0.4:
+            steps = sorted(set(int(v) for v in rng.integers(0, nstep + 5, size=int(rng.integers(1, 5)))))
+            kw["anneal"] = [(st, 300.0 + 5 * k) for k, st in enumerate(steps)]
+        elif rng.random() < 0.5:
+            nrep = int(rng.integers(2, 5))
+            kw["nstep_rep_exchange"] = int(rng.integers(1, 40))
+            kw["nstep_rep_save"] = int(rng.integers(0, 40))
+        if rng.random() < 0.4 and not nrep:
+            steps = sorted(set(int(v) for v in rng.integers(0, nstep + 5, size=int(rng.integers(1, 5)))))
+            kw["timed_bias_rg"] = [(st, 1.0 + k, 10.0 + k) for k, st in enumerate(steps)]
+        twz = rng.random() < 0.3
+        kw["out_twz"] = twz
+        stop = rng.random() < 0.2
+        if stop:
+            (d / "STOP_SIS").write_text("")
+        c = MdControl(**kw)
+        temps = [300.0 + 10 * k for k in range(nrep)] if nrep else None
+        eng = FakeEngine(n_inst=max(nrep, 1), temps=temps, fr={0: fr} if twz else None)
+        monkeypatch.undo()
+        why, got, _ = _run(d, monkeypatch, c, eng, replica_temps=temps)
+        want = reference_events(c, 0, nrep=nrep, twz=twz, stop_at=(lambda s: True) if stop else None)
+        assert _order(got) == _order(want), (case, kw)
+        assert why == ("stop_file" if stop and c.nstep >= c.nstep_check_stop else "end")
+
+
 def test_replica_exchange_events_and_label_table(tmp_path, monkeypatch):
     c = MdControl(nstep=400, nstep_save=100, nstep_rep_exchange=30, nstep_rep_save=60, nstep_check_stop=1000)
     temps = [300.0, 310.0, 320.0, 330.0]
@@ -298,6 +335,27 @@ def test_wall_time_limit(tmp_path, monkeypatch):
     assert why == "wall_time" and eng.s == 200  # 400 s > 360 s at the check of step 200
     assert msgs == ["Wall-clock time limit reached at step           200. Stop the job."]
     assert read_rst(tmp_path / "md.rst").step == 200
+
+
+def test_progress_lines(tmp_path):
+    """progress.F90: a five-line header, then per [Progress] step the step,
+    million steps per day since the previous line and since the start, and
+    the hours left at the average rate."""
+    eng = FakeEngine()
+    clock = lambda: eng.s * (0.864 if eng.s <= 200 else 1.728)  # noqa: E731
+    msgs = []
+    c = MdControl(nstep=400, nstep_save=400, nstep_check_stop=1000, step_progress=100)
+    MdJob(eng, str(tmp_path / "md"), c, clock=clock, log=msgs.append).run()
+    assert msgs[:5] == ["# PROGRESS", "#1: step", "#2: million steps / day (latest cycle)",
+                        "#3: million steps / day (averaged)", "#4: remaining time / hours"]
+    # 100 steps per 86.4 s is 0.1 million steps per day; 300 steps left
+    # at that rate are 0.072 hours
+    assert msgs[5] == "         100 " + fortran_g(0.1) + " " + fortran_g(0.1) + "    0.1"
+    assert msgs[6] == "         200 " + fortran_g(0.1) + " " + fortran_g(0.1) + "    0.0"
+    # step 300 at 518.4 s: the last 100 steps took 345.6 s (0.025 million
+    # steps per day), all 300 took 518.4 s (0.05)
+    assert msgs[7].split() == ["300", "0.250000E-01", "0.500000E-01", "0.0"]
+    assert [m.split()[0] for m in msgs[5:]] == ["100", "200", "300", "400"]
 
 
 def test_restart_resumes_annealing_stage_and_skips_the_first_frame(tmp_path, monkeypatch):
