@@ -1,6 +1,7 @@
 """Generates tests/golden/outputs.json: files written by sis_gb300.outputs
-for a fixed table of frames, and what the reference's own readers
-(utils/sisout.py, utils/sisbp.py of the reference tree) make of them.
+and sis_gb300.dcd for a fixed table of frames, and what the reference's own
+readers (utils/sisout.py, utils/sisbp.py, utils/dcd.py of the reference
+tree) make of them.
 
 Run in a container that holds the reference tree:
     python tests/golden/make_output_fixtures.py /path/to/reference
@@ -18,6 +19,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
+from sis_gb300 import dcd as sdcd  # noqa: E402
 from sis_gb300.outputs import BpFile, OutFile  # noqa: E402
 
 # frames: step, T, Ekin, energies[0..10]; values chosen to exercise every
@@ -33,6 +35,13 @@ BP_FRAMES = [
     ([(5, 20), (6, 19), (7, 18), (30, 44)], [1, 1, 0, 1], [-3.2, -0.4, -5.0, -1.5]),
     ([(5, 20), (6, 19)], [1, 1], [-0.2, -2.75]),
 ]
+# optional-term energies (slots 7-10) for the .out columns
+OPT_FRAMES = [(50, 300.0, 2.5, [float(v) for v in (-1.5, 0.5, 1.0, -2.0, 0.25, 3.0, -0.75, 0.125, 1.5, 2.25, 0.0625)],
+               18.75)]
+# two DCD frames of five beads, PBC box, written with fix_com_origin
+DCD_FRAMES = [[[1.0 + i, 2.0 * i, -3.0 + 0.5 * i] for i in range(5)],
+              [[10.25 - i, 0.125 * i * i, 7.0] for i in range(5)]]
+DCD_BOX = [100.0, 110.0, 120.0]
 
 
 def main(ref: Path):
@@ -46,6 +55,7 @@ def main(ref: Path):
 
     error.MyError = MyError
     sys.modules.update({"lop": lop, "lop.elements": elements, "lop.elements.error": error})
+    import dcd as rdcd  # noqa: E402
     import sisbp  # noqa: E402
     import sisout  # noqa: E402
 
@@ -80,8 +90,42 @@ def main(ref: Path):
             frames.append({"pairs": [list(q) for q in pairs], "energies": [float(e) for e in energies]})
         f.close()
         out["bp"] = {"bytes_hex": p.read_bytes().hex(), "frames": frames}
+        p = Path(d) / "opt.out"
+        # the reference's reader knows the Estage and Etweezers columns (it
+        # raises on Erg, Rg and Erest)
+        w = OutFile(p, ele=True, stage=True, twz=True)
+        for step, T, ekin, e, rg in OPT_FRAMES:
+            w.write(step, T, ekin, e, rg=rg)
+        w.close()
+        f = sisout.SisoutFile(str(p))
+        f.open_to_read()
+        f.read_header()
+        cols = {k: v for k, v in vars(f.head_col).items() if v is not None}
+        rows = []
+        while f.has_more_data():
+            rows.append([float(v) for v in f.read_onestep()[0][0]])
+        f.close()
+        out["out_optional"] = {"text": p.read_text(), "columns": cols, "rows": rows}
+        p = Path(d) / "run.dcd"
+        with open(p, "wb") as fh:
+            sdcd.write_header(fh, 5, True)
+            for x in DCD_FRAMES:
+                sdcd.write_frame(fh, np.array(x), DCD_BOX, fix_com_origin=True)
+        f = rdcd.DcdFile(str(p))
+        f.open_to_read()
+        f.read_header()
+        h = f.get_header()
+        frames = []
+        while f.has_more_data():
+            frames.append(f.read_onestep())
+        f.close()
+        out["dcd"] = {"bytes_hex": p.read_bytes().hex(), "with_unit_cell": bool(h.with_unit_cell),
+                      "nmp_real": int(h.nmp_real), "frames": frames}
     out["frames"] = FRAMES
     out["bp_frames"] = BP_FRAMES
+    out["opt_frames"] = OPT_FRAMES
+    out["dcd_frames"] = DCD_FRAMES
+    out["dcd_box"] = DCD_BOX
     (Path(__file__).parent / "outputs.json").write_text(json.dumps(out, indent=1))
 
 

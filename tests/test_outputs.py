@@ -1,9 +1,10 @@
 """Output files in the reference's formats (sis_gb300.outputs).
 
-CPU: Fortran G/E/F editing, the .out and .bp files against
-tests/golden/outputs.json (written by tests/golden/make_output_fixtures.py,
-which parsed them with the reference's own readers, utils/sisout.py and
-utils/sisbp.py), .bpe lines and the .rst block layout.
+CPU: Fortran G/E/F editing, the .out (with and without optional columns),
+.bp and .dcd files against tests/golden/outputs.json (written by
+tests/golden/make_output_fixtures.py, which parsed them with the
+reference's own readers, utils/sisout.py, utils/sisbp.py and utils/dcd.py),
+.bpe lines and the .rst block layout.
 GPU: a run restarted from its .rst file continues bit for bit, and the
 per-frame writers write what the engine holds.
 """
@@ -75,6 +76,43 @@ def test_bp_file_matches_the_reference_reader(tmp_path):
     ref = GOLDEN["bp"]["frames"]
     assert [[(i, j) for i, j, _ in f] for f in frames] == [[tuple(q) for q in f["pairs"]] for f in ref]
     assert [[e for _, _, e in f] for f in frames] == [f["energies"] for f in ref]
+
+
+def test_out_optional_columns_match_the_reference_reader(tmp_path):
+    """Estage and Etweezers after Eele (write_out.F90); the reference's
+    reader files the Etweezers column under e_stage, and that is what the
+    fixture records."""
+    g = GOLDEN["out_optional"]
+    p = tmp_path / "a.out"
+    w = OutFile(p, ele=True, stage=True, twz=True)
+    for step, T, ekin, e, rg in GOLDEN["opt_frames"]:
+        w.write(step, T, ekin, e, rg=rg)
+    w.close()
+    assert p.read_text() == g["text"]
+    cols = read_out(p)
+    assert list(cols)[-3:] == ["Eele", "Estage", "Etweezers"]
+    assert np.array_equal(np.array(list(cols.values())).T, np.array(g["rows"]))
+    assert g["columns"]["e_ele"] == 9 and g["columns"]["e_stage"] == 11
+
+
+def test_dcd_matches_the_reference_reader(tmp_path):
+    """Unit-cell records and centroid-relative coordinates
+    (fix_com_origin), read back by the reference's utils/dcd.py."""
+    from sis_gb300 import dcd
+    g = GOLDEN["dcd"]
+    p = tmp_path / "a.dcd"
+    with open(p, "wb") as f:
+        dcd.write_header(f, 5, True)
+        for x in GOLDEN["dcd_frames"]:
+            dcd.write_frame(f, np.array(x), GOLDEN["dcd_box"], fix_com_origin=True)
+    assert p.read_bytes().hex() == g["bytes_hex"]
+    assert g["with_unit_cell"] and g["nmp_real"] == 5
+    frames, boxes = dcd.read_dcd(p)
+    assert np.array_equal(frames, np.array(g["frames"]))
+    assert np.array_equal(boxes, [GOLDEN["dcd_box"]] * 2)
+    for x, fr in zip(GOLDEN["dcd_frames"], frames):
+        x = np.array(x)
+        assert np.allclose(fr, x - x.mean(axis=0), rtol=0, atol=1e-6)
 
 
 def test_bpall_and_bpe(tmp_path):
