@@ -20,6 +20,8 @@ for several, and ``prefix.rep`` / ``prefix.twz``.
 from __future__ import annotations
 
 import os
+import queue
+import threading
 import time
 from dataclasses import dataclass
 from typing import Callable, Optional, Sequence, Tuple
@@ -76,6 +78,47 @@ class MdControl:
                 raise ValueError("timed Rg-bias rows need step >= 0, k >= 0 and rg0 > 0")
 
 
+class _Writer:
+    """Runs the file writes of a job in order, on one host thread (or
+    inline).  At most ``depth`` writes wait, so a slow disk holds the steps
+    back instead of filling memory.  The first write that fails stops the
+    others and is raised by the next ``put`` or by ``close``."""
+
+    def __init__(self, threaded: bool, depth: int = 8):
+        self.err: Optional[BaseException] = None
+        self.q: Optional[queue.Queue] = queue.Queue(maxsize=depth) if threaded else None
+        if self.q is not None:
+            self.t = threading.Thread(target=self._run, name="md-writer", daemon=True)
+            self.t.start()
+
+    def _run(self):
+        while True:
+            fn = self.q.get()
+            if fn is None:
+                return
+            if self.err is None:
+                try:
+                    fn()
+                except BaseException as e:  # noqa: BLE001 - handed to the caller
+                    self.err = e
+
+    def put(self, fn: Callable[[], None]):
+        if self.err is not None:
+            raise self.err
+        if self.q is None:
+            fn()
+        else:
+            self.q.put(fn)
+
+    def close(self):
+        if self.q is not None:
+            self.q.put(None)
+            self.t.join()
+            self.q = None
+        if self.err is not None:
+            raise self.err
+
+
 def _next_multiple(istep: int, n: int) -> int:
     return (istep // n + 1) * n
 
@@ -92,12 +135,17 @@ class MdJob:
     resumes the annealing stage and the replica labels the file holds.  ``reset_step`` starts the
     step count at 0 whatever the file holds.  ``clock``: wall-clock seconds
     (time.monotonic), measured from the job's construction.  The optional
-    .out columns and the .twz file follow the terms set on the engine."""
+    .out columns and the .twz file follow the terms set on the engine.
+    With ``threaded_writer`` the files are formatted and written on a host
+    thread while the device takes the next steps (the values are read from
+    the device first, at the step they belong to)."""
 
     def __init__(self, eng, prefix: str, control: MdControl, replica_temps: Optional[Sequence[float]] = None,
                  restart: Optional[Restart] = None, reset_step: bool = False,
-                 clock: Callable[[], float] = time.monotonic, log: Callable[[str], None] = print):
+                 clock: Callable[[], float] = time.monotonic, log: Callable[[str], None] = print,
+                 threaded_writer: bool = True):
         self.eng, self.prefix, self.c = eng, str(prefix), control
+        self.threaded_writer = threaded_writer
         self.clock, self.log = clock, log
         self.t0 = clock()
         self.n_inst = eng.n_inst
@@ -156,19 +204,25 @@ class MdJob:
         self.rep = RepFile(self.prefix + ".rep") if self.replica else None
         fr_any = any(len(eng.tweezers(k)[1]) for k in range(self.n_inst))
         self.twz = TwzFile(self.prefix + ".twz") if c.out_twz and fr_any else None
+        self.writer = _Writer(self.threaded_writer)
         self._files_open = True
 
     def close(self):
+        """Waits for the writer, then closes every file; a write that failed
+        in the writer is raised here."""
         if not self._files_open:
             return
-        for group in (self.out, self.bp, self.bpall, self.bpe, self.dcd):
-            for w in group:
+        try:
+            self.writer.close()
+        finally:
+            for group in (self.out, self.bp, self.bpall, self.bpe, self.dcd):
+                for w in group:
+                    if w is not None:
+                        w.close()
+            for w in (self.rep, self.twz):
                 if w is not None:
                     w.close()
-        for w in (self.rep, self.twz):
-            if w is not None:
-                w.close()
-        self._files_open = False
+            self._files_open = False
 
     # ---------------------------------------------------------- helpers
     def _box(self, inst: int):
@@ -181,34 +235,49 @@ class MdJob:
 
     def save_frames(self):
         """job_md.F90:487-507: energies, then .out, .bp files and the DCD
-        frame of every instance."""
-        eng = self.eng
+        frame of every instance.  The device values are read here; the
+        formatting and writing go to the writer."""
+        eng, step = self.eng, self.istep
         xyz = eng.get_state(-1)[0] if self.c.out_dcd else None
+        rows = []
         for k in range(self.n_inst):
             tK = self.temp_of(k)
             e = eng.energy_sumup(k, tK)
             rg = float(eng.rg(k)[0]) if self.out[k].rg else 0.0
-            self.out[k].write(self.istep, tK, eng.energy_kinetic(k), e,
-                              rep_label=self.labels[k] + 1 if self.replica else None, rg=rg)
+            label = self.labels[k] + 1 if self.replica else None
+            bp = None
             if self.bp[k] is not None or self.bpall[k] is not None or self.bpe[k] is not None:
-                rec, st, ene = eng.get_list(k, 2), eng.get_bp_status(k), eng.get_bp_energies(k)
-                for w in (self.bp[k], self.bpall[k], self.bpe[k]):
-                    if w is not None:
-                        w.write_frame(rec, st, ene, tK)
-            if self.dcd[k] is not None:
-                o = eng.offsets
-                dcd.write_frame(self.dcd[k], xyz[o[k]:o[k + 1]], self._box(k), self.c.fix_com_origin)
+                bp = (eng.get_list(k, 2), eng.get_bp_status(k), eng.get_bp_energies(k))
+            rows.append((tK, e, eng.energy_kinetic(k), rg, label, bp))
+        o = eng.offsets
+
+        def write():
+            for k, (tK, e, ekin, rg, label, bp) in enumerate(rows):
+                self.out[k].write(step, tK, ekin, e, rep_label=label, rg=rg)
+                if bp is not None:
+                    for w in (self.bp[k], self.bpall[k], self.bpe[k]):
+                        if w is not None:
+                            w.write_frame(*bp, tK)
+                if self.dcd[k] is not None:
+                    dcd.write_frame(self.dcd[k], xyz[o[k]:o[k + 1]], self._box(k), self.c.fix_com_origin)
+
+        self.writer.put(write)
 
     def write_restart(self):
-        eng = self.eng
+        eng, step = self.eng, self.istep
         x, v, a = eng.get_state(-1)
         o = eng.offsets
         rep2lab = [lab + 1 for lab in self.labels] if self.replica else None
         ianneal = self.ianneal if self.anneal_on else None
-        for k in range(self.n_inst):
-            s = slice(o[k], o[k + 1])
-            write_rst(self.base(k) + ".rst", self.istep, x[s], v[s], a[s], grep=k + 1, box=self._box(k),
-                      rep2lab=rep2lab if k == 0 else None, ianneal=ianneal)
+        boxes = [self._box(k) for k in range(self.n_inst)]
+
+        def write():
+            for k in range(self.n_inst):
+                s = slice(o[k], o[k + 1])
+                write_rst(self.base(k) + ".rst", step, x[s], v[s], a[s], grep=k + 1, box=boxes[k],
+                          rep2lab=rep2lab if k == 0 else None, ianneal=ianneal)
+
+        self.writer.put(write)
 
     def write_twz(self, step: int):
         """The .twz lines the reference writes from the force evaluation of
@@ -217,10 +286,14 @@ class MdJob:
             return
         x = self.eng.get_state(-1)[0]
         o = self.eng.offsets
-        for k in range(self.n_inst):
-            fr = self.eng.tweezers(k)[1]
-            if fr:
-                self.twz.write(step, x[o[k]:o[k + 1]], fr, self._box(k))
+        fr = [list(self.eng.tweezers(k)[1]) for k in range(self.n_inst)]
+
+        def write():
+            for k in range(self.n_inst):
+                if fr[k]:
+                    self.twz.write(step, x[o[k]:o[k + 1]], fr[k], self._box(k))
+
+        self.writer.put(write)
 
     # ----------------------------------------------------------- progress
     def _progress_init(self):
@@ -356,7 +429,8 @@ class MdJob:
                     self.save_frames()
                 if self.replica and c.nstep_rep_exchange > 0:
                     if c.nstep_rep_save > 0 and i % c.nstep_rep_save == 0:
-                        self.rep.write(i, [lab + 1 for lab in self.labels])
+                        labs = [lab + 1 for lab in self.labels]
+                        self.writer.put(lambda i=i, labs=labs: self.rep.write(i, labs))
                     if i % c.nstep_rep_exchange == 0:
                         r2l, acc = eng.remd_exchange(self.n_exchange % 2)
                         self.labels = [int(v) for v in r2l]

@@ -337,6 +337,41 @@ def test_wall_time_limit(tmp_path, monkeypatch):
     assert read_rst(tmp_path / "md.rst").step == 200
 
 
+def test_threaded_and_inline_writers_write_the_same_files(tmp_path):
+    fr = [ForceRampPair(0, 4, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (0.0, 0.0, 0.0)))]
+    c = MdControl(nstep=500, nstep_save=25, nstep_save_rst=100, nstep_rep_exchange=10, nstep_rep_save=20,
+                  out_twz=True, out_bpall=True, out_bpe=True)
+    files = {}
+    for threaded in (False, True):
+        d = tmp_path / str(threaded)
+        d.mkdir()
+        eng = FakeEngine(n_inst=2, temps=[300.0, 310.0], fr={0: fr})
+        MdJob(eng, str(d / "md"), c, replica_temps=[300.0, 310.0], log=lambda s: None,
+              threaded_writer=threaded).run()
+        files[threaded] = {p.name: p.read_bytes() for p in sorted(d.iterdir())}
+    assert files[False] == files[True]
+    assert sorted(files[True]) == ["md.rep", "md.twz"] + [f"md_000{k}.{x}" for k in (1, 2) for x in
+                                                          ("bp", "bpall", "bpe", "dcd", "out", "rst")]
+
+
+def test_a_failed_write_is_raised(tmp_path, monkeypatch):
+    from sis_gb300 import outputs
+    calls = []
+    real = outputs.OutFile.write
+
+    def failing(self, *a, **k):
+        calls.append(1)
+        if len(calls) == 3:
+            raise OSError("disk full")
+        return real(self, *a, **k)
+
+    monkeypatch.setattr(outputs.OutFile, "write", failing)
+    c = MdControl(nstep=200, nstep_save=10)
+    with pytest.raises(OSError, match="disk full"):
+        MdJob(FakeEngine(), str(tmp_path / "md"), c, log=lambda s: None).run()
+    assert len(calls) == 3  # the writes after the failed one are dropped
+
+
 def test_progress_lines(tmp_path):
     """progress.F90: a five-line header, then per [Progress] step the step,
     million steps per day since the previous line and since the start, and
