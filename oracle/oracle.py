@@ -13,7 +13,7 @@ from __future__ import annotations
 import ctypes as C
 import subprocess
 from pathlib import Path
-from typing import Optional, Sequence
+from typing import Sequence
 
 import numpy as np
 

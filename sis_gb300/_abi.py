@@ -7,7 +7,6 @@ missing or fails to load, :func:`lib` raises.
 from __future__ import annotations
 
 import ctypes as C
-import os
 from pathlib import Path
 
 import numpy as np

@@ -10,11 +10,11 @@ and after repeated failures the chain backs off a few beads.
 from __future__ import annotations
 
 import math
-from typing import List, Optional, Tuple
+from typing import List
 
 import numpy as np
 
-from .model import MIXED, Chain, ForceField, Instance, Options, System
+from .model import Chain, ForceField, Instance, Options, System
 
 AVOGADRO = 6.02214076e23
 

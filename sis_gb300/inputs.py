@@ -16,8 +16,7 @@ from typing import Dict, List, Tuple
 
 import numpy as np
 
-from .model import (BD_EM, BP_FIELDS, GJF2GJ, MOLT_CIRC, MOLT_LINEAR, NN_NAMES, NNEND_NAMES, SEQT, Chain,
-                    ForceField, Options)
+from .model import BD_EM, BP_FIELDS, GJF2GJ, NN_NAMES, NNEND_NAMES, Chain, ForceField, Options
 
 
 class InputError(ValueError):

@@ -12,7 +12,7 @@ known-answer tests.
 import numpy as np
 import pytest
 
-from helpers import cag47_system, rms_rel, t2s2hp_system, pbc_md_system
+from helpers import cag47_system, t2s2hp_system, pbc_md_system
 from oracle.oracle import MT, Oracle
 from sis_gb300.coil import random_coil, single_chain
 from sis_gb300.model import Chain, Instance, Options, System
