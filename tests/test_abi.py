@@ -77,3 +77,29 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_abi, "LIB_PATH", tmp_path / "absent.so")
     with pytest.raises(RuntimeError):
         _abi.lib()
+
+
+def _c_params(text):
+    """Parameter count of every sis_gpu_* declaration in the header."""
+    out = {}
+    decl = r"^[ \t]*(?:const[ \t]+)?\w+[ \t]*\**[ \t]*(sis_gpu_\w+)\s*\(([^;]*?)\)\s*;"
+    for name, params in re.findall(decl, text, flags=re.S | re.M):
+        params = params.strip()
+        out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_fortran_bindings_match_the_header():
+    """The ISO_C_BINDING interfaces of INTEGRATION.md bind names the header
+    declares, with as many arguments; every entry point its text names
+    exists."""
+    c = _c_params(HEADER.read_text())
+    doc = (ROOT / "INTEGRATION.md").read_text()
+    binds = re.findall(r"function\s+(\w+)\s*\(([^)]*)\)\s*&?\s*bind\(C,\s*name=\"(\w+)\"\)", doc)
+    assert len(binds) >= 20
+    for fname, args, cname in binds:
+        assert fname == cname and cname in c, cname
+        nargs = len([a for a in args.split(",") if a.strip()])
+        assert nargs == c[cname], (cname, nargs, c[cname])
+    named = set(re.findall(r"\bsis_gpu_\w+", doc)) - {"sis_gpu_mod"}
+    assert named <= set(c), named - set(c)
