@@ -183,7 +183,7 @@ def run_gpu(args):
     # the model (force_dih_cos.F90) diverges as a bond angle reaches 180 degrees;
     # a per-bead cap far above thermal forces keeps such events finite
     eng.set_force_cap(args.force_cap)
-    # replica exchange (BASELINE config c3): an attempt every exchange_interval
+    # replica exchange (64 replicas of one 120-nt chain): an attempt every exchange_interval
     # MD steps, odd and even patterns alternating, inside the timed region
     remd = args.workload == "remd"
     rx = {"since": 0, "attempts": 0, "accepted": 0}
@@ -383,7 +383,7 @@ def run_reference(args):
 
 
 def run_serve(args):
-    """BASELINE config c5 scaled: Poisson arrivals at --serve-rate jobs/s for
+    """The serving workload, scaled: Poisson arrivals at --serve-rate jobs/s for
     --serve-seconds, each job's step count times --serve-steps-scale; pools of
     slots in three length classes; latency = arrival to completion."""
     from sis_gb300.coil import sis_options
