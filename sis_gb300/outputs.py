@@ -266,11 +266,11 @@ class TwzFile:
 
     def write(self, step: int, xyz: np.ndarray, fr, box: Optional[Sequence[float]] = None):
         """xyz: the instance's coordinates at the start of ``step``; fr: its
-        ForceRampPair list (0-based beads)."""
+        ForceRampPair list (1-based beads, as the input files give them)."""
         for ipair, t in enumerate(fr, start=1):
             p1 = np.asarray(t.init[0], dtype=np.float64) + np.asarray(t.velo[0], dtype=np.float64) * step
             p2 = np.asarray(t.init[1], dtype=np.float64) + np.asarray(t.velo[1], dtype=np.float64) * step
-            x1, x2 = xyz[t.i], xyz[t.j]
+            x1, x2 = xyz[t.i - 1], xyz[t.j - 1]
             v1, v2 = pbc_vec_d(p1, x1, box), pbc_vec_d(p2, x2, box)
             n1, n2 = float(np.linalg.norm(v1)), float(np.linalg.norm(v2))
             vals = [np.linalg.norm(p2 - p1), np.linalg.norm(x2 - x1), n1, n2,

@@ -258,7 +258,7 @@ def test_random_schedules_match_the_one_step_loop(tmp_path, monkeypatch):
     """40 seeded random controls, with and without annealing, timed Rg
     bias, tweezers records, replicas and a STOP_SIS file."""
     rng = np.random.default_rng(11)
-    fr = [ForceRampPair(0, 4, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (0.0, 0.0, 0.0)))]
+    fr = [ForceRampPair(1, 5, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (0.0, 0.0, 0.0)))]
     for case in range(40):
         d = tmp_path / f"c{case}"
         d.mkdir()
@@ -338,7 +338,7 @@ def test_wall_time_limit(tmp_path, monkeypatch):
 
 
 def test_threaded_and_inline_writers_write_the_same_files(tmp_path):
-    fr = [ForceRampPair(0, 4, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (0.0, 0.0, 0.0)))]
+    fr = [ForceRampPair(1, 5, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (0.0, 0.0, 0.0)))]
     c = MdControl(nstep=500, nstep_save=25, nstep_save_rst=100, nstep_rep_exchange=10, nstep_rep_save=20,
                   out_twz=True, out_bpall=True, out_bpe=True)
     files = {}
@@ -430,7 +430,7 @@ def test_replica_labels_restored_from_the_restart(tmp_path, monkeypatch):
 
 
 def test_twz_records_take_the_positions_the_step_starts_from(tmp_path, monkeypatch):
-    fr = [ForceRampPair(0, 4, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (-0.02, 0.01, 0.0)))]
+    fr = [ForceRampPair(1, 5, (0.3, 0.2), ((0.0, 0.0, 20.0), (60.0, 5.0, 25.0)), ((0.01, 0.0, 0.0), (-0.02, 0.01, 0.0)))]
     c = MdControl(nstep=300, nstep_save=100, nstep_check_stop=1000, out_twz=True)
     eng = FakeEngine(fr={0: fr})
     why, got, _ = _run(tmp_path, monkeypatch, c, eng)
@@ -459,7 +459,7 @@ def job_md_pn():
 
 
 def test_twz_line_format(tmp_path):
-    fr = [ForceRampPair(0, 1, (1.0, 2.0), ((0.0, 0.0, 0.0), (10.0, 0.0, 0.0)), ((0.0, 0.0, 0.0), (0.0, 0.0, 0.0)))]
+    fr = [ForceRampPair(1, 2, (1.0, 2.0), ((0.0, 0.0, 0.0), (10.0, 0.0, 0.0)), ((0.0, 0.0, 0.0), (0.0, 0.0, 0.0)))]
     x = np.array([[0.0, 3.0, 4.0], [10.0, 0.0, 0.0]])
     p = tmp_path / "a.twz"
     w = TwzFile(p)
