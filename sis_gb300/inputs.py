@@ -16,7 +16,8 @@ from typing import Dict, List, Tuple
 
 import numpy as np
 
-from .model import BD_EM, BP_FIELDS, GJF2GJ, NN_NAMES, NNEND_NAMES, Chain, ForceField, Options
+from .model import (BD_EM, BP_FIELDS, GJF2GJ, NN_NAMES, NNEND_NAMES, Chain, ConstantForcePair, ForceField,
+                    ForceRampPair, Options, Restraint)
 
 
 class InputError(ValueError):
@@ -165,3 +166,78 @@ def read_pdb(path) -> np.ndarray:
         if line.startswith(("ATOM", "HETATM")):
             xyz.append([float(line[30:38]), float(line[38:46]), float(line[46:54])])
     return np.array(xyz)
+
+
+# ------------------------------------------------------- optional terms
+# const_phys.F90 JOUL2KCAL_MOL: forces in pN times JOUL2KCAL_MOL x 1e-22 are
+# kcal/mol/A (read_input.F90:1060)
+JOUL2KCAL_MOL = (1.0 / 4184.0) * 6.02214076e23
+PN_TO_KCAL_MOL_A = JOUL2KCAL_MOL * 1.0e-22
+
+
+def parse_restraints(text: str) -> List[Restraint]:
+    """Restraints of a restraint file (read_restraint.F90): lines starting
+    with ``Sigmoid-to-bead`` or ``Sigmoid`` followed by the two bead numbers
+    (1-based), epsilon, d, s and r_cut; ``#`` lines and blank lines are
+    skipped, any other line is an error."""
+    out: List[Restraint] = []
+    for n, line in enumerate(text.splitlines(), start=1):
+        if line.startswith("#") or not line.strip():
+            continue
+        if line.startswith("Sigmoid-to-bead"):
+            rest, to_bead = line[15:], True
+        elif line.startswith("Sigmoid"):
+            rest, to_bead = line[7:], False
+        else:
+            raise InputError(f"line {n}: unknown restraint type: {line.strip()}")
+        f = rest.replace(",", " ").split()
+        if len(f) < 6:
+            raise InputError(f"line {n}: a restraint needs two beads, epsilon, d, s and r_cut")
+        try:
+            i, j = int(f[0]), int(f[1])
+            eps, d, s, rcut = (float(v) for v in f[2:6])
+        except ValueError as e:
+            raise InputError(f"line {n}: {e}") from None
+        out.append(Restraint(i, j, eps, d, s, rcut, to_bead=to_bead))
+    return out
+
+
+def read_restraints(path) -> List[Restraint]:
+    return parse_restraints(Path(path).read_text())
+
+
+def constant_force_pairs(id_pairs, forces_pN) -> List[ConstantForcePair]:
+    """[Tweezers.Dual_Constant_Force] id_pairs and forces_pN
+    (read_input.F90:983-1063): the forces in kcal/mol/A."""
+    if len(id_pairs) != len(forces_pN):
+        raise InputError("forces_pN needs one vector per pair of id_pairs")
+    out = []
+    for (i, j), fv in zip(id_pairs, forces_pN):
+        if int(i) < 1 or int(j) < 1 or len(fv) != 3:
+            raise InputError("invalid id_pairs or forces_pN in [Tweezers.Dual_Constant_Force]")
+        out.append(ConstantForcePair(int(i), int(j), tuple(float(v) * PN_TO_KCAL_MOL_A for v in fv)))
+    return out
+
+
+def force_ramp_pairs(xyz: np.ndarray, id_pairs, spring_const, trap_speed, init=None) -> List[ForceRampPair]:
+    """[Tweezers.Force_Ramp] pairs with their moving traps (init_tweezers.F90):
+    the traps start on the two beads (or at ``init``, the (n, 2, 3) starting
+    positions a restart file holds) and move apart along the axis from the
+    first trap to the second, trap 1 at -speed_1 and trap 2 at +speed_2
+    (A per step)."""
+    n = len(id_pairs)
+    if len(spring_const) != n or len(trap_speed) != n:
+        raise InputError("spring_const and trap_speed need one pair of values per pair of id_pairs")
+    xyz = np.asarray(xyz, dtype=np.float64)
+    out = []
+    for q, ((i, j), k, sp) in enumerate(zip(id_pairs, spring_const, trap_speed)):
+        i, j = int(i), int(j)
+        if not (1 <= i <= len(xyz) and 1 <= j <= len(xyz)) or len(k) != 2 or len(sp) != 2:
+            raise InputError("invalid id_pairs, spring_const or trap_speed in [Tweezers.Force_Ramp]")
+        p = (np.array([xyz[i - 1], xyz[j - 1]]) if init is None
+             else np.asarray(init, dtype=np.float64).reshape(-1, 2, 3)[q])
+        v = p[1] - p[0]
+        u = v / np.sqrt(np.dot(v, v))
+        velo = (tuple(-u * float(sp[0])), tuple(u * float(sp[1])))
+        out.append(ForceRampPair(i, j, (float(k[0]), float(k[1])), (tuple(p[0]), tuple(p[1])), velo))
+    return out

@@ -26,6 +26,8 @@ import time
 from dataclasses import dataclass
 from typing import Callable, Optional, Sequence, Tuple
 
+import numpy as np
+
 from . import dcd
 from .outputs import (BpeFile, BpFile, OutFile, RepFile, Restart, TwzFile, fortran_f, fortran_g, fortran_i,
                       write_rst)
@@ -270,12 +272,15 @@ class MdJob:
         rep2lab = [lab + 1 for lab in self.labels] if self.replica else None
         ianneal = self.ianneal if self.anneal_on else None
         boxes = [self._box(k) for k in range(self.n_inst)]
+        # write_rst.F90:98-111: the force-ramp traps' starting positions
+        twz = [np.array([t.init for t in eng.tweezers(k)[1]], dtype=np.float64).reshape(-1, 2, 3)
+               for k in range(self.n_inst)]
 
         def write():
             for k in range(self.n_inst):
                 s = slice(o[k], o[k + 1])
                 write_rst(self.base(k) + ".rst", step, x[s], v[s], a[s], grep=k + 1, box=boxes[k],
-                          rep2lab=rep2lab if k == 0 else None, ianneal=ianneal)
+                          rep2lab=rep2lab if k == 0 else None, ianneal=ianneal, twz_init=twz[k])
 
         self.writer.put(write)
 

@@ -326,14 +326,17 @@ class Restart:
     rep2lab: Optional[List[int]] = None
     box: Optional[np.ndarray] = None
     ianneal: Optional[int] = None  # 1-based stage of the annealing schedule
+    twz_init: Dict[int, np.ndarray] = field(default_factory=dict)  # by replica: force-ramp traps at step 0, (n, 2, 3)
 
 
 def write_rst(path, step: int, xyz: np.ndarray, velos: np.ndarray, accels: np.ndarray, grep: int = 1,
               box: Optional[Sequence[float]] = None, rep2lab: Optional[Sequence[int]] = None,
-              ianneal: Optional[int] = None):
+              ianneal: Optional[int] = None, twz_init: Optional[np.ndarray] = None):
     """One replica's restart file in the block order of write_rst.F90
     (replica table first in the first replica's file, then step, annealing
-    stage, coordinates, velocities, accelerations, PBC box)."""
+    stage, coordinates, velocities, accelerations, the force-ramp traps'
+    starting positions (int32 replica, int32 n, n x 2 x 3 float64), PBC
+    box)."""
     xyz, velos, accels = (np.ascontiguousarray(a, dtype="<f8").reshape(-1, 3) for a in (xyz, velos, accels))
     nmp = xyz.shape[0]
     if velos.shape[0] != nmp or accels.shape[0] != nmp:
@@ -353,6 +356,10 @@ def write_rst(path, step: int, xyz: np.ndarray, velos: np.ndarray, accels: np.nd
             f.write(struct.pack("<ii", blk, 4 * 2 + 8 * nmp * 3))
             f.write(struct.pack("<ii", int(grep), nmp))
             f.write(arr.tobytes())
+        if twz_init is not None and len(twz_init) > 0:
+            t = np.ascontiguousarray(twz_init, dtype="<f8").reshape(-1, 2, 3)
+            f.write(struct.pack("<iiii", RST_TWZ, 4 * 2 + 8 * t.size, int(grep), t.shape[0]))
+            f.write(t.tobytes())
         if box is not None:
             f.write(struct.pack("<ii", RST_PBC, 8 * 3))
             f.write(np.asarray(box, dtype="<f8").tobytes())
@@ -402,6 +409,11 @@ def read_rst(path) -> Restart:
                 raise ValueError(f"{path}: replica block of {size} bytes for {n} replicas")
             pairs = struct.unpack(f"<{2 * n}i", payload[4:])
             r.rep2lab = [pairs[2 * k + 1] for k in range(n)]
+        elif blk == RST_TWZ:
+            grep, n = struct.unpack("<ii", payload[:8]) if size >= 8 else (0, -1)
+            if n < 0 or size != 8 + 48 * n:
+                raise ValueError(f"{path}: tweezers block of {size} bytes for {n} trap pairs")
+            r.twz_init[grep] = np.frombuffer(payload[8:], dtype="<f8").reshape(n, 2, 3).copy()
         elif blk == RST_PBC:
             if size != 24:
                 raise ValueError(f"{path}: PBC block of {size} bytes, expected 24")

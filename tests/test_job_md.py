@@ -437,6 +437,8 @@ def test_twz_records_take_the_positions_the_step_starts_from(tmp_path, monkeypat
     assert _order(got) == _order(reference_events(c, 0, twz=True))
     lines = (tmp_path / "md.twz").read_text().splitlines()
     assert lines[0] == TwzFile.HEADER
+    # the restart file keeps where the traps started
+    assert np.array_equal(read_rst(tmp_path / "md.rst").twz_init[1], [fr[0].init])
     # the record of step 200: beads at step 199, traps at step 200
     x = np.zeros((5, 3))
     x[:, 0] = 199
