@@ -103,3 +103,26 @@ def test_fortran_bindings_match_the_header():
         assert nargs == c[cname], (cname, nargs, c[cname])
     named = set(re.findall(r"\bsis_gpu_\w+", doc)) - {"sis_gpu_mod"}
     assert named <= set(c), named - set(c)
+
+
+def test_header_is_plain_c_and_links(lib, tmp_path):
+    """include/sis_gpu.h is plain C99 (-pedantic), and a C program that takes
+    the address of every entry point links against the library (nothing is
+    run)."""
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    names = declared()
+    src = tmp_path / "use.c"
+    src.write_text('#include "sis_gpu.h"\n#include <stdio.h>\nint main(void) {\n'
+                   + "".join(f'    printf("%p\\n", (void *)&{n});\n' for n in names)
+                   + "    return 0;\n}\n")
+    hdr = tmp_path / "hdr.c"
+    hdr.write_text('#include "sis_gpu.h"\nint sis_header_check(void) { return (int)sizeof(sis_params); }\n')
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", f"-I{ROOT / 'include'}",
+                        "-fsyntax-only", str(hdr)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    libdir = ROOT / "sis_gb300" / "_lib"
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src), f"-L{libdir}",
+                        "-lsisgpu", "-o", str(tmp_path / "use")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
