@@ -194,6 +194,13 @@ int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic
  * Debye-Hueckel parameters keep the temperature they were set at, as the
  * reference calls no set_ele there. */
 int sis_gpu_set_temperature(sis_ctx *ctx, int32_t inst, double tempK);
+/* [Freeze] (set_md_coef, src/job_md.F90:713-729,745-748): beads[n] are
+ * 1-based bead numbers of instance inst whose positions stay fixed (the
+ * GJF-2GJ position coefficient sqrt(b) h, or the Ermak-McCammon h/gamma and
+ * noise, set to zero); the call replaces the instance's earlier set, n = 0
+ * frees all.  Under replica exchange every replica must freeze the same
+ * beads (the reference freezes by bead number in all replicas). */
+int sis_gpu_set_frozen(sis_ctx *ctx, int32_t inst, const int32_t *beads, int32_t n);
 /* Caps the magnitude of every bead's total force at fmax (kcal/mol/A) in
  * sis_gpu_step; 0 removes the cap.  An equilibration aid for starting
  * structures with overlapping beads; it has no counterpart in the reference

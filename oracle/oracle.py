@@ -105,6 +105,7 @@ def lib() -> C.CDLL:
             "or_set_rg_bias": (None, [vp, i32, d, vp]),
             "or_set_restraints": (None, [vp, i32, vp, vp]),
             "or_set_tweezers": (None, [vp, i32, vp, vp, i32, vp, vp, vp, vp]),
+            "or_set_frozen": (None, [vp, i32, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -267,6 +268,12 @@ class Oracle:
         fv = np.array([q.velo for q in fr], dtype=np.float64).reshape(-1, 2, 3)
         self._twz = (dp, df, fp, fk, fi, fv)
         self.L.or_set_tweezers(self.h, len(dcf), _p(dp), _p(df), len(fr), _p(fp), _p(fk), _p(fi), _p(fv))
+
+    def set_frozen(self, beads):
+        """[Freeze]: 1-based bead numbers whose positions stay fixed."""
+        b = np.ascontiguousarray(beads, dtype=np.int32)
+        self._frozen = b
+        self.L.or_set_frozen(self.h, b.size, _p(b))
 
     def force_term(self, r, term):
         f = np.empty((self.nmp, 3))

@@ -112,6 +112,7 @@ struct or_system {
     int bp3_hash[4097];
     std::vector<int> bond_mp, angl_mp, dih_mp;
     std::vector<double> mass, fric, md_coef;
+    std::vector<char> frozen; /* [Freeze]: is_frozen per bead (empty: none) */
     std::vector<Rep> rep;
     bool flg_bp_energy;
     int64_t nrebuild;
@@ -379,6 +380,19 @@ void set_md_coef(or_system *s) {
             }
         }
     }
+    /* job_md.F90:713-729,745-748: a frozen bead's position coefficient is
+     * zero (GJF-2GJ sqrt(b) h; Ermak-McCammon h/gamma and its noise) */
+    if (!s->frozen.empty()) {
+        for (int i = 0; i < n; ++i) {
+            if (!s->frozen[i]) continue;
+            if (s->p.integrator == 1) {
+                s->md_coef[3 * i + 2] = 0.0;
+            } else {
+                s->md_coef[3 * i + 0] = 0.0;
+                for (int r = 0; r < s->nrep; ++r) s->rep[r].md_coef_rep[i] = 0.0;
+            }
+        }
+    }
 }
 
 /* pbc.F90:196-226 pbc_wrap: into [0, L) */
@@ -522,6 +536,14 @@ extern "C" void or_set_temperature(or_system *s, int32_t irep, double tempK, dou
     s->rep[irep].tempK = tempK;
     s->rep[irep].ionstr = ionstr;
     set_ele(s, irep);
+    set_md_coef(s);
+}
+
+/* [Freeze] id_ranges, as 1-based bead numbers (the same in every replica) */
+extern "C" void or_set_frozen(or_system *s, int32_t n, const int32_t *beads) {
+    s->frozen.assign(s->nmp, 0);
+    for (int q = 0; q < n; ++q)
+        if (beads[q] >= 1 && beads[q] <= s->nmp) s->frozen[beads[q] - 1] = 1;
     set_md_coef(s);
 }
 

@@ -157,6 +157,7 @@ int32_t or_get_bp_status(const or_system *s, int32_t irep, uint8_t *out, int32_t
 void or_set_stage(or_system *s, double sigma, double eps);
 void or_set_rg_bias(or_system *s, int32_t pott, double k, const double *rg0);
 void or_set_restraints(or_system *s, int32_t n, const int32_t *ids3, const double *para4);
+void or_set_frozen(or_system *s, int32_t n, const int32_t *beads);
 void or_set_tweezers(or_system *s, int32_t ndcf, const int32_t *dcf_pairs, const double *dcf_f, int32_t nfr,
                      const int32_t *fr_pairs, const double *fr_k, const double *fr_init, const double *fr_velo);
 

@@ -88,6 +88,7 @@ EXPORTS = {
     "sis_gpu_step": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "sis_gpu_set_condition": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double]),
     "sis_gpu_set_temperature": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
+    "sis_gpu_set_frozen": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]),
     "sis_gpu_get_ele": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "sis_gpu_get_md_coef": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "sis_gpu_set_force_cap": (C.c_int, [C.c_void_p, C.c_double]),

@@ -67,6 +67,7 @@ struct sis_ctx {
     std::vector<int4> binfo;
     std::vector<int> seq;
     std::vector<double> mass;
+    std::vector<uint8_t> frozen; // [Freeze] per bead (empty: none)
     std::vector<double> fric;
     std::vector<double> ionic;
     InstP *ip_d = nullptr;
@@ -219,6 +220,16 @@ void md_coefs(sis_ctx *ctx, std::vector<double4> &mdc) {
             mdc[i] = make_double4((1.0 - c1) / (1.0 + c1), c2 * dt / m, c2 * dt, noise_coef(p, fric, m, T));
         } else {
             mdc[i] = make_double4(dt / fric, 0.0, 0.0, noise_coef(p, fric, m, T));
+        }
+        // job_md.F90:713-729,745-748: a frozen bead's position coefficient is
+        // zero (GJF-2GJ sqrt(b) h; Ermak-McCammon h/gamma and its noise)
+        if (!ctx->frozen.empty() && ctx->frozen[i]) {
+            if (p.integrator == SIS_INTGRT_GJF2GJ) {
+                mdc[i].z = 0.0;
+            } else {
+                mdc[i].x = 0.0;
+                mdc[i].w = 0.0;
+            }
         }
     }
 }
@@ -1245,6 +1256,22 @@ extern "C" int sis_gpu_set_temperature(sis_ctx *ctx, int32_t inst, double tempK)
     return SIS_OK;
 }
 
+extern "C" int sis_gpu_set_frozen(sis_ctx *ctx, int32_t inst, const int32_t *beads, int32_t n) {
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || n < 0 || (n > 0 && !beads)) return SIS_ERR_ARG;
+    const InstP &I = ctx->ip[inst];
+    for (int q = 0; q < n; ++q)
+        if (beads[q] < 1 || beads[q] > I.n) return fail(ctx, SIS_ERR_ARG, "set_frozen: bead number out of range");
+    if (ctx->frozen.size() != (size_t)ctx->n) ctx->frozen.assign((size_t)ctx->n, 0);
+    std::fill(ctx->frozen.begin() + I.bead_off, ctx->frozen.begin() + I.bead_off + I.n, (uint8_t)0);
+    for (int q = 0; q < n; ++q) ctx->frozen[(size_t)I.bead_off + beads[q] - 1] = 1;
+    std::vector<double4> mdc;
+    md_coefs(ctx, mdc);
+    CK(cudaMemcpyAsync(ctx->D.mdc + I.bead_off, mdc.data() + I.bead_off, sizeof(double4) * I.n, cudaMemcpyHostToDevice,
+                       ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
 // ------------------------------------------------------- optional terms
 namespace {
 void bias_flags(sis_ctx *ctx) {
@@ -1595,7 +1622,11 @@ extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
                 if (I0.cell_len[d] < sqrt(c2) * 1.0005)
                     return fail(ctx, SIS_ERR_ARG, "remd: a rung's electrostatic cutoff exceeds the cell grid of the box");
         }
-        for (int i = 0; i < nl; ++i) lab_w[(size_t)l * nl + i] = noise_coef(ctx->p, fric, ctx->mass[I0.bead_off + i], temps[l]);
+        for (int i = 0; i < nl; ++i) {
+            const bool still = ctx->p.integrator != SIS_INTGRT_GJF2GJ && !ctx->frozen.empty() &&
+                               ctx->frozen[I0.bead_off + i];
+            lab_w[(size_t)l * nl + i] = still ? 0.0 : noise_coef(ctx->p, fric, ctx->mass[I0.bead_off + i], temps[l]);
+        }
         dgf_row(ctx, temps[l], lab_dgf.data() + (size_t)l * 469);
     }
     RemdDev &R = ctx->remd;
@@ -1717,6 +1748,8 @@ extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, c
     unsigned long long sc = 0;
     CK(cudaMemcpy(&sc, ctx->D.step_ctr, sizeof(sc), cudaMemcpyDeviceToHost));
     I.step0 = sc;
+    // a new job starts with no frozen beads
+    if (!ctx->frozen.empty()) std::fill(ctx->frozen.begin() + off, ctx->frozen.begin() + off + n, (uint8_t)0);
     std::vector<double4> mdc;
     md_coefs(ctx, mdc);
     for (int i = off + L; i < off + n; ++i) mdc[i] = make_double4(0.0, 0.0, 0.0, 0.0);

@@ -142,6 +142,12 @@ class Engine:
         for k in (range(self.n_inst) if inst < 0 else [inst]):
             self.system.instances[k].tempK = tempK
 
+    def set_frozen(self, inst: int, beads):
+        """[Freeze]: 1-based bead numbers of an instance whose positions stay
+        fixed; replaces the instance's earlier set (an empty list frees all)."""
+        b = np.ascontiguousarray(beads, dtype=np.int32).ravel()
+        self._ck(self.L.sis_gpu_set_frozen(self.h, int(inst), b.ctypes.data_as(C.c_void_p), b.size))
+
     def set_force_cap(self, fmax: float):
         """Equilibration aid: caps each bead's force magnitude (0 = off)."""
         self._ck(self.L.sis_gpu_set_force_cap(self.h, float(fmax)))

@@ -223,3 +223,38 @@ def test_set_ele_values_are_physical(sis_ff):
     assert cut == 50.0
     kB = orc.L.or_const(1)
     assert abs(kB - 0.0019872) < 1e-6
+
+
+@pytest.mark.parametrize("integ", ["GJF2GJ", "BD_EM"])
+def test_frozen_beads_stay_where_they_are(integ, sis_ff):
+    """[Freeze] (job_md.F90:713-729,745-748): the position coefficient of a
+    frozen bead is zero, so it keeps its place through a run while the
+    others move; GJF-2GJ velocities of frozen beads still evolve."""
+    from sis_gb300 import model
+    from sis_gb300.coil import single_chain
+
+    sysm = single_chain(sis_ff, n=16, seed=12)
+    sysm.opts.integrator = getattr(model, integ)
+    orc = Oracle.from_instance(sysm, 0)
+    md0 = orc.get_md_coef(0)
+    frozen = [1, 6, 7, 16]
+    orc.set_frozen(frozen)
+    md = orc.get_md_coef(0)
+    idx = np.array(frozen) - 1
+    other = np.setdiff1d(np.arange(16), idx)
+    if integ == "GJF2GJ":
+        keep = np.ix_(idx, [0, 1, 3])
+        assert np.all(md[idx, 2] == 0.0) and np.array_equal(md[keep], md0[keep])
+    else:
+        assert np.all(md[idx, 0] == 0.0) and np.all(md[idx, 3] == 0.0)
+    assert np.array_equal(md[other], md0[other])
+    x0 = orc.get_xyz(0)
+    rng = np.random.default_rng(4)
+    orc.set_velos(0, rng.normal(size=(16, 3)) * 0.05)
+    orc.md_init()
+    orc.run(20, rng.normal(size=(20, 1, 16, 3)))
+    x1 = orc.get_xyz(0)
+    assert np.array_equal(x1[idx], x0[idx])
+    assert np.all(np.abs(x1[other] - x0[other]).max(axis=1) > 0)
+    if integ == "GJF2GJ":
+        assert np.abs(orc.get_velos(0)[idx]).max() > 0
