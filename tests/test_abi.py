@@ -126,3 +126,51 @@ def test_header_is_plain_c_and_links(lib, tmp_path):
     r = subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", f"-I{ROOT / 'include'}", str(src), f"-L{libdir}",
                         "-lsisgpu", "-o", str(tmp_path / "use")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def _c_struct_fields(text, name):
+    body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", text, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    ctype = {"double": "real(c_double)", "int32_t": "integer(c_int32_t)", "uint64_t": "integer(c_int64_t)",
+             "int64_t": "integer(c_int64_t)"}
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        m = re.match(r"(?:const\s+)?(\w+)\s*(\**)\s*(.*)", decl, flags=re.S)
+        base, star, rest = m.groups()
+        for var in rest.split(","):
+            var = var.strip()
+            ptr_ = star or var.startswith("*")
+            nm = re.match(r"\**\s*(\w+)", var).group(1)
+            n = 1
+            for d in re.findall(r"\[(\d+)\]", var):
+                n *= int(d)
+            out.append((nm.lower(), "type(c_ptr)" if ptr_ else ctype[base], n))
+    return out
+
+
+def _fortran_type_fields(doc, name):
+    body = re.search(r"type, bind\(C\) :: " + name + r"\n(.*?)\n\s*end type", doc, flags=re.S).group(1)
+    out = []
+    for line in body.splitlines():
+        line = line.split("!")[0].strip()
+        if not line:
+            continue
+        ftype, names = (x.strip() for x in line.split("::"))
+        for var in re.findall(r"(\w+)(\([^)]*\))?", names):
+            n = 1
+            for d in re.findall(r"\d+", var[1]):
+                n *= int(d)
+            out.append((var[0].lower(), ftype.replace(" ", ""), n))
+    return out
+
+
+@pytest.mark.parametrize("name", ["sis_params", "sis_topology"])
+def test_fortran_struct_types_match_the_header(name):
+    """The bind(C) derived types of INTEGRATION.md list the C structs'
+    fields in order, with matching kinds and array sizes."""
+    c = _c_struct_fields(HEADER.read_text(), name)
+    f = _fortran_type_fields((ROOT / "INTEGRATION.md").read_text(), name)
+    assert f == c
