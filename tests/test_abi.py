@@ -174,3 +174,60 @@ def test_fortran_struct_types_match_the_header(name):
     c = _c_struct_fields(HEADER.read_text(), name)
     f = _fortran_type_fields((ROOT / "INTEGRATION.md").read_text(), name)
     assert f == c
+
+
+def _c_param_lists(text):
+    decl = r"^[ \t]*(?:const[ \t]+)?\w+[ \t]*\**[ \t]*(sis_gpu_\w+)\s*\(([^;]*?)\)\s*;"
+    out = {}
+    for name, params in re.findall(decl, text, flags=re.S | re.M):
+        ps = []
+        for prm in params.split(","):
+            prm = prm.strip()
+            if not prm or prm == "void":
+                continue
+            m = re.match(r"(?:const\s+)?(\w+)\s*(\**)\s*(\w+)$", prm)
+            base, stars, pname = m.groups()
+            ps.append((pname.lower(), base, len(stars)))
+        out[name] = ps
+    return out
+
+
+def test_fortran_argument_kinds_match_the_header():
+    """Each dummy argument of the ISO_C_BINDING interfaces passes what the C
+    parameter in the same position expects: scalars by value with the same
+    kind, pointers as type(c_ptr) by value or as an array or scalar by
+    reference of the same kind."""
+    kind = {"double": "real(c_double)", "int32_t": "integer(c_int32_t)", "int64_t": "integer(c_int64_t)",
+            "uint64_t": "integer(c_int64_t)", "uint8_t": "integer(c_int8_t)", "float": "real(c_float)",
+            "sis_ctx": "type(c_ptr)", "sis_topology": "type(sis_topology)", "sis_params": "type(sis_params)",
+            "sis_stats": "type(sis_stats)"}
+    c = _c_param_lists(HEADER.read_text())
+    doc = (ROOT / "INTEGRATION.md").read_text()
+    blocks = re.findall(r"(?:function|subroutine)\s+\w+\s*\(([^)]*)\)\s*&?\s*bind\(C,\s*name=\"(\w+)\"\)(.*?)end (?:function|subroutine)",
+                        doc, flags=re.S)
+    checked = 0
+    for args, cname, body in blocks:
+        f = {}
+        for line in body.splitlines():
+            line = line.split("!")[0].strip()
+            if "::" not in line or line.startswith("import"):
+                continue
+            attrs, names = (x.strip() for x in line.split("::"))
+            parts = [a.strip() for a in re.split(r",(?![^(]*\))", attrs)]
+            ftype, by_value = parts[0].replace(" ", ""), "value" in parts[1:]
+            for nm in re.findall(r"(\w+)(?:\([^)]*\))?", names):
+                f[nm.lower()] = (ftype, by_value)
+        fargs = [a.strip().lower() for a in args.split(",") if a.strip()]
+        assert len(fargs) == len(c[cname]), cname
+        for (pname, base, stars), farg in zip(c[cname], fargs):
+            ftype, by_value = f[farg]
+            if stars == 0:
+                assert by_value and ftype == kind[base], (cname, pname)
+            elif base == "sis_ctx" and stars == 1:
+                assert by_value and ftype == "type(c_ptr)", (cname, pname)
+            elif stars == 1:
+                assert (by_value and ftype == "type(c_ptr)") or (not by_value and ftype == kind[base]), (cname, pname)
+            else:  # sis_ctx **: the handle returned by reference
+                assert not by_value and ftype == "type(c_ptr)", (cname, pname)
+            checked += 1
+    assert checked >= 60
