@@ -231,3 +231,28 @@ def test_fortran_argument_kinds_match_the_header():
                 assert not by_value and ftype == "type(c_ptr)", (cname, pname)
             checked += 1
     assert checked >= 60
+
+
+def test_ctypes_argtypes_match_the_header():
+    """sis_gb300._abi declares every entry point with the header's parameter
+    count and kinds (pointers as c_void_p or a POINTER, scalars by their
+    width) and an int status (or the header's return type)."""
+    from sis_gb300 import _abi
+
+    scalar = {"double": C.c_double, "int32_t": C.c_int32, "int64_t": C.c_int64, "uint64_t": C.c_uint64,
+              "uint32_t": C.c_uint32, "float": C.c_float}
+    text = HEADER.read_text()
+    c = _c_param_lists(text)
+    rets = dict((n, r.strip()) for r, n in re.findall(r"^[ \t]*((?:const[ \t]+)?\w+[ \t]*\**)[ \t]*(sis_gpu_\w+)\s*\(",
+                                                      text, flags=re.M))
+    ret_kind = {"int": C.c_int, "void": None, "const char *": C.c_char_p, "int64_t": C.c_int64}
+    for name, (restype, argtypes) in _abi.EXPORTS.items():
+        assert restype is ret_kind[" ".join(rets[name].replace("*", " *").split())], name
+        params = c[name]
+        assert len(argtypes) == len(params), name
+        for (pname, base, stars), at in zip(params, argtypes):
+            if stars:
+                assert at is C.c_void_p or at is C.c_char_p or hasattr(at, "_type_") and issubclass(at, C._Pointer), \
+                    (name, pname, at)
+            else:
+                assert at is scalar[base], (name, pname, at)
