@@ -57,3 +57,22 @@ def test_reference_arm_prints_on_rank_zero_only():
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
     assert out1.strip() == ""
+
+
+def test_reference_arm_line_carries_the_contract_keys():
+    """One process, no torchrun: the reference arm's JSON line has the keys
+    the benchmark contract lists, with e2e and cpu_baseline describing this
+    run."""
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "chain64", "--steps", "1",
+                        "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["n_gpus"] == 1 and line["steps"] == 1 and line["warmup"] == 3
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["unit"] == line["unit"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference") and cb["sample"]
+    assert "workload" in line["config"]
