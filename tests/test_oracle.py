@@ -258,3 +258,63 @@ def test_frozen_beads_stay_where_they_are(integ, sis_ff):
     assert np.all(np.abs(x1[other] - x0[other]).max(axis=1) > 0)
     if integ == "GJF2GJ":
         assert np.abs(orc.get_velos(0)[idx]).max() > 0
+
+
+@pytest.mark.parametrize("seq,lists,terms", [
+    ("A", (0, 0, 0), ()),
+    ("AC", (0, 0, 0), (1,)),
+    ("ACG", (0, 0, 0), (1, 2)),
+    ("ACGU", (1, 1, 0), (1, 2, 3, 5, 6)),  # (1,4): WCA and Debye-Hueckel; no base pair within min_loop
+    ("DDDD", (0, 0, 0), (1, 2, 3)),  # dummy beads: no WCA (neighbor_list.F90:123), no charge
+    ("AAAAAAAAAA", (22, 28, 0), (1, 2, 3, 5, 6)),  # A-A never pairs; |i-j| >= 3 for WCA and ele
+])
+def test_short_and_dummy_chains(seq, lists, terms, sis_ff):
+    """Edge cases of the list rules and term counts: chains of one to four
+    beads, a chain of dummy beads and one that cannot pair; forces stay
+    finite and equal minus the energy gradient."""
+    n = len(seq)
+    # a helix (bond 6.8 A, bend 98 degrees): no angle comes near straight,
+    # where force_angl.F90:57-60 clamps |v21 x v32|^2 to 1 on purpose
+    ph = np.radians(100.0) * np.arange(n)
+    x = np.stack([4.0 * np.cos(ph), 4.0 * np.sin(ph), 3.0 * np.arange(n)], axis=1)
+    sysm = System(sis_ff, Options(bp_model=1), [Instance([Chain.from_string(seq)], xyz=x)])
+    o = Oracle.from_instance(sysm, 0)
+    o.neighbor_list(0)
+    assert tuple(len(o.get_list(0, k)) for k in range(3)) == lists
+    e = o.energy_sumup(0)
+    assert [k for k in range(1, 7) if e[k] != 0.0] == list(terms)
+    f = o.force(0)
+    assert np.all(np.isfinite(f))
+    h = 1e-5
+    for i in range(n):
+        for a in range(3):
+            ep = []
+            for s in (h, -h):
+                y = x.copy()
+                y[i, a] += s
+                o.set_xyz(0, y)
+                o.set_bp_energy_flag(0)
+                ep.append(o.energy_sumup(0)[0])
+            assert abs(-(ep[0] - ep[1]) / (2 * h) - f[i, a]) <= 1e-5 * max(1.0, abs(f[i, a]))
+    o.set_xyz(0, x)
+
+
+def test_near_straight_angle_force_is_clamped_as_the_reference_does(sis_ff):
+    """force_angl.F90:50-64: below |v21 x v32|^2 = 1 A^4 the denominator is
+    held at 1, so near 180 degrees the force is smaller than minus the energy
+    gradient, by design.  Checked against the formula written out here."""
+    x = np.array([[0.0, 0.0, 0.0], [5.9, 0.05, 0.0], [11.8, 0.0, 0.08]])
+    sysm = System(sis_ff, Options(bp_model=1), [Instance([Chain.from_string("ACG")], xyz=x)])
+    o = Oracle.from_instance(sysm, 0)
+    o.neighbor_list(0)
+    f = o.force_term(0, 2)
+    v21, v32 = x[1] - x[0], x[2] - x[1]
+    d21, d32, d2132 = v21 @ v21, v32 @ v32, v32 @ v21
+    assert d21 * d32 - d2132 ** 2 < 1.0
+    k, t0 = sis_ff.angl_k, sis_ff.angl_t0
+    delta = np.arccos(max(-1.0, min(1.0, -d2132 / np.sqrt(d21 * d32)))) - t0
+    g = k * delta / 1.0
+    f21 = g * (v21 * (d2132 / d21) - v32)
+    f32 = g * (v32 * (d2132 / d32) - v21)
+    want = np.array([-f21, f21 - f32, f32])
+    assert np.allclose(f, want, rtol=1e-12, atol=1e-14)
