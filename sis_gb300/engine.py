@@ -29,6 +29,10 @@ class Engine:
         self.L = _abi.lib()
         self.system = system
         self.precision = precision
+        # the Philox key and the noise stream of every instance: with the
+        # step counter they determine the noise (restart files keep them)
+        self.seed = int(seed)
+        self.streams = [int(v) for v in streams] if streams is not None else list(range(len(system.instances)))
         self._topo = _abi.TopologyArrays(system, streams)
         self._par = _abi.pack_params(system, precision, seed, nbr_cap, bp_cap)
         h = C.c_void_p()
@@ -195,6 +199,7 @@ class Engine:
         self._ck(self.L.sis_gpu_load_slot(self.h, int(inst), len(chains), lens.ctypes.data_as(vp), molt.ctypes.data_as(vp),
                                           seq.ctypes.data_as(vp), None, float(tempK), float(ionic_strength), int(stream),
                                           x.ctypes.data_as(vp), int(bool(init_velocities))))
+        self.streams[inst] = int(stream)
 
     def bp_mc(self, inst: int = -1, draws: Optional[np.ndarray] = None):
         """Request a base-pair Monte Carlo pass at the next force or step evaluation."""

@@ -275,12 +275,13 @@ class MdJob:
         # write_rst.F90:98-111: the force-ramp traps' starting positions
         twz = [np.array([t.init for t in eng.tweezers(k)[1]], dtype=np.float64).reshape(-1, 2, 3)
                for k in range(self.n_inst)]
+        noise = [(eng.seed, eng.streams[k]) if hasattr(eng, "seed") else None for k in range(self.n_inst)]
 
         def write():
             for k in range(self.n_inst):
                 s = slice(o[k], o[k + 1])
                 write_rst(self.base(k) + ".rst", step, x[s], v[s], a[s], grep=k + 1, box=boxes[k],
-                          rep2lab=rep2lab if k == 0 else None, ianneal=ianneal, twz_init=twz[k])
+                          rep2lab=rep2lab if k == 0 else None, ianneal=ianneal, twz_init=twz[k], noise=noise[k])
 
         self.writer.put(write)
 

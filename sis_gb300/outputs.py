@@ -17,15 +17,16 @@
   int64 step), XYZ/VELO/ACCEL (int32 replica, int32 nmp, nmp x 3 float64),
   REPLICA (int32 n, then n pairs of int32 replica, label) and PBC (3 float64)
   are written as the reference writes them.  The noise state is not an MT
-  stream here but the Philox counter, which the step number determines, so
-  no PRNG block is written; the reference's reader (read_rst.F90) skips
-  blocks by their size and needs none of them to load the rest.
+  stream here but a Philox key and counter, which the stored key (block
+  RST_NOISE) and the step number determine, so no PRNG block is written; the
+  reference's reader (read_rst.F90) skips blocks it does not want by their
+  size.
 """
 from __future__ import annotations
 
 import struct
 from dataclasses import dataclass, field
-from typing import Dict, List, Optional, Sequence
+from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -36,6 +37,9 @@ ENE_TOTAL, ENE_BOND, ENE_ANGL, ENE_DIHE, ENE_BP, ENE_EXV, ENE_ELE = 0, 1, 2, 3, 
 ENE_STAGE, ENE_TWZ, ENE_RG, ENE_REST = 7, 8, 9, 10
 # const_idx.F90 RSTBLK
 RST_STEP, RST_ANNEAL, RST_XYZ, RST_VELO, RST_ACCEL, RST_REPLICA, RST_PRNG, RST_PRNGREP, RST_TWZ, RST_PBC = range(1, 11)
+# the noise key of the engine (Philox key and stream); not a block id of
+# const_idx.F90 RSTBLK, so the reference's reader skips it by its size
+RST_NOISE = 101
 # var_io.F90 KIND_OUT_BP, KIND_OUT_BPE
 KIND_OUT_BP, KIND_OUT_BPE = 2, 4
 
@@ -327,16 +331,21 @@ class Restart:
     box: Optional[np.ndarray] = None
     ianneal: Optional[int] = None  # 1-based stage of the annealing schedule
     twz_init: Dict[int, np.ndarray] = field(default_factory=dict)  # by replica: force-ramp traps at step 0, (n, 2, 3)
+    noise: Dict[int, tuple] = field(default_factory=dict)  # by replica: (Philox key, stream)
 
 
 def write_rst(path, step: int, xyz: np.ndarray, velos: np.ndarray, accels: np.ndarray, grep: int = 1,
               box: Optional[Sequence[float]] = None, rep2lab: Optional[Sequence[int]] = None,
-              ianneal: Optional[int] = None, twz_init: Optional[np.ndarray] = None):
+              ianneal: Optional[int] = None, twz_init: Optional[np.ndarray] = None,
+              noise: Optional[Tuple[int, int]] = None):
     """One replica's restart file in the block order of write_rst.F90
     (replica table first in the first replica's file, then step, annealing
     stage, coordinates, velocities, accelerations, the force-ramp traps'
     starting positions (int32 replica, int32 n, n x 2 x 3 float64), PBC
-    box)."""
+    box), and last the noise key ``noise`` = (Philox key, stream) in block
+    RST_NOISE (int32 replica, uint32 stream, uint64 key).  The reference keeps
+    its MT19937 state in PRNG blocks instead; the step number and this key
+    determine the noise here, so no PRNG block is written."""
     xyz, velos, accels = (np.ascontiguousarray(a, dtype="<f8").reshape(-1, 3) for a in (xyz, velos, accels))
     nmp = xyz.shape[0]
     if velos.shape[0] != nmp or accels.shape[0] != nmp:
@@ -363,6 +372,9 @@ def write_rst(path, step: int, xyz: np.ndarray, velos: np.ndarray, accels: np.nd
         if box is not None:
             f.write(struct.pack("<ii", RST_PBC, 8 * 3))
             f.write(np.asarray(box, dtype="<f8").tobytes())
+        if noise is not None:
+            f.write(struct.pack("<iiiIQ", RST_NOISE, 16, int(grep), int(noise[1]) & 0xFFFFFFFF,
+                                int(noise[0]) & 0xFFFFFFFFFFFFFFFF))
 
 
 def read_rst(path) -> Restart:
@@ -414,6 +426,11 @@ def read_rst(path) -> Restart:
             if n < 0 or size != 8 + 48 * n:
                 raise ValueError(f"{path}: tweezers block of {size} bytes for {n} trap pairs")
             r.twz_init[grep] = np.frombuffer(payload[8:], dtype="<f8").reshape(n, 2, 3).copy()
+        elif blk == RST_NOISE:
+            if size != 16:
+                raise ValueError(f"{path}: noise-key block of {size} bytes, expected 16")
+            grep, stream, key = struct.unpack("<iIQ", payload)
+            r.noise[grep] = (key, stream)
         elif blk == RST_PBC:
             if size != 24:
                 raise ValueError(f"{path}: PBC block of {size} bytes, expected 24")
@@ -442,10 +459,18 @@ def save_frame(eng, inst: int, step: int, out: Optional[OutFile] = None, bp: Opt
                 w.write_frame(rec, st, ene, tK)
 
 
-def restart_engine(eng, path, inst: int = 0, grep: int = 1):
+def restart_engine(eng, path, inst: int = 0, grep: int = 1, check_noise: bool = True):
     """Loads one replica's coordinates, velocities, accelerations and step
-    from a restart file into instance inst of an Engine."""
+    from a restart file into instance inst of an Engine.  When the file
+    holds the noise key it was written with, the engine must have the same
+    key and stream, or the run would go on with other noise (the reference
+    restores its MT19937 state); ``check_noise=False`` accepts a change."""
     r = read_rst(path)
+    if check_noise and grep in r.noise and hasattr(eng, "seed"):
+        have = (int(eng.seed) & 0xFFFFFFFFFFFFFFFF, int(eng.streams[inst]) & 0xFFFFFFFF)
+        if have != tuple(r.noise[grep]):
+            raise ValueError(f"{path}: written with noise key {r.noise[grep][0]} stream {r.noise[grep][1]}, the engine "
+                             f"has key {have[0]} stream {have[1]}; pass check_noise=False to continue with other noise")
     n = eng.nmp(inst)
     for name, d in (("coordinates", r.xyz), ("velocities", r.velos), ("accelerations", r.accels)):
         if grep not in d:

@@ -216,3 +216,41 @@ def test_frame_writers_write_what_the_engine_holds(sis_ff, tmp_path):
     assert [[(i, j) for i, j, _ in f] for f in frames] == [[(i, j) for i, j, _ in p] for p in want_pairs]
     assert all(np.allclose([e for *_, e in f], [e for *_, e in p], rtol=1e-6) for f, p in zip(frames, want_pairs))
     assert len((tmp_path / "a.bpe").read_text().splitlines()) == 3
+
+
+class _KeyedEngine:
+    """What restart_engine needs of an engine, with a noise key."""
+
+    def __init__(self, seed, stream, n=7):
+        self.seed, self.streams, self.n = seed, [stream], n
+        self.loaded = None
+
+    def nmp(self, inst):
+        return self.n
+
+    def set_state(self, inst, x, v, a):
+        self.loaded = (x, v, a)
+
+    def set_step(self, s):
+        self.step = s
+
+
+def test_rst_noise_key(tmp_path):
+    """The engine's Philox key and stream go into a block the reference's
+    reader skips by size; a restart into an engine with another key is
+    refused unless asked for, since the run would draw other noise."""
+    from sis_gb300.outputs import RST_NOISE
+    x = np.zeros((7, 3))
+    p = tmp_path / "a.rst"
+    write_rst(p, 10, x, x, x, grep=2, noise=(2 ** 63 + 5, 7))
+    b = p.read_bytes()
+    assert struct.unpack("<iiiIQ", b[-24:]) == (RST_NOISE, 16, 2, 7, 2 ** 63 + 5)
+    assert read_rst(p).noise == {2: (2 ** 63 + 5, 7)}
+    eng = _KeyedEngine(2 ** 63 + 5, 7)
+    restart_engine(eng, p, grep=2)
+    assert eng.step == 10 and eng.loaded is not None
+    with pytest.raises(ValueError, match="noise key"):
+        restart_engine(_KeyedEngine(2 ** 63 + 5, 8), p, grep=2)
+    with pytest.raises(ValueError, match="noise key"):
+        restart_engine(_KeyedEngine(12345, 7), p, grep=2)
+    restart_engine(_KeyedEngine(12345, 7), p, grep=2, check_noise=False)
