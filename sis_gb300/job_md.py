@@ -134,8 +134,9 @@ class MdJob:
     per instance, by label; ``Engine.remd_init`` is called with it).
     ``restart``: the Restart the engine was loaded from (outputs.read_rst and
     restart_engine); a restarted job writes no frame at its first step and
-    resumes the annealing stage and the replica labels the file holds.  ``reset_step`` starts the
-    step count at 0 whatever the file holds.  ``clock``: wall-clock seconds
+    resumes the annealing stage and the replica labels the file holds.
+    ``reset_step`` starts the step count at 0 whatever the file holds.
+    ``clock``: wall-clock seconds
     (time.monotonic), measured from the job's construction.  The optional
     .out columns and the .twz file follow the terms set on the engine.
     With ``threaded_writer`` the files are formatted and written on a host
@@ -162,6 +163,9 @@ class MdJob:
                 for k, lab in enumerate(restart.rep2lab):
                     inst = eng.system.instances[k]
                     eng.set_condition(k, self.temps[lab - 1], inst.ionic_strength)
+            off = [float(i.tempK) for i in eng.system.instances if float(i.tempK) not in self.temps]
+            if off:
+                raise ValueError(f"every replica must start on a rung of replica_temps; {off} are not rungs")
             eng.remd_init(self.temps)
             self.labels = [self.temps.index(float(i.tempK)) for i in eng.system.instances]
         elif self.c.nstep_rep_exchange > 0:

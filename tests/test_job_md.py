@@ -666,3 +666,9 @@ def test_job_on_the_engine(sis_ff, tmp_path):
     assert list(read_out(Path(tmp_path / "b" / "b2.out"))["nframe"]) == [60, 80, 100]
     for u, w in zip(a.get_state(0), b2.get_state(0)):
         assert np.array_equal(u, w)
+
+
+def test_replicas_must_start_on_rungs():
+    with pytest.raises(ValueError, match="not rungs"):
+        MdJob(FakeEngine(n_inst=2, temps=[300.0, 305.0]), "x", MdControl(nstep=10, nstep_save=5),
+              replica_temps=[300.0, 310.0])
