@@ -136,7 +136,13 @@ typedef struct sis_stats {
 /* Creates a context and uploads topology and parameters.  Replaces the
  * set-up the reference does in init_bp, init_ele/set_ele, list_local and
  * set_md_coef (src/init_bp.F90, src/set_ele.F90, src/list_local.F90,
- * src/job_md.F90:94-133,700-767). */
+ * src/job_md.F90:94-133,700-767).  Before any device work it refuses with
+ * SIS_ERR_ARG: a sequence code outside A U G C D (0-4), a molecule type
+ * other than 1 or 2, an empty chain, a non-positive or non-finite
+ * temperature, salt (with electrostatics) or time step, a negative or
+ * non-finite box component, viscosity <= 0, a negative list margin or
+ * capacity, an unknown precision, integrator, base-pair model (0-5) or
+ * cutoff type, and base-pair Monte Carlo with max_bp_per_nt < 1. */
 int sis_gpu_create(const sis_topology *top, const sis_params *par, sis_ctx **out);
 void sis_gpu_destroy(sis_ctx *ctx);
 /* number of beads of instance inst (nmp), or of all instances for inst = -1 */

@@ -18,6 +18,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libsisgpu.so"
 SIS_OK = 0
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "list overflow", -4: "non-finite values", -5: "out of device memory",
           -6: "call out of order", -7: "device wait timed out"}
+SIS_ERR_ARG = -1
 SIS_ERR_TIMEOUT = -7
 
 

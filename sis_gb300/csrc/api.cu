@@ -577,9 +577,50 @@ int autotune(sis_ctx *ctx) {
 
 } // namespace
 
+namespace {
+bool finite_pos(double v) { return std::isfinite(v) && v > 0.0; }
+
+// Host-side checks of everything that later indexes a device table or
+// divides: codes, counts and physical constants.  They run before any CUDA
+// call, so a bad input is refused without touching the device.
+bool inputs_valid(const sis_topology *top, const sis_params *p) {
+    if (!top->inst_chain_off || !top->chain_len || !top->chain_moltype || !top->seq || !top->tempK ||
+        !top->ionic_strength)
+        return false;
+    if (top->inst_chain_off[0] < 0) return false;
+    long long nb = 0;
+    for (int k = 0; k < top->n_inst; ++k) {
+        if (top->inst_chain_off[k + 1] < top->inst_chain_off[k]) return false;
+        if (!finite_pos(top->tempK[k])) return false;
+        if (p->flg_ele && !finite_pos(top->ionic_strength[k])) return false;
+        if (top->box)
+            for (int d = 0; d < 3; ++d)
+                if (!std::isfinite(top->box[3 * k + d]) || top->box[3 * k + d] < 0.0) return false;
+        for (int c = top->inst_chain_off[k]; c < top->inst_chain_off[k + 1]; ++c) {
+            const int len = top->chain_len[c];
+            if (len < 1 || (top->chain_moltype[c] != 1 && top->chain_moltype[c] != 2)) return false;
+            for (int l = 0; l < len; ++l)
+                if (top->seq[nb + l] < 0 || top->seq[nb + l] > 4) return false; // SEQT A U G C D
+            nb += len;
+            if (nb >= (1LL << 30)) return false;
+        }
+    }
+    if (p->precision != SIS_PREC_FP64 && p->precision != SIS_PREC_MIXED) return false;
+    if (p->integrator != SIS_INTGRT_GJF2GJ && p->integrator != SIS_INTGRT_BD_EM) return false;
+    if (!finite_pos(p->dt) || !finite_pos(p->viscosity_Pas) || !std::isfinite(p->nl_margin) || p->nl_margin < 0.0)
+        return false;
+    if (p->bp_model < 0 || p->bp_model > 5 || p->nbr_cap < 0 || p->bp_cap < 0 || p->nstep_bp_mc < 0) return false;
+    if (p->nstep_bp_mc > 0 && p->max_bp_per_nt < 1) return false;
+    if (p->flg_ele && p->ele_cutoff_type != 1 && p->ele_cutoff_type != 2) return false;
+    return true;
+}
+} // namespace
+
 // ====================================================================== API
 extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, sis_ctx **out) {
     if (!top || !par || !out || top->n_inst <= 0) return SIS_ERR_ARG;
+    *out = nullptr;
+    if (!inputs_valid(top, par)) return SIS_ERR_ARG;
     sis_ctx *ctx = new sis_ctx();
     *out = nullptr;
     ctx->p = *par;
