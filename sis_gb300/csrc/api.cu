@@ -1764,6 +1764,13 @@ extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, c
     }
     if (L > n) return fail(ctx, SIS_ERR_ARG, "load_slot: the job has more beads than the slot");
     if (L > 0 && (!seq || !xyz)) return SIS_ERR_ARG;
+    if (!std::isfinite(tempK) || !std::isfinite(ionic)) return SIS_ERR_ARG;
+    // every code is checked before the slot is touched, so a refused job
+    // leaves the slot as it was
+    for (int i = 0; i < L; ++i)
+        if (seq[i] < 0 || seq[i] > 4) return fail(ctx, SIS_ERR_ARG, "load_slot: sequence code outside A U G C D");
+    for (int c = 0; chain_moltype && c < n_chains; ++c)
+        if (chain_moltype[c] != 1 && chain_moltype[c] != 2) return fail(ctx, SIS_ERR_ARG, "load_slot: molecule type");
     // topology: the job's chains, then inert single-bead fillers (sequence D,
     // uncharged: no list, bonded or base-pair term takes them; frozen below)
     int b = off;
