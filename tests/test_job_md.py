@@ -672,3 +672,19 @@ def test_replicas_must_start_on_rungs():
     with pytest.raises(ValueError, match="not rungs"):
         MdJob(FakeEngine(n_inst=2, temps=[300.0, 305.0]), "x", MdControl(nstep=10, nstep_save=5),
               replica_temps=[300.0, 310.0])
+
+
+def test_restart_files_keep_the_noise_key(tmp_path):
+    """With an engine that has a Philox key, every replica's .rst holds the
+    key and that replica's stream, and restart_engine checks them."""
+    eng = FakeEngine(n_inst=2, temps=[300.0, 310.0])
+    eng.seed, eng.streams = 77, [5, 9]
+    MdJob(eng, str(tmp_path / "md"), MdControl(nstep=20, nstep_save=10), log=lambda s: None).run()
+    assert read_rst(tmp_path / "md_0001.rst").noise == {1: (77, 5)}
+    assert read_rst(tmp_path / "md_0002.rst").noise == {2: (77, 9)}
+    other = FakeEngine(n_inst=2)
+    other.seed, other.streams = 77, [5, 9]
+    restart_engine(other, tmp_path / "md_0002.rst", inst=1, grep=2)
+    other.streams = [5, 5]
+    with pytest.raises(ValueError, match="noise key"):
+        restart_engine(other, tmp_path / "md_0002.rst", inst=1, grep=2)
