@@ -47,17 +47,24 @@ def write_dcd(path, frames: List[np.ndarray], box=None) -> None:
 
 
 def read_dcd(path) -> Tuple[np.ndarray, Optional[np.ndarray]]:
-    """Returns (frames (nframe, natom, 3) float64, boxes (nframe, 3) or None)."""
+    """Returns (frames (nframe, natom, 3) float64, boxes (nframe, 3) or None).
+    The file may end only between frames; a record cut short or framed by
+    unequal sizes raises ValueError (the reference's read_onestep stops
+    there too)."""
     data = open(path, "rb").read()
     pos = 0
 
     def block():
         nonlocal pos
+        if pos + 4 > len(data):
+            raise ValueError(f"{path}: truncated DCD record at byte {pos}")
         (sz,) = struct.unpack_from("<i", data, pos)
+        if sz < 0 or pos + 8 + sz > len(data):
+            raise ValueError(f"{path}: truncated DCD record at byte {pos}")
         payload = data[pos + 4: pos + 4 + sz]
         (sz2,) = struct.unpack_from("<i", data, pos + 4 + sz)
         if sz != sz2:
-            raise ValueError("corrupt DCD record")
+            raise ValueError(f"{path}: corrupt DCD record at byte {pos}")
         pos += 8 + sz
         return payload
 
@@ -74,5 +81,7 @@ def read_dcd(path) -> Tuple[np.ndarray, Optional[np.ndarray]]:
             uc = struct.unpack("<6d", block())
             boxes.append((uc[0], uc[2], uc[5]))
         xs = [np.frombuffer(block(), dtype="<f4") for _ in range(3)]
+        if any(x.size != natom for x in xs):
+            raise ValueError(f"{path}: a frame holds a coordinate block of another atom count than {natom}")
         frames.append(np.stack(xs, axis=1).astype(np.float64))
     return np.array(frames).reshape(-1, natom, 3), (np.array(boxes) if unitcell else None)

@@ -254,3 +254,16 @@ def test_rst_noise_key(tmp_path):
     with pytest.raises(ValueError, match="noise key"):
         restart_engine(_KeyedEngine(12345, 7), p, grep=2)
     restart_engine(_KeyedEngine(12345, 7), p, grep=2, check_noise=False)
+
+
+@pytest.mark.parametrize("cut", [10, 100, -5, -40])
+def test_truncated_dcd_raises(tmp_path, cut):
+    from sis_gb300 import dcd
+    p = tmp_path / "a.dcd"
+    dcd.write_dcd(p, [np.zeros((4, 3)), np.ones((4, 3))], box=(10.0, 10.0, 10.0))
+    b = p.read_bytes()
+    frames, _ = dcd.read_dcd(p)
+    assert frames.shape == (2, 4, 3)
+    p.write_bytes(b[:cut])
+    with pytest.raises(ValueError, match="truncated DCD"):
+        dcd.read_dcd(p)
