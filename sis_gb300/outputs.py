@@ -187,22 +187,28 @@ class BpFile:
 
 
 def read_bp(path) -> List[List[tuple]]:
-    """Frames of a .bp/.bpall file: lists of (i, j, energy)."""
+    """Frames of a .bp/.bpall file: lists of (i, j, energy).  A file cut
+    inside its header or a record, or whose last frame lacks its (0, 0, 0)
+    terminator, raises ValueError."""
     with open(path, "rb") as f:
-        ki, kr = struct.unpack("<ii", f.read(8))
-        if (ki, kr) != (KIND_OUT_BP, KIND_OUT_BPE):
-            raise ValueError(f"unsupported kinds {ki}, {kr}")
-        frames, cur = [], []
-        while True:
-            b = f.read(8)
-            if len(b) < 8:
-                break
-            i, j, e = struct.unpack("<hhf", b)
-            if i == 0:
-                frames.append(cur)
-                cur = []
-            else:
-                cur.append((i, j, e))
+        data = f.read()
+    if len(data) < 8:
+        raise ValueError(f"{path}: truncated .bp header")
+    ki, kr = struct.unpack_from("<ii", data, 0)
+    if (ki, kr) != (KIND_OUT_BP, KIND_OUT_BPE):
+        raise ValueError(f"{path}: unsupported kinds {ki}, {kr}")
+    if (len(data) - 8) % 8:
+        raise ValueError(f"{path}: truncated .bp record at byte {8 + (len(data) - 8) // 8 * 8}")
+    frames, cur = [], []
+    for off in range(8, len(data), 8):
+        i, j, e = struct.unpack_from("<hhf", data, off)
+        if i == 0:
+            frames.append(cur)
+            cur = []
+        else:
+            cur.append((i, j, e))
+    if cur:
+        raise ValueError(f"{path}: the last frame has no terminator")
     return frames
 
 

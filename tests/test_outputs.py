@@ -267,3 +267,16 @@ def test_truncated_dcd_raises(tmp_path, cut):
     p.write_bytes(b[:cut])
     with pytest.raises(ValueError, match="truncated DCD"):
         dcd.read_dcd(p)
+
+
+@pytest.mark.parametrize("cut,what", [(5, "header"), (-3, "record"), (-8, "terminator")])
+def test_truncated_bp_raises(tmp_path, cut, what):
+    p = tmp_path / "a.bp"
+    w = BpFile(p)
+    for pairs, st, ene in GOLDEN["bp_frames"]:
+        w.write_frame(np.array(pairs), np.array(st), np.array(ene), 300.0)
+    w.close()
+    assert len(read_bp(p)) == 2
+    p.write_bytes(p.read_bytes()[:cut])
+    with pytest.raises(ValueError, match=what):
+        read_bp(p)
