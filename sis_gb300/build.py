@@ -1,7 +1,8 @@
 """In-tree build of libsisgpu.so for sm_103a (nvcc, no cmake).
 
 Each translation unit is compiled in parallel, then linked with the static
-CUDA runtime so that the library has no dependency beyond the driver.
+CUDA runtime so that the library needs nothing beyond the NVIDIA kernel-mode
+and user-mode driver libraries (libcuda).
 Objects go to ``_build/``, the library to ``sis_gb300/_lib/``.
 """
 from __future__ import annotations

@@ -1,7 +1,7 @@
 """The MD job driver (sis_gb300.job_md) and the files around it.
 
 CPU, against a stand-in engine that records every call:
-* the driver runs the steps between two events as one Engine.step call and
+* the job runs the steps between two events as one Engine.step call and
   still acts at exactly the steps of job_md.F90's one-step-at-a-time loop
   (restated below): frames, restart files, replica label table and
   exchanges (alternating pair patterns), annealing and timed Rg-bias
@@ -45,7 +45,7 @@ class _System:
 
 
 class FakeEngine:
-    """Records what the driver asks for, with the step it was at.  The
+    """Records what the job asks for, with the step it was at.  The
     coordinates of bead i at step s are (s, i, 0), so a record of positions
     names the step it was taken at."""
 
