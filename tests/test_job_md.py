@@ -1,4 +1,4 @@
-"""The MD job driver (sis_gb300.job_md) and the files around it.
+"""The MD job (sis_gb300.job_md) and the files around it.
 
 CPU, against a stand-in engine that records every call:
 * the job runs the steps between two events as one Engine.step call and
