@@ -7,7 +7,9 @@ Objects go to ``_build/``, the library to ``sis_gb300/_lib/``.
 """
 from __future__ import annotations
 
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -31,14 +33,28 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+STAMP = LIB.with_suffix(".so.sha256")
+
+
+def source_key(cc: str) -> str:
+    """Hash of every source, the flags, the compiler path and the machine:
+    the library is rebuilt whenever any of them differs from the build that
+    made it (file times are not trusted: copies between machines keep them)."""
+    h = hashlib.sha256()
+    for p in sorted(CSRC.glob("*")) + [ROOT / "include" / "sis_gpu.h"]:
+        h.update(p.name.encode())
+        h.update(p.read_bytes())
+    h.update(" ".join([cc, *FLAGS, *ARCH, platform.machine()]).encode())
+    return h.hexdigest()
+
+
 def build_lib(verbose: bool = False, force: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
     LIB.parent.mkdir(exist_ok=True)
-    deps = list(CSRC.glob("*")) + [ROOT / "include" / "sis_gpu.h"]
-    newest = max(p.stat().st_mtime for p in deps)
-    if LIB.exists() and not force and LIB.stat().st_mtime > newest:
-        return LIB
     cc = nvcc()
+    key = source_key(cc)
+    if LIB.exists() and not force and STAMP.exists() and STAMP.read_text().strip() == key:
+        return LIB
 
     def compile_one(src: str):
         out = OBJ / (Path(src).stem + ".o")
@@ -58,6 +74,7 @@ def build_lib(verbose: bool = False, force: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    STAMP.write_text(key + "\n")
     return LIB
 
 

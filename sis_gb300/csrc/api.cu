@@ -56,6 +56,7 @@ int nnt_index(int i, int j, int k, int l) {
 } // namespace
 
 struct sis_ctx {
+    int dev = 0; // the CUDA device the context was created on; every entry point runs with it current
     Dev D{};
     GlobP g{};
     sis_params p{};
@@ -126,6 +127,23 @@ struct sis_ctx {
 };
 
 namespace {
+
+// Makes the context's device current for the duration of an entry point and
+// restores the caller's device afterwards, so that one host thread can drive
+// contexts on several GPUs.
+struct DevGuard {
+    int prev = -1;
+    explicit DevGuard(const sis_ctx *c) {
+        if (!c) return;
+        int d = -1;
+        if (cudaGetDevice(&d) == cudaSuccess && d != c->dev && cudaSetDevice(c->dev) == cudaSuccess) prev = d;
+    }
+    ~DevGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DevGuard(const DevGuard &) = delete;
+    DevGuard &operator=(const DevGuard &) = delete;
+};
 
 int fail(sis_ctx *c, int code, const std::string &msg) {
     if (c) c->err = msg;
@@ -623,6 +641,10 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     if (!inputs_valid(top, par)) return SIS_ERR_ARG;
     sis_ctx *ctx = new sis_ctx();
     *out = nullptr;
+    if (cudaGetDevice(&ctx->dev) != cudaSuccess) {
+        delete ctx;
+        return SIS_ERR_CUDA;
+    }
     ctx->p = *par;
     const sis_params &p = ctx->p;
     ctx->n_inst = top->n_inst;
@@ -969,6 +991,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
 }
 
 extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
+    DevGuard dg_(ctx);
     if (!ctx) return;
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
@@ -995,6 +1018,7 @@ extern "C" int sis_gpu_nmp(const sis_ctx *ctx, int32_t inst) {
 }
 
 extern "C" int sis_gpu_set_state(sis_ctx *ctx, int32_t inst, const double *xyz, const double *velos, const double *accels) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     int off, cnt;
     if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
@@ -1020,6 +1044,7 @@ extern "C" int sis_gpu_set_state(sis_ctx *ctx, int32_t inst, const double *xyz, 
 }
 
 extern "C" int sis_gpu_get_state(sis_ctx *ctx, int32_t inst, double *xyz, double *velos, double *accels) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     int off, cnt;
     if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
@@ -1041,6 +1066,7 @@ extern "C" int sis_gpu_get_state(sis_ctx *ctx, int32_t inst, double *xyz, double
 }
 
 extern "C" int sis_gpu_init_velocities(sis_ctx *ctx) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     const unsigned long long ctr = (1ull << 62) + 2ull * (unsigned long long)(ctx->n_vel_init++);
     CK(launch_init_velocities(ctx->D, ctx->g, ctr, ctx->st));
@@ -1050,6 +1076,7 @@ extern "C" int sis_gpu_init_velocities(sis_ctx *ctx) {
 }
 
 extern "C" int sis_gpu_neighbor_list(sis_ctx *ctx, int32_t inst) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < -1 || inst >= ctx->n_inst) return SIS_ERR_ARG;
     if (!ctx->state_set) return fail(ctx, SIS_ERR_STATE, "coordinates have not been set");
     if (!ctx->lists_valid) inst = -1;
@@ -1064,6 +1091,7 @@ extern "C" int sis_gpu_neighbor_list(sis_ctx *ctx, int32_t inst) {
 }
 
 extern "C" int sis_gpu_get_list(sis_ctx *ctx, int32_t inst, int32_t kind, int32_t *out, int32_t cap, int32_t *n_out) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || kind < 0 || kind > 2 || !n_out) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
@@ -1110,6 +1138,7 @@ extern "C" int sis_gpu_get_list(sis_ctx *ctx, int32_t inst, int32_t kind, int32_
 }
 
 extern "C" int sis_gpu_get_bp_coef(sis_ctx *ctx, int32_t inst, double *out, int32_t cap, int32_t *n_out) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || !n_out) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
@@ -1162,16 +1191,19 @@ static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
 }
 
 extern "C" int sis_gpu_force(sis_ctx *ctx, int32_t inst, double *forces) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     return force_common(ctx, inst, 63 | 128, forces);
 }
 
 extern "C" int sis_gpu_force_term(sis_ctx *ctx, int32_t inst, int32_t term, double *forces) {
+    DevGuard dg_(ctx);
     if (!ctx || term < 1 || term > 7) return SIS_ERR_ARG;
     return force_common(ctx, inst, term == 7 ? 128 : 1 << (term - 1), forces);
 }
 
 extern "C" int sis_gpu_rg(sis_ctx *ctx, int32_t inst, double *rg) {
+    DevGuard dg_(ctx);
     if (!ctx || !rg || inst < -1 || inst >= ctx->n_inst) return SIS_ERR_ARG;
     if (!ctx->state_set) return fail(ctx, SIS_ERR_STATE, "coordinates have not been set");
     CK(launch_rg(ctx->D, ctx->g, ctx->cur, ctx->fout_d, ctx->st));
@@ -1183,12 +1215,14 @@ extern "C" int sis_gpu_rg(sis_ctx *ctx, int32_t inst, double *rg) {
 }
 
 extern "C" int sis_gpu_invalidate_bp_cache(sis_ctx *ctx) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     ctx->bp_cache = false;
     return SIS_OK;
 }
 
 extern "C" int sis_gpu_energy_sumup(sis_ctx *ctx, int32_t inst, double tempK, double *E) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || !E) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
@@ -1211,6 +1245,7 @@ extern "C" int sis_gpu_energy_sumup(sis_ctx *ctx, int32_t inst, double tempK, do
 }
 
 extern "C" int sis_gpu_energy_kinetic(sis_ctx *ctx, int32_t inst, double *ekin) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || !ekin) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
@@ -1225,6 +1260,7 @@ extern "C" int sis_gpu_energy_kinetic(sis_ctx *ctx, int32_t inst, double *ekin) 
 }
 
 extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
+    DevGuard dg_(ctx);
     if (!ctx || nsteps < 0) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
@@ -1261,6 +1297,7 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
 }
 
 extern "C" int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, double ionic) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || tempK <= 0 || ionic <= 0) return SIS_ERR_ARG;
     ctx->ip[inst].tempK = tempK;
     ctx->ionic[inst] = ionic;
@@ -1277,6 +1314,7 @@ extern "C" int sis_gpu_set_condition(sis_ctx *ctx, int32_t inst, double tempK, d
 }
 
 extern "C" int sis_gpu_set_temperature(sis_ctx *ctx, int32_t inst, double tempK) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < -1 || inst >= ctx->n_inst || !(tempK > 0.0)) return SIS_ERR_ARG;
     // the temperature ladder of replica exchange owns the temperatures
     if (ctx->remd_on) return fail(ctx, SIS_ERR_ARG, "set_temperature: replica exchange is on");
@@ -1298,6 +1336,7 @@ extern "C" int sis_gpu_set_temperature(sis_ctx *ctx, int32_t inst, double tempK)
 }
 
 extern "C" int sis_gpu_set_frozen(sis_ctx *ctx, int32_t inst, const int32_t *beads, int32_t n) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || n < 0 || (n > 0 && !beads)) return SIS_ERR_ARG;
     const InstP &I = ctx->ip[inst];
     for (int q = 0; q < n; ++q)
@@ -1327,6 +1366,7 @@ void bias_flags(sis_ctx *ctx) {
 } // namespace
 
 extern "C" int sis_gpu_set_stage(sis_ctx *ctx, double sigma, double eps) {
+    DevGuard dg_(ctx);
     if (!ctx || !(sigma >= 0.0)) return SIS_ERR_ARG;
     ctx->g.flg_stage = sigma > 0.0;
     ctx->g.stage_sigma = sigma;
@@ -1336,6 +1376,7 @@ extern "C" int sis_gpu_set_stage(sis_ctx *ctx, double sigma, double eps) {
 }
 
 extern "C" int sis_gpu_set_rg_bias(sis_ctx *ctx, int32_t inst, int32_t pott, double k, double rg0) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < -1 || inst >= ctx->n_inst || pott < 0 || pott > 2) return SIS_ERR_ARG;
     for (int q = 0; q < ctx->n_inst; ++q) {
         if (inst >= 0 && q != inst) continue;
@@ -1350,6 +1391,7 @@ extern "C" int sis_gpu_set_rg_bias(sis_ctx *ctx, int32_t inst, int32_t pott, dou
 }
 
 extern "C" int sis_gpu_set_bias_items(sis_ctx *ctx, int32_t inst, int32_t n, const int32_t *kind_ij, const double *par) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || n < 0 || (n > 0 && (!kind_ij || !par))) return SIS_ERR_ARG;
     if (ctx->bias_items.empty()) ctx->bias_items.resize(ctx->n_inst);
     const InstP &I = ctx->ip[inst];
@@ -1385,12 +1427,14 @@ extern "C" int sis_gpu_set_bias_items(sis_ctx *ctx, int32_t inst, int32_t n, con
 }
 
 extern "C" int sis_gpu_set_force_cap(sis_ctx *ctx, double fmax) {
+    DevGuard dg_(ctx);
     if (!ctx || fmax < 0.0) return SIS_ERR_ARG;
     ctx->g.fcap = fmax;
     return SIS_OK;
 }
 
 extern "C" int sis_gpu_get_md_coef(sis_ctx *ctx, int32_t inst, double *o) {
+    DevGuard dg_(ctx);
     if (!ctx || !o) return SIS_ERR_ARG;
     int off, cnt;
     if (inst_range(ctx, inst, off, cnt)) return fail(ctx, SIS_ERR_ARG, "bad instance");
@@ -1400,6 +1444,7 @@ extern "C" int sis_gpu_get_md_coef(sis_ctx *ctx, int32_t inst, double *o) {
 }
 
 extern "C" int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *o) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || !o) return SIS_ERR_ARG;
     const InstP &I = ctx->ip[inst];
     o[0] = I.ele_coef;
@@ -1410,6 +1455,7 @@ extern "C" int sis_gpu_get_ele(sis_ctx *ctx, int32_t inst, double *o) {
 }
 
 extern "C" int sis_gpu_get_step(sis_ctx *ctx, uint64_t *step) {
+    DevGuard dg_(ctx);
     if (!ctx || !step) return SIS_ERR_ARG;
     unsigned long long v = 0;
     CK(cudaMemcpyAsync(&v, ctx->D.step_ctr, sizeof(v), cudaMemcpyDeviceToHost, ctx->st));
@@ -1419,6 +1465,7 @@ extern "C" int sis_gpu_get_step(sis_ctx *ctx, uint64_t *step) {
 }
 
 extern "C" int sis_gpu_set_step(sis_ctx *ctx, uint64_t step) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     unsigned long long v = step;
     CK(cudaMemcpyAsync(ctx->D.step_ctr, &v, sizeof(v), cudaMemcpyHostToDevice, ctx->st));
@@ -1430,6 +1477,7 @@ extern "C" int sis_gpu_set_step(sis_ctx *ctx, uint64_t step) {
 }
 
 extern "C" int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes) {
+    DevGuard dg_(ctx);
     if (!ctx || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32))
         return SIS_ERR_ARG;
     ctx->lanes_fixed = lanes != 0;
@@ -1440,12 +1488,14 @@ extern "C" int sis_gpu_set_lanes(sis_ctx *ctx, int32_t lanes) {
 }
 
 extern "C" int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable) {
+    DevGuard dg_(ctx);
     if (!ctx || (enable != 0 && enable != 1)) return SIS_ERR_ARG;
     ctx->use_graphs = enable != 0;
     return SIS_OK;
 }
 
 extern "C" int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable) {
+    DevGuard dg_(ctx);
     if (!ctx || (enable != 0 && enable != 1 && enable != -1)) return SIS_ERR_ARG;
     ctx->overlap_mode = enable;
     if (enable >= 0) ctx->overlap = enable != 0;
@@ -1454,6 +1504,7 @@ extern "C" int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable) {
 }
 
 extern "C" int sis_gpu_probe_barrier_timeout(sis_ctx *ctx) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     CK(launch_barrier_probe(ctx->D, ctx->coop_grid, ctx->coop_grid - 1, ctx->st));
     ctx->launches++;
@@ -1461,6 +1512,7 @@ extern "C" int sis_gpu_probe_barrier_timeout(sis_ctx *ctx) {
 }
 
 extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
+    DevGuard dg_(ctx);
     if (!ctx || !s) return SIS_ERR_ARG;
     memset(s, 0, sizeof(*s));
     s->steps = ctx->steps;
@@ -1490,22 +1542,26 @@ extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
 extern "C" const char *sis_gpu_last_error(const sis_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
 extern "C" int sis_gpu_event_record(sis_ctx *ctx, int32_t slot) {
+    DevGuard dg_(ctx);
     if (!ctx || slot < 0 || slot >= kEvents) return SIS_ERR_ARG;
     CK(cudaEventRecord(ctx->ev[slot], ctx->st));
     return SIS_OK;
 }
 extern "C" int sis_gpu_event_elapsed(sis_ctx *ctx, int32_t a, int32_t b, float *ms) {
+    DevGuard dg_(ctx);
     if (!ctx || a < 0 || b < 0 || a >= kEvents || b >= kEvents || !ms) return SIS_ERR_ARG;
     CK(cudaEventSynchronize(ctx->ev[b]));
     CK(cudaEventElapsedTime(ms, ctx->ev[a], ctx->ev[b]));
     return SIS_OK;
 }
 extern "C" int sis_gpu_synchronize(sis_ctx *ctx) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     CK(cudaStreamSynchronize(ctx->st));
     return SIS_OK;
 }
 extern "C" int sis_gpu_flush_l2(sis_ctx *ctx) {
+    DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
     if (!ctx->flush_d) {
         ctx->flush_bytes = (size_t)512 << 20;
@@ -1517,6 +1573,7 @@ extern "C" int sis_gpu_flush_l2(sis_ctx *ctx) {
 extern "C" int64_t sis_gpu_kernel_launches(const sis_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
 extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
+    DevGuard dg_(ctx);
     if (!ctx || nsteps < 0 || !ms3) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
@@ -1574,13 +1631,12 @@ constexpr int kMaxDevices = 64;
 std::mutex g_noise_mu;
 double *g_noise_addr[kMaxDevices] = {};
 
-// Address of g_noise_scratch on the current device, looked up once per
+// Address of g_noise_scratch on the context's device, looked up once per
 // device with that device current (the first call on a device does this
 // set-up; a caller that captures its stream should make that first call
 // before it starts capturing).
 int noise_scratch(sis_ctx *ctx, double **out) {
-    int dev = -1;
-    CK(cudaGetDevice(&dev));
+    const int dev = ctx->dev; // current: the entry point's DevGuard made it so
     if (dev < 0 || dev >= kMaxDevices) return fail(ctx, SIS_ERR_ARG, "sis_gpu_step_noise_static: device index out of range");
     std::lock_guard<std::mutex> lock(g_noise_mu);
     if (!g_noise_addr[dev]) {
@@ -1595,6 +1651,7 @@ int noise_scratch(sis_ctx *ctx, double **out) {
 } // namespace
 
 extern "C" int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const double *noise) {
+    DevGuard dg_(ctx);
     if (!ctx || nsteps < 0 || (nsteps > 0 && !noise)) return SIS_ERR_ARG;
     if (ctx->n > kStaticNoiseBeads)
         return fail(ctx, SIS_ERR_ARG,
@@ -1615,11 +1672,15 @@ extern "C" int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const dou
     ctx->steps += nsteps;
     ctx->bp_cache = true;
     CK(cudaStreamSynchronize(ctx->st));
+    // caller-supplied Monte Carlo uniforms apply to one call only, as in sis_gpu_step
+    ctx->D.mc_draws = nullptr;
+    ctx->mc_pending = false;
     return check_err(ctx);
 }
 
 // ========================================================= replica exchange
 extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
+    DevGuard dg_(ctx);
     if (!ctx || !temps || ctx->n_inst < 2) return SIS_ERR_ARG;
     const int ni = ctx->n_inst;
     for (int l = 1; l < ni; ++l)
@@ -1706,6 +1767,7 @@ extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
 }
 
 extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, int32_t *rep2lab, int32_t *n_accepted) {
+    DevGuard dg_(ctx);
     if (!ctx || (parity != 0 && parity != 1)) return SIS_ERR_ARG;
     if (!ctx->remd_on) return fail(ctx, SIS_ERR_STATE, "remd: sis_gpu_remd_init has not been called");
     int rc = ensure_lists(ctx);
@@ -1754,6 +1816,7 @@ extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double 
 extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, const int32_t *chain_len,
                                  const int32_t *chain_moltype, const int32_t *seq, const uint8_t *has_charge, double tempK,
                                  double ionic, uint32_t stream, const double *xyz, int32_t init_velocities) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || n_chains < 0 || !(tempK > 0.0) || !(ionic > 0.0)) return SIS_ERR_ARG;
     InstP &I = ctx->ip[inst];
     const int off = I.bead_off, n = I.n;
@@ -1838,6 +1901,7 @@ extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, c
 
 // ============================================== base-pair Monte Carlo pass
 extern "C" int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, int32_t n_draws) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < -1 || inst >= ctx->n_inst || n_draws < 0 || (n_draws > 0 && !draws)) return SIS_ERR_ARG;
     if (ctx->g.nstep_mc <= 0) return fail(ctx, SIS_ERR_STATE, "bp_mc: the context has no base-pair Monte Carlo (nstep_bp_mc = 0)");
     const int one = 1;
@@ -1860,6 +1924,7 @@ extern "C" int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, in
 }
 
 extern "C" int sis_gpu_get_bp_energies(sis_ctx *ctx, int32_t inst, double *out, int32_t cap, int32_t *n_out) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || !n_out) return SIS_ERR_ARG;
     const InstP &I = ctx->ip[inst];
     int c = 0;
@@ -1875,6 +1940,7 @@ extern "C" int sis_gpu_get_bp_energies(sis_ctx *ctx, int32_t inst, double *out, 
 }
 
 extern "C" int sis_gpu_get_bp_status(sis_ctx *ctx, int32_t inst, uint8_t *out, int32_t cap, int32_t *n_out) {
+    DevGuard dg_(ctx);
     if (!ctx || inst < 0 || inst >= ctx->n_inst || !n_out) return SIS_ERR_ARG;
     const InstP &I = ctx->ip[inst];
     int c = 0;

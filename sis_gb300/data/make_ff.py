@@ -4,7 +4,7 @@ reference's own .ff files (Hori-Lab/SIS ``sis.ff`` and
 so that the engine's .ff reader (sis_gb300/inputs.py) reads them as it reads
 the originals.  Run only where the reference tree is present:
 
-    python sis_gb300/data/make_ff.py /root/reference
+    python sis_gb300/data/make_ff.py <path of the SIS source tree>
 """
 import sys
 import tomllib
@@ -44,4 +44,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python sis_gb300/data/make_ff.py <path of the SIS source tree>")
+    main(sys.argv[1])

@@ -3,7 +3,7 @@
 Run where the reference is present (it is read-only and absent on GPU hosts;
 the fixtures are committed):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the SIS source tree>
 
 Fixtures written:
 
@@ -49,4 +49,6 @@ def main(ref: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the SIS source tree>")
+    main(Path(sys.argv[1]))

@@ -11,6 +11,7 @@ import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 HEADER = ROOT / "include" / "sis_gpu.h"
+FMODULE = ROOT / "include" / "sis_gpu.f90"
 
 
 @pytest.fixture(scope="module")
@@ -90,17 +91,18 @@ def _c_params(text):
 
 
 def test_fortran_bindings_match_the_header():
-    """The ISO_C_BINDING interfaces of INTEGRATION.md bind names the header
-    declares, with as many arguments; every entry point its text names
-    exists."""
+    """The ISO_C_BINDING interfaces of include/sis_gpu.f90 bind names the
+    header declares, with as many arguments; every entry point the module and
+    INTEGRATION.md name exists."""
     c = _c_params(HEADER.read_text())
-    doc = (ROOT / "INTEGRATION.md").read_text()
-    binds = re.findall(r"function\s+(\w+)\s*\(([^)]*)\)\s*&?\s*bind\(C,\s*name=\"(\w+)\"\)", doc)
+    mod = FMODULE.read_text()
+    binds = re.findall(r"function\s+(\w+)\s*\(([^)]*)\)\s*&?\s*bind\(C,\s*name=\"(\w+)\"\)", mod)
     assert len(binds) >= 20
     for fname, args, cname in binds:
         assert fname == cname and cname in c, cname
         nargs = len([a for a in args.split(",") if a.strip()])
         assert nargs == c[cname], (cname, nargs, c[cname])
+    doc = mod + (ROOT / "INTEGRATION.md").read_text()
     named = set(re.findall(r"\bsis_gpu_\w+", doc)) - {"sis_gpu_mod"}
     assert named <= set(c), named - set(c)
 
@@ -169,10 +171,10 @@ def _fortran_type_fields(doc, name):
 
 @pytest.mark.parametrize("name", ["sis_params", "sis_topology"])
 def test_fortran_struct_types_match_the_header(name):
-    """The bind(C) derived types of INTEGRATION.md list the C structs'
+    """The bind(C) derived types of include/sis_gpu.f90 list the C structs'
     fields in order, with matching kinds and array sizes."""
     c = _c_struct_fields(HEADER.read_text(), name)
-    f = _fortran_type_fields((ROOT / "INTEGRATION.md").read_text(), name)
+    f = _fortran_type_fields(FMODULE.read_text(), name)
     assert f == c
 
 
@@ -202,7 +204,7 @@ def test_fortran_argument_kinds_match_the_header():
             "sis_ctx": "type(c_ptr)", "sis_topology": "type(sis_topology)", "sis_params": "type(sis_params)",
             "sis_stats": "type(sis_stats)"}
     c = _c_param_lists(HEADER.read_text())
-    doc = (ROOT / "INTEGRATION.md").read_text()
+    doc = FMODULE.read_text()
     blocks = re.findall(r"(?:function|subroutine)\s+\w+\s*\(([^)]*)\)\s*&?\s*bind\(C,\s*name=\"(\w+)\"\)(.*?)end (?:function|subroutine)",
                         doc, flags=re.S)
     checked = 0

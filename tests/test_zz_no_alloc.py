@@ -16,7 +16,7 @@ import pytest
 from sis_gb300 import FP64, MIXED, _abi
 from sis_gb300.coil import sis_options, uneven_batch
 from sis_gb300.engine import Engine
-from sis_gb300.model import Chain, Instance, System
+from sis_gb300.model import Chain, Instance, Options, System
 
 pytestmark = pytest.mark.gpu
 
@@ -47,6 +47,43 @@ def test_static_noise_step_matches_step(prec, sis_ff):
             else:
                 assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max(), call
     assert ref.stats()["steps"] == got.stats()["steps"] == 50
+
+
+@pytest.mark.parametrize("prec", [MIXED, FP64])
+def test_static_noise_step_releases_monte_carlo_draws(prec, nn_ff):
+    """Uniforms given to sis_gpu_bp_mc serve the next call only: a second
+    call whose Monte Carlo passes (every 5 steps) find no caller uniforms
+    draws from Philox, in both entry points alike."""
+    from sis_gb300.coil import random_coil
+
+    rng = np.random.default_rng(5)
+    x = random_coil(rng, 30, amin_deg=60.0, amax_deg=100.0, rmin=3.0)
+    inst = Instance([Chain.from_string("GGGGCAAAAGCCCCAAAAGGGGAAAACCCC")], tempK=300.0, ionic_strength=0.15, xyz=x)
+    opts = Options(bp_model=5, nstep_bp_mc=5, max_bp_per_nt=1, ele_cutoff_type=2, ele_cutoff=20.0)
+    sysm = System(nn_ff, opts, [inst])
+    ref = Engine(sysm, precision=prec, seed=3)
+    got = Engine(sysm, precision=prec, seed=3)
+    draws = np.random.default_rng(11).uniform(size=100000)
+    ref.bp_mc(0, draws)
+    got.bp_mc(0, draws)
+    for call in range(2):
+        noise = np.ascontiguousarray(rng.normal(size=(12, sysm.nmp, 3)))
+        ref.step(12, noise)
+        rc, msg = _static_step(got, noise)
+        assert rc == 0, msg
+        for a, b in zip(ref.get_state(-1), got.get_state(-1)):
+            if prec == MIXED:
+                assert np.array_equal(a, b), call
+            else:
+                assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max(), call
+    # and a plain call afterwards runs as it does after sis_gpu_step
+    ref.step(20)
+    got.step(20)
+    for a, b in zip(ref.get_state(-1), got.get_state(-1)):
+        if prec == MIXED:
+            assert np.array_equal(a, b)
+        else:
+            assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
 
 
 def test_static_noise_step_rejects_too_many_beads(sis_ff):
