@@ -236,6 +236,14 @@ class Oracle:
         self.L.or_get_mc_draws(self.h, _p(out), n)
         return out
 
+    def bp_state(self, r=0):
+        """(energy, status) of every base-pair record of the last force evaluation."""
+        n = self.L.or_get_bp_state(self.h, r, None, None, 0)
+        e = np.zeros(n)
+        st = np.zeros(n, dtype=np.uint8)
+        self.L.or_get_bp_state(self.h, r, _p(e), st.ctypes.data_as(C.c_void_p), n)
+        return e, st
+
     def bp_status(self, r=0):
         n = self.L.or_get_bp_status(self.h, r, None, 0)
         out = np.zeros(n, dtype=np.uint8)
