@@ -53,13 +53,28 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+RELAXED = ROOT / "sis_gb300" / "data" / "crowded_relaxed.npz"
+
+
 def make_system(name, seed_offset=0):
+    """The workload's system.  The crowded box starts from its relaxed
+    positions (sis_gb300/data/crowded_relaxed.npz, written by make_relaxed.py)
+    when they are present, so that every arm starts from the same state."""
     from sis_gb300.coil import crowded_box, remd_batch, single_chain, uneven_batch
     from sis_gb300.inputs import read_ff
 
     ff = read_ff(ROOT / "sis_gb300" / "data" / "sis.ff")
     if name == "crowded":
-        return crowded_box(ff, 200, 500, 0.01, seed=1002 + seed_offset)
+        if RELAXED.exists():
+            # every rank: the same relaxed box (its ranks differ in their noise)
+            seed_offset = 0
+        sysm = crowded_box(ff, 200, 500, 0.01, seed=1002 + seed_offset)
+        if RELAXED.exists():
+            x = np.load(RELAXED)["xyz"].astype(np.float64)
+            if x.shape == (sysm.nmp, 3):
+                sysm.instances[0].xyz = x
+                sysm.relaxed_start = True
+        return sysm
     if name == "uneven":
         return uneven_batch(ff, 256, seed=1004 + seed_offset)
     if name == "remd":
@@ -176,9 +191,16 @@ def run_gpu(args):
     if args.overlap >= 0:
         eng.set_overlap(bool(args.overlap))
     eng.init_velocities()
-    # equilibrate before timing (force-capped, then free dynamics; neither is
-    # timed): the coil start has no WCA overlap but is far from equilibrium
-    eng.relax(capped_steps=args.relax, fmax=1000.0, free_steps=args.relax)
+    relaxed = getattr(sysm, "relaxed_start", False)
+    relax = args.relax if args.relax >= 0 else (500 if relaxed else 3000)
+    if relaxed:
+        # the relaxed start: velocities from the noise, then free dynamics
+        eng.set_force_cap(args.force_cap)
+        eng.step(relax)
+    else:
+        # equilibrate before timing (force-capped, then free dynamics; neither
+        # is timed): a coil start is far from equilibrium
+        eng.relax(capped_steps=relax, fmax=1000.0, free_steps=relax)
     # singularity guard for the production steps: the cosine dihedral force of
     # the model (force_dih_cos.F90) diverges as a bond angle reaches 180 degrees;
     # a per-bead cap far above thermal forces keeps such events finite
@@ -276,7 +298,8 @@ def run_gpu(args):
            "list_entries_per_bead": round(L, 3), "steps_per_rebuild": k_rebuild, "lanes_per_bead": st1["lanes_per_bead"], "pair_kernel_beside_bonded": bool(st1["overlap"]), "bp_blocks": st1["bp_blocks"],
            "l2": "flushed between timed steps (512 MiB write)", "fp64_value": fp64_value,
            "speedup_vs_fp64": value / fp64_value, "force_rms_rel_err_vs_fp64": err,
-           "relax_steps": {"force_capped": args.relax, "free": args.relax},
+           "start": "relaxed positions of sis_gb300/data/crowded_relaxed.npz" if relaxed else "random coil",
+           "relax_steps": {"force_capped": 0 if relaxed else relax, "free": relax},
            "force_cap": args.force_cap, "capped_bead_steps": st1["capped"] - cap0,
            "launches_before_timed": int(launches0), "step_graphs": not args.no_graphs,
            **({"exchange_interval": args.exchange_interval, "exchange_attempts_timed": rx_timed["attempts"],
@@ -293,40 +316,107 @@ def run_gpu(args):
                         "bonded_bp_ms": ms3[0] / prof_steps, "trigger_rebuild_ms": ms3[2] / prof_steps,
                         "bytes_per_bead_step": bytes_per_bead},
            "clocks": clk.summary()}
-    if rank == 0:
-        out["cpu_baseline"] = cpu_baseline(args, sysm, eng)
     eng.close()
+    if not args.no_sub and args.workload == "crowded":
+        # the batched-chain workload the >= 20x target is stated on, and the serving stream
+        cfg["uneven"] = uneven_record(args, rank, world)
+        cfg["serve"] = serve_record(args, rank, world)
+    if rank == 0:
+        out["cpu_baseline"] = cpu_baseline(args, sysm)
     return out, rank
+
+
+def uneven_record(args, rank, world):
+    """The uneven batch (256 chains of U[20,500] nt, each with its own salt and
+    temperature, no PBC), the workload the >= 20x target is stated on: mixed
+    path against the plain FP64 path from the same state, L2 flushed between
+    timed blocks, max over ranks."""
+    from sis_gb300 import FP64, MIXED
+    from sis_gb300.engine import Engine
+
+    sysm = make_system("uneven", seed_offset=rank)
+    N, S = sysm.nmp, args.md_steps
+    eng = Engine(sysm, precision=MIXED, seed=2024 + rank)
+    eng.init_velocities()
+    eng.relax(capped_steps=2000, fmax=1000.0, free_steps=2000)
+    eng.set_force_cap(args.force_cap)
+    for _ in range(3):
+        eng.flush_l2()
+        eng.step(S)
+    st0 = eng.stats()
+    t = []
+    for _ in range(5):
+        eng.flush_l2()
+        eng.event(0)
+        eng.step(S)
+        eng.event(1)
+        t.append(eng.elapsed_ms(0, 1))
+    st1 = eng.stats()
+    ms = max_over_ranks(sum(t), world)
+    value = world * N * S * len(t) / (ms * 1e-3)
+    x, v, a = eng.get_state(-1)
+    e64 = Engine(sysm, precision=FP64, seed=2024 + rank)
+    e64.set_state(-1, x, v, a)
+    e64.set_force_cap(args.force_cap)
+    f64 = np.concatenate([e64.force(k) for k in range(e64.n_inst)])
+    f32 = np.concatenate([eng.force(k) for k in range(eng.n_inst)])
+    err = float(np.sqrt(np.mean(np.sum((f32 - f64) ** 2, axis=1)) / np.mean(np.sum(f64 ** 2, axis=1))))
+    e64.step(S)
+    t64 = []
+    for _ in range(3):
+        e64.flush_l2()
+        e64.event(0)
+        e64.step(S)
+        e64.event(1)
+        t64.append(e64.elapsed_ms(0, 1))
+    v64 = world * N * S * len(t64) / (max_over_ranks(sum(t64), world) * 1e-3)
+    e64.close()
+    eng.close()
+    reb = st1["rebuilds"] - st0["rebuilds"]
+    return {"description": WORKLOADS["uneven"], "n_beads": N, "n_instances": len(sysm.instances), "value": value,
+            "unit": UNIT, "ms_per_md_step": ms / (len(t) * S), "fp64_value": v64, "speedup_vs_fp64": value / v64,
+            "target_speedup_vs_fp64": 20.0, "force_rms_rel_err_vs_fp64": err,
+            "steps_per_rebuild": S * len(t) * len(sysm.instances) / reb if reb else None,
+            "lanes_per_bead": st1["lanes_per_bead"], "timed_blocks": len(t), "md_steps_per_block": S,
+            "relax_steps": {"force_capped": 2000, "free": 2000}, "l2": "flushed between timed blocks (512 MiB write)"}
+
+
+def serve_record(args, rank, world, seconds=4.0, scale=0.01):
+    """The serving stream at a stated scale: Poisson arrivals at --serve-rate
+    jobs/s for `seconds`, every job's step count times `scale`; latency is
+    arrival to completion."""
+    summ, cfg, value, _ = serve_run(args, rank, world, seconds, scale)
+    return {"description": WORKLOADS["serve"], "arrival_rate_per_s": args.serve_rate, "arrival_window_s": seconds,
+            "steps_scale": scale, "jobs": cfg["jobs"], "jobs_completed": summ["jobs"], "jobs_failed": summ["failed"],
+            "p50_latency_ms": summ["p50_ms"], "p99_latency_ms": summ["p99_ms"],
+            "offered_bead_steps_per_s": cfg["offered_bead_steps_per_s"], "achieved_bead_steps_per_s": value, "unit": UNIT}
 
 
 class CpuSampler:
     """The FP64 oracle (C++ restatement of the reference, OpenMP over all host
-    threads) on up to 8 instances of the workload.  Its lists are built once
-    (untimed); each sample then runs MD until the displacement trigger has
-    rebuilt the lists once, so the reference's O(N^2) rebuild enters at its
-    natural rate: one rebuild per rebuild interval."""
+    threads) on up to 8 instances of the workload, from the workload's start
+    (for the crowded box its relaxed positions, the GPU arm's start too) with
+    velocities from the oracle's own MT19937 + polar Box-Muller noise.  Its
+    lists are built once (untimed); each sample then runs MD until the
+    displacement trigger has rebuilt the lists once, so the reference's O(N^2)
+    rebuild enters at its natural rate: one rebuild per rebuild interval."""
 
-    def __init__(self, sysm, eng=None, seed=1234):
+    def __init__(self, sysm, seed=1234):
         from oracle.oracle import Oracle
 
         self.cores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(self.cores))
         n_inst = len(sysm.instances)
         insts = range(0, n_inst, max(1, n_inst // 8)) if n_inst > 8 else range(n_inst)
-        off = sysm.offsets()
-        state = eng.get_state(-1) if eng is not None else None
         self.oracles = []
         for k in insts:
             o = Oracle.from_instance(sysm, k)
-            if state is not None:
-                x, v, a = state
-                o.set_xyz(0, x[off[k]:off[k + 1]])
-                o.set_velos(0, v[off[k]:off[k + 1]])
-                o.set_accels(0, a[off[k]:off[k + 1]])
             o.seed(seed + k)
             o.md_init()
+            o.init_velocities()
             self.oracles.append(o)
-        self.start = "relaxed GPU state" if state is not None else "the workload's start"
+        self.start = ("relaxed positions (sis_gb300/data/crowded_relaxed.npz)" if getattr(sysm, "relaxed_start", False)
+                      else "the workload's start")
 
     def sample(self, max_seconds=30.0, max_steps=4000, chunk=10):
         """Per instance: steps in chunks until a rebuild happened (or the caps)."""
@@ -345,15 +435,28 @@ class CpuSampler:
 
     def describe(self, steps, rebuilds):
         n = sum(o.nmp for o in self.oracles)
-        return (f"{steps} MD steps over {len(self.oracles)} instance(s) ({n} beads) from {self.start}, each run until the "
-                f"displacement trigger rebuilt its lists ({rebuilds} O(N^2) rebuilds timed); FP64 C++ restatement of the "
-                f"reference with OpenMP")
+        return (f"{steps} MD steps over {len(self.oracles)} instance(s) ({n} beads) from {self.start}, velocities from the "
+                f"oracle's MT19937 noise, after one untimed rebuild interval; each sample ran until the displacement trigger "
+                f"rebuilt its lists ({rebuilds} O(N^2) rebuilds timed); FP64 C++ restatement of the reference with OpenMP")
 
 
-def cpu_baseline(args, sysm, eng=None):
-    smp = CpuSampler(sysm, eng)
-    bs, secs, steps, reb = smp.sample()
-    return {"value": bs / secs, "unit": UNIT, "cores": smp.cores, "kind": "port", "sample": smp.describe(steps, reb)}
+def cpu_samples(sysm, n_samples, warmup=1):
+    """Timed samples of the CPU sampler after `warmup` untimed ones (the first
+    leaves the start's transient and ends right after a rebuild)."""
+    smp = CpuSampler(sysm)
+    for w in range(warmup):
+        smp.sample() if w == 0 else smp.sample(max_steps=2)
+    tot_bs, tot_s, tot_steps, tot_reb = 0, 0.0, 0, 0
+    for _ in range(n_samples):
+        bs, secs, steps, reb = smp.sample()
+        tot_bs, tot_s, tot_steps, tot_reb = tot_bs + bs, tot_s + secs, tot_steps + steps, tot_reb + reb
+    return smp, tot_bs, tot_s, tot_steps, tot_reb
+
+
+def cpu_baseline(args, sysm):
+    smp, bs, secs, steps, reb = cpu_samples(sysm, 1)
+    return {"value": bs / secs, "unit": UNIT, "cores": smp.cores, "kind": "port", "sample": smp.describe(steps, reb),
+            "steps_per_rebuild": steps / reb if reb else None}
 
 
 def run_reference(args):
@@ -361,59 +464,60 @@ def run_reference(args):
     if rank != 0:
         return None, rank
     sysm = make_system(args.workload)
-    smp = CpuSampler(sysm)
     # warm-up: the first sample leaves the start's transient and ends right
     # after a rebuild, so every timed sample spans one rebuild interval
-    for w in range(args.warmup):
-        smp.sample() if w == 0 else smp.sample(max_steps=2)
-    tot_bs, tot_s, tot_steps, tot_reb = 0, 0.0, 0, 0
-    for _ in range(args.steps):
-        bs, secs, steps, reb = smp.sample()
-        tot_bs, tot_s, tot_steps, tot_reb = tot_bs + bs, tot_s + secs, tot_steps + steps, tot_reb + reb
+    smp, tot_bs, tot_s, tot_steps, tot_reb = cpu_samples(sysm, args.steps, args.warmup)
     value = tot_bs / tot_s
-    cb = {"value": value, "unit": UNIT, "cores": smp.cores, "kind": "port", "sample": smp.describe(tot_steps, tot_reb)}
+    cb = {"value": value, "unit": UNIT, "cores": smp.cores, "kind": "port", "sample": smp.describe(tot_steps, tot_reb),
+          "steps_per_rebuild": tot_steps / tot_reb if tot_reb else None}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "fp64", "data": "synthetic (seeded sequences and random-coil starts)", "impl": "reference",
            "config": {"workload": args.workload, "description": WORKLOADS[args.workload], "n_beads": sysm.nmp,
+                      "start": smp.start, "steps_per_rebuild": cb["steps_per_rebuild"],
                       "note": "Fortran reference unavailable on this box (no Fortran compiler, toml-f not vendored); "
                               "timed arm is the FP64 C++ restatement of its algorithms"},
            "cpu_baseline": cb, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return out, rank
 
 
-def run_serve(args):
-    """The serving workload, scaled: Poisson arrivals at --serve-rate jobs/s for
-    --serve-seconds, each job's step count times --serve-steps-scale; pools of
-    slots in three length classes; latency = arrival to completion."""
+def serve_run(args, rank, world, seconds, scale):
     from sis_gb300.coil import sis_options
     from sis_gb300.inputs import read_ff
     from sis_gb300.serve import Server, job_stream
 
-    rank, world, local = dist_env()
     ff = read_ff(ROOT / "sis_gb300" / "data" / "sis.ff")
-    jobs = job_stream(1005 + rank, args.serve_rate, args.serve_seconds, steps_scale=args.serve_steps_scale)
+    jobs = job_stream(1005 + rank, args.serve_rate, seconds, steps_scale=scale)
     classes = [(128, 16), (512, 16), (2048, 8)]
     # warm-up session (graph capture, first-touch of every pool), not timed
     warm = Server(ff, sis_options(), classes=classes, seed=2024 + rank, force_cap=args.force_cap)
-    warm.run(job_stream(7, 20.0, 0.5, steps_scale=args.serve_steps_scale))
+    warm.run(job_stream(7, 20.0, 0.5, steps_scale=scale))
     warm.close()
     srv = Server(ff, sis_options(), classes=classes, seed=2024 + rank, force_cap=args.force_cap)
     barrier(world)
-    with Clocks(local) as clk:
+    with Clocks(dist_env()[2]) as clk:
         srv.run(jobs)
     summ = srv.summary()
     done_bead_steps = sum(r.job.nmp * r.job.nsteps for r in srv.results)
     srv.close()
-    offered = sum(j.nmp * j.nsteps for j in jobs) / args.serve_seconds
+    offered = sum(j.nmp * j.nsteps for j in jobs) / seconds
     # every rank serves its own stream; the slowest rank's wall time bounds the job
     value = world * done_bead_steps / max_over_ranks(summ["wall_s"], world)
     cfg = {"workload": "serve", "description": WORKLOADS["serve"], "jobs": len(jobs), "arrival_rate_per_s": args.serve_rate,
-           "arrival_window_s": args.serve_seconds, "steps_scale": args.serve_steps_scale,
+           "arrival_window_s": seconds, "steps_scale": scale,
            "offered_bead_steps_per_s": offered, "p50_latency_ms": summ["p50_ms"], "p99_latency_ms": summ["p99_ms"],
            "jobs_completed": summ["jobs"], "jobs_failed": summ["failed"], "force_cap": args.force_cap,
            "pool_classes": [{"capacity": c, "slots": n} for c, n in classes], "precision": "FP32 terms / FP64 accumulate+integrate",
            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+    return summ, cfg, value, (clk, jobs)
+
+
+def run_serve(args):
+    """The serving workload, scaled: Poisson arrivals at --serve-rate jobs/s for
+    --serve-seconds, each job's step count times --serve-steps-scale; pools of
+    slots in three length classes; latency = arrival to completion."""
+    rank, world, local = dist_env()
+    summ, cfg, value, (clk, jobs) = serve_run(args, rank, world, args.serve_seconds, args.serve_steps_scale)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 1,
            "ms_per_step": summ["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "fp32+fp64", "data": "synthetic (seeded sequences and random-coil starts, Poisson arrivals)", "config": cfg,
@@ -431,7 +535,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="crowded", choices=list(WORKLOADS))
     ap.add_argument("--md-steps", type=int, default=100)
-    ap.add_argument("--relax", type=int, default=3000)
+    ap.add_argument("--relax", type=int, default=-1,
+                    help="relaxation steps before timing (-1: 500 free steps from a relaxed start, else 3000 capped + 3000 free)")
+    ap.add_argument("--no-sub", action="store_true", help="leave out the uneven-batch and serving records of the default line")
     ap.add_argument("--force-cap", type=float, default=1000.0)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per bead of the step kernel (0: autotune)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel from the host instead of step graphs")

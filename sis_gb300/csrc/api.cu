@@ -409,21 +409,28 @@ int pre_step_kernels(const sis_ctx *ctx) { return 1 + bp_kernels(ctx->g) + (ctx-
 // The forces and update of one step at buffer parity `cur` on ctx->st:
 // the bonded and base-pair pass, then k_step; with overlap, k_pairs runs on
 // st3 beside that pass and k_step takes its pair forces from fpair.
+// The mixed path always takes its pair forces from the cluster-pair kernel:
+// beside the pass with overlap, before it on ctx->st without.
 cudaError_t enqueue_forces_update(sis_ctx *ctx, int cur, const double *noise, long long ns) {
     cudaError_t e;
+    const bool split = ctx->overlap || ctx->g.prec != 0;
     if ((e = cudaEventRecord(ctx->ev_fork, ctx->st)) != cudaSuccess) return e;
     if (ctx->overlap) {
         if ((e = cudaStreamWaitEvent(ctx->st3, ctx->ev_fork, 0)) != cudaSuccess) return e;
         if ((e = launch_pairs(ctx->G, ctx->D, ctx->g, cur, ctx->st3)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(ctx->ev_join, ctx->st3)) != cudaSuccess) return e;
+    } else if (split && (e = launch_pairs(ctx->G, ctx->D, ctx->g, cur, ctx->st)) != cudaSuccess) {
+        return e;
     }
     if ((e = enqueue_pre(ctx, cur)) != cudaSuccess) return e;
     if ((e = launch_bias(ctx->D, ctx->g, cur, 1, ctx->st)) != cudaSuccess) return e;
-    if (!ctx->overlap) return launch_step(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
-    if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
+    if (!split) return launch_step(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
+    if (ctx->overlap && (e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
     return launch_step_split(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
 }
-int step_kernels(const sis_ctx *ctx) { return pre_step_kernels(ctx) + bias_kernels(ctx->g) + 1 + (ctx->overlap ? 1 : 0); }
+int step_kernels(const sis_ctx *ctx) {
+    return pre_step_kernels(ctx) + bias_kernels(ctx->g) + 1 + (ctx->overlap || ctx->g.prec != 0 ? 1 : 0);
+}
 
 int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
     CK(enqueue_forces_update(ctx, ctx->cur, noise, ns));
@@ -527,6 +534,7 @@ int autotune(sis_ctx *ctx) {
                      : cudaMemcpyAsync(msave + mo[f], ms[f], sizeof(unsigned long long) * mc[f], k, ctx->st);
         return e;
     };
+    const bool mixed = ctx->g.prec != 0;
     auto pass = [&](int G, int ov) -> cudaError_t {
         cudaError_t e;
         if ((e = cudaEventRecord(ctx->ev_fork, ctx->st)) != cudaSuccess) return e;
@@ -534,6 +542,8 @@ int autotune(sis_ctx *ctx) {
             if ((e = cudaStreamWaitEvent(ctx->st3, ctx->ev_fork, 0)) != cudaSuccess) return e;
             if ((e = launch_pairs(G, D, ctx->g, ctx->cur, ctx->st3)) != cudaSuccess) return e;
             if ((e = cudaEventRecord(ctx->ev_join, ctx->st3)) != cudaSuccess) return e;
+        } else if (mixed && (e = launch_pairs(G, D, ctx->g, ctx->cur, ctx->st)) != cudaSuccess) {
+            return e;
         }
         if (with_bp) {
             if ((e = cudaStreamWaitEvent(ctx->st4, ctx->ev_fork, 0)) != cudaSuccess) return e;
@@ -544,10 +554,8 @@ int autotune(sis_ctx *ctx) {
         } else if ((e = launch_bonded(D, ctx->g, ctx->cur, ctx->st)) != cudaSuccess) {
             return e;
         }
-        if (ov) {
-            if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
-            return launch_step_split(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st);
-        }
+        if (ov && (e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
+        if (ov || mixed) return launch_step_split(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st);
         return launch_step(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st);
     };
     cudaError_t e = copy(false);
@@ -572,7 +580,7 @@ int autotune(sis_ctx *ctx) {
             if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev[13]);
             if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->ev[12], ctx->ev[13]);
             if (ge) cudaGraphExecDestroy(ge);
-            ctx->launches += 8 * (2 + (ov ? 1 : 0) + (with_bp ? bp_kernels(ctx->g) : 0));
+            ctx->launches += 8 * (2 + (ov || mixed ? 1 : 0) + (with_bp ? bp_kernels(ctx->g) : 0));
             if (e == cudaSuccess && ms < best) {
                 best = ms;
                 bestG = G;
@@ -757,11 +765,19 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     }
     cap = (cap + 31) / 32 * 32;
     if (p.nbr_cap > 0) cap = p.nbr_cap;
+    // i-clusters of the mixed path's pair kernel: kCl consecutive beads of an instance
+    int n_cl = 0;
+    for (int k = 0; k < ctx->n_inst; ++k) {
+        ctx->ip[k].cl_off = n_cl;
+        n_cl += (ctx->ip[k].n + kCl - 1) / kCl;
+    }
     // ------------------------------------------------------ global params
     GlobP &g = ctx->g;
     g.n = ctx->n;
     g.n_inst = ctx->n_inst;
     g.cap = cap;
+    g.n_cl = n_cl;
+    g.ccap = std::min(kClCapMax, std::max(32, cap / 2));
     g.prec = p.precision;
     g.integrator = p.integrator;
     g.angl_reb = p.angl_reb;
@@ -812,8 +828,17 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     int rc = 0;
     rc |= dalloc(ctx, &D.x[0], n);
     rc |= dalloc(ctx, &D.x[1], n);
-    rc |= dalloc(ctx, &D.mir[0], n);
-    rc |= dalloc(ctx, &D.mir[1], n);
+    // the mirrors carry kCl beads of padding: the cluster-pair kernel loads
+    // whole j-clusters, past the last bead of the last instance too
+    rc |= dalloc(ctx, &D.mir[0], (size_t)n + kCl);
+    rc |= dalloc(ctx, &D.mir[1], (size_t)n + kCl);
+    if (p.precision != SIS_PREC_FP64) {
+        rc |= dalloc(ctx, &D.mir0, n);
+        rc |= dalloc(ctx, &D.cl_first, n_cl);
+        rc |= dalloc(ctx, &D.ncl, n_cl);
+        rc |= dalloc(ctx, &D.cl_j, (size_t)n_cl * g.ccap);
+        rc |= dalloc(ctx, &D.cl_m, (size_t)n_cl * g.ccap);
+    }
     rc |= dalloc(ctx, &D.res[0], n);
     rc |= dalloc(ctx, &D.res[1], n);
     rc |= dalloc(ctx, &D.v, n);
@@ -977,6 +1002,13 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
         // job_md.F90:270-273: the first evaluation runs the base-pair Monte Carlo pass
         std::vector<int> due(ni, 1);
         ok &= cudaMemcpy(D.mc_due, due.data(), sizeof(int) * ni, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (D.cl_first) {
+        std::vector<int> cf;
+        cf.reserve(g.n_cl);
+        for (int k = 0; k < ni; ++k)
+            for (int c = 0; c < ctx->ip[k].n; c += kCl) cf.push_back(ctx->ip[k].bead_off + c);
+        ok &= cudaMemcpy(D.cl_first, cf.data(), sizeof(int) * cf.size(), cudaMemcpyHostToDevice) == cudaSuccess;
     }
     ok &= cudaMemcpy(ctx->items_d, items.data(), sizeof(int2) * std::max<size_t>(1, items.size()), cudaMemcpyHostToDevice) ==
           cudaSuccess;
@@ -1180,7 +1212,7 @@ static int force_common(sis_ctx *ctx, int32_t inst, int mask, double *forces) {
         ctx->launches += bias_kernels(ctx->g);
     }
     CK(launch_force(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->fout_d, mask, ctx->st));
-    ctx->launches++;
+    ctx->launches += force_kernels(ctx->g, mask);
     if (forces) CK(cudaMemcpyAsync(forces, ctx->fout_d + 3 * (size_t)off, sizeof(double) * 3 * cnt, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     if (do_bp) {
@@ -1588,7 +1620,7 @@ extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
         CK(launch_bias(ctx->D, ctx->g, ctx->cur, 1, ctx->st));
         ctx->launches += pre_step_kernels(ctx) + bias_kernels(ctx->g);
         CK(cudaEventRecord(e[1], ctx->st));
-        if (ctx->overlap) {
+        if (ctx->overlap || ctx->g.prec != 0) {
             CK(launch_pairs(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->st));
             CK(launch_step_split(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
             ctx->launches += 2;

@@ -21,6 +21,16 @@
 //                        local index | seq<<24 | charge<<28)
 //   nbr       int32     per-bead pair list, stride cap: j | WCA<<31 | ELE<<30
 //   nnbr      int32     entries per bead
+//   cl_*                cluster-pair lists of the mixed path's pair kernel: an
+//                       i-cluster is 8 consecutive beads of one instance
+//                       (local beads 8c .. 8c+7); for each, the j-clusters
+//                       holding its pair-list partners in ascending order, as
+//                       the j-cluster's first bead and two 64-bit masks (bit
+//                       8a+b: i-bead a with j-bead b is a WCA / an electrostatic
+//                       pair of the reference's lists)
+//   mir0      uint4     mirror at the last list rebuild (mixed path): the
+//                       displacement of the rebuild trigger is the exact
+//                       integer difference of the current mirror and this one
 //   bps/bps_n int4      base-pair candidates in per-instance segments:
 //                       (i, j, type|hash<<8, inst) and neighbour beads
 //                       (i-1, j-1, i+1, j+1); a prefix over instance counts
@@ -43,6 +53,11 @@ constexpr int ERR_BP_OVERFLOW = 2;
 constexpr int ERR_NONFINITE = 4;
 constexpr int ERR_TIMEOUT = 8; // a grid barrier wait of k_trigger_rebuild ran out
 constexpr int kMaxCoopBlocks = 4096;
+// cluster-pair lists: beads per cluster, the per-warp hash table of the
+// conversion from per-bead lists, and the largest j-cluster count per i-cluster
+constexpr int kCl = 8;
+constexpr int kClHash = 512;
+constexpr int kClCapMax = 256;
 
 // Fixed-point base-pair force accumulation of the mixed path: one unit is
 // 2^-32 kcal/mol/A; contributions of magnitude 2^30 or more are reported as
@@ -60,6 +75,12 @@ __device__ __forceinline__ long long fx_of(float v) {
     return (long long)__float2int_rz(h) * 2147483648LL + (long long)__float2int_rn(l);
 }
 __device__ __forceinline__ long long fx_of(double v) { return __double2ll_rn(v * 4294967296.0); }
+// the fixed-point word as FP32 kcal/mol/A from 32-bit conversions only
+// (the high word scaled exactly, the low word rounded once)
+__device__ __forceinline__ float fx_float(double word) {
+    const long long w = __double_as_longlong(word);
+    return fmaf((float)(int)(w >> 32), 1.0f, (float)(unsigned int)w * 2.3283064365386963e-10f);
+}
 __device__ __forceinline__ double fx_value(double word) { return (double)__double_as_longlong(word) * FX_UNIT; }
 
 struct InstP {
@@ -69,6 +90,7 @@ struct InstP {
     float finv[3];     // Angstrom per unit
     int pbc;
     int bead_off, n;   // beads [bead_off, bead_off + n)
+    int cl_off;        // first i-cluster of the instance
     int bp_off, bp_cap;// base-pair staging segment
     double tempK;
     double ele_coef, rcdist, ele_cut, ele_cut2, diele_dTcoef;
@@ -88,6 +110,7 @@ struct InstP {
 
 struct GlobP {
     int n, n_inst, cap, prec, integrator;
+    int n_cl, ccap; // i-clusters of all instances; j-cluster slots per i-cluster
     int angl_reb, dih_type, bp_model, flg_ele, temp_indep;
     int bp_min_loop, bp_jnext_compat, ele_excl_bond, ele_excl_angle;
     double bond_k, bond_r0, angl_k, angl_t0, cos_t0, dih_k, dih_w, dih_p0;
@@ -146,6 +169,13 @@ struct Dev {
     double *rgv;
     double *mass;
     int *nbr, *nnbr;
+    // cluster-pair lists (mixed path): per i-cluster its first bead, its
+    // j-cluster count (-1: more than ccap, the pair kernel then walks the
+    // per-bead lists of its beads), and ccap slots of (j-cluster first bead,
+    // WCA mask, electrostatic mask)
+    int *cl_first, *ncl, *cl_j;
+    ulonglong2 *cl_m;
+    uint4 *mir0;            // [n] mirror at the last rebuild (mixed path)
     // base-pair lists
     int4 *bps, *bps_n;      // per-instance staging segments (records, neighbour beads)
     int *bp_cnt;            // [2*n_inst] staging counts, then their exclusive prefix
@@ -244,13 +274,27 @@ template <> struct Pos<float> {
     __device__ __forceinline__ V3<float> d(int a, int b, const InstP &ip) const { return dvec32(m[a], m[b], ip); }
 };
 
-// mirror component q = llrint(x*S) mod 2^32 and the residual x*S - q (units
-// of 1/S, |r| <= 1/2) that the mirror drops
+// Mirror component q = round(x*S) mod 2^32 and the residual x*S - q (units of
+// 1/S, |r| <= 1/2) that the mirror drops, with two FP64 operations: adding
+// M = 1.5 * 2^40 to t = x*S leaves round(t * 2^12) + 2^51 in the low 52
+// mantissa bits of the sum (valid for |t| < 2^39), so the integer part and
+// the residual (to 2^-12 units) follow from integer arithmetic.  q rounds t
+// half up after t has been rounded to 2^-12 units; every mirror of the
+// library comes from this function, so all agree.  Returns false when t is
+// out of range or not finite (then q and r are meaningless).
+__device__ __forceinline__ bool fixed_mirror(double x, double s, unsigned int &q, float &r) {
+    const double u = __dadd_rn(__dmul_rn(x, s), 1649267441664.0); // 1.5 * 2^40
+    const long long b = __double_as_longlong(u);
+    const long long w = (b & 0xFFFFFFFFFFFFFLL) - (1LL << 51);  // round(t * 2^12)
+    const long long qq = (w + 2048) >> 12;
+    q = (unsigned int)(unsigned long long)qq;
+    r = (float)(int)(w - (qq << 12)) * 0.000244140625f;
+    return (b >> 52) == 0x427; // exponent of [2^40, 2^41): |t| < 2^39 and finite
+}
 __device__ __forceinline__ unsigned int fixed_res(double x, double s, float &r) {
-    const double t = x * s;
-    const double q = rint(t);
-    r = (float)(t - q);
-    return (unsigned int)(unsigned long long)(long long)q;
+    unsigned int q;
+    fixed_mirror(x, s, q, r);
+    return q;
 }
 
 // A separation in fixed-point units: the exact mirror difference d (int32,

@@ -32,10 +32,7 @@ __device__ __forceinline__ double comp(const V3<double> &a, int c) { return c ==
 
 // Gaussian deviate of component c of local bead i of a noise stream at step s
 // (Box-Muller on one Philox4x32-10 block: components 0,1 share one pair).
-template <typename R>
-__device__ __forceinline__ double gauss3(unsigned long long seed, int i, unsigned long long s, int c, unsigned stream);
-template <> __device__ __forceinline__ double gauss3<float>(unsigned long long seed, int i, unsigned long long s, int c,
-                                                            unsigned stream) {
+__device__ __forceinline__ float gauss_f(unsigned long long seed, int i, unsigned long long s, int c, unsigned stream) {
     const uint4 r = philox4x32_10(make_uint4((unsigned)i, (unsigned)s, (unsigned)(s >> 32), stream),
                                   make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
     const unsigned a = c < 2 ? r.x : r.z, b = c < 2 ? r.y : r.w;
@@ -43,7 +40,13 @@ template <> __device__ __forceinline__ double gauss3<float>(unsigned long long s
     const float u2 = (float)(b >> 8) * (1.0f / 16777216.0f);
     float sn, cs;
     sincospif(2.0f * u2, &sn, &cs);
-    return (double)(sqrtf(-2.0f * logf(u1)) * (c == 1 ? sn : cs));
+    return sqrtf(-2.0f * logf(u1)) * (c == 1 ? sn : cs);
+}
+template <typename R>
+__device__ __forceinline__ double gauss3(unsigned long long seed, int i, unsigned long long s, int c, unsigned stream);
+template <> __device__ __forceinline__ double gauss3<float>(unsigned long long seed, int i, unsigned long long s, int c,
+                                                            unsigned stream) {
+    return (double)gauss_f(seed, i, s, c, stream);
 }
 template <> __device__ __forceinline__ double gauss3<double>(unsigned long long seed, int i, unsigned long long s, int c,
                                                              unsigned stream) {
@@ -825,6 +828,116 @@ template <typename R, int G> __global__ void __launch_bounds__(256, 5) k_pairs(D
     }
 }
 
+// FP32 force coefficient c (F_i = c (x_i - x_j)) of one listed pair at
+// squared distance d2: WCA (force_wca.F90:34-67) when the pair is on the WCA
+// list and inside sigma, Debye-Hueckel (force_ele_DH.F90:39-82) when it is on
+// the electrostatic list and inside the cutoff
+struct PairCoef {
+    float sig2, wcoef, ecoef, rc, cut2;
+};
+__device__ __forceinline__ float pair_c(bool wca, bool ele, float d2, const PairCoef &P) {
+    float c = 0.f;
+    if (wca && d2 < P.sig2) {
+        const float sq = __fdiv_rn(P.sig2, d2);
+        const float s2 = sq * sq, s4 = s2 * s2;
+        c += P.wcoef * (s4 * s2 * sq - s4);
+    }
+    if (ele && d2 <= P.cut2) {
+        float ri = rsqrtf(d2);
+        ri = ri * fmaf(-0.5f * d2 * ri, ri, 1.5f);
+        const float r = d2 * ri;
+        c += P.ecoef * ri * ri * (ri + P.rc) * __expf(-r * P.rc);
+    }
+    return c;
+}
+
+// Pair forces of the mixed path over the cluster-pair lists (lists.cu
+// cluster_lists) into fpair: one warp per i-cluster of 8 beads.  Lane
+// (a = lane & 7, q = lane >> 3) pairs i-bead a with j-beads q and q + 4 of
+// every j-cluster, in list order; the four partial sums of an i-bead are
+// then combined (xor 8, then 16).  Lanes fetch the j-cluster entries 32 at a
+// time, one each, and broadcast them by shuffles, so a pair costs one
+// coalesced 16-byte position load and no list-word load.  mask bit 16: WCA,
+// bit 32: electrostatics.  An i-cluster whose j-clusters did not fit (count
+// -1) walks its beads' per-bead lists, 4 lanes per bead.
+__global__ void __launch_bounds__(256) k_pairs_cl(Dev D, GlobP g, int cur, int mask) {
+    const int lane = threadIdx.x & 31;
+    const int ic = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (ic >= g.n_cl) return;
+    const int a = lane & 7, q = lane >> 3;
+    const int first = D.cl_first[ic];
+    const InstP &ip = D.ip[D.binfo[first].x];
+    const int cnt = min(kCl, ip.bead_off + ip.n - first);
+    const uint4 *__restrict__ mir = D.mir[cur];
+    const uint4 mi = mir[first + (a < cnt ? a : 0)];
+    const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
+    PairCoef P;
+    P.sig2 = g.f_wca_sig2;
+    P.wcoef = g.f_wca_coef;
+    P.ecoef = ip.ele_coef_f;
+    P.rc = ip.rcdist_f;
+    P.cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+    const unsigned wsel = (mask & 16) ? 0xffu : 0u, esel = (mask & 32) ? 0xffu : 0u;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    const int nc = D.ncl[ic];
+    if (nc >= 0) {
+        const size_t base = (size_t)ic * g.ccap;
+        for (int k0 = 0; k0 < nc; k0 += 32) {
+            int jf = 0;
+            unsigned long long mw = 0ull, me = 0ull;
+            if (k0 + lane < nc) {
+                jf = __ldg(D.cl_j + base + k0 + lane);
+                const ulonglong2 m = D.cl_m[base + k0 + lane];
+                mw = m.x;
+                me = m.y;
+            }
+            const int kn = min(32, nc - k0);
+            for (int k = 0; k < kn; ++k) {
+                const int j0 = __shfl_sync(0xffffffffu, jf, k);
+                const unsigned wb = (unsigned)(__shfl_sync(0xffffffffu, mw, k) >> (a * kCl)) & wsel;
+                const unsigned eb = (unsigned)(__shfl_sync(0xffffffffu, me, k) >> (a * kCl)) & esel;
+                const uint4 mj0 = __ldg(mir + j0 + q), mj1 = __ldg(mir + j0 + q + 4);
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {
+                    const uint4 mj = t ? mj1 : mj0;
+                    const int b = q + 4 * t;
+                    const float vx = (float)(int)(mi.x - mj.x) * f0;
+                    const float vy = (float)(int)(mi.y - mj.y) * f1;
+                    const float vz = (float)(int)(mi.z - mj.z) * f2;
+                    const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+                    const float c = pair_c((wb >> b) & 1u, (eb >> b) & 1u, d2, P);
+                    ax = fmaf(c, vx, ax);
+                    ay = fmaf(c, vy, ay);
+                    az = fmaf(c, vz, az);
+                }
+            }
+        }
+    } else if (a < cnt) {
+        const int gi = first + a;
+        const int m = min(D.nnbr[gi], g.cap);
+        const int *__restrict__ nb = D.nbr + (size_t)gi * g.cap;
+        for (int k = q; k < m; k += 4) {
+            const int e = __ldg(nb + k);
+            const uint4 mj = __ldg(mir + (e & IDX_MASK));
+            const float vx = (float)(int)(mi.x - mj.x) * f0;
+            const float vy = (float)(int)(mi.y - mj.y) * f1;
+            const float vz = (float)(int)(mi.z - mj.z) * f2;
+            const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+            const float c = pair_c((e & WCA_BIT) && (mask & 16), (e & ELE_BIT) && (mask & 32), d2, P);
+            ax = fmaf(c, vx, ax);
+            ay = fmaf(c, vy, ay);
+            az = fmaf(c, vz, az);
+        }
+    }
+#pragma unroll
+    for (int o = 8; o <= 16; o <<= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, o);
+        ay += __shfl_xor_sync(0xffffffffu, ay, o);
+        az += __shfl_xor_sync(0xffffffffu, az, o);
+    }
+    if (q == 0 && a < cnt) reinterpret_cast<float4 *>(D.fpair)[first + a] = make_float4(ax, ay, az, 0.f);
+}
+
 template <typename R, int G, int MODE>
 __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
                                               double *__restrict__ fout, int mask) {
@@ -832,6 +945,8 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     __shared__ R sA[3][BPB], sB[3][BPB];
     __shared__ float sScale[BPB];
     __shared__ double sM[3][BPB];
+    __shared__ float sCf[2][BPB];       // mixed path: FP32 force and noise coefficients of the update
+    __shared__ unsigned int sQ[3][BPB]; // mixed path: the new mirror
     __shared__ unsigned long long s_m1[32], s_m2[32];
     __shared__ int s_lo, s_cnt;
     const int b = threadIdx.x / G;
@@ -923,6 +1038,12 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
             }
         }
         sScale[b] = sc;
+        if constexpr (sizeof(R) == 4) {
+            // GJF-2GJ: F -> sqrt(b) h / m, noise -> its amplitude; Ermak-McCammon: F -> h / gamma
+            const double4 m = D.mdc[i];
+            sCf[0][b] = (float)(g.integrator == 1 ? m.y : m.x);
+            sCf[1][b] = (float)m.w;
+        }
     }
     __syncthreads();
 
@@ -936,56 +1057,90 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
         const int c = t / BPB, bb = t - c * BPB;
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
-        double Fc;
         double *fp = reinterpret_cast<double *>(D.fbp + ii) + c;
         if constexpr (sizeof(R) == 4) {
-            // FP32 lane sums plus the fixed-point base-pair force, one conversion to FP64
+            // Mixed path: the force (FP32 lane sums plus the fixed-point
+            // base-pair force) and the noise enter as FP32 increments; the
+            // velocity and the position accumulate in FP64.  The mirror and
+            // its residual come from the new FP64 position (fixed_mirror).
             float fb = 0.f;
             if (mask & 136) {
-                fb = (float)__double_as_longlong(*fp) * (float)FX_UNIT;
+                fb = fx_float(*fp);
                 *fp = 0.0;
             }
-            Fc = (double)(sA[c][bb] + sB[c][bb] + fb);
+            float F = sA[c][bb] + sB[c][bb] + fb;
+            if (MODE == 1) {
+                fout[3 * (size_t)ii + c] = (double)F;
+                continue;
+            }
+            F *= sScale[bb];
+            const int4 bj = D.binfo[ii];
+            const InstP &jp = D.ip[bj.x];
+            const float xi = noise ? (float)noise[((size_t)noise_step * g.n + ii) * 3 + c]
+                                   : gauss_f(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
+            double *vp = reinterpret_cast<double *>(D.v + ii) + c;
+            double *bp = reinterpret_cast<double *>(D.beta + ii) + c;
+            double dx;
+            if (g.integrator == 1) {
+                const double4 m = D.mdc[ii];
+                const float bn = sCf[1][bb] * xi;
+                const double vn = fma(m.x, *vp, *bp) + (double)fmaf(sCf[0][bb], F, bn);
+                *bp = (double)bn;
+                *vp = vn;
+                dx = m.z * vn;
+            } else {
+                dx = (double)fmaf(sCf[0][bb], F, sCf[1][bb] * xi);
+            }
+            const double xn = reinterpret_cast<const double *>(D.x[cur] + ii)[c] + dx;
+            unsigned int qm;
+            float r;
+            if (!fixed_mirror(xn, jp.fsc[c], qm, r)) atomicOr(D.err, ERR_NONFINITE);
+            reinterpret_cast<double *>(D.x[cur ^ 1] + ii)[c] = xn;
+            reinterpret_cast<unsigned int *>(D.mir[cur ^ 1] + ii)[c] = qm;
+            reinterpret_cast<float *>(D.res[cur ^ 1] + ii)[c] = r;
+            sQ[c][bb] = qm;
+            continue;
         } else {
+            double Fc;
             double fb = 0.0;
             if (mask & 136) {
                 fb = *fp;
                 *fp = 0.0;
             }
             Fc = sA[c][bb] + sB[c][bb] + fb;
+            if (MODE == 1) {
+                fout[3 * (size_t)ii + c] = Fc;
+                continue;
+            }
+            if (sScale[bb] != 1.f) Fc = Fc * (double)sScale[bb];
+            const int4 bj = D.binfo[ii];
+            const InstP &jp = D.ip[bj.x];
+            const double4 m = D.mdc[ii];
+            const double xi = noise ? noise[((size_t)noise_step * g.n + ii) * 3 + c]
+                                    : gauss3<R>(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
+            double *vp = reinterpret_cast<double *>(D.v + ii) + c;
+            double *bp = reinterpret_cast<double *>(D.beta + ii) + c;
+            double *mp = reinterpret_cast<double *>(D.move + ii) + c;
+            double dx;
+            if (g.integrator == 1) {
+                const double bn = m.w * xi;
+                const double vn = m.x * *vp + m.y * Fc + (*bp + bn);
+                *bp = bn;
+                *vp = vn;
+                dx = m.z * vn;
+            } else {
+                dx = m.x * Fc + m.w * xi;
+            }
+            const double xn = reinterpret_cast<const double *>(D.x[cur] + ii)[c] + dx;
+            if (!isfinite(xn)) atomicOr(D.err, ERR_NONFINITE);
+            const double mc = *mp + dx;
+            *mp = mc;
+            sM[c][bb] = mc;
+            reinterpret_cast<double *>(D.x[cur ^ 1] + ii)[c] = xn;
+            float r;
+            reinterpret_cast<unsigned int *>(D.mir[cur ^ 1] + ii)[c] = fixed_res(xn, jp.fsc[c], r);
+            reinterpret_cast<float *>(D.res[cur ^ 1] + ii)[c] = r;
         }
-        if (MODE == 1) {
-            fout[3 * (size_t)ii + c] = Fc;
-            continue;
-        }
-        if (sScale[bb] != 1.f) Fc = Fc * (double)sScale[bb];
-        const int4 bj = D.binfo[ii];
-        const InstP &jp = D.ip[bj.x];
-        const double4 m = D.mdc[ii];
-        const double xi = noise ? noise[((size_t)noise_step * g.n + ii) * 3 + c]
-                                : gauss3<R>(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
-        double *vp = reinterpret_cast<double *>(D.v + ii) + c;
-        double *bp = reinterpret_cast<double *>(D.beta + ii) + c;
-        double *mp = reinterpret_cast<double *>(D.move + ii) + c;
-        double dx;
-        if (g.integrator == 1) {
-            const double bn = m.w * xi;
-            const double vn = m.x * *vp + m.y * Fc + (*bp + bn);
-            *bp = bn;
-            *vp = vn;
-            dx = m.z * vn;
-        } else {
-            dx = m.x * Fc + m.w * xi;
-        }
-        const double xn = reinterpret_cast<const double *>(D.x[cur] + ii)[c] + dx;
-        if (!isfinite(xn)) atomicOr(D.err, ERR_NONFINITE);
-        const double mc = *mp + dx;
-        *mp = mc;
-        sM[c][bb] = mc;
-        reinterpret_cast<double *>(D.x[cur ^ 1] + ii)[c] = xn;
-        float r;
-        reinterpret_cast<unsigned int *>(D.mir[cur ^ 1] + ii)[c] = fixed_res(xn, jp.fsc[c], r);
-        reinterpret_cast<float *>(D.res[cur ^ 1] + ii)[c] = r;
     }
     if (MODE == 1) return;
     __syncthreads();
@@ -998,9 +1153,20 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
-        const double mx = sM[0][bb], my = sM[1][bb], mz = sM[2][bb];
-        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
-        if (!isfinite(d2)) atomicOr(D.err, ERR_NONFINITE);
+        double d2;
+        if constexpr (sizeof(R) == 4) {
+            // mixed path: the exact integer displacement since the last rebuild
+            const uint4 m0 = D.mir0[ii];
+            const float* fi = D.ip[D.binfo[ii].x].finv;
+            const float dx = (float)(int)(sQ[0][bb] - m0.x) * fi[0];
+            const float dy = (float)(int)(sQ[1][bb] - m0.y) * fi[1];
+            const float dz = (float)(int)(sQ[2][bb] - m0.z) * fi[2];
+            d2 = (double)fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        } else {
+            const double mx = sM[0][bb], my = sM[1][bb], mz = sM[2][bb];
+            d2 = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
+            if (!isfinite(d2)) atomicOr(D.err, ERR_NONFINITE);
+        }
         const unsigned long long bits = (unsigned long long)__double_as_longlong(d2);
         const int inst = D.binfo[ii].x;
         if (s_cnt <= 32) {
@@ -1167,15 +1333,26 @@ template <typename R> static cudaError_t launch_pairs_r(int G, const Dev &D, con
     default: return launch_pairs_g<R, 32>(D, g, cur, st);
     }
 }
+// pair forces into fpair: per-bead lists in the FP64 path, cluster pairs in the mixed path
 cudaError_t launch_pairs(int G, const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
     if (g.prec == 0) return launch_pairs_r<double>(G, D, g, cur, st);
-    return launch_pairs_r<float>(G, D, g, cur, st);
+    k_pairs_cl<<<(g.n_cl + 7) / 8, 256, 0, st>>>(D, g, cur, 48);
+    return cudaGetLastError();
 }
 
+// forces of the terms in mask into fout (MODE 1 of the step kernel); the
+// mixed path takes its pair forces from k_pairs_cl
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st) {
     if (g.prec == 0) return launch_step_r<double, 1>(G, D, g, cur, nullptr, 0, fout, mask, st);
+    if (mask & 48) {
+        k_pairs_cl<<<(g.n_cl + 7) / 8, 256, 0, st>>>(D, g, cur, mask & 48);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        mask |= 64;
+    }
     return launch_step_r<float, 1>(G, D, g, cur, nullptr, 0, fout, mask, st);
 }
+int force_kernels(const GlobP &g, int mask) { return 1 + (g.prec != 0 && (mask & 48) ? 1 : 0); }
 
 // bonded terms (if do_bonded) and base-pair forces (if do_bp) of one step
 cudaError_t launch_bonded(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {

@@ -30,6 +30,7 @@ struct RemdDev {
 
 cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long noise_step, cudaStream_t st);
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
+int force_kernels(const GlobP &g, int mask); // kernels launch_force launches
 // the step split in two: pair forces of every bead into fpair, then the step proper
 cudaError_t launch_pairs(int G, const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 cudaError_t launch_step_split(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st);

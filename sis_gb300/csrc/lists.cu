@@ -210,6 +210,8 @@ __device__ __forceinline__ void bead_begin(const Dev &D, int cur, int gi, const 
     if (lane == 0) {
         if (ip.pbc) D.x[cur][gi] = xi_w;
         D.move[gi] = make_double4(0.0, 0.0, 0.0, 0.0);
+        // the mirror is the same before and after the wrap (the box is 2^32 units)
+        if (D.mir0) D.mir0[gi] = D.mir[cur][gi];
     }
 }
 __device__ __forceinline__ void bead_end(const Dev &D, const GlobP &g, int gi, int lane, int count) {
@@ -558,6 +560,99 @@ __device__ void cell_search(const Dev &D, const GlobP &g, int cur, const int2 *l
     }
 }
 
+// ------------------------------------------------------ cluster pairs
+// The mixed path's pair kernel walks cluster pairs instead of per-bead lists
+// (kernels.cu k_pairs_cl).  For every i-cluster of a rebuilt instance one
+// warp gathers the clusters J (local index of the partner / 8) of its beads'
+// list entries into a hash table in shared memory, ranks the distinct J in
+// ascending order, and ORs each entry's bit 8a+b (a, b: the beads' places in
+// their clusters) into the WCA or electrostatic mask of its J.  The order is
+// that of the local indices, so an instance gives the same lists alone and
+// in any batch.  An i-cluster with more than ccap distinct J gets the count
+// -1, and the pair kernel walks its beads' per-bead lists instead.
+__device__ __forceinline__ unsigned cl_hash(int J) { return ((unsigned)J * 2654435761u) >> 23; } // 9 bits: kClHash
+__device__ __forceinline__ int cl_find(const int *key, int J) {
+    unsigned h = cl_hash(J);
+    for (int p = 0; p < kClHash; ++p) {
+        if (key[h] == J) return (int)h;
+        h = (h + 1) & (kClHash - 1);
+    }
+    return -1;
+}
+__device__ void cluster_lists(const Dev &D, const GlobP &g, int *sh) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *key = sh + warp * 2 * kClHash;
+    int *rank = key + kClHash;
+    for (int ic = blockIdx.x * 8 + warp; ic < g.n_cl; ic += gridDim.x * 8) {
+        const int first = D.cl_first[ic];
+        const int inst = D.binfo[first].x;
+        if (__ldcg(D.flag + inst) == 0) continue;
+        const InstP &ip = D.ip[inst];
+        const int cnt = min(kCl, ip.bead_off + ip.n - first);
+        for (int h = lane; h < kClHash; h += 32) key[h] = -1;
+        __syncwarp();
+        // distinct clusters of the entries (the table holds at most kClHash)
+        int full = 0;
+        for (int a = 0; a < cnt; ++a) {
+            const int gi = first + a;
+            const int m = min(__ldcg(D.nnbr + gi), g.cap);
+            const int *nb = D.nbr + (size_t)gi * g.cap;
+            for (int k = lane; k < m; k += 32) {
+                const int J = ((__ldcg(nb + k) & IDX_MASK) - ip.bead_off) / kCl;
+                unsigned h = cl_hash(J);
+                int p = 0;
+                for (; p < kClHash; ++p) {
+                    const int old = atomicCAS(&key[h], -1, J);
+                    if (old == -1 || old == J) break;
+                    h = (h + 1) & (kClHash - 1);
+                }
+                full |= p == kClHash;
+            }
+        }
+        __syncwarp();
+        int nu = 0;
+        for (int h0 = 0; h0 < kClHash; h0 += 32) nu += __popc(__ballot_sync(0xffffffffu, key[h0 + lane] >= 0));
+        full = __any_sync(0xffffffffu, full);
+        size_t base = (size_t)ic * g.ccap;
+        if (full || nu > g.ccap) {
+            if (lane == 0) D.ncl[ic] = -1;
+            __syncwarp();
+            continue;
+        }
+        // rank of every distinct cluster: the number of smaller ones
+        for (int h = lane; h < kClHash; h += 32) {
+            const int v = key[h];
+            if (v < 0) continue;
+            int r = 0;
+            for (int q = 0; q < kClHash; ++q) {
+                const int w = key[q];
+                r += w >= 0 && w < v;
+            }
+            rank[h] = r;
+            D.cl_j[base + r] = ip.bead_off + v * kCl;
+            D.cl_m[base + r] = make_ulonglong2(0ull, 0ull);
+        }
+        __syncwarp();
+        for (int a = 0; a < cnt; ++a) {
+            const int gi = first + a;
+            const int m = min(__ldcg(D.nnbr + gi), g.cap);
+            const int *nb = D.nbr + (size_t)gi * g.cap;
+            for (int k = lane; k < m; k += 32) {
+                const int e = __ldcg(nb + k);
+                const int jl = (e & IDX_MASK) - ip.bead_off;
+                const int h = cl_find(key, jl / kCl);
+                if (h < 0) continue; // not reached: every cluster was inserted
+                const unsigned long long bit = 1ull << (a * kCl + jl % kCl);
+                ulonglong2 *dst = D.cl_m + base + rank[h];
+                if (e & WCA_BIT) atomicOr(&dst->x, bit);
+                if (e & ELE_BIT) atomicOr(&dst->y, bit);
+            }
+        }
+        if (lane == 0) D.ncl[ic] = nu;
+        __syncwarp();
+    }
+}
+
 // ------------------------------------------------------------ finish
 // Block 0: base-pair prefix counts over the instances and rebuild
 // bookkeeping; every block: reset of its share of the cell counters.
@@ -612,6 +707,7 @@ __device__ void rebuild_finish(const Dev &D, const GlobP &g) {
 // and the all-pairs scan of small instances; finish.
 __global__ void __launch_bounds__(256) k_trigger_rebuild(Dev D, GlobP g, int cur, RebuildPlan pl, int nparts, int after_step) {
     __shared__ int s_red[8];
+    __shared__ int s_cl[8 * 2 * kClHash]; // per warp: cluster hash keys and ranks
     const float slack = 1.001f;
     if (after_step) {
         const unsigned long long ctr = *(volatile unsigned long long *)D.step_ctr;
@@ -662,6 +758,10 @@ __global__ void __launch_bounds__(256) k_trigger_rebuild(Dev D, GlobP g, int cur
         cell_search(D, g, cur, pl.large_items, pl.n_large_items, slack);
     }
     if (pl.n_small_items > 0) rebuild_small(D, g, cur, pl.small_items, pl.n_small_items, slack);
+    if (g.prec != 0) {
+        if (!grid_sync(D)) return;
+        cluster_lists(D, g, s_cl);
+    }
     if (!grid_sync(D)) return;
     rebuild_finish(D, g);
 }
