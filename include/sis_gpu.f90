@@ -119,6 +119,23 @@ module sis_gpu_mod
       integer(c_int32_t), value :: inst, n
       integer(c_int32_t), intent(in) :: beads(*)  ! [Freeze] bead numbers (1-based)
     end function
+    integer(c_int) function sis_gpu_set_ss_pairs(ctx, inst, n, pairs) bind(C, name="sis_gpu_set_ss_pairs")
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: inst, n
+      integer(c_int32_t), intent(in) :: pairs(2, *)  ! bp_map pairs (imp, jmp) of read_ss, 1-based
+    end function
+    integer(c_int) function sis_gpu_set_bias_ss(ctx, on, force) bind(C, name="sis_gpu_set_bias_ss")
+      import :: c_int, c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: on              ! flg_bias_ss
+      real(c_double), value :: force               ! bias_ss_force (kcal/mol/A)
+    end function
+    integer(c_int) function sis_gpu_set_small(ctx, mode) bind(C, name="sis_gpu_set_small")
+      import :: c_int, c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: mode
+    end function
     integer(c_int) function sis_gpu_get_list(ctx, inst, kind, out, cap, n_out) bind(C, name="sis_gpu_get_list")
       import :: c_int, c_int32_t, c_ptr
       type(c_ptr), value :: ctx

@@ -131,6 +131,8 @@ typedef struct sis_stats {
     int64_t capped;         /* bead-steps at which sis_gpu_set_force_cap's cap bound */
     int32_t bp_blocks;      /* block count of the base-pair evaluation */
     int32_t overlap;        /* 1: pair forces in their own kernel (sis_gpu_set_overlap) */
+    int32_t small_blocks;   /* blocks of the per-block kernel of small instances (0: not used) */
+    int32_t small_threads;  /* threads per block of that kernel */
 } sis_stats;
 
 /* Creates a context and uploads topology and parameters.  Replaces the
@@ -207,6 +209,21 @@ int sis_gpu_set_temperature(sis_ctx *ctx, int32_t inst, double tempK);
  * frees all.  Under replica exchange every replica must freeze the same
  * beads (the reference freezes by bead number in all replicas). */
 int sis_gpu_set_frozen(sis_ctx *ctx, int32_t inst, const int32_t *beads, int32_t n);
+/* Base pairs restricted to a given secondary structure (read_ss.F90 sets
+ * bp_map from the ct, bpseq or bpl file of [Files.In]; init_bp.F90:207-209
+ * then skips every other pair): pairs[2n] are (imp, jmp), 1-based
+ * nucleotide numbers of instance inst, after read_ss's checks (chain ends,
+ * minimum loop, isolated pairs, known pair types; sis_gb300/inputs.py
+ * filter_ss_pairs); the candidate rules of init_bp still apply.  n = 0 lifts
+ * the restriction.  The lists are rebuilt at the next call that needs them. */
+int sis_gpu_set_ss_pairs(sis_ctx *ctx, int32_t inst, int32_t n, const int32_t *pairs);
+/* [Bias_SS] (read_input.F90:1198-1217): on != 0 pulls an allowed pair whose
+ * distance lies outside its window toward each other with a constant force
+ * (kcal/mol/A; the input's force_pN times 1e-22 J->kcal/mol) in the triplet
+ * models 4 and 5 (force_bp_triplet.F90:85-92), and lists every allowed pair
+ * whatever its distance (neighbor_list.F90:89-93).  It needs a secondary
+ * structure (sis_gpu_set_ss_pairs), as the reference does. */
+int sis_gpu_set_bias_ss(sis_ctx *ctx, int32_t on, double force);
 /* Caps the magnitude of every bead's total force at fmax (kcal/mol/A) in
  * sis_gpu_step; 0 removes the cap.  An equilibration aid for starting
  * structures with overlapping beads; it has no counterpart in the reference
@@ -257,6 +274,16 @@ int sis_gpu_set_graphs(sis_ctx *ctx, int32_t enable);
  * kernel computes them; -1 (default): the autotuner chooses, with the lanes
  * per bead, on the first long run.  Results are identical. */
 int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable);
+/* Per-block kernel of small instances (mixed path): when every instance has
+ * at most 2048 beads and an all-pairs list (no cell grid), no base-pair Monte
+ * Carlo and no optional term is on, sis_gpu_step runs all its steps in one
+ * launch per 1000 steps, each block owning a bucket of whole instances in
+ * shared memory (job_md.F90:360-460 for every instance at once).  The
+ * buckets and the block width are picked by timing on the first long run.
+ * -1 (default): used where eligible; 0: never (the general kernels);
+ * 1: as -1.  Trajectories do not depend on the buckets or the block width;
+ * they differ from the general kernels' in the order of FP32 sums only. */
+int sis_gpu_set_small(sis_ctx *ctx, int32_t mode);
 
 int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *st);
 /* Failure-detection self-test (no counterpart in the reference): one block of

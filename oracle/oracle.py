@@ -106,6 +106,8 @@ def lib() -> C.CDLL:
             "or_set_restraints": (None, [vp, i32, vp, vp]),
             "or_set_tweezers": (None, [vp, i32, vp, vp, i32, vp, vp, vp, vp]),
             "or_set_frozen": (None, [vp, i32, vp]),
+            "or_set_ss_pairs": (None, [vp, i32, vp]),
+            "or_set_bias_ss": (None, [vp, i32, d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -276,6 +278,16 @@ class Oracle:
         fv = np.array([q.velo for q in fr], dtype=np.float64).reshape(-1, 2, 3)
         self._twz = (dp, df, fp, fk, fi, fv)
         self.L.or_set_tweezers(self.h, len(dcf), _p(dp), _p(df), len(fr), _p(fp), _p(fk), _p(fi), _p(fv))
+
+    def set_ss_pairs(self, pairs):
+        """read_ss.F90 bp_map: base pairs only between these (imp, jmp), 1-based."""
+        a = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        self._ss = a
+        self.L.or_set_ss_pairs(self.h, a.shape[0], _p(a))
+
+    def set_bias_ss(self, force_kcal_per_mol_A, on=True):
+        """[Bias_SS]: constant pull of allowed pairs outside the distance window."""
+        self.L.or_set_bias_ss(self.h, int(on), float(force_kcal_per_mol_A))
 
     def set_frozen(self, beads):
         """[Freeze]: 1-based bead numbers whose positions stay fixed."""

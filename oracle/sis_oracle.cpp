@@ -136,6 +136,13 @@ struct or_system {
     std::vector<int> fr_pairs;     /* [n][2] twz_FR_pairs */
     std::vector<double> fr_k;      /* [n][2] twz_FR_k */
     std::vector<double> fr_init, fr_velo; /* [n][2][3] twz_FR_init, twz_FR_velo */
+    /* base pairs restricted to a given secondary structure (read_ss.F90 sets
+     * bp_map from a ct/bpseq/bpl file; init_bp.F90:207-209 skips other pairs),
+     * and the [Bias_SS] constant pull (force_bp_triplet.F90:85-92) */
+    bool ss_on = false;
+    std::vector<std::vector<int>> ss_part; /* per bead (0-based): 1-based partners */
+    bool bias_ss = false;
+    double bias_ss_force = 0.0;           /* kcal/mol/A */
 };
 
 namespace {
@@ -540,6 +547,24 @@ extern "C" void or_set_temperature(or_system *s, int32_t irep, double tempK, dou
 }
 
 /* [Freeze] id_ranges, as 1-based bead numbers (the same in every replica) */
+/* read_ss.F90: the pairs (imp, jmp), 1-based, that bp_map allows; n = 0
+ * lifts the restriction */
+extern "C" void or_set_ss_pairs(or_system *s, int32_t n, const int32_t *pairs) {
+    s->ss_on = n > 0;
+    s->ss_part.assign(s->nmp, {});
+    for (int q = 0; q < n; ++q) {
+        const int i = pairs[2 * q], j = pairs[2 * q + 1];
+        if (i < 1 || j < 1 || i > s->nmp || j > s->nmp) continue;
+        s->ss_part[i - 1].push_back(j);
+        s->ss_part[j - 1].push_back(i);
+    }
+}
+/* read_input.F90:1198-1217 [Bias_SS]: on, force in kcal/mol/A */
+extern "C" void or_set_bias_ss(or_system *s, int32_t on, double force) {
+    s->bias_ss = on != 0;
+    s->bias_ss_force = force;
+}
+
 extern "C" void or_set_frozen(or_system *s, int32_t n, const int32_t *beads) {
     s->frozen.assign(s->nmp, 0);
     for (int q = 0; q < n; ++q)
@@ -607,7 +632,10 @@ extern "C" void or_neighbor_list(or_system *s, int32_t irep) {
         ele_nl_cut2 = (R.ele_cutoff + p.nl_margin) * (R.ele_cutoff + p.nl_margin);
     }
     const double wca_nl_cut2 = (p.wca_sigma + p.nl_margin) * (p.wca_sigma + p.nl_margin);
-    const double bp_nl_cut2 = (s->bp_cutoff_dist + p.nl_margin) * (s->bp_cutoff_dist + p.nl_margin);
+    /* neighbor_list.F90:89-93: with [Bias_SS] every allowed pair is listed
+     * (the REAL(4) literal 9999999999.9 is 1e10 exactly) */
+    const double bp_nl_cut2 =
+        s->bias_ss ? (double)9999999999.9f : (s->bp_cutoff_dist + p.nl_margin) * (s->bp_cutoff_dist + p.nl_margin);
     std::vector<NlRow> rows;
     for (int ic = 0; ic < s->nchains; ++ic)
         for (int jc = ic; jc < s->nchains; ++jc)
@@ -658,7 +686,10 @@ extern "C" void or_neighbor_list(or_system *s, int32_t irep) {
                         o.ele.push_back(jmp);
                     }
                 }
-                if (d2 <= bp_nl_cut2) {
+                bool ss_ok = !s->ss_on;
+                if (!ss_ok)
+                    for (int jj : s->ss_part[imp - 1]) ss_ok |= jj == jmp;
+                if (d2 <= bp_nl_cut2 && ss_ok) {
                     int bp3;
                     int type = bp_candidate(s, imp, jmp, &bp3);
                     if (bp3 > 0) {
@@ -859,7 +890,8 @@ void force_ele(const or_system *s, int irep, double *F, int lo, int hi) {
 
 /* force_bp.F90:44-204 (model 1/3) and force_bp_triplet.F90:62-240 (model 4/5):
  * one record.  Returns true when the pair is formed (ene <= cutoff). */
-bool bp_one(const or_system *s, int irep, int ibp, double tK, double *F, double *ene_out, double (*fout)[3] = nullptr) {
+bool bp_one(const or_system *s, int irep, int ibp, double tK, double *F, double *ene_out, double (*fout)[3] = nullptr,
+            double *Fpull = nullptr) {
     const Rep &R = s->rep[irep];
     const int *rec = &R.bp_mp[7 * ibp];
     const int i1 = rec[0], i2 = rec[1], i3 = rec[2], i4 = rec[3], i5 = rec[4], i6 = rec[5];
@@ -875,7 +907,18 @@ bool bp_one(const or_system *s, int irep, int ibp, double tK, double *F, double 
     double d1212 = dot(v12, v12);
     double a12 = sqrt(d1212);
     double d = a12 - b.bond_r;
-    if (fabs(d) > b.cutoff_ddist) return false;
+    if (fabs(d) > b.cutoff_ddist) {
+        /* force_bp_triplet.F90:85-92 / force_bp_limit_triplet.F90:104-111: a
+         * constant pull of i toward j outside the distance window */
+        double *Fp = F ? F : Fpull;
+        if (s->bias_ss && triplet && Fp) {
+            double f[3];
+            for (int k = 0; k < 3; ++k) f[k] = s->bias_ss_force / a12 * v12[k];
+            addf(Fp, i1, f, -1.0);
+            addf(Fp, i2, f, 1.0);
+        }
+        return false;
+    }
     double u = b.bond_k * (d * d);
     for (int k = 0; k < 3; ++k) {
         fi[k] = (2.0 * b.bond_k * d / a12) * v12[k];
@@ -1009,7 +1052,7 @@ void bp_mc(or_system *s, int irep, double tK, double *F) {
     R.ene_bp.assign(nbp, 0.0);
     for (int ibp = 0; ibp < nbp; ++ibp) {
         double e;
-        if (bp_one(s, irep, ibp, tK, nullptr, &e, (double(*)[3]) & fr[(size_t)18 * ibp])) {
+        if (bp_one(s, irep, ibp, tK, nullptr, &e, (double(*)[3]) & fr[(size_t)18 * ibp], F)) {
             R.bp_status[ibp] = 1;
             R.ene_bp[ibp] = e;
             excess[R.bp_mp[7 * ibp] - 1]++;

@@ -66,7 +66,7 @@ class sis_stats(C.Structure):
         ("steps", C.c_int64), ("rebuilds", C.c_int64), ("pair_entries", C.c_int64), ("wca_pairs", C.c_int64),
         ("ele_pairs", C.c_int64), ("bp_pairs", C.c_int64), ("error_flags", C.c_int32), ("n_beads", C.c_int32),
         ("n_inst", C.c_int32), ("lanes_per_bead", C.c_int32), ("capped", C.c_int64),
-        ("bp_blocks", C.c_int32), ("overlap", C.c_int32),
+        ("bp_blocks", C.c_int32), ("overlap", C.c_int32), ("small_blocks", C.c_int32), ("small_threads", C.c_int32),
     ]
 
 
@@ -98,6 +98,9 @@ EXPORTS = {
     "sis_gpu_set_lanes": (C.c_int, [C.c_void_p, C.c_int32]),
     "sis_gpu_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
     "sis_gpu_set_overlap": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sis_gpu_set_small": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sis_gpu_set_ss_pairs": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "sis_gpu_set_bias_ss": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
     "sis_gpu_set_step": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sis_gpu_last_error": (C.c_char_p, [C.c_void_p]),
     "sis_gpu_event_record": (C.c_int, [C.c_void_p, C.c_int32]),

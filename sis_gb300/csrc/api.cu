@@ -124,6 +124,18 @@ struct sis_ctx {
     unsigned long long remd_ctr = 0;
     int n_vel_init = 0;
     bool tuned = false;
+    // per-block kernel of small instances (k_md_small): eligible by size and
+    // list kind (set at creation), the caller's mode, the bucket plan
+    // secondary structure per instance: allowed pairs (global beads, lo < hi)
+    std::vector<std::vector<int2>> ss_pairs;
+    int *ss_start_d = nullptr, *ss_part_d = nullptr;
+    bool small_ok = false;
+    int small_mode = -1;
+    bool small_tuned = false;
+    int small_threads = 256;
+    int *sp_off_d = nullptr, *sp_inst_d = nullptr;
+    SmallPlan sp{};
+    int sms = 152;
 };
 
 namespace {
@@ -601,6 +613,124 @@ int autotune(sis_ctx *ctx) {
     return SIS_OK;
 }
 
+// ------------------------------------------------------ small instances
+bool small_active(const sis_ctx *ctx) {
+    return ctx->small_ok && ctx->small_mode != 0 && ctx->g.nstep_mc == 0 && !ctx->g.flg_bias && !ctx->mc_pending;
+}
+
+// Buckets of whole instances for k_md_small: longest first into the bucket
+// with the fewest beads (at most kSmallMaxInst instances and kSmallMaxBeads
+// beads each), about `target` buckets; each bucket lists its instances in
+// ascending order.
+int small_plan(sis_ctx *ctx, int target) {
+    const int ni = ctx->n_inst;
+    std::vector<int> order(ni);
+    for (int k = 0; k < ni; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ctx->ip[a].n > ctx->ip[b].n; });
+    const int nbins = std::max(1, std::min(target, ni));
+    std::vector<std::vector<int>> bins(nbins);
+    std::vector<int> beads(nbins, 0);
+    for (int k : order) {
+        int best = -1;
+        for (int b = 0; b < (int)bins.size(); ++b)
+            if ((int)bins[b].size() < kSmallMaxInst && beads[b] + ctx->ip[k].n <= kSmallMaxBeads &&
+                (best < 0 || beads[b] < beads[best]))
+                best = b;
+        if (best < 0) {
+            bins.emplace_back();
+            beads.push_back(0);
+            best = (int)bins.size() - 1;
+        }
+        bins[best].push_back(k);
+        beads[best] += ctx->ip[k].n;
+    }
+    std::vector<int> off(1, 0), inst;
+    int cap = 1;
+    for (size_t b = 0; b < bins.size(); ++b) {
+        if (bins[b].empty()) continue;
+        std::sort(bins[b].begin(), bins[b].end());
+        inst.insert(inst.end(), bins[b].begin(), bins[b].end());
+        off.push_back((int)inst.size());
+        cap = std::max(cap, beads[b]);
+    }
+    CK(cudaMemcpyAsync(ctx->sp_off_d, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->sp_inst_d, inst.data(), sizeof(int) * inst.size(), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->sp.cta_off = ctx->sp_off_d;
+    ctx->sp.inst = ctx->sp_inst_d;
+    ctx->sp.n_cta = (int)off.size() - 1;
+    ctx->sp.cap = cap;
+    return SIS_OK;
+}
+
+// nsteps steps through k_md_small, at most kSmallChunk per launch; noise: the
+// device copy of fed noise (nsteps x n x 3) or NULL
+constexpr int kSmallChunk = 1000;
+int run_small(sis_ctx *ctx, int64_t nsteps, const double *noise) {
+    for (int64_t s = 0; s < nsteps;) {
+        const int chunk = (int)std::min<int64_t>(kSmallChunk, nsteps - s);
+        const double *nz = noise ? noise + (size_t)s * ctx->n * 3 : nullptr;
+        CK(launch_md_small(ctx->D, ctx->g, ctx->cur, ctx->sp, chunk, nz, ctx->small_threads, ctx->st));
+        CK(launch_cluster_flagged(ctx->D, ctx->g, ctx->st));
+        CK(launch_small_finish(ctx->D, ctx->g, (unsigned long long)chunk, ctx->st));
+        ctx->launches += 3;
+        ctx->cur ^= chunk & 1;
+        s += chunk;
+    }
+    return SIS_OK;
+}
+
+// Picks the bucket count and the block width of k_md_small by timing a few
+// real steps of each candidate; the per-bead arithmetic is the same for all,
+// so the steps are part of the trajectory.  Returns the steps it took.
+int64_t small_autotune(sis_ctx *ctx, int64_t budget, int *rc) {
+    *rc = SIS_OK;
+    const int sms = ctx->sms;
+    std::vector<int> targets;
+    for (int f : {1, 2, 3, 4}) {
+        const int t = std::min(ctx->n_inst, f * sms);
+        if (targets.empty() || targets.back() != t) targets.push_back(t);
+    }
+    const std::vector<int> widths = {128, 256, 512};
+    const int per = 8;
+    const int64_t need = (int64_t)(targets.size() * widths.size() + 1) * per;
+    if (budget < need) {
+        if (!ctx->sp.n_cta && (*rc = small_plan(ctx, std::min(ctx->n_inst, 2 * sms)))) return 0;
+        return 0;
+    }
+    float best = 1e30f;
+    int best_t = targets[0], best_w = widths[0];
+    int64_t taken = 0;
+    // the first pass warms up (list state, first-touch), untimed
+    if ((*rc = small_plan(ctx, targets[0]))) return taken;
+    ctx->small_threads = widths[0];
+    if ((*rc = run_small(ctx, per, nullptr))) return taken;
+    taken += per;
+    for (int t : targets) {
+        if ((*rc = small_plan(ctx, t))) return taken;
+        for (int w : widths) {
+            if (small_smem_bytes(ctx->sp.cap) > 200 * 1024) continue;
+            ctx->small_threads = w;
+            cudaEventRecord(ctx->ev[12], ctx->st);
+            if ((*rc = run_small(ctx, per, nullptr))) return taken;
+            cudaEventRecord(ctx->ev[13], ctx->st);
+            cudaEventSynchronize(ctx->ev[13]);
+            float ms = 1e30f;
+            cudaEventElapsedTime(&ms, ctx->ev[12], ctx->ev[13]);
+            taken += per;
+            if (ms < best) {
+                best = ms;
+                best_t = t;
+                best_w = w;
+            }
+        }
+    }
+    if ((*rc = small_plan(ctx, best_t))) return taken;
+    ctx->small_threads = best_w;
+    ctx->small_tuned = true;
+    return taken;
+}
+
 } // namespace
 
 namespace {
@@ -815,8 +945,10 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     {
         int dev = 0, sms = 0;
         if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
-            sms > 0)
+            sms > 0) {
             ctx->bpb = 2 * sms;
+            ctx->sms = sms;
+        }
         ctx->bpt = std::max(1, std::min((bp_total_cap + 255) / 256, 8 * (sms > 0 ? sms : 152)));
         // the trigger/rebuild kernel: two blocks per SM (fewer if they do not fit)
         const int per = std::min(2, coop_blocks_per_sm());
@@ -833,6 +965,14 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.mir[0], (size_t)n + kCl);
     rc |= dalloc(ctx, &D.mir[1], (size_t)n + kCl);
     if (p.precision != SIS_PREC_FP64) {
+        // the per-block kernel of small instances: every instance at most
+        // kSmallMaxBeads beads with an all-pairs list
+        ctx->small_ok = true;
+        for (int k = 0; k < ni; ++k) ctx->small_ok &= ctx->ip[k].n <= kSmallMaxBeads && !ctx->ip[k].large;
+        if (ctx->small_ok) {
+            rc |= dalloc(ctx, &ctx->sp_off_d, (size_t)ni + 1);
+            rc |= dalloc(ctx, &ctx->sp_inst_d, ni);
+        }
         rc |= dalloc(ctx, &D.mir0, n);
         rc |= dalloc(ctx, &D.cl_first, n_cl);
         rc |= dalloc(ctx, &D.ncl, n_cl);
@@ -1040,6 +1180,8 @@ extern "C" void sis_gpu_destroy(sis_ctx *ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
+    if (ctx->ss_start_d) cudaFree(ctx->ss_start_d);
+    if (ctx->ss_part_d) cudaFree(ctx->ss_part_d);
     if (ctx->bias_d) cudaFree(ctx->bias_d);
     delete ctx;
 }
@@ -1296,7 +1438,7 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     if (!ctx || nsteps < 0) return SIS_ERR_ARG;
     int rc = ensure_lists(ctx);
     if (rc) return rc;
-    if (!noise && nsteps >= 64 && (rc = autotune(ctx))) return rc;
+    if (!noise && nsteps >= 64 && !small_active(ctx) && (rc = autotune(ctx))) return rc;
     if (noise) {
         const size_t need = (size_t)nsteps * ctx->n * 3;
         if (need > ctx->noise_cap) {
@@ -1306,6 +1448,22 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
             ctx->noise_cap = need;
         }
         CK(cudaMemcpyAsync(ctx->noise_d, noise, sizeof(double) * need, cudaMemcpyHostToDevice, ctx->st));
+    }
+    if (small_active(ctx)) {
+        int64_t done = 0;
+        if (!noise && !ctx->small_tuned) {
+            done = small_autotune(ctx, nsteps, &rc);
+            if (rc) return rc;
+        } else if (!ctx->sp.n_cta && (rc = small_plan(ctx, std::min(ctx->n_inst, 2 * ctx->sms)))) {
+            return rc;
+        }
+        if ((rc = run_small(ctx, nsteps - done, noise ? ctx->noise_d + (size_t)done * ctx->n * 3 : nullptr))) return rc;
+        ctx->steps += nsteps;
+        ctx->bp_cache = true;
+        CK(cudaStreamSynchronize(ctx->st));
+        ctx->D.mc_draws = nullptr;
+        ctx->mc_pending = false;
+        return check_err(ctx);
     }
     int64_t s = 0;
     bool graphs = false;
@@ -1381,6 +1539,82 @@ extern "C" int sis_gpu_set_frozen(sis_ctx *ctx, int32_t inst, const int32_t *bea
     CK(cudaMemcpyAsync(ctx->D.mdc + I.bead_off, mdc.data() + I.bead_off, sizeof(double4) * I.n, cudaMemcpyHostToDevice,
                        ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    return SIS_OK;
+}
+
+// -------------------------------------------------- secondary structure
+namespace {
+// the partner table of every instance's allowed pairs (CSR over global beads)
+int upload_ss(sis_ctx *ctx) {
+    std::vector<std::vector<int>> part(ctx->n);
+    int any = 0;
+    for (int k = 0; k < ctx->n_inst; ++k) {
+        ctx->ip[k].ss_on = ctx->ss_pairs[k].empty() ? 0 : 1;
+        any |= ctx->ip[k].ss_on;
+        for (const int2 &pq : ctx->ss_pairs[k]) {
+            part[pq.x].push_back(pq.y);
+            part[pq.y].push_back(pq.x);
+        }
+    }
+    std::vector<int> start(ctx->n + 1, 0), flat;
+    for (int i = 0; i < ctx->n; ++i) {
+        std::sort(part[i].begin(), part[i].end());
+        part[i].erase(std::unique(part[i].begin(), part[i].end()), part[i].end());
+        start[i + 1] = start[i] + (int)part[i].size();
+        flat.insert(flat.end(), part[i].begin(), part[i].end());
+    }
+    if (ctx->ss_start_d) cudaFree(ctx->ss_start_d);
+    if (ctx->ss_part_d) cudaFree(ctx->ss_part_d);
+    ctx->ss_start_d = ctx->ss_part_d = nullptr;
+    CK(cudaMalloc(&ctx->ss_start_d, sizeof(int) * start.size()));
+    CK(cudaMalloc(&ctx->ss_part_d, sizeof(int) * std::max<size_t>(1, flat.size())));
+    CK(cudaMemcpy(ctx->ss_start_d, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice));
+    if (!flat.empty()) CK(cudaMemcpy(ctx->ss_part_d, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice));
+    ctx->D.ss_start = ctx->ss_start_d;
+    ctx->D.ss_part = ctx->ss_part_d;
+    ctx->g.any_ss = any;
+    return SIS_OK;
+}
+
+// base-pair list cutoff of every instance: (bp_cutoff_dist + margin)^2, or
+// with [Bias_SS] the reference's 9999999999.9 (a REAL(4) literal: 1e10)
+void bp_list_cut(sis_ctx *ctx) {
+    const double m = ctx->p.nl_margin;
+    for (int k = 0; k < ctx->n_inst; ++k)
+        ctx->ip[k].bp_nl_cut2 = ctx->g.flg_bias_ss ? (double)9999999999.9f : (ctx->bp_cutoff_dist + m) * (ctx->bp_cutoff_dist + m);
+}
+} // namespace
+
+extern "C" int sis_gpu_set_ss_pairs(sis_ctx *ctx, int32_t inst, int32_t n, const int32_t *pairs) {
+    DevGuard dg_(ctx);
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || n < 0 || (n > 0 && !pairs)) return SIS_ERR_ARG;
+    const InstP &I = ctx->ip[inst];
+    std::vector<int2> pq;
+    for (int q = 0; q < n; ++q) {
+        int i = pairs[2 * q], j = pairs[2 * q + 1];
+        if (i < 1 || j < 1 || i > I.n || j > I.n || i == j)
+            return fail(ctx, SIS_ERR_ARG, "set_ss_pairs: nucleotide number out of range");
+        if (j < i) std::swap(i, j);
+        pq.push_back(make_int2(I.bead_off + i - 1, I.bead_off + j - 1));
+    }
+    if (ctx->ss_pairs.size() != (size_t)ctx->n_inst) ctx->ss_pairs.assign(ctx->n_inst, {});
+    ctx->ss_pairs[inst] = pq;
+    int rc = upload_ss(ctx);
+    if (rc) return rc;
+    if ((rc = upload_ip(ctx))) return rc;
+    ctx->lists_valid = false;
+    return SIS_OK;
+}
+
+extern "C" int sis_gpu_set_bias_ss(sis_ctx *ctx, int32_t on, double force) {
+    DevGuard dg_(ctx);
+    if (!ctx || !std::isfinite(force) || force < 0.0) return SIS_ERR_ARG;
+    ctx->g.flg_bias_ss = on ? 1 : 0;
+    ctx->g.bias_ss_force = force;
+    bp_list_cut(ctx);
+    const int rc = upload_ip(ctx);
+    if (rc) return rc;
+    ctx->lists_valid = false;
     return SIS_OK;
 }
 
@@ -1535,6 +1769,13 @@ extern "C" int sis_gpu_set_overlap(sis_ctx *ctx, int32_t enable) {
     return SIS_OK;
 }
 
+extern "C" int sis_gpu_set_small(sis_ctx *ctx, int32_t mode) {
+    DevGuard dg_(ctx);
+    if (!ctx || mode < -1 || mode > 1) return SIS_ERR_ARG;
+    ctx->small_mode = mode;
+    return SIS_OK;
+}
+
 extern "C" int sis_gpu_probe_barrier_timeout(sis_ctx *ctx) {
     DevGuard dg_(ctx);
     if (!ctx) return SIS_ERR_ARG;
@@ -1553,6 +1794,8 @@ extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
     s->lanes_per_bead = ctx->G;
     s->bp_blocks = bp_blocks(ctx);
     s->overlap = ctx->overlap ? 1 : 0;
+    s->small_blocks = small_active(ctx) ? ctx->sp.n_cta : 0;
+    s->small_threads = small_active(ctx) ? ctx->small_threads : 0;
     long long rb = 0;
     unsigned long long cp = 0;
     int e = 0;
@@ -1695,10 +1938,12 @@ extern "C" int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const dou
     rc = ensure_lists(ctx);
     if (rc) return rc;
     const size_t per = (size_t)ctx->n * 3;
+    const bool small = small_active(ctx);
+    if (small && !ctx->sp.n_cta && (rc = small_plan(ctx, std::min(ctx->n_inst, 2 * ctx->sms)))) return rc;
     for (int64_t s = 0; s < nsteps; ++s) {
         // stream-ordered: the copy waits for the previous step's kernels
         CK(cudaMemcpyAsync(buf, noise + (size_t)s * per, sizeof(double) * per, cudaMemcpyHostToDevice, ctx->st));
-        rc = enqueue_step(ctx, buf, 0);
+        rc = small ? run_small(ctx, 1, buf) : enqueue_step(ctx, buf, 0);
         if (rc) return rc;
     }
     ctx->steps += nsteps;
@@ -1942,6 +2187,8 @@ extern "C" int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, in
     if (n_draws > 0) {
         if (n_draws > ctx->mc_draws_cap) {
             if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
+    if (ctx->ss_start_d) cudaFree(ctx->ss_start_d);
+    if (ctx->ss_part_d) cudaFree(ctx->ss_part_d);
             ctx->mc_draws_d = nullptr;
             if (cudaMalloc(&ctx->mc_draws_d, sizeof(double) * n_draws) != cudaSuccess) return fail(ctx, SIS_ERR_NOMEM, "bp_mc draws");
             ctx->mc_draws_cap = n_draws;

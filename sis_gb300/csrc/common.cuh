@@ -75,6 +75,13 @@ __device__ __forceinline__ long long fx_of(float v) {
     return (long long)__float2int_rz(h) * 2147483648LL + (long long)__float2int_rn(l);
 }
 __device__ __forceinline__ long long fx_of(double v) { return __double2ll_rn(v * 4294967296.0); }
+// exact, order-independent addition of a fixed-point force to bead i
+__device__ __forceinline__ void fx_scatter(double4 *fbp, int i, long long fx, long long fy, long long fz) {
+    unsigned long long *p = reinterpret_cast<unsigned long long *>(fbp + i);
+    atomicAdd(p + 0, (unsigned long long)fx);
+    atomicAdd(p + 1, (unsigned long long)fy);
+    atomicAdd(p + 2, (unsigned long long)fz);
+}
 // the fixed-point word as FP32 kcal/mol/A from 32-bit conversions only
 // (the high word scaled exactly, the low word rounded once)
 __device__ __forceinline__ float fx_float(double word) {
@@ -106,6 +113,9 @@ struct InstP {
     // Rg bias (force_rg.F90): rg_pott 0 off, 1 harmonic, 2 flat-bottomed
     int rg_pott;
     double rg_k, rg0;
+    // base pairs only between the pairs of a given secondary structure
+    // (read_ss.F90 bp_map): their records come from the partner table ss_*
+    int ss_on;
 };
 
 struct GlobP {
@@ -126,6 +136,10 @@ struct GlobP {
     // bias on some instance; restraint and trap items
     int flg_bias, flg_stage, flg_rg, n_bias;
     double stage_sigma, stage_eps;
+    // [Bias_SS] (force_bp_triplet.F90:85-92): a constant pull of an allowed
+    // pair outside its distance window; any_ss: some instance has a structure
+    int flg_bias_ss, any_ss;
+    double bias_ss_force;
 };
 
 // One sigmoid restraint or tweezers trap pair (force_restraint.F90,
@@ -225,7 +239,16 @@ struct Dev {
     const double *mc_draws; // caller-supplied uniforms for the next pass, or NULL (Philox)
     int *mc_draw_pos;       // [1] next caller-supplied uniform
     int mc_n_draws;
+    // secondary-structure partners: bead i's allowed partners (global bead
+    // indices, ascending) are ss_part[ss_start[i] .. ss_start[i+1])
+    const int *ss_start, *ss_part;
 };
+
+// buffer `cur` of the double-buffered arrays, as a select rather than an
+// indexed load, so that a copy of Dev made inside a kernel stays in registers
+__device__ __forceinline__ uint4 *mir_at(const Dev &D, int cur) { return cur ? D.mir[1] : D.mir[0]; }
+__device__ __forceinline__ float4 *res_at(const Dev &D, int cur) { return cur ? D.res[1] : D.res[0]; }
+__device__ __forceinline__ double4 *x_at(const Dev &D, int cur) { return cur ? D.x[1] : D.x[0]; }
 
 // ----------------------------------------------------------------- vectors
 template <typename R> struct V3 {

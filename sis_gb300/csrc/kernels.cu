@@ -18,6 +18,7 @@
 //             the lists of the instances that fired.
 #include "common.cuh"
 #include "kernels.h"
+#include "listcore.cuh"
 #include "terms.cuh"
 
 #include <algorithm>
@@ -25,8 +26,8 @@
 namespace sisg {
 
 template <typename R> __device__ __forceinline__ Pos<R> pos_of(const Dev &D, int cur);
-template <> __device__ __forceinline__ Pos<double> pos_of<double>(const Dev &D, int cur) { return Pos<double>{D.x[cur]}; }
-template <> __device__ __forceinline__ Pos<float> pos_of<float>(const Dev &D, int cur) { return Pos<float>{D.mir[cur]}; }
+template <> __device__ __forceinline__ Pos<double> pos_of<double>(const Dev &D, int cur) { return Pos<double>{x_at(D, cur)}; }
+template <> __device__ __forceinline__ Pos<float> pos_of<float>(const Dev &D, int cur) { return Pos<float>{mir_at(D, cur)}; }
 
 __device__ __forceinline__ double comp(const V3<double> &a, int c) { return c == 0 ? a.x : (c == 1 ? a.y : a.z); }
 
@@ -101,12 +102,12 @@ __device__ __forceinline__ bool bp_record(const Dev &D, int r, int total, int n_
 template <typename R> struct PosLd;
 template <> struct PosLd<float> {
     using T = uint4;
-    __device__ static T ld(const Dev &D, int cur, int i) { return __ldg(D.mir[cur] + i); }
+    __device__ static T ld(const Dev &D, int cur, int i) { return mir_at(D, cur)[i]; }
     __device__ static V3<float> sep(const T &a, const T &b, const InstP &ip) { return dvec32(a, b, ip); }
 };
 template <> struct PosLd<double> {
     using T = double4;
-    __device__ static T ld(const Dev &D, int cur, int i) { return D.x[cur][i]; }
+    __device__ static T ld(const Dev &D, int cur, int i) { return x_at(D, cur)[i]; }
     __device__ static V3<double> sep(const T &a, const T &b, const InstP &ip) { return dvec64(a, b, ip); }
 };
 
@@ -156,8 +157,8 @@ __device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int c
     }
     if constexpr (sizeof(R) == 4) {
         if (*angle_near || *dih_near) {
-            const uint4 *mr = D.mir[cur];
-            const float4 *rr = D.res[cur];
+            const uint4 *mr = mir_at(D, cur);
+            const float4 *rr = res_at(D, cur);
             const FxV a01 = fxv(mr, rr, s, q1), a21 = fxv(mr, rr, q2, q1);
             float s2;
             if (*angle_near) {
@@ -187,7 +188,7 @@ __device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, 
     const size_t pl = (size_t)g.n;
     const int4 bi = D.binfo[s];
     const InstP &ip = D.ip[bi.x];
-    const double4 *__restrict__ x64 = D.x[cur];
+    const double4 *__restrict__ x64 = x_at(D, cur);
     const int l = bi_lidx(bi);
     const int q1 = chain_bead(bi, l + 1), q2 = chain_bead(bi, l + 2), q3 = chain_bead(bi, l + 3);
     if (kind == 0) {
@@ -211,18 +212,69 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
     const int type = rec.z & 0xff;
     const InstP &ip = D.ip[rec.w];
     bool pass;
+    const bool triplet = g.bp_model == 4 || g.bp_model == 5;
     if (g.nstep_mc > 0 && !D.mc_due[rec.w] && !D.bp_mask[slot]) {
         // removed by the last Monte Carlo pass (force_bp_triplet.F90:64-66)
         pass = false;
+    } else if (g.flg_bias_ss && triplet) {
+        // [Bias_SS] (force_bp_triplet.F90:78-92, force_bp_limit_triplet.F90:
+        // 97-113): dG < 0 first, then the exact distance window, the test the
+        // evaluation repeats; outside it, a constant pull of i toward j
+        const int h = rec.z >> 8;
+        if constexpr (sizeof(R) == 4) pass = D.bp_dgf[rec.w * 469 + h] < 0.f;
+        else pass = __dsub_rn(D.bp3_dH[h], __dmul_rn(ip.tempK, D.bp3_dS[h])) < 0.0;
+        if (pass) {
+            double a12, fx, fy, fz;
+            bool out;
+            if constexpr (sizeof(R) == 4) {
+                const BPPf &bf = D.bppf[type];
+                const V3<float> v = dvec32(mir_at(D, cur)[rec.x], mir_at(D, cur)[rec.y], ip);
+                const float af = sqrtf(dot3(v, v));
+                out = fabsf(af - bf.bond_r) > bf.cutoff_ddist;
+                a12 = af;
+                fx = v.x, fy = v.y, fz = v.z;
+            } else {
+                const BPP &b = D.bpp[type];
+                const V3<double> v = dvec64(x_at(D, cur)[rec.x], x_at(D, cur)[rec.y], ip);
+                a12 = sqrt(dot3(v, v));
+                out = fabs(a12 - b.bond_r) > b.cutoff_ddist;
+                fx = v.x, fy = v.y, fz = v.z;
+            }
+            if (out) {
+                const double c = g.bias_ss_force / a12;
+                fx *= c;
+                fy *= c;
+                fz *= c;
+                if (g.prec == 0) {
+                    atomicAdd(&D.fbp[rec.x].x, -fx);
+                    atomicAdd(&D.fbp[rec.x].y, -fy);
+                    atomicAdd(&D.fbp[rec.x].z, -fz);
+                    atomicAdd(&D.fbp[rec.y].x, fx);
+                    atomicAdd(&D.fbp[rec.y].y, fy);
+                    atomicAdd(&D.fbp[rec.y].z, fz);
+                } else if (fabs(fx) < FX_LIMIT && fabs(fy) < FX_LIMIT && fabs(fz) < FX_LIMIT) {
+                    fx_scatter(D.fbp, rec.x, -fx_of(fx), -fx_of(fy), -fx_of(fz));
+                    fx_scatter(D.fbp, rec.y, fx_of(fx), fx_of(fy), fx_of(fz));
+                } else {
+                    atomicOr(D.err, ERR_NONFINITE);
+                }
+                pass = false;
+            }
+        }
+        if (!pass) {
+            D.ene_bp[slot] = 0.0;
+            D.bp_status[slot] = 0;
+        }
+        return pass;
     } else if constexpr (sizeof(R) == 4) {
         const BPPf &bf = D.bppf[type];
-        const V3<float> v = dvec32(D.mir[cur][rec.x], D.mir[cur][rec.y], ip);
+        const V3<float> v = dvec32(mir_at(D, cur)[rec.x], mir_at(D, cur)[rec.y], ip);
         const float d2 = fmaf(v.x, v.x, fmaf(v.y, v.y, v.z * v.z));
         // window widened by 1e-5 relative; the exact test follows
         pass = d2 >= bf.lo2 * 0.99999f && d2 <= bf.hi2 * 1.00001f;
     } else {
         const BPP &b = D.bpp[type];
-        const V3<double> v = dvec64(D.x[cur][rec.x], D.x[cur][rec.y], ip);
+        const V3<double> v = dvec64(x_at(D, cur)[rec.x], x_at(D, cur)[rec.y], ip);
         pass = fabs(sqrt(dot3(v, v)) - b.bond_r) <= b.cutoff_ddist;
     }
     if (pass && (g.bp_model == 4 || g.bp_model == 5)) {
@@ -243,15 +295,9 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
 // contributions with exp(-u) < 2e-9 (u > 20) are not scattered (their forces
 // are below the FP32 rounding of the remaining terms) but their energy is
 // still cached, and forces go to fbp as fixed point.
-__device__ __forceinline__ void fx_scatter(const Dev &D, int i, long long fx, long long fy, long long fz) {
-    unsigned long long *p = reinterpret_cast<unsigned long long *>(D.fbp + i);
-    atomicAdd(p + 0, (unsigned long long)fx);
-    atomicAdd(p + 1, (unsigned long long)fy);
-    atomicAdd(p + 2, (unsigned long long)fz);
-}
 
 __device__ __forceinline__ void bp_finish(const Dev &D, const GlobP &g, int slot, const int4 &rec, const int4 &nb, double dG,
-                                          const V3<double> *fd, double ud, bool ok, bool scatter_all) {
+                                          const V3<double> *fd, double ud, bool ok, bool scatter_all, double4 *fbp) {
     const int type = rec.z & 0xff;
     const bool triplet = g.bp_model == 4 || g.bp_model == 5;
     double ene = 0.0;
@@ -285,16 +331,16 @@ __device__ __forceinline__ void bp_finish(const Dev &D, const GlobP &g, int slot
 #pragma unroll
                 for (int q = 0; q < 6; ++q) {
                     if (g.prec == 0) {
-                        atomicAdd(&D.fbp[ids[q]].x, e * fd[q].x);
-                        atomicAdd(&D.fbp[ids[q]].y, e * fd[q].y);
-                        atomicAdd(&D.fbp[ids[q]].z, e * fd[q].z);
+                        atomicAdd(&fbp[ids[q]].x, e * fd[q].x);
+                        atomicAdd(&fbp[ids[q]].y, e * fd[q].y);
+                        atomicAdd(&fbp[ids[q]].z, e * fd[q].z);
                     } else {
                         const V3<double> c = e * fd[q];
                         if (!(fabs(c.x) < FX_LIMIT && fabs(c.y) < FX_LIMIT && fabs(c.z) < FX_LIMIT)) {
                             atomicOr(D.err, ERR_NONFINITE);
                             continue;
                         }
-                        fx_scatter(D, ids[q], fx_of(c.x), fx_of(c.y), fx_of(c.z));
+                        fx_scatter(fbp, ids[q], fx_of(c.x), fx_of(c.y), fx_of(c.z));
                     }
                 }
             }
@@ -311,8 +357,9 @@ __device__ __forceinline__ double bp_dG(const Dev &D, const GlobP &g, const int4
 }
 
 // FP64 evaluation (FP64 path, and records flagged near +-1 by the FP32 path)
-__device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, int slot) {
-    const double4 *__restrict__ x64 = D.x[cur];
+// fbp: the scatter target (the context's fbp, or a block's shared copy)
+__device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, int slot, double4 *fbp) {
+    const double4 *__restrict__ x64 = x_at(D, cur);
     const int4 rec = D.bps[slot];
     const int4 nb = D.bps_n[slot];
     const InstP &ip = D.ip[rec.w];
@@ -322,7 +369,7 @@ __device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, in
     const bool ok = bp_force_core<double, BPP>(dvec64(x64[rec.x], x64[rec.y], ip), dvec64(x64[rec.x], x64[nb.x], ip),
                                                dvec64(x64[rec.x], x64[nb.z], ip), dvec64(x64[nb.y], x64[rec.y], ip),
                                                dvec64(x64[nb.w], x64[rec.y], ip), D.bpp[rec.z & 0xff], fd, &ud, &nr);
-    bp_finish(D, g, slot, rec, nb, bp_dG(D, g, rec), fd, ud, ok, g.prec == 0);
+    bp_finish(D, g, slot, rec, nb, bp_dG(D, g, rec), fd, ud, ok, g.prec == 0, fbp);
 }
 
 // FP32 evaluation.  A record with a bond angle within 0.03 rad of 0 or 180
@@ -331,7 +378,7 @@ __device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, in
 // 1e-6 rad does it return true (writing nothing), so that the caller redoes
 // the record in FP64.
 __device__ __forceinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, int slot) {
-    const uint4 *__restrict__ m = D.mir[cur];
+    const uint4 *__restrict__ m = mir_at(D, cur);
     const int4 rec = D.bps[slot];
     const int4 nb = D.bps_n[slot];
     const InstP &ip = D.ip[rec.w];
@@ -344,7 +391,7 @@ __device__ __forceinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur,
                     v62 = dvec32(m[nb.w], m[rec.y], ip);
     bool ok = bp_force_core_f(v12, v13, v15, v42, v62, bf, nullptr, f, &u, &nr);
     if (ok && nr) {
-        const float4 *r = D.res[cur];
+        const float4 *r = res_at(D, cur);
         const FxV a12 = fxv(m, r, rec.x, rec.y);
         const V3<float> cc[4] = {cross_fx(a12, fxv(m, r, rec.x, nb.x), ip), cross_fx(a12, fxv(m, r, rec.x, nb.z), ip),
                                  cross_fx(fxv(m, r, nb.y, rec.y), a12, ip), cross_fx(fxv(m, r, nb.w, rec.y), a12, ip)};
@@ -383,7 +430,7 @@ __device__ __forceinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur,
                     atomicOr(D.err, ERR_NONFINITE);
                     continue;
                 }
-                fx_scatter(D, ids[q], fx_of(cx), fx_of(cy), fx_of(cz));
+                fx_scatter(D.fbp, ids[q], fx_of(cx), fx_of(cy), fx_of(cz));
             }
         }
     }
@@ -428,7 +475,7 @@ template <typename R> __device__ __forceinline__ void bp_eval(const Dev &D, cons
     if constexpr (sizeof(R) == 4) {
         if (bp_eval_f(D, g, cur, slot)) D.bp_fixq[atomicAdd(D.bp_fixn, 1)] = slot;
     } else {
-        bp_eval_d(D, g, cur, slot);
+        bp_eval_d(D, g, cur, slot, D.fbp);
     }
 }
 
@@ -459,7 +506,7 @@ template <typename R> __global__ void __launch_bounds__(256) k_bp_eval(Dev D, Gl
     __threadfence();
     if constexpr (sizeof(R) == 4) {
         const int nf = *(volatile int *)D.bp_fixn;
-        for (int k = threadIdx.x; k < nf; k += blockDim.x) bp_eval_d(D, g, cur, D.bp_fixq[k]);
+        for (int k = threadIdx.x; k < nf; k += blockDim.x) bp_eval_d(D, g, cur, D.bp_fixq[k], D.fbp);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -598,7 +645,7 @@ template <typename R> __global__ void __launch_bounds__(256) k_bp_mc(Dev D, Glob
         const long long *fr = D.bp_frec + (size_t)slot * 18;
         for (int b = 0; b < 6; ++b) {
             if constexpr (sizeof(R) == 4) {
-                fx_scatter(D, ids[b], fr[3 * b], fr[3 * b + 1], fr[3 * b + 2]);
+                fx_scatter(D.fbp, ids[b], fr[3 * b], fr[3 * b + 1], fr[3 * b + 2]);
             } else {
                 atomicAdd(&D.fbp[ids[b]].x, __longlong_as_double(fr[3 * b]));
                 atomicAdd(&D.fbp[ids[b]].y, __longlong_as_double(fr[3 * b + 1]));
@@ -622,7 +669,7 @@ cudaError_t launch_bp_mc(const Dev &D, const GlobP &g, cudaStream_t st) {
 // energy_bp.F90 / energy_bp_triplet.F90 for every record at temperature tK
 // (tK < 0: each instance's own): clamped angles, FP64 from the FP64 positions.
 __global__ void __launch_bounds__(256) k_bp_energy(Dev D, GlobP g, int cur, double tK_in) {
-    const double4 *__restrict__ x64 = D.x[cur];
+    const double4 *__restrict__ x64 = x_at(D, cur);
     const int total = *D.bp_total;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < total; r += gridDim.x * blockDim.x) {
         int slot;
@@ -698,8 +745,8 @@ __device__ __forceinline__ V3<R> pair_sum(const Dev &D, const GlobP &g, int cur,
     const int cnt = min(D.nnbr[i], g.cap);
     const int *__restrict__ nb = D.nbr + (size_t)i * g.cap;
     if constexpr (sizeof(R) == 4) {
-        const uint4 mi = D.mir[cur][i];
-        const uint4 *__restrict__ mir = D.mir[cur];
+        const uint4 mi = mir_at(D, cur)[i];
+        const uint4 *__restrict__ mir = mir_at(D, cur);
         const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
         const float sig2 = g.f_wca_sig2, wcoef = g.f_wca_coef;
         const float ecoef = ip.ele_coef_f, rc = ip.rcdist_f;
@@ -750,8 +797,8 @@ __device__ __forceinline__ V3<R> pair_sum_b(const Dev &D, const GlobP &g, int cu
     const int cnt = min(D.nnbr[i], g.cap);
     const int *__restrict__ nb = D.nbr + (size_t)i * g.cap;
     if constexpr (sizeof(R) == 4) {
-        const uint4 mi = D.mir[cur][i];
-        const uint4 *__restrict__ mir = D.mir[cur];
+        const uint4 mi = mir_at(D, cur)[i];
+        const uint4 *__restrict__ mir = mir_at(D, cur);
         const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
         const float sig2 = g.f_wca_sig2, wcoef = g.f_wca_coef;
         const float ecoef = ip.ele_coef_f, rc = ip.rcdist_f;
@@ -805,6 +852,38 @@ __device__ __forceinline__ V3<R> pair_sum_b(const Dev &D, const GlobP &g, int cu
         }
     }
     return an;
+}
+
+// The bonded forces on bead (bi) from the slot planes k_bonded wrote: the 9
+// contributions (bond l-1|l, l|l+1; angles starting at l-2, l-1, l;
+// dihedrals starting at l-3 .. l), lane `lane` of G taking every G-th
+template <typename R>
+__device__ __forceinline__ V3<R> bonded_gather(const Dev &D, const GlobP &g, const int4 &bi, int lane, int G, int mask) {
+    using V4 = typename Vec4<R>::type;
+    const V4 *__restrict__ S = (const V4 *)D.slot;
+    const int l = bi_lidx(bi);
+    V3<R> ab = mk<R>(0, 0, 0);
+    for (int t = lane; t < 9; t += G) {
+        int start, k, cls;
+        R sgn = R(1);
+        if (t < 2) {
+            cls = 1;
+            start = l - 1 + t;
+            k = 0;
+            if (t == 1) sgn = R(-1);
+        } else if (t < 5) {
+            cls = 2;
+            start = l - 2 + (t - 2);
+            k = 1 + (2 - (t - 2));
+        } else {
+            cls = 4;
+            start = l - 3 + (t - 5);
+            k = 4 + (3 - (t - 5));
+        }
+        const int q = chain_bead(bi, start);
+        if ((mask & cls) && q >= 0) ab = ab + sgn * v3(S[(size_t)k * g.n + q]);
+    }
+    return ab;
 }
 
 // Pair forces of every bead into fpair (float4 / double4), the step kernel's
@@ -868,7 +947,7 @@ __global__ void __launch_bounds__(256) k_pairs_cl(Dev D, GlobP g, int cur, int m
     const int first = D.cl_first[ic];
     const InstP &ip = D.ip[D.binfo[first].x];
     const int cnt = min(kCl, ip.bead_off + ip.n - first);
-    const uint4 *__restrict__ mir = D.mir[cur];
+    const uint4 *__restrict__ mir = mir_at(D, cur);
     const uint4 mi = mir[first + (a < cnt ? a : 0)];
     const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
     PairCoef P;
@@ -938,6 +1017,40 @@ __global__ void __launch_bounds__(256) k_pairs_cl(Dev D, GlobP g, int cur, int m
     if (q == 0 && a < cnt) reinterpret_cast<float4 *>(D.fpair)[first + a] = make_float4(ax, ay, az, 0.f);
 }
 
+// One component c of bead ii of the mixed path's GJF-2GJ / Ermak-McCammon
+// update (job_md.F90:415-456): the force F and the noise enter as FP32
+// increments (cf: the force and noise coefficients of mdc in FP32), the
+// velocity and the position accumulate in FP64; writes the new position,
+// velocity, noise term, mirror and residual (buffer cur ^ 1) and returns the
+// new mirror component (r: its residual).
+__device__ __forceinline__ unsigned int mixed_update(const Dev &D, const GlobP &g, int cur, int ii, int c, float F, float cf0,
+                                                     float cf1, const double *noise, long long noise_step,
+                                                     unsigned long long step, float &r) {
+    const InstP &jp = D.ip[D.binfo[ii].x];
+    const float xi = noise ? (float)noise[((size_t)noise_step * g.n + ii) * 3 + c]
+                           : gauss_f(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
+    double *vp = reinterpret_cast<double *>(D.v + ii) + c;
+    double *bp = reinterpret_cast<double *>(D.beta + ii) + c;
+    double dx;
+    if (g.integrator == 1) {
+        const double4 m = D.mdc[ii];
+        const float bn = cf1 * xi;
+        const double vn = fma(m.x, *vp, *bp) + (double)fmaf(cf0, F, bn);
+        *bp = (double)bn;
+        *vp = vn;
+        dx = m.z * vn;
+    } else {
+        dx = (double)fmaf(cf0, F, cf1 * xi);
+    }
+    const double xn = reinterpret_cast<const double *>(x_at(D, cur) + ii)[c] + dx;
+    unsigned int qm;
+    if (!fixed_mirror(xn, jp.fsc[c], qm, r)) atomicOr(D.err, ERR_NONFINITE);
+    reinterpret_cast<double *>(x_at(D, cur ^ 1) + ii)[c] = xn;
+    reinterpret_cast<unsigned int *>(mir_at(D, cur ^ 1) + ii)[c] = qm;
+    reinterpret_cast<float *>(res_at(D, cur ^ 1) + ii)[c] = r;
+    return qm;
+}
+
 template <typename R, int G, int MODE>
 __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
                                               double *__restrict__ fout, int mask) {
@@ -981,33 +1094,7 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
         an = pair_sum<R, G>(D, g, cur, i, lane, ip, mask);
     }
     // bonded: gather of slot forces, 9 contributions spread over the lanes
-    V3<R> ab = mk<R>(0, 0, 0);
-    if (mask & 7) {
-        using V4 = typename Vec4<R>::type;
-        const V4 *__restrict__ S = (const V4 *)D.slot;
-        const int l = bi_lidx(bi);
-        for (int t = lane; t < 9; t += G) {
-            // t: 0 bond(l-1,l) 1 bond(l,l+1) 2 angle@l-2 3 angle@l-1 4 angle@l 5..8 dihedral@l-3..l
-            int start, k, cls;
-            R sgn = R(1);
-            if (t < 2) {
-                cls = 1;
-                start = l - 1 + t;
-                k = 0;
-                if (t == 1) sgn = R(-1);
-            } else if (t < 5) {
-                cls = 2;
-                start = l - 2 + (t - 2);
-                k = 1 + (2 - (t - 2));
-            } else {
-                cls = 4;
-                start = l - 3 + (t - 5);
-                k = 4 + (3 - (t - 5));
-            }
-            const int q = chain_bead(bi, start);
-            if ((mask & cls) && q >= 0) ab = ab + sgn * v3(S[(size_t)k * g.n + q]);
-        }
-    }
+    V3<R> ab = (mask & 7) ? bonded_gather<R>(D, g, bi, lane, G, mask) : mk<R>(0, 0, 0);
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
         an.x += __shfl_xor_sync(0xffffffffu, an.x, o, G);
@@ -1074,31 +1161,8 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
                 continue;
             }
             F *= sScale[bb];
-            const int4 bj = D.binfo[ii];
-            const InstP &jp = D.ip[bj.x];
-            const float xi = noise ? (float)noise[((size_t)noise_step * g.n + ii) * 3 + c]
-                                   : gauss_f(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
-            double *vp = reinterpret_cast<double *>(D.v + ii) + c;
-            double *bp = reinterpret_cast<double *>(D.beta + ii) + c;
-            double dx;
-            if (g.integrator == 1) {
-                const double4 m = D.mdc[ii];
-                const float bn = sCf[1][bb] * xi;
-                const double vn = fma(m.x, *vp, *bp) + (double)fmaf(sCf[0][bb], F, bn);
-                *bp = (double)bn;
-                *vp = vn;
-                dx = m.z * vn;
-            } else {
-                dx = (double)fmaf(sCf[0][bb], F, sCf[1][bb] * xi);
-            }
-            const double xn = reinterpret_cast<const double *>(D.x[cur] + ii)[c] + dx;
-            unsigned int qm;
             float r;
-            if (!fixed_mirror(xn, jp.fsc[c], qm, r)) atomicOr(D.err, ERR_NONFINITE);
-            reinterpret_cast<double *>(D.x[cur ^ 1] + ii)[c] = xn;
-            reinterpret_cast<unsigned int *>(D.mir[cur ^ 1] + ii)[c] = qm;
-            reinterpret_cast<float *>(D.res[cur ^ 1] + ii)[c] = r;
-            sQ[c][bb] = qm;
+            sQ[c][bb] = mixed_update(D, g, cur, ii, c, F, sCf[0][bb], sCf[1][bb], noise, noise_step, step, r);
             continue;
         } else {
             double Fc;
@@ -1131,15 +1195,15 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
             } else {
                 dx = m.x * Fc + m.w * xi;
             }
-            const double xn = reinterpret_cast<const double *>(D.x[cur] + ii)[c] + dx;
+            const double xn = reinterpret_cast<const double *>(x_at(D, cur) + ii)[c] + dx;
             if (!isfinite(xn)) atomicOr(D.err, ERR_NONFINITE);
             const double mc = *mp + dx;
             *mp = mc;
             sM[c][bb] = mc;
-            reinterpret_cast<double *>(D.x[cur ^ 1] + ii)[c] = xn;
+            reinterpret_cast<double *>(x_at(D, cur ^ 1) + ii)[c] = xn;
             float r;
-            reinterpret_cast<unsigned int *>(D.mir[cur ^ 1] + ii)[c] = fixed_res(xn, jp.fsc[c], r);
-            reinterpret_cast<float *>(D.res[cur ^ 1] + ii)[c] = r;
+            reinterpret_cast<unsigned int *>(mir_at(D, cur ^ 1) + ii)[c] = fixed_res(xn, jp.fsc[c], r);
+            reinterpret_cast<float *>(res_at(D, cur ^ 1) + ii)[c] = r;
         }
     }
     if (MODE == 1) return;
@@ -1195,6 +1259,264 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     }
 }
 
+// ======================================================== small instances
+// k_md_small: nsteps MD steps of the mixed path in one launch, for contexts
+// whose instances are all small (all-pairs lists, at most kSmallMaxBeads
+// beads).  Each block owns a bucket of whole instances (SmallPlan), keeps
+// their position mirrors, residuals, base-pair force sums and step forces in
+// shared memory, and runs every phase of every step for them with block
+// barriers only: base-pair terms (one thread per record), bonded terms (one
+// thread per term start), pair forces over the per-bead lists (one thread
+// per bead, partners' mirrors gathered from shared memory), the update (one
+// thread per bead component), the displacement trigger of each instance and,
+// for the instances whose trigger fired, their all-pairs list rebuild (one
+// warp per bead).  Blocks never wait on one another.  The per-bead
+// arithmetic does not depend on how instances are bucketed or how many
+// threads a block has, so every plan gives the same trajectory bit for bit.
+// The FP64 state (x, v, beta), the lists and the base-pair records stay in
+// global memory, current after every step, for the other entry points.
+// One thread per bead walks the bead's whole list in order: a partner beyond
+// every cutoff adds an exact zero, so the sum does not depend on when the
+// list was last rebuilt (a restarted run continues bit for bit).
+constexpr int kSmallLanes = 1;
+
+// the context as seen by one instance of a bucket: its beads' mirrors,
+// residuals and base-pair force sums at their shared-memory slots, addressed
+// by global bead index (sb: the instance's first slot, off: its first bead)
+// (both buffers name the shared copy: the block keeps one mirror)
+__device__ __forceinline__ Dev small_view(const Dev &D, uint4 *s_mir, float4 *s_res, double4 *s_fbp, int sb, int off) {
+    Dev E = D;
+    E.mir[0] = E.mir[1] = s_mir + (sb - off);
+    E.res[0] = E.res[1] = s_res + (sb - off);
+    E.fbp = s_fbp + (sb - off);
+    return E;
+}
+
+// bucket-local instance of slot s (s_sb: the instances' first slots, ascending)
+__device__ __forceinline__ int small_inst(const int *s_sb, int ni, int s) {
+    int lo = 0, hi = ni - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_sb[mid] <= s) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, SmallPlan sp, int nsteps, const double *noise) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    const int cap = sp.cap;
+    uint4 *s_mir = (uint4 *)s_dyn;
+    float4 *s_res = (float4 *)(s_mir + cap);
+    double4 *s_fbp = (double4 *)(s_res + cap);
+    float4 *s_F = (float4 *)(s_fbp + cap);   // force of the step (xyz) and the force coefficient (w)
+    float *s_cn = (float *)(s_F + cap);      // noise coefficient
+    __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst];
+    __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
+    __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
+    __shared__ int s_fire[kSmallMaxInst];
+    __shared__ int s_any;
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+    const int k0 = sp.cta_off[blockIdx.x], ni = sp.cta_off[blockIdx.x + 1] - k0;
+    if (tid == 0) {
+        int sb = 0, nbp = 0;
+        for (int q = 0; q < ni; ++q) {
+            const int id = sp.inst[k0 + q];
+            const InstP &ip = D.ip[id];
+            s_iid[q] = id;
+            s_off[q] = ip.bead_off;
+            s_n[q] = ip.n;
+            s_sb[q] = sb;
+            s_bp[q] = nbp;
+            sb += ip.n;
+            nbp += min(D.bp_cnt[id], ip.bp_cap);
+        }
+        s_sb[ni] = sb;
+        s_bp[ni] = nbp;
+    }
+    __syncthreads();
+    const int nb = s_sb[ni];
+    for (int s = tid; s < nb; s += nt) {
+        const int q = small_inst(s_sb, ni, s);
+        const int gi = s_off[q] + (s - s_sb[q]);
+        s_mir[s] = mir_at(D, cur)[gi];
+        s_res[s] = res_at(D, cur)[gi];
+    }
+    const unsigned long long step0 = *D.step_ctr;
+    for (int st = 0; st < nsteps; ++st) {
+        // ------------------------------------------------ base pairs and bonded
+        for (int s = tid; s < nb; s += nt) s_fbp[s] = make_double4(0.0, 0.0, 0.0, 0.0);
+        if (tid < ni) s_m1[tid] = s_m2[tid] = 0u;
+        if (tid == 0) s_any = 0;
+        __syncthreads();
+        if (g.bp_model > 0)
+            for (int r = tid; r < s_bp[ni]; r += nt) {
+                const int q = small_inst(s_bp, ni, r);
+                const int slot = D.ip[s_iid[q]].bp_off + (r - s_bp[q]);
+                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+                if (bp_test<float>(E, g, cur, slot) && bp_eval_f(E, g, cur, slot)) bp_eval_d(D, g, cur, slot, E.fbp);
+            }
+        for (int s = tid; s < nb; s += nt) {
+            const int q = small_inst(s_sb, ni, s);
+            const int gi = s_off[q] + (s - s_sb[q]);
+            const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+            bool an, dn;
+            bonded_terms<float>(E, g, cur, gi, &an, &dn);
+            if (an) bonded_fp64(D, g, cur, gi, 0);
+            if (dn) bonded_fp64(D, g, cur, gi, 1);
+        }
+        __syncthreads();
+        // ------------------------------------------------ pair forces and sums
+        {
+            constexpr int BPW = 32 / kSmallLanes; // beads per warp and pass
+            const int sub = lane & (kSmallLanes - 1);
+            for (int base = warp * BPW; base < nb; base += nwarps * BPW) {
+                // every lane of a warp runs the same passes (shuffles below)
+                const int s0 = base + lane / kSmallLanes;
+                const int s = min(s0, nb - 1);
+                const int q = small_inst(s_sb, ni, s);
+                const int off = s_off[q], sb = s_sb[q];
+                const int gi = off + (s - sb);
+                const int4 bi = D.binfo[gi];
+                const InstP &ip = D.ip[bi.x];
+                const uint4 mi = s_mir[s];
+                PairCoef P;
+                P.sig2 = g.f_wca_sig2;
+                P.wcoef = g.f_wca_coef;
+                P.ecoef = ip.ele_coef_f;
+                P.rc = ip.rcdist_f;
+                P.cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+                const int m = min(D.nnbr[gi], g.cap);
+                const int *__restrict__ nbl = D.nbr + (size_t)gi * g.cap;
+                V3<float> an = mk<float>(0.f, 0.f, 0.f);
+                for (int k = sub; k < m; k += kSmallLanes) {
+                    const int e = __ldg(nbl + k);
+                    const uint4 mj = s_mir[sb + (e & IDX_MASK) - off];
+                    const float vx = (float)(int)(mi.x - mj.x) * ip.finv[0];
+                    const float vy = (float)(int)(mi.y - mj.y) * ip.finv[1];
+                    const float vz = (float)(int)(mi.z - mj.z) * ip.finv[2];
+                    const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+                    const float c = pair_c(e & WCA_BIT, e & ELE_BIT, d2, P);
+                    an.x = fmaf(c, vx, an.x);
+                    an.y = fmaf(c, vy, an.y);
+                    an.z = fmaf(c, vz, an.z);
+                }
+                V3<float> ab = bonded_gather<float>(D, g, bi, sub, kSmallLanes, 7);
+#pragma unroll
+                for (int o = kSmallLanes / 2; o > 0; o >>= 1) {
+                    an.x += __shfl_xor_sync(0xffffffffu, an.x, o, kSmallLanes);
+                    an.y += __shfl_xor_sync(0xffffffffu, an.y, o, kSmallLanes);
+                    an.z += __shfl_xor_sync(0xffffffffu, an.z, o, kSmallLanes);
+                    ab.x += __shfl_xor_sync(0xffffffffu, ab.x, o, kSmallLanes);
+                    ab.y += __shfl_xor_sync(0xffffffffu, ab.y, o, kSmallLanes);
+                    ab.z += __shfl_xor_sync(0xffffffffu, ab.z, o, kSmallLanes);
+                }
+                if (sub == 0 && s0 < nb) {
+                    const double4 fb = s_fbp[s];
+                    float fx = an.x + ab.x + fx_float(fb.x), fy = an.y + ab.y + fx_float(fb.y), fz = an.z + ab.z + fx_float(fb.z);
+                    if (g.fcap > 0.0) {
+                        const float fm = sqrtf(fx * fx + fy * fy + fz * fz);
+                        if (fm > (float)g.fcap) {
+                            const float sc = (float)g.fcap / fm;
+                            fx *= sc;
+                            fy *= sc;
+                            fz *= sc;
+                            atomicAdd(D.capped, 1ull);
+                        }
+                    }
+                    const double4 mc = D.mdc[gi];
+                    s_F[s] = make_float4(fx, fy, fz, (float)(g.integrator == 1 ? mc.y : mc.x));
+                    s_cn[s] = (float)mc.w;
+                }
+            }
+        }
+        __syncthreads();
+        // ------------------------------------------------ update
+        const unsigned long long step = step0 + (unsigned long long)st;
+        for (int t = tid; t < 3 * nb; t += nt) {
+            const int s = t / 3, c = t - 3 * s;
+            const int q = small_inst(s_sb, ni, s);
+            const int gi = s_off[q] + (s - s_sb[q]);
+            const float4 F = s_F[s];
+            float r;
+            const unsigned int qm = mixed_update(D, g, cur, gi, c, c == 0 ? F.x : (c == 1 ? F.y : F.z), F.w, s_cn[s], noise, st, step, r);
+            reinterpret_cast<unsigned int *>(s_mir + s)[c] = qm;
+            reinterpret_cast<float *>(s_res + s)[c] = r;
+        }
+        __syncthreads();
+        // ------------------------------------------------ trigger (job_md.F90:376-395)
+        for (int s = tid; s < nb; s += nt) {
+            const int q = small_inst(s_sb, ni, s);
+            const int gi = s_off[q] + (s - s_sb[q]);
+            const uint4 m0 = D.mir0[gi], m1 = s_mir[s];
+            const float *fi = D.ip[s_iid[q]].finv;
+            const float dx = (float)(int)(m1.x - m0.x) * fi[0];
+            const float dy = (float)(int)(m1.y - m0.y) * fi[1];
+            const float dz = (float)(int)(m1.z - m0.z) * fi[2];
+            const unsigned int bits = __float_as_uint(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            const unsigned int old = atomicMax(&s_m1[q], bits);
+            atomicMax(&s_m2[q], old < bits ? old : bits);
+        }
+        __syncthreads();
+        if (tid < ni) {
+            const bool f = sqrtf(__uint_as_float(s_m1[tid])) + sqrtf(__uint_as_float(s_m2[tid])) > (float)g.nl_margin;
+            s_fire[tid] = f;
+            if (f) {
+                s_any = 1;
+                D.bp_cnt[s_iid[tid]] = 0;
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+        if (s_any) {
+            // ------------------------------------------------ rebuild (neighbor_list.F90)
+            for (int q = 0; q < ni; ++q) {
+                if (!s_fire[q]) continue;
+                const int id = s_iid[q], off = s_off[q];
+                const InstP &ip = D.ip[id];
+                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], off);
+                const float maxcut2f = scan_cut2f(ip, 1.001f);
+                for (int li = warp; li < ip.n; li += nwarps) {
+                    const int gi = off + li;
+                    double4 xi_w;
+                    bead_begin(E, cur, gi, ip, lane, xi_w);
+                    const int4 bii = D.binfo[gi];
+                    const uint4 mi = s_mir[s_sb[q] + li];
+                    int count = 0;
+                    for (int jb = 0; jb < ip.n; jb += 32) {
+                        const int lj = jb + lane;
+                        int f = 0;
+                        const int gj = off + lj;
+                        if (lj < ip.n && lj != li) f = test_pair(E, g, ip, cur, gi, bii, mi, xi_w, gj, maxcut2f, id);
+                        warp_append(D, g, gi, lane, f, gj, count);
+                    }
+                    bead_end(D, g, gi, lane, count);
+                }
+            }
+            __syncthreads();
+            if (g.any_ss)
+                for (int q = 0; q < ni; ++q)
+                    if (s_fire[q] && D.ip[s_iid[q]].ss_on)
+                        for (int li = tid; li < s_n[q]; li += nt) ss_records(D, g, cur, s_off[q] + li, s_iid[q]);
+            __syncthreads();
+            if (tid == 0) {
+                int nbp = 0, nfired = 0;
+                for (int q = 0; q < ni; ++q) {
+                    s_bp[q] = nbp;
+                    nbp += min(__ldcg(D.bp_cnt + s_iid[q]), D.ip[s_iid[q]].bp_cap);
+                    if (s_fire[q]) {
+                        D.flag[s_iid[q]] = 1;
+                        ++nfired;
+                    }
+                }
+                s_bp[ni] = nbp;
+                atomicAdd((unsigned long long *)D.rebuilds, (unsigned long long)nfired);
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // --------------------------------------------------------------- energies
 // Per-instance energy slots ene[inst*12 + k]: 1 bond 2 angle 3 dihedral
 // 5 WCA 6 DH (bp, total and kinetic are added by k_energy_finish).
@@ -1204,7 +1526,7 @@ template <typename R> __global__ void __launch_bounds__(256) k_energy(Dev D, Glo
     const int4 bi = D.binfo[i];
     const InstP &ip = D.ip[bi.x];
     const Pos<R> P = pos_of<R>(D, cur);
-    const double4 *x64 = D.x[cur];
+    const double4 *x64 = x_at(D, cur);
     double eb, ea, ed, ew = 0.0, ee = 0.0;
     bonded_energy_owned<R>(i, bi, P, x64, ip, g, &eb, &ea, &ed);
     const int cnt = min(D.nnbr[i], g.cap);
@@ -1277,10 +1599,10 @@ __global__ void k_mirror(Dev D, GlobP g, int cur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= g.n) return;
     const InstP &ip = D.ip[D.binfo[i].x];
-    const double4 x = D.x[cur][i];
+    const double4 x = x_at(D, cur)[i];
     float r[3];
-    D.mir[cur][i] = make_uint4(fixed_res(x.x, ip.fsc[0], r[0]), fixed_res(x.y, ip.fsc[1], r[1]), fixed_res(x.z, ip.fsc[2], r[2]), 0u);
-    D.res[cur][i] = make_float4(r[0], r[1], r[2], 0.f);
+    mir_at(D, cur)[i] = make_uint4(fixed_res(x.x, ip.fsc[0], r[0]), fixed_res(x.y, ip.fsc[1], r[1]), fixed_res(x.z, ip.fsc[2], r[2]), 0u);
+    res_at(D, cur)[i] = make_float4(r[0], r[1], r[2], 0.f);
 }
 
 // ------------------------------------------------------------- launchers
@@ -1419,7 +1741,7 @@ __device__ __forceinline__ double block_sum(double v, double *s) {
 __global__ void __launch_bounds__(256) k_rg(Dev D, int cur, double *out) {
     __shared__ double s[256];
     const InstP &ip = D.ip[blockIdx.x];
-    const double4 *x = D.x[cur] + ip.bead_off;
+    const double4 *x = x_at(D, cur) + ip.bead_off;
     double cx = 0.0, cy = 0.0, cz = 0.0;
     for (int i = threadIdx.x; i < ip.n; i += blockDim.x) {
         cx += x[i].x;
@@ -1458,7 +1780,7 @@ __device__ __forceinline__ void bias_scatter(const Dev &D, const GlobP &g, int i
         atomicOr(D.err, ERR_NONFINITE);
         return;
     }
-    fx_scatter(D, i, fx_of(fx), fx_of(fy), fx_of(fz));
+    fx_scatter(D.fbp, i, fx_of(fx), fx_of(fy), fx_of(fz));
 }
 
 // force_rg.F90:17-31 / energy_rg.F90: the centre and radius of gyration of
@@ -1468,7 +1790,7 @@ __global__ void __launch_bounds__(256) k_bias_rg(Dev D, GlobP g, int cur) {
     __shared__ double s[256];
     const InstP &ip = D.ip[blockIdx.x];
     if (ip.rg_pott == 0) return;
-    const double4 *x = D.x[cur] + ip.bead_off;
+    const double4 *x = x_at(D, cur) + ip.bead_off;
     double cx = 0.0, cy = 0.0, cz = 0.0;
     for (int i = threadIdx.x; i < ip.n; i += blockDim.x) {
         cx += x[i].x;
@@ -1498,7 +1820,7 @@ __global__ void __launch_bounds__(256) k_bias_rg(Dev D, GlobP g, int cur) {
 // the steps taken plus 1 inside a step, plus 0 outside the MD loop.
 __global__ void __launch_bounds__(256) k_bias(Dev D, GlobP g, int cur, int in_step) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const double4 *x = D.x[cur];
+    const double4 *x = x_at(D, cur);
     if (t < g.n) {
         const int inst = D.binfo[t].x;
         const double4 xi = x[t];
@@ -1550,7 +1872,7 @@ __global__ void __launch_bounds__(256) k_bias(Dev D, GlobP g, int cur, int in_st
 // into the energy slots 7-10 (k_bias_rg ran first)
 __global__ void __launch_bounds__(256) k_bias_energy(Dev D, GlobP g, int cur) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const double4 *x = D.x[cur];
+    const double4 *x = x_at(D, cur);
     if (t < g.n) {
         if (!g.flg_stage) return;
         const int inst = D.binfo[t].x;
@@ -1591,6 +1913,50 @@ cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream
     if (!g.flg_bias) return cudaSuccess;
     if (g.flg_rg) k_bias_rg<<<g.n_inst, 256, 0, st>>>(D, g, cur);
     k_bias_energy<<<(g.n + g.n_inst + g.n_bias + 255) / 256, 256, 0, st>>>(D, g, cur);
+    return cudaGetLastError();
+}
+
+size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4) + sizeof(float)); }
+
+cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
+                            cudaStream_t st) {
+    const size_t smem = small_smem_bytes(sp.cap);
+    cudaError_t e = cudaFuncSetAttribute(k_md_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_md_small<<<sp.n_cta, threads, smem, st>>>(D, g, cur, sp, nsteps, noise);
+    return cudaGetLastError();
+}
+
+// the bookkeeping after k_md_small: base-pair prefix counts over the
+// instances (as rebuild_finish forms them), the Philox step counter, and the
+// rebuild flags (after the cluster lists of the rebuilt instances were formed)
+__global__ void __launch_bounds__(256) k_small_finish(Dev D, GlobP g, unsigned long long nsteps) {
+    __shared__ int s[256];
+    const int n = g.n_inst;
+    const int per = (n + 255) / 256;
+    const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
+    int sum = 0;
+    for (int k = lo; k < hi; ++k) sum += min(D.bp_cnt[k], D.ip[k].bp_cap);
+    s[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+        const int v = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0;
+        __syncthreads();
+        s[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int run = s[threadIdx.x] - sum;
+    for (int k = lo; k < hi; ++k) {
+        D.bp_cnt[n + k] = run;
+        run += min(D.bp_cnt[k], D.ip[k].bp_cap);
+        D.flag[k] = 0;
+    }
+    if (threadIdx.x == 255) *D.bp_total = s[255];
+    if (threadIdx.x == 0) *D.step_ctr += nsteps;
+}
+
+cudaError_t launch_small_finish(const Dev &D, const GlobP &g, unsigned long long nsteps, cudaStream_t st) {
+    k_small_finish<<<1, 256, 0, st>>>(D, g, nsteps);
     return cudaGetLastError();
 }
 

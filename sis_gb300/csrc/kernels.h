@@ -5,6 +5,16 @@
 
 namespace sisg {
 
+// buckets of small instances for k_md_small: bucket b holds the instances
+// inst[cta_off[b] .. cta_off[b+1]); cap: beads of the largest bucket
+constexpr int kSmallMaxInst = 128;
+constexpr int kSmallMaxBeads = 2048;
+struct SmallPlan {
+    const int *cta_off;
+    const int *inst;
+    int n_cta, cap;
+};
+
 struct RebuildPlan {
     const int2 *small_items; // device: (instance, first local bead), 32 beads per item
     int n_small_items, small_grid;
@@ -49,6 +59,14 @@ cudaError_t launch_remd_partner_ip(const Dev &D, const RemdDev &R, int n_inst, i
 cudaError_t launch_remd_decide(const Dev &D, const RemdDev &R, const GlobP &g, int parity, const double *u, double kB,
                                unsigned long long ctr, cudaStream_t st);
 cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
+// nsteps mixed-path MD steps of every instance in one launch (k_md_small);
+// then the cluster lists of the instances it rebuilt (launch_cluster_flagged)
+// and launch_small_finish
+cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
+                            cudaStream_t st);
+size_t small_smem_bytes(int cap);
+cudaError_t launch_cluster_flagged(const Dev &D, const GlobP &g, cudaStream_t st);
+cudaError_t launch_small_finish(const Dev &D, const GlobP &g, unsigned long long nsteps, cudaStream_t st);
 cudaError_t launch_rg(const Dev &D, const GlobP &g, int cur, double *out, cudaStream_t st);
 // the optional terms' forces into fbp (in_step 1 inside a step, 0 outside)
 // and their energies into slots 7-10; nothing when none is on

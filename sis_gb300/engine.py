@@ -305,6 +305,19 @@ class Engine:
         self._ck(self.L.sis_gpu_remd_exchange(self.h, int(parity), ptr(u), r2l.ctypes.data_as(C.c_void_p), C.byref(acc)))
         return r2l, int(acc.value)
 
+    def set_ss_pairs(self, inst: int, pairs):
+        """Base pairs of instance inst only between these (imp, jmp), 1-based."""
+        a = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        self._ck(self.L.sis_gpu_set_ss_pairs(self.h, int(inst), a.shape[0], a.ctypes.data_as(C.c_void_p)))
+
+    def set_bias_ss(self, force_kcal_per_mol_A: float, on: bool = True):
+        """[Bias_SS]: constant pull of allowed pairs outside their distance window."""
+        self._ck(self.L.sis_gpu_set_bias_ss(self.h, int(on), float(force_kcal_per_mol_A)))
+
+    def set_small(self, mode: int):
+        """Per-block kernel of small instances: -1 where eligible (default), 0 never."""
+        self._ck(self.L.sis_gpu_set_small(self.h, int(mode)))
+
     def set_overlap(self, enable):
         """Pair forces in their own kernel beside the bonded/base-pair pass
         (True) or in the step kernel (False); None lets the autotuner choose."""

@@ -241,3 +241,106 @@ def force_ramp_pairs(xyz: np.ndarray, id_pairs, spring_const, trap_speed, init=N
         velo = (tuple(-u * float(sp[0])), tuple(u * float(sp[1])))
         out.append(ForceRampPair(i, j, (float(k[0]), float(k[1])), (tuple(p[0]), tuple(p[1])), velo))
     return out
+
+
+# ------------------------------------------------------- secondary structure
+# [Files.In] ct / bpseq / bpl (read_ss.F90): the base pairs that the
+# base-pair term may form.  The readers return (imp, jmp) pairs, 1-based
+# nucleotide numbers over all chains of an instance, as the files give them.
+def parse_ct(text: str, nmp: int) -> List[Tuple[int, int]]:
+    """CT: a header line whose first field is the nucleotide count, then one
+    line per nucleotide: index, base, prev, next, partner (0: none), index."""
+    lines = [l for l in text.splitlines() if l.strip()]
+    if not lines or int(lines[0].split()[0]) != nmp:
+        raise ValueError("CT file: the total number of nucleotides does not match")
+    out = []
+    for l, line in enumerate(lines[1:nmp + 1], start=1):
+        f = line.split()
+        if len(f) < 6 or int(f[0]) != l:
+            raise ValueError(f"CT file: line of nucleotide {l} cannot be read")
+        if int(f[4]) != 0:
+            out.append((l, int(f[4])))
+    if len(lines) < nmp + 1:
+        raise ValueError("CT file: fewer lines than nucleotides")
+    return out
+
+
+def parse_bpseq(text: str, nmp: int) -> List[Tuple[int, int]]:
+    """BPSEQ: one line per nucleotide: index, base, partner (0: none)."""
+    lines = [l for l in text.splitlines() if l.strip()]
+    if len(lines) < nmp:
+        raise ValueError("BPSEQ file: fewer lines than nucleotides")
+    out = []
+    for l, line in enumerate(lines[:nmp], start=1):
+        f = line.split()
+        if len(f) < 3 or int(f[0]) != l:
+            raise ValueError(f"BPSEQ file: line of nucleotide {l} cannot be read")
+        if int(f[2]) != 0:
+            out.append((l, int(f[2])))
+    return out
+
+
+def parse_bpl(text: str) -> List[Tuple[int, int]]:
+    """BPL: one pair per line: imp, jmp."""
+    out = []
+    for k, line in enumerate(l for l in text.splitlines() if l.strip()):
+        f = line.split()
+        if len(f) < 2:
+            raise ValueError(f"BPL file: line {k + 1} cannot be read")
+        out.append((int(f[0]), int(f[1])))
+    return out
+
+
+def read_ss(path, nmp: int) -> List[Tuple[int, int]]:
+    """The pairs of a .ct, .bpseq or .bpl file (by its suffix)."""
+    path = Path(path)
+    text = path.read_text()
+    suf = path.suffix.lower()
+    if suf == ".ct":
+        return parse_ct(text, nmp)
+    if suf == ".bpseq":
+        return parse_bpseq(text, nmp)
+    if suf == ".bpl":
+        return parse_bpl(text)
+    raise ValueError(f"{path}: expected a .ct, .bpseq or .bpl file")
+
+
+def filter_ss_pairs(inst, pairs, bp_model: int, bp_min_loop: int = 3):
+    """read_ss.F90's checks of every listed pair: a chain end (i or j first
+    or last of its chain), a loop shorter than the minimum, an isolated pair
+    (models 3-5: neither i-1/j+1 nor i+1/j-1 complementary), or a pair of no
+    known type (GC CG AU UA GU UG) is dropped with a warning.  Returns the
+    kept pairs (imp < jmp, 1-based) and the warnings."""
+    comp = {(0, 1), (1, 0), (1, 2), (2, 3), (2, 1), (3, 2)}  # const_idx.F90 is_complement
+    canon = {(2, 3), (3, 2), (0, 1), (1, 0), (2, 1), (1, 2)}
+    seq = inst.seq()
+    chain_of, local = [], []
+    for c, ch in enumerate(inst.chains):
+        chain_of += [c] * len(ch)
+        local += list(range(1, len(ch) + 1))
+    kept, warn = [], []
+    for imp, jmp in pairs:
+        if jmp < imp:
+            imp, jmp = jmp, imp
+        if not (1 <= imp <= len(seq) and 1 <= jmp <= len(seq)):
+            raise ValueError(f"secondary structure pair ({imp}, {jmp}) is outside the {len(seq)} nucleotides")
+        i, j = local[imp - 1], local[jmp - 1]
+        ic, jc = chain_of[imp - 1], chain_of[jmp - 1]
+        ni, nj = len(inst.chains[ic]), len(inst.chains[jc])
+        if i == 1 or i == ni:
+            warn.append(f"pair ({imp}, {jmp}) not considered: i is a chain end")
+            continue
+        if j == 1 or j == nj:
+            warn.append(f"pair ({imp}, {jmp}) not considered: j is a chain end")
+            continue
+        if ic == jc and i + bp_min_loop >= j:
+            warn.append(f"pair ({imp}, {jmp}) not considered: minimum loop length")
+            continue
+        if bp_model in (3, 4, 5) and (seq[imp - 2], seq[jmp]) not in comp and (seq[imp], seq[jmp - 2]) not in comp:
+            warn.append(f"pair ({imp}, {jmp}) not considered: isolated base pair")
+            continue
+        if (seq[imp - 1], seq[jmp - 1]) not in canon:
+            warn.append(f"pair ({imp}, {jmp}) does not form any known type of base pair")
+            continue
+        kept.append((imp, jmp))
+    return kept, warn

@@ -357,6 +357,7 @@ def test_step_graph_equals_single_steps(name, prec, systems, sis_ff):
     a = Engine(sysm, precision=prec, seed=5)
     b = Engine(sysm, precision=prec, seed=5)
     for e in (a, b):
+        e.set_small(0)  # the general kernels, whose graphs are under test
         e.set_lanes(8)
         e.set_force_cap(1000.0)
         e.init_velocities()
@@ -407,11 +408,13 @@ def test_autotune_leaves_the_state_as_it_was(name, sis_ff):
     else:
         sysm = crowded_box(sis_ff, n_chains=12, n=500, molar=0.05, seed=23, rmin=4.0)
     a = Engine(sysm, precision=MIXED, seed=9)
+    a.set_small(0)  # the general kernels, whose tuner is under test
     a.set_force_cap(1000.0)
     a.init_velocities()
     a.step(80)
     st = a.stats()
     b = Engine(sysm, precision=MIXED, seed=9)
+    b.set_small(0)
     b.set_lanes(st["lanes_per_bead"])
     b.set_overlap(bool(st["overlap"]))
     b.set_force_cap(1000.0)
@@ -423,12 +426,17 @@ def test_autotune_leaves_the_state_as_it_was(name, sis_ff):
     assert a.stats()["capped"] == b.stats()["capped"]
 
 
-def test_instance_alone_equals_instance_in_batch(sis_ff):
+@pytest.mark.parametrize("small", [-1, 0])
+def test_instance_alone_equals_instance_in_batch(small, sis_ff):
+    """With the per-block kernel of small instances (-1) and the general
+    kernels (0)."""
     big = uneven_batch(sis_ff, n_inst=6, lmin=30, lmax=80, seed=5)
     alone = System(big.ff, big.opts, [big.instances[3]])
     e1 = Engine(big, precision=MIXED, seed=99)
     # the noise of an instance is keyed by its stream id (here the batch index)
     e2 = Engine(alone, precision=MIXED, seed=99, streams=[3])
+    e1.set_small(small)
+    e2.set_small(small)
     e1.step(50)
     e2.step(50)
     x1 = e1.get_state(3)[0]
