@@ -166,6 +166,13 @@ module sis_gpu_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(in) :: temps(*)     ! the ladder by label
     end function
+    integer(c_int) function sis_gpu_remd_init_vars(ctx, nvar, kinds, values) bind(C, name="sis_gpu_remd_init_vars")
+      import :: c_int, c_int32_t, c_double, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: nvar
+      integer(c_int32_t), intent(in) :: kinds(*)    ! REPT%TEMP, %ION, %TWZDCF, %RG
+      real(c_double), intent(in) :: values(*)       ! (nvar, nrep_all): lab2val
+    end function
     integer(c_int) function sis_gpu_remd_exchange(ctx, parity, uniforms, rep2lab, n_accepted) &
         bind(C, name="sis_gpu_remd_exchange")
       import :: c_int, c_int32_t, c_ptr

@@ -329,6 +329,18 @@ int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3);
  * device Philox uniforms.  rep2lab (out, may be NULL): the label of every
  * instance afterwards; n_accepted (out, may be NULL). */
 int sis_gpu_remd_init(sis_ctx *ctx, const double *temps);
+/* Replica exchange over any of the reference's replica variables
+ * (var_replica.F90 REPT: 1 temperature in K, 2 ionic strength in M,
+ * 3 constant trap force magnitude in kcal/mol/A, 4 Rg bias target in A;
+ * energy_replica.F90:72-121 sets them to the partner label's values for the
+ * partner energy).  kinds[nvar] names the columns of values[n_inst][nvar];
+ * row l holds label l's values and replica k starts on label k, taking its
+ * values now.  A trap-force variable scales the constant-force pairs of
+ * sis_gpu_set_bias_items (their force vectors then give the direction per
+ * unit force, twz_DCF_direction); an Rg variable needs the Rg bias on every
+ * replica.  Exchanges are sis_gpu_remd_exchange's, with T_m = T_n when the
+ * temperature is not a variable (no velocity scaling then). */
+int sis_gpu_remd_init_vars(sis_ctx *ctx, int32_t nvar, const int32_t *kinds, const double *values);
 int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, int32_t *rep2lab, int32_t *n_accepted);
 
 /* Base-pair Monte Carlo removal (src/force_bp_limit_triplet.F90,

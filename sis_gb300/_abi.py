@@ -115,6 +115,7 @@ EXPORTS = {
     "sis_gpu_step_profiled": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_float)]),
     "sis_gpu_step_noise_static": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "sis_gpu_remd_init": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sis_gpu_remd_init_vars": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "sis_gpu_bp_mc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32]),
     "sis_gpu_get_bp_status": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "sis_gpu_get_bp_energies": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),

@@ -121,6 +121,7 @@ struct sis_ctx {
     bool remd_on = false;
     RemdDev remd{};
     double *remd_u = nullptr; // [n_inst / 2 + 1] caller's uniforms
+    std::vector<double> remd_lab_ion; // ionic strength of every label
     unsigned long long remd_ctr = 0;
     int n_vel_init = 0;
     bool tuned = false;
@@ -812,6 +813,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
         }
         I.n = nb - I.bead_off;
         I.stream = top->stream ? top->stream[k] : (unsigned)k;
+        I.twz_scale = 1.0;
         I.step0 = 0ull;
         I.tempK = top->tempK[k];
         ctx->ionic[k] = top->ionic_strength[k];
@@ -1956,18 +1958,24 @@ extern "C" int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const dou
 }
 
 // ========================================================= replica exchange
-extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
-    DevGuard dg_(ctx);
-    if (!ctx || !temps || ctx->n_inst < 2) return SIS_ERR_ARG;
+// The replica variables of var_replica.F90 (REPT: 1 temperature, 2 ionic
+// strength, 3 constant trap force, 4 Rg bias target).  Labels are the rows
+// of `values` ([n_inst][nvar], kinds[v] naming column v); with `assign`,
+// replica k starts on label assign[k], else on label k.
+namespace {
+int remd_setup(sis_ctx *ctx, int nvar, const int *kinds, const double *values, const int *assign) {
     const int ni = ctx->n_inst;
-    for (int l = 1; l < ni; ++l)
-        if (!(temps[l] > temps[l - 1])) return fail(ctx, SIS_ERR_ARG, "remd: the temperature ladder must be strictly ascending");
     // replicas of one topology, salt and box
     const InstP &I0 = ctx->ip[0];
     const int nl = I0.n;
+    bool has[5] = {false, false, false, false, false};
+    for (int v = 0; v < nvar; ++v) {
+        if (kinds[v] < 1 || kinds[v] > 4 || has[kinds[v]]) return fail(ctx, SIS_ERR_ARG, "remd: unknown or repeated replica variable");
+        has[kinds[v]] = true;
+    }
     for (int k = 1; k < ni; ++k) {
         const InstP &I = ctx->ip[k];
-        bool same = I.n == nl && ctx->ionic[k] == ctx->ionic[0] && I.pbc == I0.pbc;
+        bool same = I.n == nl && (has[2] || ctx->ionic[k] == ctx->ionic[0]) && I.pbc == I0.pbc;
         for (int d = 0; d < 3 && same; ++d) same = I.box[d] == I0.box[d];
         for (int i = 0; i < nl && same; ++i) {
             const int4 a = ctx->binfo[I0.bead_off + i], b = ctx->binfo[I.bead_off + i];
@@ -1976,37 +1984,64 @@ extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
         }
         if (!same) return fail(ctx, SIS_ERR_ARG, "remd: instances must be replicas of one topology, salt and box");
     }
-    // each replica starts on the label of its temperature
-    std::vector<int> rep2lab(ni, -1), lab2rep(ni, -1);
+    if (has[4])
+        for (int k = 0; k < ni; ++k)
+            if (ctx->ip[k].rg_pott == 0) return fail(ctx, SIS_ERR_ARG, "remd: an Rg replica variable needs the Rg bias on every replica");
+    for (int l = 0; l < ni; ++l)
+        for (int v = 0; v < nvar; ++v) {
+            const double x = values[(size_t)l * nvar + v];
+            if (!std::isfinite(x) || ((kinds[v] == 1 || kinds[v] == 2) && !(x > 0.0)))
+                return fail(ctx, SIS_ERR_ARG, "remd: a replica variable value is not valid");
+        }
+    std::vector<int> rep2lab(ni), lab2rep(ni, -1);
     for (int k = 0; k < ni; ++k) {
-        for (int l = 0; l < ni; ++l)
-            if (temps[l] == ctx->ip[k].tempK && lab2rep[l] < 0) {
-                rep2lab[k] = l;
-                lab2rep[l] = k;
-                break;
-            }
-        if (rep2lab[k] < 0) return fail(ctx, SIS_ERR_ARG, "remd: every instance's temperature must be a distinct rung of the ladder");
+        rep2lab[k] = assign ? assign[k] : k;
+        if (rep2lab[k] < 0 || rep2lab[k] >= ni || lab2rep[rep2lab[k]] >= 0) return fail(ctx, SIS_ERR_ARG, "remd: labels do not form a permutation");
+        lab2rep[rep2lab[k]] = k;
     }
-    // per-label tables: temperature fields, noise coefficient per local bead, FP32 triplet free energies
+    // per-label records: temperature, salt (electrostatic fields), Rg target,
+    // trap magnitude; noise coefficient per local bead; FP32 triplet free energies
+    auto val = [&](int l, int kind, double dflt) {
+        for (int v = 0; v < nvar; ++v)
+            if (kinds[v] == kind) return values[(size_t)l * nvar + v];
+        return dflt;
+    };
     std::vector<InstP> lab_ip(ni, I0);
+    std::vector<double> lab_ion(ni);
     std::vector<double> lab_w((size_t)ni * nl);
     std::vector<float> lab_dgf((size_t)ni * 469);
     const double fric = friction_of(ctx->p);
     for (int l = 0; l < ni; ++l) {
-        lab_ip[l].tempK = temps[l];
-        set_ele_fields(ctx, lab_ip[l], ctx->ionic[0]);
+        InstP &L = lab_ip[l];
+        L.tempK = val(l, 1, I0.tempK);
+        lab_ion[l] = val(l, 2, ctx->ionic[0]);
+        L.twz_scale = val(l, 3, I0.twz_scale);
+        L.rg0 = val(l, 4, I0.rg0);
+        set_ele_fields(ctx, L, lab_ion[l]);
         if (I0.large) {
-            const double c2 = std::max(std::max(lab_ip[l].wca_nl_cut2, lab_ip[l].ele_nl_cut2), lab_ip[l].bp_nl_cut2);
+            const double c2 = std::max(std::max(L.wca_nl_cut2, L.ele_nl_cut2), L.bp_nl_cut2);
             for (int d = 0; d < 3; ++d)
                 if (I0.cell_len[d] < sqrt(c2) * 1.0005)
-                    return fail(ctx, SIS_ERR_ARG, "remd: a rung's electrostatic cutoff exceeds the cell grid of the box");
+                    return fail(ctx, SIS_ERR_ARG, "remd: a label's electrostatic cutoff exceeds the cell grid of the box");
         }
         for (int i = 0; i < nl; ++i) {
-            const bool still = ctx->p.integrator != SIS_INTGRT_GJF2GJ && !ctx->frozen.empty() &&
-                               ctx->frozen[I0.bead_off + i];
-            lab_w[(size_t)l * nl + i] = still ? 0.0 : noise_coef(ctx->p, fric, ctx->mass[I0.bead_off + i], temps[l]);
+            const bool still = ctx->p.integrator != SIS_INTGRT_GJF2GJ && !ctx->frozen.empty() && ctx->frozen[I0.bead_off + i];
+            lab_w[(size_t)l * nl + i] = still ? 0.0 : noise_coef(ctx->p, fric, ctx->mass[I0.bead_off + i], L.tempK);
         }
-        dgf_row(ctx, temps[l], lab_dgf.data() + (size_t)l * 469);
+        dgf_row(ctx, L.tempK, lab_dgf.data() + (size_t)l * 469);
+    }
+    // every replica takes its label's values now (its own record otherwise unchanged)
+    bool recut = false;
+    for (int k = 0; k < ni; ++k) {
+        InstP &I = ctx->ip[k];
+        const InstP &L = lab_ip[rep2lab[k]];
+        const double cut = I.ele_nl_cut2;
+        I.tempK = L.tempK;
+        I.twz_scale = L.twz_scale;
+        I.rg0 = L.rg0;
+        ctx->ionic[k] = lab_ion[rep2lab[k]];
+        set_ele(ctx, k);
+        recut |= I.ele_nl_cut2 != cut;
     }
     RemdDev &R = ctx->remd;
     if (!ctx->remd_on) {
@@ -2038,9 +2073,48 @@ extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
     CK(cudaMemcpyAsync((void *)R.lab_dgf, lab_dgf.data(), sizeof(float) * lab_dgf.size(), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(R.rep2lab, rep2lab.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(R.lab2rep, lab2rep.data(), sizeof(int) * ni, cudaMemcpyHostToDevice, ctx->st));
+    int rc = upload_ip(ctx);
+    if (rc) return rc;
+    // the replicas' noise coefficients and FP32 triplet tables at their labels' temperatures
+    std::vector<double4> mdc;
+    md_coefs(ctx, mdc);
+    CK(cudaMemcpyAsync(ctx->D.mdc, mdc.data(), sizeof(double4) * ctx->n, cudaMemcpyHostToDevice, ctx->st));
+    for (int k = 0; k < ni; ++k)
+        if ((rc = upload_dgf(ctx, k))) return rc;
     CK(cudaStreamSynchronize(ctx->st));
+    if (recut) ctx->lists_valid = false;
+    ctx->remd_lab_ion = lab_ion;
+    ctx->bp_cache = false;
     ctx->remd_on = true;
     return SIS_OK;
+}
+} // namespace
+
+extern "C" int sis_gpu_remd_init(sis_ctx *ctx, const double *temps) {
+    DevGuard dg_(ctx);
+    if (!ctx || !temps || ctx->n_inst < 2) return SIS_ERR_ARG;
+    const int ni = ctx->n_inst;
+    for (int l = 1; l < ni; ++l)
+        if (!(temps[l] > temps[l - 1])) return fail(ctx, SIS_ERR_ARG, "remd: the temperature ladder must be strictly ascending");
+    // each replica starts on the label of its temperature
+    std::vector<int> rep2lab(ni, -1), lab2rep(ni, -1);
+    for (int k = 0; k < ni; ++k) {
+        for (int l = 0; l < ni; ++l)
+            if (temps[l] == ctx->ip[k].tempK && lab2rep[l] < 0) {
+                rep2lab[k] = l;
+                lab2rep[l] = k;
+                break;
+            }
+        if (rep2lab[k] < 0) return fail(ctx, SIS_ERR_ARG, "remd: every instance's temperature must be a distinct rung of the ladder");
+    }
+    const int kind = 1;
+    return remd_setup(ctx, 1, &kind, temps, rep2lab.data());
+}
+
+extern "C" int sis_gpu_remd_init_vars(sis_ctx *ctx, int32_t nvar, const int32_t *kinds, const double *values) {
+    DevGuard dg_(ctx);
+    if (!ctx || nvar < 1 || nvar > 4 || !kinds || !values || ctx->n_inst < 2) return SIS_ERR_ARG;
+    return remd_setup(ctx, nvar, kinds, values, nullptr);
 }
 
 extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double *uniforms, int32_t *rep2lab, int32_t *n_accepted) {
@@ -2082,6 +2156,7 @@ extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double 
     CK(cudaStreamSynchronize(ctx->st));
     for (int k = 0; k < ni; ++k) {
         if (rep2lab) rep2lab[k] = r2l[k];
+        ctx->ionic[k] = ctx->remd_lab_ion[r2l[k]];
         if (ctx->g.bp_model == 4 || ctx->g.bp_model == 5) dgf_row(ctx, ctx->ip[k].tempK, ctx->dgf.data() + (size_t)k * 469);
     }
     if (n_accepted) *n_accepted = nacc;

@@ -113,6 +113,10 @@ struct InstP {
     // Rg bias (force_rg.F90): rg_pott 0 off, 1 harmonic, 2 flat-bottomed
     int rg_pott;
     double rg_k, rg0;
+    // magnitude of the constant-force trap pairs (kind 3 items carry the force
+    // per unit of it; 1 unless the force is a replica-exchange variable,
+    // energy_replica.F90:105-107 twz_DCF_forces = value * direction)
+    double twz_scale;
     // base pairs only between the pairs of a given secondary structure
     // (read_ss.F90 bp_map): their records come from the partner table ss_*
     int ss_on;

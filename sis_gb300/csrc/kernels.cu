@@ -1854,8 +1854,9 @@ __global__ void __launch_bounds__(256) k_bias(Dev D, GlobP g, int cur, int in_st
         bias_scatter(D, g, b.i, -coef * v.x, -coef * v.y, -coef * v.z);
         if (b.kind == 1) bias_scatter(D, g, b.j, coef * v.x, coef * v.y, coef * v.z);
     } else if (b.kind == 3) {
-        bias_scatter(D, g, b.i, b.p[0], b.p[1], b.p[2]);
-        bias_scatter(D, g, b.j, -b.p[0], -b.p[1], -b.p[2]);
+        const double sc = ip.twz_scale;
+        bias_scatter(D, g, b.i, sc * b.p[0], sc * b.p[1], sc * b.p[2]);
+        bias_scatter(D, g, b.j, -sc * b.p[0], -sc * b.p[1], -sc * b.p[2]);
     } else {
         const double istep = (double)(*D.step_ctr + (unsigned long long)in_step);
         for (int tt = 0; tt < 2; ++tt) {
@@ -1897,7 +1898,8 @@ __global__ void __launch_bounds__(256) k_bias_energy(Dev D, GlobP g, int cur) {
         if (r < b.p[3]) atomicAdd(E + 10, -0.5 * b.p[0] * (1.0 - tanh((r - b.p[1]) / b.p[2])));
     } else if (b.kind == 3) {
         const V3<double> v = dvec64(x[b.i], x[b.j], ip);
-        atomicAdd(E + 8, -(v.x * b.p[0] + v.y * b.p[1] + v.z * b.p[2]));
+        const double sc = ip.twz_scale;
+        atomicAdd(E + 8, -(v.x * (sc * b.p[0]) + v.y * (sc * b.p[1]) + v.z * (sc * b.p[2])));
     }
 }
 

@@ -1,7 +1,8 @@
-// Temperature replica exchange on the device (src/replica_exchange.F90,
+// Replica exchange on the device (src/replica_exchange.F90,
 // src/energy_replica.F90, src/var_replica.F90:105-259): every replica is one
-// instance of the context, all of one topology; a label is a rung of the
-// temperature ladder.  An exchange computes each replica's total potential
+// instance of the context, all of one topology; a label is one set of
+// values of the replica variables (temperature, ionic strength, constant
+// trap force, Rg bias target).  An exchange computes each replica's total potential
 // energy at its own and at its partner's temperature with the ordinary
 // energy kernels (the partner energies through a second set of instance
 // records that carry the partner's temperature fields), decides every pair
@@ -14,9 +15,14 @@
 
 namespace sisg {
 
-// the fields of an instance record that depend on its temperature (set_ele)
+// the fields of an instance record that a label sets: its temperature, the
+// electrostatic fields of its temperature and ionic strength (set_ele), the
+// Rg bias target and the constant-force trap magnitude (REPT TEMP, ION, RG,
+// TWZDCF of var_replica.F90)
 __device__ __forceinline__ void copy_temperature_fields(InstP &d, const InstP &s) {
     d.tempK = s.tempK;
+    d.rg0 = s.rg0;
+    d.twz_scale = s.twz_scale;
     d.ele_coef = s.ele_coef;
     d.rcdist = s.rcdist;
     d.ele_cut = s.ele_cut;

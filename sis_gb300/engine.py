@@ -293,6 +293,13 @@ class Engine:
             raise ValueError("one temperature per instance")
         self._ck(self.L.sis_gpu_remd_init(self.h, ptr(t)))
 
+    def remd_init_vars(self, kinds, values):
+        """Replica exchange over replica variables (1 T, 2 ionic strength,
+        3 trap force, 4 Rg target); values[label][variable]."""
+        k = np.ascontiguousarray(kinds, dtype=np.int32)
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(self.n_inst, k.size))
+        self._ck(self.L.sis_gpu_remd_init_vars(self.h, k.size, ptr(k), ptr(v)))
+
     def remd_exchange(self, parity: int, uniforms: Optional[np.ndarray] = None):
         """One exchange attempt; returns (label of every instance, accepted pairs)."""
         u = None

@@ -136,3 +136,86 @@ def test_device_uniforms_give_a_permutation(ladder):
         assert sorted(r2l) == list(range(N_REP))
         assert 0 <= nacc <= N_REP // 2
         eng.step(50)
+
+
+# ------------------------------------------------ other replica variables
+def _same_temperature(sysm, T=300.0):
+    insts = [dataclasses.replace(i, tempK=T) for i in sysm.instances]
+    return System(sysm.ff, sysm.opts, insts)
+
+
+def _oracle_with(sysm, k, x, T, ion=None, rg=None, twz=None):
+    """An oracle of replica k at the given variables: ionic strength, Rg bias
+    (k_rg, rg0) and a constant-force trap pair (i, j, force vector)."""
+    from sis_gb300.model import ConstantForcePair
+
+    inst = dataclasses.replace(sysm.instances[k], tempK=T, xyz=x)
+    if ion is not None:
+        inst = dataclasses.replace(inst, ionic_strength=ion)
+    o = Oracle.from_instance(System(sysm.ff, sysm.opts, [inst]), 0)
+    if rg is not None:
+        o.set_rg_bias(rg[0], rg[1])
+    if twz is not None:
+        o.set_tweezers(dcf=[ConstantForcePair(twz[0], twz[1], list(twz[2]))])
+    o.neighbor_list(0)
+    o.set_bp_energy_flag(0)
+    return o
+
+
+@pytest.mark.parametrize("var", ["ion", "rg", "twz"])
+@pytest.mark.parametrize("parity", [0, 1])
+def test_replica_variable_exchange_matches_restatement(var, parity, ladder):
+    """Ionic strength (REPT%ION), Rg target (REPT%RG) and trap force
+    (REPT%TWZDCF) as the replica variable at one temperature: partner
+    energies at the partner label's value (energy_replica.F90:95-107),
+    delta with T_m = T_n, no velocity scaling (replica_exchange.F90:132-147)."""
+    from sis_gb300.model import ConstantForcePair
+
+    base, _ = ladder
+    sysm = _same_temperature(base)
+    T = 300.0
+    vals = {"ion": [0.02, 0.05, 0.1, 0.2, 0.35, 0.5], "rg": [14.0, 15.0, 16.0, 17.0, 18.0, 19.0],
+            "twz": [0.0, 0.1, 0.2, 0.3, 0.4, 0.5]}[var]
+    kind = {"ion": 2, "rg": 4, "twz": 3}[var]
+    direction = np.array([0.6, 0.0, 0.8])
+    eng = Engine(sysm, precision=FP64, seed=7)
+    if var == "rg":
+        eng.set_rg_bias(-1, 2.0, 15.0)
+    if var == "twz":
+        for k in range(N_REP):
+            eng.set_tweezers(k, dcf=[ConstantForcePair(1, 40, list(direction))])
+    eng.remd_init_vars([kind], np.array(vals).reshape(N_REP, 1))
+    eng.init_velocities()
+    eng.step(300)
+    state = [eng.get_state(k) for k in range(N_REP)]
+
+    def energy(k, l):
+        x = state[k][0]
+        if var == "ion":
+            return _oracle_with(sysm, k, x, T, ion=vals[l]).energy_sumup(0)[0]
+        if var == "rg":
+            return _oracle_with(sysm, k, x, T, rg=(2.0, vals[l])).energy_sumup(0)[0]
+        return _oracle_with(sysm, k, x, T, twz=(1, 40, vals[l] * direction)).energy_sumup(0)[0]
+
+    own = [energy(k, k) for k in range(N_REP)]
+    par = [energy(k, partner(k, parity, N_REP)) if partner(k, parity, N_REP) >= 0 else 0.0 for k in range(N_REP)]
+    u = np.array([1e-300 if q % 2 == 0 else 1.0 for q in range(N_REP // 2 + 1)])
+    labels = list(range(N_REP))
+    for q in range(N_REP):
+        li, lj = 2 * q + parity, 2 * q + parity + 1
+        if lj >= N_REP:
+            break
+        delta = ((par[lj] - own[li]) / T - (own[lj] - par[li]) / T) / KB
+        if delta < 0.0 or u[q] <= np.exp(-delta):
+            labels[li], labels[lj] = lj, li
+    r2l, nacc = eng.remd_exchange(parity, u)
+    assert list(r2l) == labels and nacc >= 1
+    for k in range(N_REP):
+        x, v, a = eng.get_state(k)
+        assert np.array_equal(v, state[k][1])  # no temperature variable: no scaling
+        l = labels[k]
+        o = (_oracle_with(sysm, k, x, T, ion=vals[l]) if var == "ion" else
+             _oracle_with(sysm, k, x, T, rg=(2.0, vals[l])) if var == "rg" else
+             _oracle_with(sysm, k, x, T, twz=(1, 40, vals[l] * direction)))
+        e = o.energy_sumup(0)[0]
+        assert abs(eng.energy_sumup(k)[0] - e) <= 1e-12 * max(1.0, abs(e)), (k, l)
