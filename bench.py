@@ -411,7 +411,7 @@ class CpuSampler:
         self.oracles = []
         for k in insts:
             o = Oracle.from_instance(sysm, k)
-            o.seed(seed + k)
+            o.seed_streams(seed + k)  # MT19937 stream as init_mts.F90 derives it
             o.md_init()
             o.init_velocities()
             self.oracles.append(o)

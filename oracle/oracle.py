@@ -100,6 +100,8 @@ def lib() -> C.CDLL:
             "or_mt_int32": (C.c_uint32, [vp]), "or_mt_double1": (d, [vp]), "or_mt_double3": (d, [vp]),
             "or_mt_boxmuller": (d, [vp]),
             "or_seed": (None, [vp, i32]),
+            "or_mt_jump": (None, [vp, i32, i32, vp]),
+            "or_seed_streams": (None, [vp, i32, i32]),
             "or_const": (d, [i32]),
             "or_set_stage": (None, [vp, d, d]),
             "or_set_rg_bias": (None, [vp, i32, d, vp]),
@@ -342,6 +344,12 @@ class Oracle:
     def init_velocities(self):
         self.L.or_init_velocities(self.h)
 
+    def seed_streams(self, seed, replica_run=False):
+        """Replica noise streams as the reference derives them (init_mts.F90):
+        stream (replica + 1 + replica_run) * 2^256 outputs ahead of the
+        MT19937 stream initialised by `seed`."""
+        self.L.or_seed_streams(self.h, int(seed), int(bool(replica_run)))
+
     def seed(self, s):
         self.L.or_seed(self.h, int(s))
 
@@ -378,3 +386,10 @@ class MT:
 
     def boxmuller(self):
         return float(self.L.or_mt_boxmuller(self.h))
+
+    def jumped(self, jp: int, stream_id: int) -> "MT":
+        """A new stream stream_id * 2^jp outputs ahead of this one
+        (mt_create_stream; this stream's pointer is put at 624 first)."""
+        out = MT(0)
+        self.L.or_mt_jump(self.h, int(jp), int(stream_id), out.h)
+        return out

@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <vector>
 
 #ifdef _OPENMP
@@ -1553,10 +1554,181 @@ static double boxmuller_draw(or_mt *m, bool &stored, double &stored_value) {
 }
 extern "C" double or_mt_boxmuller(or_mt *m) { return boxmuller_draw(m, m->stored, m->stored_value); }
 
+/* ---------------------------------------------- MT19937 jump-ahead streams
+ * mt_stream.F90:580-706 (mt_create_stream, mt_jumpahead) with f_get_coeff.F90
+ * and gf2xe.F90: the state that is J = id * 2^jp outputs ahead is p(B) v,
+ * where v is the state vector (624 words, pointer at 624), B the one-word
+ * transition (mt_matvec) and p(x) = x^J mod f(x), f the characteristic
+ * polynomial of MT19937 in closed form from (n, m, r, w, a) (f_get_coeff.F90:
+ * 17-41).  The polynomial method is Haramoto, Matsumoto, Nishimura, Panneton
+ * and L'Ecuyer, "Efficient jump ahead for F2-linear random number
+ * generators", INFORMS J. Computing 20 (2008).  Polynomials over GF(2) are
+ * bit vectors of 64-bit words, bit k the coefficient of x^k. */
+namespace {
+using Gf2 = std::vector<uint64_t>;
+
+int gf2_deg(const Gf2 &a) {
+    for (int w = (int)a.size() - 1; w >= 0; --w)
+        if (a[w]) return 64 * w + 63 - __builtin_clzll(a[w]);
+    return -1;
+}
+void gf2_trim(Gf2 &a) {
+    while (!a.empty() && a.back() == 0) a.pop_back();
+}
+void gf2_set(Gf2 &a, int k) {
+    if ((int)a.size() <= k / 64) a.resize(k / 64 + 1, 0);
+    a[k / 64] ^= 1ull << (k % 64);
+}
+void gf2_add(Gf2 &a, const Gf2 &b) {
+    if (a.size() < b.size()) a.resize(b.size(), 0);
+    for (size_t i = 0; i < b.size(); ++i) a[i] ^= b[i];
+    gf2_trim(a);
+}
+/* carry-less product of two words: (hi, lo) */
+inline void clmul64(uint64_t a, uint64_t b, uint64_t &hi, uint64_t &lo) {
+    uint64_t h = 0, l = 0;
+    for (int i = 0; i < 64; ++i)
+        if ((b >> i) & 1ull) {
+            l ^= a << i;
+            if (i) h ^= a >> (64 - i);
+        }
+    hi = h;
+    lo = l;
+}
+Gf2 gf2_mul(const Gf2 &a, const Gf2 &b) {
+    if (a.empty() || b.empty()) return {};
+    Gf2 c(a.size() + b.size(), 0);
+    for (size_t i = 0; i < a.size(); ++i) {
+        if (!a[i]) continue;
+        for (size_t j = 0; j < b.size(); ++j) {
+            if (!b[j]) continue;
+            uint64_t hi, lo;
+            clmul64(a[i], b[j], hi, lo);
+            c[i + j] ^= lo;
+            c[i + j + 1] ^= hi;
+        }
+    }
+    gf2_trim(c);
+    return c;
+}
+Gf2 gf2_sqr(const Gf2 &a) {
+    Gf2 c(2 * a.size(), 0);
+    for (size_t i = 0; i < a.size(); ++i)
+        for (int k = 0; k < 64; ++k)
+            if ((a[i] >> k) & 1ull) gf2_set(c, (int)(128 * i) + 2 * k);
+    gf2_trim(c);
+    return c;
+}
+/* a mod f (long division, bit by bit from the top) */
+void gf2_mod(Gf2 &a, const Gf2 &f, int df) {
+    for (int d = gf2_deg(a); d >= df; d = gf2_deg(a)) {
+        const int sh = d - df, ws = sh / 64, bs = sh % 64;
+        for (size_t i = 0; i < f.size(); ++i) {
+            if (!f[i]) continue;
+            a[i + ws] ^= f[i] << bs;
+            if (bs && i + ws + 1 < a.size()) a[i + ws + 1] ^= f[i] >> (64 - bs);
+        }
+        gf2_trim(a);
+    }
+}
+Gf2 gf2_pow(const Gf2 &a, int e) {
+    Gf2 r{1};
+    for (int k = 0; k < e; ++k) r = gf2_mul(r, a);
+    return r;
+}
+/* f_get_coeff.F90:17-41: the characteristic polynomial of MT19937 */
+const Gf2 &mt_charpoly() {
+    static Gf2 ff;
+    if (!ff.empty()) return ff;
+    const int nn = 624, mm = 397, rr = 31, ww = 32;
+    const uint32_t avec = 0x9908b0dfu;
+    Gf2 af, bf;
+    gf2_set(af, nn);
+    gf2_set(af, mm);
+    gf2_set(bf, nn - 1);
+    gf2_set(bf, mm - 1);
+    const Gf2 f1 = gf2_pow(af, ww - rr);
+    ff = gf2_mul(f1, gf2_pow(bf, rr));
+    for (int i = 0; i < rr; ++i)
+        if ((avec >> (i % ww)) & 1u) gf2_add(ff, gf2_mul(gf2_pow(bf, rr - 1 - i), f1));
+    for (int i = rr; i < ww; ++i)
+        if ((avec >> (i % ww)) & 1u) gf2_add(ff, gf2_pow(af, ww - 1 - i));
+    return ff;
+}
+/* x^(id * 2^jp) mod f, cached by (jp, id) */
+Gf2 mt_jump_poly(int jp, int id) {
+    static std::map<std::pair<int, int>, Gf2> cache;
+    static std::map<int, Gf2> base;
+    const auto key = std::make_pair(jp, id);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    const Gf2 &f = mt_charpoly();
+    const int df = gf2_deg(f);
+    auto bt = base.find(jp);
+    if (bt == base.end()) {
+        Gf2 p;
+        gf2_set(p, 1); /* x */
+        for (int k = 0; k < jp; ++k) {
+            p = gf2_sqr(p);
+            gf2_mod(p, f, df);
+        }
+        bt = base.emplace(jp, p).first;
+    }
+    Gf2 r{1};
+    for (int k = 0; k < id; ++k) {
+        r = gf2_mul(r, bt->second);
+        gf2_mod(r, f, df);
+    }
+    cache.emplace(key, r);
+    return r;
+}
+/* mt_stream.F90:551-578 mt_matvec: w = B v */
+void mt_matvec(const uint32_t *v, uint32_t *w) {
+    const uint32_t UM = 0x80000000u, LM = 0x7fffffffu, A = 0x9908b0dfu;
+    w[0] = v[1] & UM;
+    for (int k = 1; k < 623; ++k) w[k] = v[k + 1];
+    const uint32_t is = (v[0] & UM) | (v[1] & LM);
+    w[623] = v[397] ^ (is >> 1) ^ ((is & 1u) ? A : 0u);
+}
+} // namespace
+
+/* mt_create_stream: `that` = `base` jumped id * 2^jp outputs ahead (the
+ * base's pointer is put at 624 first, as mt_jumpahead does) */
+extern "C" void or_mt_jump(or_mt *base, int32_t jp, int32_t id, or_mt *that) {
+    base->i = 624;
+    const Gf2 p = mt_jump_poly(jp, id);
+    const int np = gf2_deg(p) + 1;
+    uint32_t v[624], w[624], t[624];
+    memcpy(v, base->st, sizeof v);
+    memcpy(w, v, sizeof w); /* the top coefficient is 1 */
+    for (int i = np - 2; i >= 0; --i) {
+        mt_matvec(w, t);
+        if ((p[i / 64] >> (i % 64)) & 1ull)
+            for (int k = 0; k < 624; ++k) w[k] = v[k] ^ t[k];
+        else
+            memcpy(w, t, sizeof w);
+    }
+    memcpy(that->st, w, sizeof w);
+    that->i = 624;
+    that->stored = false;
+    that->stored_value = 0.0;
+}
+
+/* init_mts.F90:21-43: one base stream from rng_seed; replica irep (grep =
+ * irep, 1-based) draws from the stream jumped (grep + id_offset) * 2^256
+ * ahead, id_offset = 1 when the run is a replica run (stream 1 then serves
+ * the exchanges, mts_rep). */
+extern "C" void or_seed_streams(or_system *s, int32_t seed, int32_t replica_run) {
+    or_mt *base = or_mt_create(seed);
+    for (int r = 0; r < s->nrep; ++r) or_mt_jump(base, 256, r + 1 + (replica_run ? 1 : 0), &s->mts[r]);
+    or_mt_destroy(base);
+    s->spare_stored = false;
+}
+
 extern "C" void or_seed(or_system *s, int32_t seed) {
-    /* Replica r draws from an MT stream initialised by seed + r.  The reference
-     * derives replica streams by a 2^256 jump-ahead (init_mts.F90:21-43), which
-     * this restatement does not implement; fed-noise runs remove the dependence. */
+    /* Replica r draws from an MT stream initialised by seed + r: independent
+     * streams without the jump-ahead.  or_seed_streams derives the streams
+     * the reference uses (init_mts.F90:21-43). */
     for (int r = 0; r < s->nrep; ++r) {
         or_mt *m = or_mt_create(seed + r);
         s->mts[r] = *m;

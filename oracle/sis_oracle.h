@@ -133,6 +133,10 @@ double or_mt_double3(or_mt *m);
 double or_mt_boxmuller(or_mt *m);
 /* seed the replica noise streams of a system from one scalar seed (stream 0 for replica 1, ...) */
 void or_seed(or_system *s, int32_t seed);
+/* the MT stream `base` jumped id * 2^jp outputs ahead (mt_create_stream) */
+void or_mt_jump(or_mt *base, int32_t jp, int32_t id, or_mt *that);
+/* replica streams as init_mts.F90 derives them from rng_seed */
+void or_seed_streams(or_system *s, int32_t seed, int32_t replica_run);
 
 /* physical constants (const_phys.F90) for cross-checks */
 double or_const(int32_t which);

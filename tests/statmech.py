@@ -84,7 +84,7 @@ def oracle_copy(args) -> dict:
 
     T = system.instances[0].tempK
     o = Oracle.from_instance(system, 0)
-    o.seed(seed)
+    o.seed_streams(seed)  # the reference's noise stream of a run with rng_seed = seed
     o.md_init()
     o.init_velocities()
     o.run(n_equil)

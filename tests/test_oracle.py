@@ -318,3 +318,30 @@ def test_near_straight_angle_force_is_clamped_as_the_reference_does(sis_ff):
     f32 = g * (v32 * (d2132 / d32) - v21)
     want = np.array([-f21, f21 - f32, f32])
     assert np.allclose(f, want, rtol=1e-12, atol=1e-14)
+
+
+# ------------------------------------------------------ MT jump-ahead streams
+def test_mt_jump_ahead_matches_stepping():
+    """mt_create_stream at the library's _DEBUG_ distance 2^16
+    (mt_stream.F90:96-97): stream id starts id * 65536 outputs after the base
+    (whose pointer is at 624, right after init_by_scalar)."""
+    from oracle.oracle import MT
+
+    base = MT(4357)
+    outs = [base.int32() for _ in range(3 * 65536 + 16)]
+    for sid in (1, 2, 3):
+        s = MT(4357).jumped(16, sid)
+        assert [s.int32() for _ in range(16)] == outs[sid * 65536: sid * 65536 + 16], sid
+
+
+def test_reference_replica_streams():
+    """init_mts.F90:21-43: replica r draws from stream (r + 1 + replica_run)
+    * 2^256; with the seed and a replica run, replicas differ and restarting
+    the derivation gives the same draws."""
+    from oracle.oracle import MT
+
+    a = MT(1234).jumped(256, 2)
+    b = MT(1234).jumped(256, 2)
+    assert [a.int32() for _ in range(8)] == [b.int32() for _ in range(8)]
+    c = MT(1234).jumped(256, 3)
+    assert [MT(1234).jumped(256, 2).int32() for _ in range(1)] != [c.int32()]
