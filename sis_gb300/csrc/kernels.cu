@@ -494,6 +494,50 @@ template <typename R> __global__ void __launch_bounds__(256) k_bp_test(Dev D, Gl
     }
 }
 
+// Base-pair records in one pass: one thread per record tests the distance
+// window (bp_test); the records inside it, about one in ten, are queued in
+// shared memory and evaluated 256 at a time, one per thread, so the 6-bead
+// term runs on full warps.  A record the FP32 evaluation hands back (a bond
+// angle within 1e-6 rad of 0 or 180 degrees, none in ordinary dynamics) is
+// evaluated in FP64 by the same thread.  Each record writes its own energy
+// and status, and forces add exactly (fixed point) in the mixed path, so
+// the order of evaluation does not matter.
+template <typename R> __device__ __forceinline__ void bp_eval_now(const Dev &D, const GlobP &g, int cur, int slot) {
+    if constexpr (sizeof(R) == 4) {
+        if (bp_eval_f(D, g, cur, slot)) bp_eval_d(D, g, cur, slot, D.fbp);
+    } else {
+        bp_eval_d(D, g, cur, slot, D.fbp);
+    }
+}
+template <typename R> __global__ void __launch_bounds__(256, 2) k_bp(Dev D, GlobP g, int cur) {
+    __shared__ int s_q[512];
+    __shared__ int s_n;
+    const int lane = threadIdx.x & 31;
+    const int total = *D.bp_total;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    for (int base = (int)blockIdx.x * 256; base < total; base += (int)gridDim.x * 256) {
+        int slot = -1;
+        bool pass = false;
+        if (bp_record(D, base + (int)threadIdx.x, total, g.n_inst, slot)) pass = bp_test<R>(D, g, cur, slot);
+        const unsigned bal = __ballot_sync(0xffffffffu, pass);
+        int wb = 0;
+        if (lane == 0 && bal) wb = atomicAdd(&s_n, __popc(bal));
+        wb = __shfl_sync(0xffffffffu, wb, 0);
+        if (pass) s_q[wb + __popc(bal & ((1u << lane) - 1u))] = slot;
+        __syncthreads();
+        const int n = s_n; // at most 511
+        if (n >= 256) {
+            bp_eval_now<R>(D, g, cur, s_q[threadIdx.x]);
+            __syncthreads();
+            if ((int)threadIdx.x < n - 256) s_q[threadIdx.x] = s_q[256 + threadIdx.x];
+            if (threadIdx.x == 0) s_n = n - 256;
+        }
+        __syncthreads();
+    }
+    if ((int)threadIdx.x < s_n) bp_eval_now<R>(D, g, cur, s_q[threadIdx.x]);
+}
+
 template <typename R> __global__ void __launch_bounds__(256) k_bp_eval(Dev D, GlobP g, int cur) {
     __shared__ int s_last;
     const int n = *(volatile int *)D.bp_nwin;
@@ -930,16 +974,58 @@ __device__ __forceinline__ float pair_c(bool wca, bool ele, float d2, const Pair
     return c;
 }
 
+// Two pairs at once with paired FP32 instructions (FFMA2 and relatives of
+// sm_100 and later): the separations v of (i, j) and (i, j') from the mirror
+// differences, and the force coefficients c of pair_c, lane by lane the same
+// IEEE operations as pair_c (WCA in scalar form: it acts on few pairs).
+struct Pair2 {
+    float2 vx, vy, vz, c;
+};
+__device__ __forceinline__ Pair2 pair2(const uint4 &mi, const uint4 &ma, const uint4 &mb, const float2 f0, const float2 f1,
+                                       const float2 f2, bool wa, bool wb, bool ea, bool eb, const PairCoef &P) {
+    Pair2 r;
+    r.vx = __fmul2_rn(make_float2((float)(int)(mi.x - ma.x), (float)(int)(mi.x - mb.x)), f0);
+    r.vy = __fmul2_rn(make_float2((float)(int)(mi.y - ma.y), (float)(int)(mi.y - mb.y)), f1);
+    r.vz = __fmul2_rn(make_float2((float)(int)(mi.z - ma.z), (float)(int)(mi.z - mb.z)), f2);
+    const float2 d2 = __ffma2_rn(r.vx, r.vx, __ffma2_rn(r.vy, r.vy, __fmul2_rn(r.vz, r.vz)));
+    // Debye-Hueckel: ecoef ri^2 (ri + rc) exp(-r rc), ri one Newton step past rsqrt
+    float2 ri = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
+    const float2 h = __fmul2_rn(__fmul2_rn(make_float2(-0.5f, -0.5f), d2), ri);
+    ri = __fmul2_rn(ri, __ffma2_rn(h, ri, make_float2(1.5f, 1.5f)));
+    const float2 rr = __fmul2_rn(d2, ri);
+    const float2 ex = make_float2(__expf(-rr.x * P.rc), __expf(-rr.y * P.rc));
+    float2 c = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(P.ecoef, P.ecoef), __fmul2_rn(ri, ri)),
+                                     __fadd2_rn(ri, make_float2(P.rc, P.rc))),
+                          ex);
+    c.x = (ea && d2.x <= P.cut2) ? c.x : 0.f;
+    c.y = (eb && d2.y <= P.cut2) ? c.y : 0.f;
+    if ((wa && d2.x < P.sig2) || (wb && d2.y < P.sig2)) {
+        if (wa && d2.x < P.sig2) {
+            const float sq = __fdiv_rn(P.sig2, d2.x), s2 = sq * sq, s4 = s2 * s2;
+            c.x = P.wcoef * (s4 * s2 * sq - s4) + c.x;
+        }
+        if (wb && d2.y < P.sig2) {
+            const float sq = __fdiv_rn(P.sig2, d2.y), s2 = sq * sq, s4 = s2 * s2;
+            c.y = P.wcoef * (s4 * s2 * sq - s4) + c.y;
+        }
+    }
+    r.c = c;
+    return r;
+}
+
 // Pair forces of the mixed path over the cluster-pair lists (lists.cu
 // cluster_lists) into fpair: one warp per i-cluster of 8 beads.  Lane
-// (a = lane & 7, q = lane >> 3) pairs i-bead a with j-beads q and q + 4 of
-// every j-cluster, in list order; the four partial sums of an i-bead are
-// then combined (xor 8, then 16).  Lanes fetch the j-cluster entries 32 at a
-// time, one each, and broadcast them by shuffles, so a pair costs one
-// coalesced 16-byte position load and no list-word load.  mask bit 16: WCA,
-// bit 32: electrostatics.  An i-cluster whose j-clusters did not fit (count
-// -1) walks its beads' per-bead lists, 4 lanes per bead.
-__global__ void __launch_bounds__(256) k_pairs_cl(Dev D, GlobP g, int cur, int mask) {
+// (a = lane & 7, q = lane >> 3) takes i-bead a against all 8 j-beads of
+// every 4th j-cluster of the list, starting at the q-th: it loads the
+// j-cluster's first bead and masks (one 16-byte load, the same for the 8
+// lanes of a q) and the 8 partners' mirrors, then evaluates the 8 pairs two
+// at a time (pair2), so each lane keeps 8 independent loads and pair
+// evaluations in flight.  Sums: even and odd partners apart, then added, in
+// list order per lane, then over q (xor 8, then 16): a fixed order, and a
+// partner beyond every cutoff adds an exact zero.  mask bit 16: WCA, bit 32:
+// electrostatics.  An i-cluster whose j-clusters did not fit (count -1)
+// walks its beads' per-bead lists, 4 lanes per bead.
+__global__ void __launch_bounds__(256, 4) k_pairs_cl(Dev D, GlobP g, int cur, int mask) {
     const int lane = threadIdx.x & 31;
     const int ic = blockIdx.x * 8 + (threadIdx.x >> 5);
     if (ic >= g.n_cl) return;
@@ -949,7 +1035,8 @@ __global__ void __launch_bounds__(256) k_pairs_cl(Dev D, GlobP g, int cur, int m
     const int cnt = min(kCl, ip.bead_off + ip.n - first);
     const uint4 *__restrict__ mir = mir_at(D, cur);
     const uint4 mi = mir[first + (a < cnt ? a : 0)];
-    const float f0 = ip.finv[0], f1 = ip.finv[1], f2 = ip.finv[2];
+    const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
+                 f2 = make_float2(ip.finv[2], ip.finv[2]);
     PairCoef P;
     P.sig2 = g.f_wca_sig2;
     P.wcoef = g.f_wca_coef;
@@ -957,38 +1044,24 @@ __global__ void __launch_bounds__(256) k_pairs_cl(Dev D, GlobP g, int cur, int m
     P.rc = ip.rcdist_f;
     P.cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
     const unsigned wsel = (mask & 16) ? 0xffu : 0u, esel = (mask & 32) ? 0xffu : 0u;
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
     const int nc = D.ncl[ic];
     if (nc >= 0) {
         const size_t base = (size_t)ic * g.ccap;
-        for (int k0 = 0; k0 < nc; k0 += 32) {
-            int jf = 0;
-            unsigned long long mw = 0ull, me = 0ull;
-            if (k0 + lane < nc) {
-                jf = __ldg(D.cl_j + base + k0 + lane);
-                const ulonglong2 m = D.cl_m[base + k0 + lane];
-                mw = m.x;
-                me = m.y;
-            }
-            const int kn = min(32, nc - k0);
-            for (int k = 0; k < kn; ++k) {
-                const int j0 = __shfl_sync(0xffffffffu, jf, k);
-                const unsigned wb = (unsigned)(__shfl_sync(0xffffffffu, mw, k) >> (a * kCl)) & wsel;
-                const unsigned eb = (unsigned)(__shfl_sync(0xffffffffu, me, k) >> (a * kCl)) & esel;
-                const uint4 mj0 = __ldg(mir + j0 + q), mj1 = __ldg(mir + j0 + q + 4);
+        for (int k = q; k < nc; k += 4) {
+            const int j0 = __ldg(D.cl_j + base + k);
+            const ulonglong2 m = __ldg(D.cl_m + base + k);
+            const unsigned wb = (unsigned)(m.x >> (a * kCl)) & wsel, eb = (unsigned)(m.y >> (a * kCl)) & esel;
+            uint4 mj[kCl];
 #pragma unroll
-                for (int t = 0; t < 2; ++t) {
-                    const uint4 mj = t ? mj1 : mj0;
-                    const int b = q + 4 * t;
-                    const float vx = (float)(int)(mi.x - mj.x) * f0;
-                    const float vy = (float)(int)(mi.y - mj.y) * f1;
-                    const float vz = (float)(int)(mi.z - mj.z) * f2;
-                    const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
-                    const float c = pair_c((wb >> b) & 1u, (eb >> b) & 1u, d2, P);
-                    ax = fmaf(c, vx, ax);
-                    ay = fmaf(c, vy, ay);
-                    az = fmaf(c, vz, az);
-                }
+            for (int b = 0; b < kCl; ++b) mj[b] = __ldg(mir + j0 + b);
+#pragma unroll
+            for (int b = 0; b < kCl; b += 2) {
+                const Pair2 pr = pair2(mi, mj[b], mj[b + 1], f0, f1, f2, (wb >> b) & 1u, (wb >> (b + 1)) & 1u, (eb >> b) & 1u,
+                                       (eb >> (b + 1)) & 1u, P);
+                ax = __ffma2_rn(pr.c, pr.vx, ax);
+                ay = __ffma2_rn(pr.c, pr.vy, ay);
+                az = __ffma2_rn(pr.c, pr.vz, az);
             }
         }
     } else if (a < cnt) {
@@ -998,23 +1071,24 @@ __global__ void __launch_bounds__(256) k_pairs_cl(Dev D, GlobP g, int cur, int m
         for (int k = q; k < m; k += 4) {
             const int e = __ldg(nb + k);
             const uint4 mj = __ldg(mir + (e & IDX_MASK));
-            const float vx = (float)(int)(mi.x - mj.x) * f0;
-            const float vy = (float)(int)(mi.y - mj.y) * f1;
-            const float vz = (float)(int)(mi.z - mj.z) * f2;
+            const float vx = (float)(int)(mi.x - mj.x) * ip.finv[0];
+            const float vy = (float)(int)(mi.y - mj.y) * ip.finv[1];
+            const float vz = (float)(int)(mi.z - mj.z) * ip.finv[2];
             const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
             const float c = pair_c((e & WCA_BIT) && (mask & 16), (e & ELE_BIT) && (mask & 32), d2, P);
-            ax = fmaf(c, vx, ax);
-            ay = fmaf(c, vy, ay);
-            az = fmaf(c, vz, az);
+            ax.x = fmaf(c, vx, ax.x);
+            ay.x = fmaf(c, vy, ay.x);
+            az.x = fmaf(c, vz, az.x);
         }
     }
+    float sx = ax.x + ax.y, sy = ay.x + ay.y, sz = az.x + az.y;
 #pragma unroll
     for (int o = 8; o <= 16; o <<= 1) {
-        ax += __shfl_xor_sync(0xffffffffu, ax, o);
-        ay += __shfl_xor_sync(0xffffffffu, ay, o);
-        az += __shfl_xor_sync(0xffffffffu, az, o);
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
     }
-    if (q == 0 && a < cnt) reinterpret_cast<float4 *>(D.fpair)[first + a] = make_float4(ax, ay, az, 0.f);
+    if (q == 0 && a < cnt) reinterpret_cast<float4 *>(D.fpair)[first + a] = make_float4(sx, sy, sz, 0.f);
 }
 
 // One component c of bead ii of the mixed path's GJF-2GJ / Ermak-McCammon
@@ -1315,7 +1389,8 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
     __shared__ int s_fire[kSmallMaxInst];
-    __shared__ int s_any;
+    __shared__ int s_any, s_qn;
+    __shared__ int2 s_qi[1024]; // windowed base-pair records (2 block widths)
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const int k0 = sp.cta_off[blockIdx.x], ni = sp.cta_off[blockIdx.x + 1] - k0;
     if (tid == 0) {
@@ -1349,13 +1424,44 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         if (tid < ni) s_m1[tid] = s_m2[tid] = 0u;
         if (tid == 0) s_any = 0;
         __syncthreads();
-        if (g.bp_model > 0)
-            for (int r = tid; r < s_bp[ni]; r += nt) {
-                const int q = small_inst(s_bp, ni, r);
-                const int slot = D.ip[s_iid[q]].bp_off + (r - s_bp[q]);
-                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
-                if (bp_test<float>(E, g, cur, slot) && bp_eval_f(E, g, cur, slot)) bp_eval_d(D, g, cur, slot, E.fbp);
+        if (g.bp_model > 0) {
+            // records inside the distance window are queued (bucket-local
+            // instance | slot) and evaluated a block-width at a time
+            if (tid == 0) s_qn = 0;
+            __syncthreads();
+            for (int r0 = 0; r0 < s_bp[ni]; r0 += nt) {
+                const int r = r0 + tid;
+                bool pass = false;
+                int q = 0, slot = 0;
+                if (r < s_bp[ni]) {
+                    q = small_inst(s_bp, ni, r);
+                    slot = D.ip[s_iid[q]].bp_off + (r - s_bp[q]);
+                    const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+                    pass = bp_test<float>(E, g, cur, slot);
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                int wb = 0;
+                if (lane == 0 && bal) wb = atomicAdd(&s_qn, __popc(bal));
+                wb = __shfl_sync(0xffffffffu, wb, 0);
+                if (pass) s_qi[wb + __popc(bal & ((1u << lane) - 1u))] = make_int2(q, slot);
+                __syncthreads();
+                const int n = s_qn; // below 2 * nt
+                if (n >= nt) {
+                    const int2 w = s_qi[tid];
+                    const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
+                    if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
+                    __syncthreads();
+                    if (tid < n - nt) s_qi[tid] = s_qi[nt + tid];
+                    if (tid == 0) s_qn = n - nt;
+                }
+                __syncthreads();
             }
+            if (tid < s_qn) {
+                const int2 w = s_qi[tid];
+                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
+                if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
+            }
+        }
         for (int s = tid; s < nb; s += nt) {
             const int q = small_inst(s_sb, ni, s);
             const int gi = s_off[q] + (s - s_sb[q]);
@@ -1389,17 +1495,28 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const int m = min(D.nnbr[gi], g.cap);
                 const int *__restrict__ nbl = D.nbr + (size_t)gi * g.cap;
                 V3<float> an = mk<float>(0.f, 0.f, 0.f);
-                for (int k = sub; k < m; k += kSmallLanes) {
-                    const int e = __ldg(nbl + k);
-                    const uint4 mj = s_mir[sb + (e & IDX_MASK) - off];
-                    const float vx = (float)(int)(mi.x - mj.x) * ip.finv[0];
-                    const float vy = (float)(int)(mi.y - mj.y) * ip.finv[1];
-                    const float vz = (float)(int)(mi.z - mj.z) * ip.finv[2];
-                    const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
-                    const float c = pair_c(e & WCA_BIT, e & ELE_BIT, d2, P);
-                    an.x = fmaf(c, vx, an.x);
-                    an.y = fmaf(c, vy, an.y);
-                    an.z = fmaf(c, vz, an.z);
+                // batches of 8 entries: the 8 list words, then the 8 partners'
+                // mirrors, are loaded before any is used; entries still add in
+                // list order
+                for (int k0 = 0; k0 < m; k0 += 8) {
+                    int e[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) e[u] = k0 + u < m ? __ldg(nbl + k0 + u) : gi;
+                    uint4 mj[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) mj[u] = s_mir[sb + (e[u] & IDX_MASK) - off];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        if (k0 + u >= m) break;
+                        const float vx = (float)(int)(mi.x - mj[u].x) * ip.finv[0];
+                        const float vy = (float)(int)(mi.y - mj[u].y) * ip.finv[1];
+                        const float vz = (float)(int)(mi.z - mj[u].z) * ip.finv[2];
+                        const float d2 = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+                        const float c = pair_c(e[u] & WCA_BIT, e[u] & ELE_BIT, d2, P);
+                        an.x = fmaf(c, vx, an.x);
+                        an.y = fmaf(c, vy, an.y);
+                        an.z = fmaf(c, vz, an.z);
+                    }
                 }
                 V3<float> ab = bonded_gather<float>(D, g, bi, sub, kSmallLanes, 7);
 #pragma unroll
@@ -1686,16 +1803,12 @@ cudaError_t launch_bonded(const Dev &D, const GlobP &g, int cur, cudaStream_t st
 // test_blocks covers the staging capacity (grid stride beyond it), eval_blocks
 // the windowed records of an ordinary step
 cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int test_blocks, int eval_blocks, cudaStream_t st) {
-    if (g.prec == 0) {
-        k_bp_test<double><<<test_blocks, 256, 0, st>>>(D, g, cur);
-        k_bp_eval<double><<<eval_blocks, 256, 0, st>>>(D, g, cur);
-    } else {
-        k_bp_test<float><<<test_blocks, 256, 0, st>>>(D, g, cur);
-        k_bp_eval<float><<<eval_blocks, 256, 0, st>>>(D, g, cur);
-    }
+    (void)eval_blocks;
+    if (g.prec == 0) k_bp<double><<<test_blocks, 256, 0, st>>>(D, g, cur);
+    else k_bp<float><<<test_blocks, 256, 0, st>>>(D, g, cur);
     return cudaGetLastError();
 }
-int bp_kernels(const GlobP &g) { return g.bp_model > 0 ? 2 : 0; }
+int bp_kernels(const GlobP &g) { return g.bp_model > 0 ? 1 : 0; }
 
 // bonded terms (if do_bonded) and base-pair forces (if do_bp), one after the
 // other on st

@@ -51,7 +51,8 @@ def _hairpin():
 
     nn = read_ff(ROOT / "sis_gb300" / "data" / "sis_dih_ReB_NN.ff", bp_model=5)
     seq = "GGGGCAAAAGCCCCAAAAGGGGAAAACCCC"
-    x = random_coil(np.random.default_rng(5), len(seq))
+    # a coil without WCA overlaps: both arms start at rest, not from a kick
+    x = random_coil(np.random.default_rng(5), len(seq), rmin=10.0)
     inst = Instance([Chain.from_string(seq)], tempK=300.0, ionic_strength=0.15, xyz=x)
     opts = Options(bp_model=5, nstep_bp_mc=1, max_bp_per_nt=1, ele_cutoff_type=2, ele_cutoff=20.0)
     return System(nn, opts, [inst])
