@@ -43,6 +43,19 @@ __device__ __forceinline__ float gauss_f(unsigned long long seed, int i, unsigne
     sincospif(2.0f * u2, &sn, &cs);
     return sqrtf(-2.0f * logf(u1)) * (c == 1 ? sn : cs);
 }
+// the three deviates of bead i from one Philox block: gauss_f for c = 0, 1, 2
+__device__ __forceinline__ void gauss_f3(unsigned long long seed, int i, unsigned long long s, unsigned stream, float xi[3]) {
+    const uint4 r = philox4x32_10(make_uint4((unsigned)i, (unsigned)s, (unsigned)(s >> 32), stream),
+                                  make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    float sn, cs;
+    const float ra = sqrtf(-2.0f * logf((float)((r.x >> 8) + 1u) * (1.0f / 16777216.0f)));
+    sincospif(2.0f * ((float)(r.y >> 8) * (1.0f / 16777216.0f)), &sn, &cs);
+    xi[0] = ra * cs;
+    xi[1] = ra * sn;
+    const float rb = sqrtf(-2.0f * logf((float)((r.z >> 8) + 1u) * (1.0f / 16777216.0f)));
+    sincospif(2.0f * ((float)(r.w >> 8) * (1.0f / 16777216.0f)), &sn, &cs);
+    xi[2] = rb * cs;
+}
 template <typename R>
 __device__ __forceinline__ double gauss3(unsigned long long seed, int i, unsigned long long s, int c, unsigned stream);
 template <> __device__ __forceinline__ double gauss3<float>(unsigned long long seed, int i, unsigned long long s, int c,
@@ -1125,6 +1138,56 @@ __device__ __forceinline__ unsigned int mixed_update(const Dev &D, const GlobP &
     return qm;
 }
 
+// mixed_update for the three components of bead ii at once: one Philox
+// block for the noise, vector loads and stores of the bead's state; the same
+// operations, component by component, as mixed_update.  Returns the new
+// mirror (w unused).
+__device__ __forceinline__ uint4 mixed_update_bead(const Dev &D, const GlobP &g, int cur, int ii, const float F[3], float cf0, float cf1,
+                                                   const double *noise, long long noise_step, unsigned long long step) {
+    const InstP &jp = D.ip[D.binfo[ii].x];
+    float xi[3];
+    if (noise) {
+        const double *nz = noise + ((size_t)noise_step * g.n + ii) * 3;
+        xi[0] = (float)nz[0];
+        xi[1] = (float)nz[1];
+        xi[2] = (float)nz[2];
+    } else {
+        gauss_f3(g.seed, ii - jp.bead_off, step - jp.step0, jp.stream, xi);
+    }
+    const double4 x = x_at(D, cur)[ii];
+    const double4 m = D.mdc[ii];
+    double4 v = D.v[ii], b = D.beta[ii];
+    double xc[3] = {x.x, x.y, x.z}, vc[3] = {v.x, v.y, v.z}, bc[3] = {b.x, b.y, b.z};
+    unsigned int q[3];
+    float r[3];
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        double dx;
+        if (g.integrator == 1) {
+            const float bn = cf1 * xi[c];
+            const double vn = fma(m.x, vc[c], bc[c]) + (double)fmaf(cf0, F[c], bn);
+            bc[c] = (double)bn;
+            vc[c] = vn;
+            dx = m.z * vn;
+        } else {
+            dx = (double)fmaf(cf0, F[c], cf1 * xi[c]);
+        }
+        xc[c] = xc[c] + dx;
+        ok &= fixed_mirror(xc[c], jp.fsc[c], q[c], r[c]);
+    }
+    if (!ok) atomicOr(D.err, ERR_NONFINITE);
+    x_at(D, cur ^ 1)[ii] = make_double4(xc[0], xc[1], xc[2], 0.0);
+    if (g.integrator == 1) {
+        D.v[ii] = make_double4(vc[0], vc[1], vc[2], v.w);
+        D.beta[ii] = make_double4(bc[0], bc[1], bc[2], b.w);
+    }
+    const uint4 mq = make_uint4(q[0], q[1], q[2], 0u);
+    mir_at(D, cur ^ 1)[ii] = mq;
+    res_at(D, cur ^ 1)[ii] = make_float4(r[0], r[1], r[2], 0.f);
+    return mq;
+}
+
 template <typename R, int G, int MODE>
 __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
                                               double *__restrict__ fout, int mask) {
@@ -1214,6 +1277,29 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     // fraction of the FP32 rate on this part, so the block spreads it over
     // 3*BPB threads (whole warps) instead of BPB.
     const unsigned long long step = MODE == 0 ? *D.step_ctr : 0ull;
+    if constexpr (sizeof(R) == 4 && MODE == 0) {
+        // mixed path: one thread per bead (mixed_update_bead)
+        for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
+            const int ii = i0 + bb;
+            if (ii >= g.n) continue;
+            float F[3] = {sA[0][bb] + sB[0][bb], sA[1][bb] + sB[1][bb], sA[2][bb] + sB[2][bb]};
+            if (mask & 136) {
+                const double4 fb = D.fbp[ii];
+                F[0] += fx_float(fb.x);
+                F[1] += fx_float(fb.y);
+                F[2] += fx_float(fb.z);
+                D.fbp[ii] = make_double4(0.0, 0.0, 0.0, 0.0);
+            }
+            const float sc = sScale[bb];
+            F[0] *= sc;
+            F[1] *= sc;
+            F[2] *= sc;
+            const uint4 q = mixed_update_bead(D, g, cur, ii, F, sCf[0][bb], sCf[1][bb], noise, noise_step, step);
+            sQ[0][bb] = q.x;
+            sQ[1][bb] = q.y;
+            sQ[2][bb] = q.z;
+        }
+    } else
     for (int t = threadIdx.x; t < 3 * BPB; t += blockDim.x) {
         const int c = t / BPB, bb = t - c * BPB;
         const int ii = i0 + bb;
@@ -1550,15 +1636,13 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         __syncthreads();
         // ------------------------------------------------ update
         const unsigned long long step = step0 + (unsigned long long)st;
-        for (int t = tid; t < 3 * nb; t += nt) {
-            const int s = t / 3, c = t - 3 * s;
+        for (int s = tid; s < nb; s += nt) {
             const int q = small_inst(s_sb, ni, s);
             const int gi = s_off[q] + (s - s_sb[q]);
-            const float4 F = s_F[s];
-            float r;
-            const unsigned int qm = mixed_update(D, g, cur, gi, c, c == 0 ? F.x : (c == 1 ? F.y : F.z), F.w, s_cn[s], noise, st, step, r);
-            reinterpret_cast<unsigned int *>(s_mir + s)[c] = qm;
-            reinterpret_cast<float *>(s_res + s)[c] = r;
+            const float4 F4 = s_F[s];
+            const float F[3] = {F4.x, F4.y, F4.z};
+            s_mir[s] = mixed_update_bead(D, g, cur, gi, F, F4.w, s_cn[s], noise, st, step);
+            s_res[s] = res_at(D, cur ^ 1)[gi];
         }
         __syncthreads();
         // ------------------------------------------------ trigger (job_md.F90:376-395)
