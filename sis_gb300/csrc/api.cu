@@ -343,9 +343,9 @@ int upload_dgf(sis_ctx *ctx, int k) {
 
 int ensure_lists(sis_ctx *ctx);
 
-int run_rebuild(sis_ctx *ctx, int after_step = 0) {
+int run_rebuild(sis_ctx *ctx) {
     ctx->launches++;
-    CK(launch_rebuild(ctx->D, ctx->g, ctx->cur, ctx->plan, after_step, step_blocks(ctx->G, ctx->n), ctx->coop_grid, ctx->st));
+    CK(launch_rebuild(ctx->D, ctx->g, ctx->cur, ctx->plan, ctx->coop_grid, ctx->st));
     return SIS_OK;
 }
 
@@ -437,9 +437,9 @@ cudaError_t enqueue_forces_update(sis_ctx *ctx, int cur, const double *noise, lo
     }
     if ((e = enqueue_pre(ctx, cur)) != cudaSuccess) return e;
     if ((e = launch_bias(ctx->D, ctx->g, cur, 1, ctx->st)) != cudaSuccess) return e;
-    if (!split) return launch_step(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
+    if (!split) return launch_step(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st, 1);
     if (ctx->overlap && (e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
-    return launch_step_split(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st);
+    return launch_step_split(ctx->G, ctx->D, ctx->g, cur, noise, ns, ctx->st, 1);
 }
 int step_kernels(const sis_ctx *ctx) {
     return pre_step_kernels(ctx) + bias_kernels(ctx->g) + 1 + (ctx->overlap || ctx->g.prec != 0 ? 1 : 0);
@@ -449,7 +449,7 @@ int enqueue_step(sis_ctx *ctx, const double *noise, long long ns) {
     CK(enqueue_forces_update(ctx, ctx->cur, noise, ns));
     ctx->launches += step_kernels(ctx);
     ctx->cur ^= 1;
-    return run_rebuild(ctx, 1);
+    return run_rebuild(ctx);
 }
 
 // ----------------------------------------------------------- step graphs
@@ -472,7 +472,7 @@ int build_step_graph(sis_ctx *ctx) {
             e = enqueue_forces_update(ctx, cur, nullptr, 0);
             cur ^= 1;
             if (e == cudaSuccess)
-                e = launch_rebuild(ctx->D, ctx->g, cur, ctx->plan, 1, step_blocks(ctx->G, ctx->n), ctx->coop_grid, ctx->st);
+                e = launch_rebuild(ctx->D, ctx->g, cur, ctx->plan, ctx->coop_grid, ctx->st);
         }
         cudaGraph_t got = nullptr;
         const cudaError_t ee = cudaStreamEndCapture(ctx->st, &got);
@@ -514,7 +514,11 @@ int ensure_step_graph(sis_ctx *ctx) {
 // of the timing, since they would consume the pass that is due.
 int autotune(sis_ctx *ctx) {
     if (ctx->tuned) return SIS_OK;
-    std::vector<int> gs = ctx->lanes_fixed ? std::vector<int>{ctx->G} : std::vector<int>{2, 4, 8, 16};
+    // the mixed path's step kernel gathers no pair list (k_pairs_cl does), so
+    // one lane per bead is a candidate there
+    std::vector<int> gs = ctx->lanes_fixed ? std::vector<int>{ctx->G}
+                          : ctx->g.prec != 0 ? std::vector<int>{1, 2, 4, 8}
+                                             : std::vector<int>{2, 4, 8, 16};
     std::vector<int> ovs = ctx->overlap_mode >= 0 ? std::vector<int>{ctx->overlap_mode} : std::vector<int>{0, 1};
     if (gs.size() * ovs.size() == 1) {
         ctx->G = gs[0];
@@ -568,8 +572,8 @@ int autotune(sis_ctx *ctx) {
             return e;
         }
         if (ov && (e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
-        if (ov || mixed) return launch_step_split(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st);
-        return launch_step(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st);
+        if (ov || mixed) return launch_step_split(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st, 0);
+        return launch_step(G, D, ctx->g, ctx->cur, nullptr, 0, ctx->st, 0);
     };
     cudaError_t e = copy(false);
     float best = 1e30f;
@@ -1041,8 +1045,6 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     rc |= dalloc(ctx, &D.flag, ni);
     rc |= dalloc(ctx, &D.any, 1);
     rc |= dalloc(ctx, &D.ticket, 3);
-    rc |= dalloc(ctx, &D.part_inst, (size_t)2 * step_blocks(32, n));
-    rc |= dalloc(ctx, &D.part_m, (size_t)4 * step_blocks(32, n));
     rc |= dalloc(ctx, &D.step_ctr, 1);
     rc |= dalloc(ctx, &D.err, 1);
     rc |= dalloc(ctx, &D.max_need, 2);
@@ -1698,6 +1700,7 @@ extern "C" int sis_gpu_set_force_cap(sis_ctx *ctx, double fmax) {
     DevGuard dg_(ctx);
     if (!ctx || fmax < 0.0) return SIS_ERR_ARG;
     ctx->g.fcap = fmax;
+    ctx->g.fcap_f = (float)fmax;
     return SIS_OK;
 }
 
@@ -1867,15 +1870,15 @@ extern "C" int sis_gpu_step_profiled(sis_ctx *ctx, int64_t nsteps, float *ms3) {
         CK(cudaEventRecord(e[1], ctx->st));
         if (ctx->overlap || ctx->g.prec != 0) {
             CK(launch_pairs(ctx->G, ctx->D, ctx->g, ctx->cur, ctx->st));
-            CK(launch_step_split(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
+            CK(launch_step_split(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st, 1));
             ctx->launches += 2;
         } else {
-            CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st));
+            CK(launch_step(ctx->G, ctx->D, ctx->g, ctx->cur, nullptr, 0, ctx->st, 1));
             ctx->launches++;
         }
         ctx->cur ^= 1;
         CK(cudaEventRecord(e[2], ctx->st));
-        rc = run_rebuild(ctx, 1);
+        rc = run_rebuild(ctx);
         if (rc) return rc;
         CK(cudaEventRecord(e[3], ctx->st));
         CK(cudaEventSynchronize(e[3]));
@@ -2147,7 +2150,7 @@ extern "C" int sis_gpu_remd_exchange(sis_ctx *ctx, int32_t parity, const double 
     CK(launch_remd_decide(ctx->D, R, ctx->g, parity, u, BOLTZ_KCAL_MOL, ctx->remd_ctr++, ctx->st));
     ctx->launches += 2 * (2 + (ctx->g.bp_model > 0) + (ctx->g.flg_bias ? 1 + ctx->g.flg_rg : 0)) + 3;
     // lists of replicas whose electrostatic cutoff moved with the Debye length
-    if ((rc = run_rebuild(ctx, 0))) return rc;
+    if ((rc = run_rebuild(ctx))) return rc;
     int nacc = 0;
     std::vector<int> r2l(ni);
     CK(cudaMemcpyAsync(r2l.data(), R.rep2lab, sizeof(int) * ni, cudaMemcpyDeviceToHost, ctx->st));
@@ -2244,7 +2247,7 @@ extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, c
     // the slot's lists, now (with every coordinate set)
     if (ctx->state_set) {
         if ((rc = flag_all(ctx, inst))) return rc;
-        if ((rc = run_rebuild(ctx, 0))) return rc;
+        if ((rc = run_rebuild(ctx))) return rc;
     }
     ctx->bp_cache = false;
     CK(cudaStreamSynchronize(ctx->st));

@@ -135,6 +135,7 @@ struct GlobP {
     float f_wca_sig2, f_wca_coef, f_wca_sigma, f_wca_eps;
     unsigned long long seed;
     double fcap; // > 0: per-bead force magnitude cap (equilibration only)
+    float fcap_f; // the same in FP32 (the mixed path)
     int nstep_mc, max_bp_per_nt; // base-pair Monte Carlo removal (0: none)
     // optional terms (force.F90:62-75): any of them on; stage wall; an Rg
     // bias on some instance; restraint and trap items
@@ -217,11 +218,9 @@ struct Dev {
     unsigned long long *m1, *m2; // [2][n_inst] top-2 displacement^2 (bit patterns), by step parity
     int *flag;              // [n_inst] rebuild requested
     int *any;               // [1] any flag set
-    unsigned int *ticket;   // [3] last-block tickets (unused, unused, base-pair evaluation)
+    unsigned int *ticket;   // [3] last-block tickets (step kernel's trigger, unused, base-pair evaluation)
     unsigned int *gbar;     // [2] grid barrier of k_trigger_rebuild: arrivals, generation
     int *gsum;              // [kMaxCoopBlocks] per-block sums of the cell scan
-    int *part_inst;         // [2 * step blocks] per-block trigger partials: instance
-    unsigned long long *part_m; // [4 * step blocks] and its top-two displacement^2
     unsigned long long *step_ctr; // [1] Philox step counter
     int *err;               // [1] error flags
     int *max_need;          // [2] largest pair / bp count seen
@@ -322,6 +321,15 @@ __device__ __forceinline__ unsigned int fixed_res(double x, double s, float &r) 
     unsigned int q;
     fixed_mirror(x, s, q, r);
     return q;
+}
+
+// The displacement trigger of instance k (job_md.F90:376-395): the two
+// largest squared displacements since the last rebuild (FP64 bit patterns,
+// merged with integer atomics) move the instance by more than the list margin.
+__device__ __forceinline__ bool trigger_fires(const GlobP &g, const unsigned long long *m1, const unsigned long long *m2, int k) {
+    const double a = __longlong_as_double((long long)__ldcg(m1 + k));
+    const double b = __longlong_as_double((long long)__ldcg(m2 + k));
+    return sqrt(a) + sqrt(b) > g.nl_margin;
 }
 
 // A separation in fixed-point units: the exact mirror difference d (int32,

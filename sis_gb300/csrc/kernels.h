@@ -38,12 +38,16 @@ struct RemdDev {
     const float *lab_dgf; // [n_labels][469]
 };
 
-cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long noise_step, cudaStream_t st);
+// trigger != 0: the step kernel's last block decides the displacement trigger
+// and advances the step counter (off only in timing passes)
+cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long noise_step, cudaStream_t st,
+                        int trigger);
 cudaError_t launch_force(int G, const Dev &D, const GlobP &g, int cur, double *fout, int mask, cudaStream_t st);
 int force_kernels(const GlobP &g, int mask); // kernels launch_force launches
 // the step split in two: pair forces of every bead into fpair, then the step proper
 cudaError_t launch_pairs(int G, const Dev &D, const GlobP &g, int cur, cudaStream_t st);
-cudaError_t launch_step_split(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st);
+cudaError_t launch_step_split(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st,
+                              int trigger);
 cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int do_bp, int test_blocks, int eval_blocks,
                        cudaStream_t st);
 int pre_kernels(const GlobP &g, int do_bonded, int do_bp);
@@ -54,7 +58,6 @@ int bp_kernels(const GlobP &g);
 cudaError_t launch_bp_energy(const Dev &D, const GlobP &g, int cur, double tK, int bp_blocks, cudaStream_t st);
 // base-pair Monte Carlo removal of every instance whose pass is due (no-op without it)
 cudaError_t launch_bp_mc(const Dev &D, const GlobP &g, cudaStream_t st);
-int step_blocks(int G, int n);
 cudaError_t launch_remd_partner_ip(const Dev &D, const RemdDev &R, int n_inst, int parity, cudaStream_t st);
 cudaError_t launch_remd_decide(const Dev &D, const RemdDev &R, const GlobP &g, int parity, const double *u, double kB,
                                unsigned long long ctr, cudaStream_t st);
@@ -77,11 +80,9 @@ cudaError_t launch_init_velocities(const Dev &D, const GlobP &g, unsigned long l
 cudaError_t launch_mirror(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 // k_trigger_rebuild, one cooperative launch of `grid` blocks (at most
 // coop_blocks_per_sm() per SM, and at most kMaxCoopBlocks): after_step, the
-// displacement trigger of the step just taken (nparts: the step kernel's
-// blocks) and the rebuild of the instances that fired; otherwise the rebuild
-// of the instances the host flagged.
-cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, int grid,
-                           cudaStream_t st);
+// the rebuild of the flagged instances (flagged by the step kernel's trigger
+// or by the host); returns at once when none is flagged
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int grid, cudaStream_t st);
 int coop_blocks_per_sm();
 // the grid barrier with block `absent` missing (a self-test of its timeout)
 cudaError_t launch_barrier_probe(const Dev &D, int grid, int absent, cudaStream_t st);

@@ -64,53 +64,6 @@ __device__ bool grid_sync(const Dev &D) {
     return s_ok != 0;
 }
 
-// ------------------------------------------------------------ trigger
-// job_md.F90:376-395: the step kernel leaves per-block top-two squared
-// displacements (partials, or atomics into m1/m2 for blocks spanning many
-// instances); they are merged per instance into m1/m2 of the step's parity.
-__device__ __forceinline__ void top2_merge(unsigned long long &a1, unsigned long long &a2, unsigned long long b1,
-                                           unsigned long long b2) {
-    const unsigned long long lo = a1 < b1 ? a1 : b1;
-    a1 = a1 > b1 ? a1 : b1;
-    const unsigned long long m = a2 > b2 ? a2 : b2;
-    a2 = lo > m ? lo : m;
-}
-__device__ void trigger_reduce(const Dev &D, int nparts, unsigned long long *m1, unsigned long long *m2) {
-    const int lane = threadIdx.x & 31;
-    for (int base = blockIdx.x * blockDim.x; base < 2 * nparts; base += gridDim.x * blockDim.x) {
-        const int r = base + threadIdx.x;
-        const int inst = r < 2 * nparts ? D.part_inst[r] : -1;
-        unsigned long long a1 = 0ull, a2 = 0ull;
-        if (inst >= 0) {
-            a1 = D.part_m[2 * r];
-            a2 = D.part_m[2 * r + 1];
-        }
-        const int i0 = __shfl_sync(0xffffffffu, inst, 0);
-        const bool uniform = __all_sync(0xffffffffu, inst == i0 || inst < 0) && i0 >= 0;
-        if (uniform) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long b1 = __shfl_xor_sync(0xffffffffu, a1, o), b2 = __shfl_xor_sync(0xffffffffu, a2, o);
-                top2_merge(a1, a2, b1, b2);
-            }
-            if (lane == 0) {
-                const unsigned long long old = atomicMax(&m1[i0], a1);
-                const unsigned long long c2 = old < a1 ? old : a1;
-                atomicMax(&m2[i0], c2 > a2 ? c2 : a2);
-            }
-        } else if (inst >= 0) {
-            const unsigned long long old = atomicMax(&m1[inst], a1);
-            const unsigned long long c2 = old < a1 ? old : a1;
-            atomicMax(&m2[inst], c2 > a2 ? c2 : a2);
-        }
-    }
-}
-__device__ __forceinline__ bool trigger_fires(const GlobP &g, const unsigned long long *m1, const unsigned long long *m2, int k) {
-    const double a = __longlong_as_double((long long)__ldcg(m1 + k));
-    const double b = __longlong_as_double((long long)__ldcg(m2 + k));
-    return sqrt(a) + sqrt(b) > g.nl_margin;
-}
-
 // --------------------------------------------------- all-pairs (small)
 // items: (instance, first local bead); 32 beads per item, one warp per bead.
 __device__ void rebuild_small(const Dev &D, const GlobP &g, int cur, const int2 *items, int n_items, float slack) {
@@ -427,58 +380,21 @@ __device__ void rebuild_finish(const Dev &D, const GlobP &g) {
     if (threadIdx.x == 0) *D.any = 0;
 }
 
-// --------------------------------------------- trigger and rebuild kernel
-// One cooperative launch after every step (after_step) or on request.
-//  * after_step: the trigger.  Partials merge into m1/m2 of the step's parity
-//    (step counter & 1); after a grid barrier every block reads the merged
-//    values and decides alone whether any instance fired, so a step without a
-//    rebuild ends there.  Block 0 flags the instances that fired (clearing
-//    their base-pair staging counts), schedules the Monte Carlo pass
-//    (job_md.F90:364-367), clears m1/m2 of the other parity for the next
-//    step and advances the Philox step counter.
-//  * otherwise the host flagged the instances (flag, any); block 0 clears
-//    their staging counts.
-// The rebuild of the flagged instances follows, its phases separated by grid
-// barriers: wrap and cell binning; cell scan; fill; sort; the 27-cell search
-// and the all-pairs scan of small instances; finish.
-__global__ void __launch_bounds__(256) k_trigger_rebuild(Dev D, GlobP g, int cur, RebuildPlan pl, int nparts, int after_step) {
+// --------------------------------------------- rebuild kernel
+// One cooperative launch after every step, or on request: the rebuild of the
+// instances flagged by the step kernel's trigger or by the host (flag, any).
+// A step without a rebuild ends at once.  Block 0 clears the flagged
+// instances' base-pair staging counts; the rebuild phases follow, separated
+// by grid barriers: wrap and cell binning; cell scan; fill; sort; the 27-cell
+// search and the all-pairs scan of small instances; finish.
+__global__ void __launch_bounds__(256) k_trigger_rebuild(Dev D, GlobP g, int cur, RebuildPlan pl) {
     __shared__ int s_red[8];
     __shared__ int s_cl[8 * 2 * kClHash]; // per warp: cluster hash keys and ranks
     const float slack = 1.001f;
-    if (after_step) {
-        const unsigned long long ctr = *(volatile unsigned long long *)D.step_ctr;
-        const int p = (int)(ctr & 1ull);
-        unsigned long long *m1 = D.m1 + (size_t)p * g.n_inst, *m2 = D.m2 + (size_t)p * g.n_inst;
-        trigger_reduce(D, nparts, m1, m2);
-        if (!grid_sync(D)) return;
-        int fired = 0;
-        for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) fired |= trigger_fires(g, m1, m2, k);
-        const int any = __syncthreads_or(fired);
-        if (blockIdx.x == 0) {
-            unsigned long long *o1 = D.m1 + (size_t)(p ^ 1) * g.n_inst, *o2 = D.m2 + (size_t)(p ^ 1) * g.n_inst;
-            const bool mc = g.nstep_mc > 0 && (ctr + 2ull) % (unsigned long long)g.nstep_mc == 0ull;
-            for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) {
-                if (any && trigger_fires(g, m1, m2, k)) {
-                    D.flag[k] = 1;
-                    D.bp_cnt[k] = 0;
-                }
-                o1[k] = 0ull;
-                o2[k] = 0ull;
-                if (mc) D.mc_due[k] = 1;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                if (any) *D.any = 1;
-                *D.step_ctr = ctr + 1ull;
-            }
-        }
-        if (!any) return;
-    } else {
-        if (*(volatile int *)D.any == 0) return;
-        if (blockIdx.x == 0)
-            for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x)
-                if (D.flag[k]) D.bp_cnt[k] = 0;
-    }
+    if (*(volatile int *)D.any == 0) return;
+    if (blockIdx.x == 0)
+        for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x)
+            if (D.flag[k]) D.bp_cnt[k] = 0;
     if (!grid_sync(D)) return;
     if (pl.n_large_items > 0) {
         cell_bin(D, cur, pl.large_items, pl.n_large_items);
@@ -536,8 +452,7 @@ int coop_blocks_per_sm() {
     return nb;
 }
 
-cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int after_step, int nparts, int grid,
-                           cudaStream_t st) {
+cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildPlan &pl, int grid, cudaStream_t st) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(256);
@@ -548,7 +463,7 @@ cudaError_t launch_rebuild(const Dev &D, const GlobP &g, int cur, const RebuildP
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_trigger_rebuild, D, g, cur, pl, nparts, after_step);
+    return cudaLaunchKernelEx(&cfg, k_trigger_rebuild, D, g, cur, pl);
 }
 
 } // namespace sisg
