@@ -488,7 +488,8 @@ def serve_run(args, rank, world, seconds, scale):
 
     ff = read_ff(ROOT / "sis_gb300" / "data" / "sis.ff")
     jobs = job_stream(1005 + rank, args.serve_rate, seconds, steps_scale=scale)
-    classes = [(128, 16), (512, 16), (2048, 8)]
+    # one block per slot on the per-block kernel: 144 slots fill the 152 SMs
+    classes = [(128, 32), (512, 48), (2048, 64)]
     # warm-up session (graph capture, first-touch of every pool), not timed
     warm = Server(ff, sis_options(), classes=classes, seed=2024 + rank, force_cap=args.force_cap)
     warm.run(job_stream(7, 20.0, 0.5, steps_scale=scale))

@@ -82,6 +82,9 @@ struct sis_ctx {
     cudaStream_t st = nullptr;
     cudaEvent_t ev[kEvents]{};
     bool lists_valid = false, state_set = false, bp_cache = false;
+    // instances loaded by sis_gpu_load_slot whose lists the next per-block
+    // kernel launch rebuilds (flag set on the device)
+    bool stale_lists = false;
     long long launches = 0, steps = 0;
     std::string err;
     double *noise_d = nullptr;
@@ -341,7 +344,7 @@ int upload_dgf(sis_ctx *ctx, int k) {
     return SIS_OK;
 }
 
-int ensure_lists(sis_ctx *ctx);
+int ensure_lists(sis_ctx *ctx, bool small_step = false);
 
 int run_rebuild(sis_ctx *ctx) {
     ctx->launches++;
@@ -359,8 +362,20 @@ int flag_all(sis_ctx *ctx, int inst) {
     return SIS_OK;
 }
 
-int ensure_lists(sis_ctx *ctx) {
+// The lists current for every instance.  Slots loaded into a context that
+// steps through the per-block kernel are rebuilt by that kernel's next
+// launch (small_step: the caller launches it); any other caller rebuilds
+// them here.
+int ensure_lists(sis_ctx *ctx, bool small_step) {
     if (!ctx->state_set) return fail(ctx, SIS_ERR_STATE, "coordinates have not been set");
+    if (ctx->stale_lists && !small_step) {
+        const int one = 1;
+        CK(cudaMemcpyAsync(ctx->D.any, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+        int rc = run_rebuild(ctx);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(ctx->st));
+        ctx->stale_lists = false;
+    }
     if (ctx->lists_valid) return SIS_OK;
     int rc = flag_all(ctx, -1);
     if (rc) return rc;
@@ -514,10 +529,10 @@ int ensure_step_graph(sis_ctx *ctx) {
 // of the timing, since they would consume the pass that is due.
 int autotune(sis_ctx *ctx) {
     if (ctx->tuned) return SIS_OK;
-    // the mixed path's step kernel gathers no pair list (k_pairs_cl does), so
-    // one lane per bead is a candidate there
-    std::vector<int> gs = ctx->lanes_fixed ? std::vector<int>{ctx->G}
-                          : ctx->g.prec != 0 ? std::vector<int>{1, 2, 4, 8}
+    // (the mixed path's step kernel runs one thread per bead whatever G is:
+    // only the overlap is tuned there)
+    std::vector<int> gs = ctx->g.prec != 0 ? std::vector<int>{1}
+                          : ctx->lanes_fixed ? std::vector<int>{ctx->G}
                                              : std::vector<int>{2, 4, 8, 16};
     std::vector<int> ovs = ctx->overlap_mode >= 0 ? std::vector<int>{ctx->overlap_mode} : std::vector<int>{0, 1};
     if (gs.size() * ovs.size() == 1) {
@@ -681,6 +696,7 @@ int run_small(sis_ctx *ctx, int64_t nsteps, const double *noise) {
         ctx->launches += 3;
         ctx->cur ^= chunk & 1;
         s += chunk;
+        ctx->stale_lists = false;
     }
     return SIS_OK;
 }
@@ -816,6 +832,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
             nb += len;
         }
         I.n = nb - I.bead_off;
+        I.n_act = I.n;
         I.stream = top->stream ? top->stream[k] : (unsigned)k;
         I.twz_scale = 1.0;
         I.step0 = 0ull;
@@ -1440,7 +1457,7 @@ extern "C" int sis_gpu_energy_kinetic(sis_ctx *ctx, int32_t inst, double *ekin) 
 extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     DevGuard dg_(ctx);
     if (!ctx || nsteps < 0) return SIS_ERR_ARG;
-    int rc = ensure_lists(ctx);
+    int rc = ensure_lists(ctx, nsteps > 0 && small_active(ctx));
     if (rc) return rc;
     if (!noise && nsteps >= 64 && !small_active(ctx) && (rc = autotune(ctx))) return rc;
     if (noise) {
@@ -1940,10 +1957,10 @@ extern "C" int sis_gpu_step_noise_static(sis_ctx *ctx, int64_t nsteps, const dou
     double *buf = nullptr;
     int rc = noise_scratch(ctx, &buf);
     if (rc) return rc;
-    rc = ensure_lists(ctx);
+    const bool small = small_active(ctx);
+    rc = ensure_lists(ctx, nsteps > 0 && small);
     if (rc) return rc;
     const size_t per = (size_t)ctx->n * 3;
-    const bool small = small_active(ctx);
     if (small && !ctx->sp.n_cta && (rc = small_plan(ctx, std::min(ctx->n_inst, 2 * ctx->sms)))) return rc;
     for (int64_t s = 0; s < nsteps; ++s) {
         // stream-ordered: the copy waits for the previous step's kernels
@@ -2206,13 +2223,15 @@ extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, c
         ctx->binfo[b] = make_int4(inst, b, 1, 4 << 24);
         ctx->seq[b] = 4;
     }
+    I.n_act = L;
     // conditions; the noise counter of the job starts at the current step
     I.tempK = tempK;
     ctx->ionic[inst] = ionic;
     set_ele(ctx, inst);
     I.stream = stream;
     unsigned long long sc = 0;
-    CK(cudaMemcpy(&sc, ctx->D.step_ctr, sizeof(sc), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(&sc, ctx->D.step_ctr, sizeof(sc), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
     I.step0 = sc;
     // a new job starts with no frozen beads
     if (!ctx->frozen.empty()) std::fill(ctx->frozen.begin() + off, ctx->frozen.begin() + off + n, (uint8_t)0);
@@ -2233,21 +2252,33 @@ extern "C" int sis_gpu_load_slot(sis_ctx *ctx, int32_t inst, int32_t n_chains, c
         const int j = i < L ? i : 0;
         h[i] = L > 0 ? make_double4(xyz[3 * j], xyz[3 * j + 1], xyz[3 * j + 2], 0.0) : make_double4(0.0, 0.0, 0.0, 0.0);
     }
-    CK(cudaMemcpyAsync(ctx->D.x[ctx->cur] + off, h, sizeof(double4) * n, cudaMemcpyHostToDevice, ctx->st));
+    // both position buffers (and their mirrors): the per-block kernel never
+    // moves the fillers, so they stay the same in both
+    for (int c = 0; c < 2; ++c) {
+        CK(cudaMemcpyAsync(ctx->D.x[c] + off, h, sizeof(double4) * n, cudaMemcpyHostToDevice, ctx->st));
+        CK(launch_mirror(ctx->D, ctx->g, c, ctx->st));
+    }
     CK(cudaMemsetAsync(ctx->D.v + off, 0, sizeof(double4) * n, ctx->st));
     CK(cudaMemsetAsync(ctx->D.beta + off, 0, sizeof(double4) * n, ctx->st));
     CK(cudaMemsetAsync(ctx->D.move + off, 0, sizeof(double4) * n, ctx->st));
-    CK(launch_mirror(ctx->D, ctx->g, ctx->cur, ctx->st));
-    ctx->launches++;
+    ctx->launches += 2;
     // velocities as the first sis_gpu_init_velocities of a context would draw them
     if (init_velocities) {
         CK(launch_init_velocities(ctx->D, ctx->g, 1ull << 62, ctx->st, inst));
         ctx->launches++;
     }
-    // the slot's lists, now (with every coordinate set)
+    // the slot's lists (with every coordinate set): in a context that steps
+    // through the per-block kernel, that kernel's next launch rebuilds them
+    // (the slot flagged); otherwise now
     if (ctx->state_set) {
-        if ((rc = flag_all(ctx, inst))) return rc;
-        if ((rc = run_rebuild(ctx))) return rc;
+        if (small_active(ctx)) {
+            const int one = 1;
+            CK(cudaMemcpyAsync(ctx->D.flag + inst, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->st));
+            ctx->stale_lists = true;
+        } else {
+            if ((rc = flag_all(ctx, inst))) return rc;
+            if ((rc = run_rebuild(ctx))) return rc;
+        }
     }
     ctx->bp_cache = false;
     CK(cudaStreamSynchronize(ctx->st));
@@ -2265,8 +2296,6 @@ extern "C" int sis_gpu_bp_mc(sis_ctx *ctx, int32_t inst, const double *draws, in
     if (n_draws > 0) {
         if (n_draws > ctx->mc_draws_cap) {
             if (ctx->mc_draws_d) cudaFree(ctx->mc_draws_d);
-    if (ctx->ss_start_d) cudaFree(ctx->ss_start_d);
-    if (ctx->ss_part_d) cudaFree(ctx->ss_part_d);
             ctx->mc_draws_d = nullptr;
             if (cudaMalloc(&ctx->mc_draws_d, sizeof(double) * n_draws) != cudaSuccess) return fail(ctx, SIS_ERR_NOMEM, "bp_mc draws");
             ctx->mc_draws_cap = n_draws;

@@ -97,6 +97,7 @@ struct InstP {
     float finv[3];     // Angstrom per unit
     int pbc;
     int bead_off, n;   // beads [bead_off, bead_off + n)
+    int n_act;         // the first n_act of them move; the rest are inert fillers of a slot (sis_gpu_load_slot)
     int cl_off;        // first i-cluster of the instance
     int bp_off, bp_cap;// base-pair staging segment
     double tempK;

@@ -1136,60 +1136,66 @@ __global__ void __launch_bounds__(256, 5) k_pairs_cl(Dev D, GlobP g, int cur, in
     if (q == 0 && a < cnt) reinterpret_cast<float4 *>(D.fpair)[first + a] = make_float4(sx, sy, sz, 0.f);
 }
 
-// One component c of bead ii of the mixed path's GJF-2GJ / Ermak-McCammon
-// update (job_md.F90:415-456): the force F and the noise enter as FP32
-// increments (cf: the force and noise coefficients of mdc in FP32), the
-// velocity and the position accumulate in FP64; writes the new position,
-// velocity, noise term, mirror and residual (buffer cur ^ 1) and returns the
-// new mirror component (r: its residual).
-__device__ __forceinline__ unsigned int mixed_update(const Dev &D, const GlobP &g, int cur, int ii, int c, float F, float cf0,
-                                                     float cf1, const double *noise, long long noise_step,
-                                                     unsigned long long step, float &r) {
-    const InstP &jp = D.ip[D.binfo[ii].x];
-    const float xi = noise ? (float)noise[((size_t)noise_step * g.n + ii) * 3 + c]
-                           : gauss_f(g.seed, ii - jp.bead_off, step - jp.step0, c, jp.stream);
-    double *vp = reinterpret_cast<double *>(D.v + ii) + c;
-    double *bp = reinterpret_cast<double *>(D.beta + ii) + c;
-    double dx;
-    if (g.integrator == 1) {
-        const double4 m = D.mdc[ii];
-        const float bn = cf1 * xi;
-        const double vn = fma(m.x, *vp, *bp) + (double)fmaf(cf0, F, bn);
-        *bp = (double)bn;
-        *vp = vn;
-        dx = m.z * vn;
-    } else {
-        dx = (double)fmaf(cf0, F, cf1 * xi);
+// The end of a step kernel: each block merges its per-instance top two
+// squared displacements (s_m1/s_m2 for instances s_lo .. s_lo + s_cnt - 1,
+// when s_cnt <= 32; otherwise its threads merged them already) into m1/m2 of
+// the step's parity (mo).  With decide, the last block to finish decides the
+// trigger (job_md.F90:376-395) once every block's top two are merged: it
+// flags the instances that fired (clearing their base-pair staging counts)
+// for the rebuild kernel that follows, schedules the Monte Carlo pass
+// (job_md.F90:364-367), clears m1/m2 of the other parity for the next step
+// and advances the Philox step counter (every block read it before).  Called
+// by every thread of the block after a barrier.
+__device__ __forceinline__ void trigger_merge_decide(const Dev &D, const GlobP &g, const unsigned long long *s_m1,
+                                                     const unsigned long long *s_m2, int s_lo, int s_cnt, size_t mo,
+                                                     unsigned long long step, bool decide) {
+    if (s_cnt <= 32 && (int)threadIdx.x < s_cnt) {
+        const unsigned long long b1 = s_m1[threadIdx.x], b2 = s_m2[threadIdx.x];
+        const int inst = s_lo + threadIdx.x;
+        const unsigned long long old = atomicMax(&D.m1[mo + inst], b1);
+        const unsigned long long c2 = old < b1 ? old : b1;
+        atomicMax(&D.m2[mo + inst], c2 > b2 ? c2 : b2);
     }
-    const double xn = reinterpret_cast<const double *>(x_at(D, cur) + ii)[c] + dx;
-    unsigned int qm;
-    if (!fixed_mirror(xn, jp.fsc[c], qm, r)) atomicOr(D.err, ERR_NONFINITE);
-    reinterpret_cast<double *>(x_at(D, cur ^ 1) + ii)[c] = xn;
-    reinterpret_cast<unsigned int *>(mir_at(D, cur ^ 1) + ii)[c] = qm;
-    reinterpret_cast<float *>(res_at(D, cur ^ 1) + ii)[c] = r;
-    return qm;
+    if (!decide) return;
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&D.ticket[0], 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const unsigned long long *m1 = D.m1 + mo, *m2 = D.m2 + mo;
+    unsigned long long *o1 = D.m1 + (mo ? 0 : g.n_inst), *o2 = D.m2 + (mo ? 0 : g.n_inst);
+    const bool mc = g.nstep_mc > 0 && (step + 2ull) % (unsigned long long)g.nstep_mc == 0ull;
+    int fired = 0;
+    for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) {
+        if (trigger_fires(g, m1, m2, k)) {
+            D.flag[k] = 1;
+            D.bp_cnt[k] = 0;
+            fired = 1;
+        }
+        o1[k] = 0ull;
+        o2[k] = 0ull;
+        if (mc) D.mc_due[k] = 1;
+    }
+    fired = __syncthreads_or(fired);
+    if (threadIdx.x == 0) {
+        if (fired) *D.any = 1;
+        *D.step_ctr = step + 1ull;
+        D.ticket[0] = 0u;
+    }
 }
 
-// mixed_update for the three components of bead ii at once: one Philox
-// block for the noise, vector loads and stores of the bead's state; the same
-// operations, component by component, as mixed_update.  Returns the new
-// mirror (w unused).
-__device__ __forceinline__ uint4 mixed_update_bead(const Dev &D, const GlobP &g, int cur, int ii, const float F[3], float cf0, float cf1,
-                                                   const double *noise, long long noise_step, unsigned long long step,
-                                                   float4 *res_out = nullptr) {
-    const InstP &jp = D.ip[D.binfo[ii].x];
-    float xi[3];
-    if (noise) {
-        const double *nz = noise + ((size_t)noise_step * g.n + ii) * 3;
-        xi[0] = (float)nz[0];
-        xi[1] = (float)nz[1];
-        xi[2] = (float)nz[2];
-    } else {
-        gauss_f3(g.seed, ii - jp.bead_off, step - jp.step0, jp.stream, xi);
-    }
-    const double4 x = x_at(D, cur)[ii];
-    const double4 m = D.mdc[ii];
-    double4 v = D.v[ii], b = D.beta[ii];
+// The mixed path's GJF-2GJ / Ermak-McCammon update of bead ii
+// (job_md.F90:415-456) from its loaded state (x, v, beta, coefficients m):
+// the force F and the noise xi enter as FP32 increments (cf0, cf1: the force
+// and noise coefficients of m in FP32), the velocity and the position
+// accumulate in FP64.  Writes the new position, velocity, noise term, mirror
+// and residual (buffer cur ^ 1); returns the new mirror (w unused) and, if
+// asked, the residual.
+__device__ __forceinline__ uint4 mixed_update_core(const Dev &D, const GlobP &g, int cur, int ii, const InstP &jp, const float F[3],
+                                                   float cf0, float cf1, const float xi[3], const double4 &x, const double4 &m,
+                                                   const double4 &v, const double4 &b, float4 *res_out) {
     double xc[3] = {x.x, x.y, x.z}, vc[3] = {v.x, v.y, v.z}, bc[3] = {b.x, b.y, b.z};
     unsigned int q[3];
     float r[3];
@@ -1222,6 +1228,93 @@ __device__ __forceinline__ uint4 mixed_update_bead(const Dev &D, const GlobP &g,
     if (res_out) *res_out = rq;
     return mq;
 }
+// the noise of bead ii at a step: fed (FP64, rounded to FP32) or Philox
+__device__ __forceinline__ void mixed_noise(const GlobP &g, int ii, const InstP &jp, const double *noise, long long noise_step,
+                                            unsigned long long step, float xi[3]) {
+    if (noise) {
+        const double *nz = noise + ((size_t)noise_step * g.n + ii) * 3;
+        xi[0] = (float)nz[0];
+        xi[1] = (float)nz[1];
+        xi[2] = (float)nz[2];
+    } else {
+        gauss_f3(g.seed, ii - jp.bead_off, step - jp.step0, jp.stream, xi);
+    }
+}
+// The mixed path's step, one thread per bead, after k_pairs_cl: every load
+// of the bead's step (pair force, bonded slot planes, base-pair sum, FP64
+// state, coefficients, the mirror at the last rebuild) issues before any is
+// used; then the force sum (pair + bonded in slot order + base pair), the
+// cap, the update (mixed_update_core) and the squared displacement since
+// the last rebuild into its instance's top two; the block's top two are
+// merged and the last block decides the trigger (mask bit 256).
+__global__ void __launch_bounds__(256) k_step_mixed(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
+                                                    int mask) {
+    __shared__ unsigned long long s_m1[32], s_m2[32];
+    __shared__ int s_lo, s_cnt;
+    const int i0 = blockIdx.x * blockDim.x;
+    const int ii = i0 + threadIdx.x;
+    const bool active = ii < g.n;
+    const int i = active ? ii : g.n - 1;
+    if (threadIdx.x < 32) {
+        s_m1[threadIdx.x] = 0ull;
+        s_m2[threadIdx.x] = 0ull;
+    }
+    if (threadIdx.x == 0) {
+        const int i1 = min(i0 + (int)blockDim.x - 1, g.n - 1);
+        s_lo = D.binfo[i0].x;
+        s_cnt = D.binfo[i1].x - s_lo + 1;
+    }
+    const int4 bi = D.binfo[i];
+    const InstP &jp = D.ip[bi.x];
+    const float4 fp = reinterpret_cast<const float4 *>(D.fpair)[i];
+    const double4 fb = D.fbp[i];
+    const double4 x = x_at(D, cur)[i], m = D.mdc[i], v = D.v[i], b = D.beta[i];
+    const uint4 m0 = D.mir0[i];
+    const unsigned long long step = *D.step_ctr;
+    const V3<float> ab = (mask & 7) ? bonded_gather<float>(D, g, bi, 0, 1, mask) : mk<float>(0.f, 0.f, 0.f);
+    float xi[3];
+    mixed_noise(g, i, jp, noise, noise_step, step, xi);
+    float F[3] = {fp.x + ab.x, fp.y + ab.y, fp.z + ab.z};
+    if (mask & 136) {
+        F[0] += fx_float(fb.x);
+        F[1] += fx_float(fb.y);
+        F[2] += fx_float(fb.z);
+        if (active) D.fbp[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+    }
+    if (g.fcap_f > 0.f) {
+        const float fm = sqrtf(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+        if (fm > g.fcap_f) {
+            const float sc = g.fcap_f / fm;
+            F[0] *= sc;
+            F[1] *= sc;
+            F[2] *= sc;
+            if (active) atomicAdd(D.capped, 1ull);
+        }
+    }
+    // GJF-2GJ: F -> sqrt(b) h / m, noise -> its amplitude; Ermak-McCammon: F -> h / gamma
+    const float cf0 = (float)(g.integrator == 1 ? m.y : m.x), cf1 = (float)m.w;
+    uint4 q = m0;
+    if (active) q = mixed_update_core(D, g, cur, i, jp, F, cf0, cf1, xi, x, m, v, b, nullptr);
+    // the exact integer displacement since the last rebuild
+    const float dx = (float)(int)(q.x - m0.x) * jp.finv[0];
+    const float dy = (float)(int)(q.y - m0.y) * jp.finv[1];
+    const float dz = (float)(int)(q.z - m0.z) * jp.finv[2];
+    const unsigned long long bits = (unsigned long long)__double_as_longlong((double)fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+    const size_t mo = (size_t)(step & 1ull) * g.n_inst;
+    __syncthreads();
+    if (active) {
+        if (s_cnt <= 32) {
+            const int k = bi.x - s_lo;
+            const unsigned long long old = atomicMax(&s_m1[k], bits);
+            atomicMax(&s_m2[k], old < bits ? old : bits);
+        } else {
+            const unsigned long long old = atomicMax(&D.m1[mo + bi.x], bits);
+            atomicMax(&D.m2[mo + bi.x], old < bits ? old : bits);
+        }
+    }
+    __syncthreads();
+    trigger_merge_decide(D, g, s_m1, s_m2, s_lo, s_cnt, mo, step, mask & 256);
+}
 
 template <typename R, int G, int MODE>
 __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const double *__restrict__ noise, long long noise_step,
@@ -1230,8 +1323,6 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     __shared__ R sA[3][BPB], sB[3][BPB];
     __shared__ float sScale[BPB];
     __shared__ double sM[3][BPB];
-    __shared__ float sCf[2][BPB];       // mixed path: FP32 force and noise coefficients of the update
-    __shared__ unsigned int sQ[3][BPB]; // mixed path: the new mirror
     __shared__ unsigned long long s_m1[32], s_m2[32];
     __shared__ int s_lo, s_cnt;
     const int b = threadIdx.x / G;
@@ -1276,38 +1367,7 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
         ab.y += __shfl_xor_sync(0xffffffffu, ab.y, o, G);
         ab.z += __shfl_xor_sync(0xffffffffu, ab.z, o, G);
     }
-    if constexpr (sizeof(R) == 4 && MODE == 0) {
-        // mixed path: the step's whole FP32 force, pair + bonded + base pair
-        // (fixed point, consumed and cleared here), capped, then its update
-        // coefficients; the update below reads them from shared memory
-        if (lane == 0) {
-            float fx = an.x + ab.x, fy = an.y + ab.y, fz = an.z + ab.z;
-            if ((mask & 136) && active) {
-                const double4 fb = D.fbp[i];
-                fx += fx_float(fb.x);
-                fy += fx_float(fb.y);
-                fz += fx_float(fb.z);
-                D.fbp[i] = make_double4(0.0, 0.0, 0.0, 0.0);
-            }
-            if (g.fcap_f > 0.f) {
-                const float fm = sqrtf(fx * fx + fy * fy + fz * fz);
-                if (fm > g.fcap_f) {
-                    const float sc = g.fcap_f / fm;
-                    fx *= sc;
-                    fy *= sc;
-                    fz *= sc;
-                    if (active) atomicAdd(D.capped, 1ull);
-                }
-            }
-            sA[0][b] = fx;
-            sA[1][b] = fy;
-            sA[2][b] = fz;
-            // GJF-2GJ: F -> sqrt(b) h / m, noise -> its amplitude; Ermak-McCammon: F -> h / gamma
-            const double4 m = D.mdc[i];
-            sCf[0][b] = (float)(g.integrator == 1 ? m.y : m.x);
-            sCf[1][b] = (float)m.w;
-        }
-    } else if (lane == 0) {
+    if (lane == 0) {
         sA[0][b] = an.x;
         sA[1][b] = an.y;
         sA[2][b] = an.z;
@@ -1337,41 +1397,20 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     // fraction of the FP32 rate on this part, so the block spreads it over
     // 3*BPB threads (whole warps) instead of BPB.
     const unsigned long long step = MODE == 0 ? *D.step_ctr : 0ull;
-    if constexpr (sizeof(R) == 4 && MODE == 0) {
-        // mixed path: one thread per bead (mixed_update_bead)
-        for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
-            const int ii = i0 + bb;
-            if (ii >= g.n) continue;
-            const float F[3] = {sA[0][bb], sA[1][bb], sA[2][bb]};
-            const uint4 q = mixed_update_bead(D, g, cur, ii, F, sCf[0][bb], sCf[1][bb], noise, noise_step, step);
-            sQ[0][bb] = q.x;
-            sQ[1][bb] = q.y;
-            sQ[2][bb] = q.z;
-        }
-    } else
     for (int t = threadIdx.x; t < 3 * BPB; t += blockDim.x) {
         const int c = t / BPB, bb = t - c * BPB;
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
         double *fp = reinterpret_cast<double *>(D.fbp + ii) + c;
         if constexpr (sizeof(R) == 4) {
-            // Mixed path: the force (FP32 lane sums plus the fixed-point
-            // base-pair force) and the noise enter as FP32 increments; the
-            // velocity and the position accumulate in FP64.  The mirror and
-            // its residual come from the new FP64 position (fixed_mirror).
+            // mixed path, forces only (its step is k_step_mixed): the FP32
+            // sums plus the fixed-point base-pair force
             float fb = 0.f;
             if (mask & 136) {
                 fb = fx_float(*fp);
                 *fp = 0.0;
             }
-            float F = sA[c][bb] + sB[c][bb] + fb;
-            if (MODE == 1) {
-                fout[3 * (size_t)ii + c] = (double)F;
-                continue;
-            }
-            F *= sScale[bb];
-            float r;
-            sQ[c][bb] = mixed_update(D, g, cur, ii, c, F, sCf[0][bb], sCf[1][bb], noise, noise_step, step, r);
+            fout[3 * (size_t)ii + c] = (double)(sA[c][bb] + sB[c][bb] + fb);
             continue;
         } else {
             double Fc;
@@ -1425,20 +1464,9 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
     for (int bb = threadIdx.x; bb < BPB; bb += blockDim.x) {
         const int ii = i0 + bb;
         if (ii >= g.n) continue;
-        double d2;
-        if constexpr (sizeof(R) == 4) {
-            // mixed path: the exact integer displacement since the last rebuild
-            const uint4 m0 = D.mir0[ii];
-            const float* fi = D.ip[D.binfo[ii].x].finv;
-            const float dx = (float)(int)(sQ[0][bb] - m0.x) * fi[0];
-            const float dy = (float)(int)(sQ[1][bb] - m0.y) * fi[1];
-            const float dz = (float)(int)(sQ[2][bb] - m0.z) * fi[2];
-            d2 = (double)fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        } else {
-            const double mx = sM[0][bb], my = sM[1][bb], mz = sM[2][bb];
-            d2 = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
-            if (!isfinite(d2)) atomicOr(D.err, ERR_NONFINITE);
-        }
+        const double mx = sM[0][bb], my = sM[1][bb], mz = sM[2][bb];
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(mx, mx), __dmul_rn(my, my)), __dmul_rn(mz, mz));
+        if (!isfinite(d2)) atomicOr(D.err, ERR_NONFINITE);
         const unsigned long long bits = (unsigned long long)__double_as_longlong(d2);
         const int inst = D.binfo[ii].x;
         if (s_cnt <= 32) {
@@ -1451,47 +1479,7 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
         }
     }
     __syncthreads();
-    if (s_cnt <= 32 && (int)threadIdx.x < s_cnt) {
-        const unsigned long long b1 = s_m1[threadIdx.x], b2 = s_m2[threadIdx.x];
-        const int inst = s_lo + threadIdx.x;
-        const unsigned long long old = atomicMax(&D.m1[mo + inst], b1);
-        const unsigned long long c2 = old < b1 ? old : b1;
-        atomicMax(&D.m2[mo + inst], c2 > b2 ? c2 : b2);
-    }
-    if (!(mask & 256)) return;
-    // The trigger (job_md.F90:376-395), decided by the last block to finish
-    // once every block's top two are merged: it flags the instances that
-    // fired (clearing their base-pair staging counts) for the rebuild kernel
-    // that follows, schedules the Monte Carlo pass (job_md.F90:364-367),
-    // clears m1/m2 of the other parity for the next step and advances the
-    // Philox step counter (every block read it above).
-    __shared__ int s_last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&D.ticket[0], 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (!s_last) return;
-    __threadfence();
-    const unsigned long long *m1 = D.m1 + mo, *m2 = D.m2 + mo;
-    unsigned long long *o1 = D.m1 + (mo ? 0 : g.n_inst), *o2 = D.m2 + (mo ? 0 : g.n_inst);
-    const bool mc = g.nstep_mc > 0 && (step + 2ull) % (unsigned long long)g.nstep_mc == 0ull;
-    int fired = 0;
-    for (int k = threadIdx.x; k < g.n_inst; k += blockDim.x) {
-        if (trigger_fires(g, m1, m2, k)) {
-            D.flag[k] = 1;
-            D.bp_cnt[k] = 0;
-            fired = 1;
-        }
-        o1[k] = 0ull;
-        o2[k] = 0ull;
-        if (mc) D.mc_due[k] = 1;
-    }
-    fired = __syncthreads_or(fired);
-    if (threadIdx.x == 0) {
-        if (fired) *D.any = 1;
-        *D.step_ctr = step + 1ull;
-        D.ticket[0] = 0u;
-    }
+    trigger_merge_decide(D, g, s_m1, s_m2, s_lo, s_cnt, mo, step, mask & 256);
 }
 
 // ======================================================== small instances
@@ -1543,8 +1531,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     uint4 *s_mir = (uint4 *)s_dyn;
     float4 *s_res = (float4 *)(s_mir + cap);
     double4 *s_fbp = (double4 *)(s_res + cap);
-    float4 *s_F = (float4 *)(s_fbp + cap);   // force of the step (xyz) and the force coefficient (w)
-    float *s_cn = (float *)(s_F + cap);      // noise coefficient
+    float4 *s_F = (float4 *)(s_fbp + cap);   // pair force of the step (xyz)
     __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst];
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
@@ -1560,10 +1547,10 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const InstP &ip = D.ip[id];
             s_iid[q] = id;
             s_off[q] = ip.bead_off;
-            s_n[q] = ip.n;
+            s_n[q] = ip.n_act;
             s_sb[q] = sb;
             s_bp[q] = nbp;
-            sb += ip.n;
+            sb += ip.n_act;
             nbp += min(D.bp_cnt[id], ip.bp_cap);
         }
         s_sb[ni] = sb;
@@ -1581,6 +1568,71 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         s_fbp[s] = make_double4(0.0, 0.0, 0.0, 0.0);
     }
     __syncthreads();
+    // the rebuild of the instances with s_fire set (neighbor_list.F90), from
+    // the mirrors of buffer c, over their moving beads (a slot's fillers take
+    // part in no term: with all_beads, their lists are emptied too); ends
+    // with s_any cleared
+    auto rebuild = [&](int c, bool all_beads) {
+        const int cur = c;
+        for (int q = 0; q < ni; ++q) {
+            if (!s_fire[q]) continue;
+            const int id = s_iid[q], off = s_off[q], na = s_n[q];
+            const InstP &ip = D.ip[id];
+            const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], off);
+            const float maxcut2f = scan_cut2f(ip, 1.001f);
+            for (int li = warp; li < na; li += nwarps) {
+                const int gi = off + li;
+                double4 xi_w;
+                bead_begin(E, cur, gi, ip, lane, xi_w);
+                const int4 bii = D.binfo[gi];
+                const uint4 mi = s_mir[s_sb[q] + li];
+                int count = 0;
+                for (int jb = 0; jb < na; jb += 32) {
+                    const int lj = jb + lane;
+                    int f = 0;
+                    const int gj = off + lj;
+                    if (lj < na && lj != li) f = test_pair(E, g, ip, cur, gi, bii, mi, xi_w, gj, maxcut2f, id);
+                    warp_append(D, g, gi, lane, f, gj, count);
+                }
+                bead_end(D, g, gi, lane, count);
+            }
+            if (all_beads)
+                for (int li = na + tid; li < ip.n; li += nt) D.nnbr[off + li] = 0;
+        }
+        __syncthreads();
+        if (g.any_ss)
+            for (int q = 0; q < ni; ++q)
+                if (s_fire[q] && D.ip[s_iid[q]].ss_on)
+                    for (int li = tid; li < s_n[q]; li += nt) ss_records(D, g, cur, s_off[q] + li, s_iid[q]);
+        __syncthreads();
+        if (tid == 0) {
+            int nbp = 0, nfired = 0;
+            for (int q = 0; q < ni; ++q) {
+                s_bp[q] = nbp;
+                nbp += min(__ldcg(D.bp_cnt + s_iid[q]), D.ip[s_iid[q]].bp_cap);
+                if (s_fire[q]) {
+                    D.flag[s_iid[q]] = 1;
+                    ++nfired;
+                }
+            }
+            s_bp[ni] = nbp;
+            atomicAdd((unsigned long long *)D.rebuilds, (unsigned long long)nfired);
+        }
+        __syncthreads();
+        if (tid == 0) s_any = 0;
+    };
+    // instances flagged before the launch (slots loaded since the last
+    // launch): their lists first
+    if (tid < ni) {
+        const int f = __ldcg(D.flag + s_iid[tid]) != 0;
+        s_fire[tid] = f;
+        if (f) {
+            s_any = 1;
+            D.bp_cnt[s_iid[tid]] = 0;
+        }
+    }
+    __syncthreads();
+    if (s_any) rebuild(cur, true);
     const unsigned long long step0 = *D.step_ctr;
     for (int st = 0; st < nsteps; ++st) {
         // Forces.  Base pairs, bonded terms and pair forces need no barrier
@@ -1689,11 +1741,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                     fy += __shfl_xor_sync(0xffffffffu, fy, o, kSmallLanes);
                     fz += __shfl_xor_sync(0xffffffffu, fz, o, kSmallLanes);
                 }
-                if (sub == 0 && s0 < nb) {
-                    const double4 mc = D.mdc[gi];
-                    s_F[s] = make_float4(fx, fy, fz, (float)(g.integrator == 1 ? mc.y : mc.x));
-                    s_cn[s] = (float)mc.w;
-                }
+                if (sub == 0 && s0 < nb) s_F[s] = make_float4(fx, fy, fz, 0.f);
             }
         }
         __syncthreads();
@@ -1704,9 +1752,14 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         for (int s = tid; s < nb; s += nt) {
             const int q = small_inst(s_sb, ni, s);
             const int gi = s_off[q] + (s - s_sb[q]);
+            // every global load of the bead's update first
             const uint4 m0 = D.mir0[gi];
             const int4 bi = D.binfo[gi];
+            const double4 x = x_at(D, cur)[gi], mc = D.mdc[gi], v = D.v[gi], b = D.beta[gi];
+            const InstP &jp = D.ip[s_iid[q]];
             const V3<float> ab = bonded_gather<float>(D, g, bi, 0, 1, 7);
+            float xi[3];
+            mixed_noise(g, gi, jp, noise, st, step, xi);
             const float4 F4 = s_F[s];
             const double4 fb = s_fbp[s];
             s_fbp[s] = make_double4(0.0, 0.0, 0.0, 0.0);
@@ -1722,10 +1775,12 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 }
             }
             float4 r4;
-            const uint4 m1 = mixed_update_bead(D, g, cur, gi, F, F4.w, s_cn[s], noise, st, step, &r4);
+            // GJF-2GJ: F -> sqrt(b) h / m, noise -> its amplitude; Ermak-McCammon: F -> h / gamma
+            const float cf0 = (float)(g.integrator == 1 ? mc.y : mc.x), cf1 = (float)mc.w;
+            const uint4 m1 = mixed_update_core(D, g, cur, gi, jp, F, cf0, cf1, xi, x, mc, v, b, &r4);
             s_mir[s] = m1;
             s_res[s] = r4;
-            const float *fi = D.ip[s_iid[q]].finv;
+            const float *fi = jp.finv;
             const float dx = (float)(int)(m1.x - m0.x) * fi[0];
             const float dy = (float)(int)(m1.y - m0.y) * fi[1];
             const float dz = (float)(int)(m1.z - m0.z) * fi[2];
@@ -1745,53 +1800,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         }
         __syncthreads();
         cur ^= 1;
-        if (s_any) {
-            // ------------------------------------------------ rebuild (neighbor_list.F90)
-            for (int q = 0; q < ni; ++q) {
-                if (!s_fire[q]) continue;
-                const int id = s_iid[q], off = s_off[q];
-                const InstP &ip = D.ip[id];
-                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], off);
-                const float maxcut2f = scan_cut2f(ip, 1.001f);
-                for (int li = warp; li < ip.n; li += nwarps) {
-                    const int gi = off + li;
-                    double4 xi_w;
-                    bead_begin(E, cur, gi, ip, lane, xi_w);
-                    const int4 bii = D.binfo[gi];
-                    const uint4 mi = s_mir[s_sb[q] + li];
-                    int count = 0;
-                    for (int jb = 0; jb < ip.n; jb += 32) {
-                        const int lj = jb + lane;
-                        int f = 0;
-                        const int gj = off + lj;
-                        if (lj < ip.n && lj != li) f = test_pair(E, g, ip, cur, gi, bii, mi, xi_w, gj, maxcut2f, id);
-                        warp_append(D, g, gi, lane, f, gj, count);
-                    }
-                    bead_end(D, g, gi, lane, count);
-                }
-            }
-            __syncthreads();
-            if (g.any_ss)
-                for (int q = 0; q < ni; ++q)
-                    if (s_fire[q] && D.ip[s_iid[q]].ss_on)
-                        for (int li = tid; li < s_n[q]; li += nt) ss_records(D, g, cur, s_off[q] + li, s_iid[q]);
-            __syncthreads();
-            if (tid == 0) {
-                int nbp = 0, nfired = 0;
-                for (int q = 0; q < ni; ++q) {
-                    s_bp[q] = nbp;
-                    nbp += min(__ldcg(D.bp_cnt + s_iid[q]), D.ip[s_iid[q]].bp_cap);
-                    if (s_fire[q]) {
-                        D.flag[s_iid[q]] = 1;
-                        ++nfired;
-                    }
-                }
-                s_bp[ni] = nbp;
-                atomicAdd((unsigned long long *)D.rebuilds, (unsigned long long)nfired);
-            }
-            __syncthreads();
-            if (tid == 0) s_any = 0;
-        }
+        if (s_any) rebuild(cur, false);
     }
 }
 
@@ -1908,11 +1917,16 @@ static cudaError_t launch_step_r(int G, const Dev &D, const GlobP &g, int cur, c
 
 // (trigger: the last block decides the displacement trigger and advances the
 // step counter; off only in the autotuner's timing passes)
+static cudaError_t launch_step_mixed(const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, int mask,
+                                     cudaStream_t st) {
+    k_step_mixed<<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur, noise, ns, mask);
+    return cudaGetLastError();
+}
+// (the mixed path always takes its pair forces from k_pairs_cl)
 cudaError_t launch_step(int G, const Dev &D, const GlobP &g, int cur, const double *noise, long long ns, cudaStream_t st,
                         int trigger) {
-    const int mask = 63 | (trigger ? 256 : 0);
-    if (g.prec == 0) return launch_step_r<double, 0>(G, D, g, cur, noise, ns, nullptr, mask, st);
-    return launch_step_r<float, 0>(G, D, g, cur, noise, ns, nullptr, mask, st);
+    if (g.prec == 0) return launch_step_r<double, 0>(G, D, g, cur, noise, ns, nullptr, 63 | (trigger ? 256 : 0), st);
+    return launch_step_mixed(D, g, cur, noise, ns, 63 | 64 | (trigger ? 256 : 0), st);
 }
 
 // the step with its pair forces taken from fpair (k_pairs ran before it, with
@@ -1921,7 +1935,7 @@ cudaError_t launch_step_split(int G, const Dev &D, const GlobP &g, int cur, cons
                               int trigger) {
     const int mask = 63 | 64 | (trigger ? 256 : 0);
     if (g.prec == 0) return launch_step_r<double, 0>(G, D, g, cur, noise, ns, nullptr, mask, st);
-    return launch_step_r<float, 0>(G, D, g, cur, noise, ns, nullptr, mask, st);
+    return launch_step_mixed(D, g, cur, noise, ns, mask, st);
 }
 
 template <typename R, int G> static cudaError_t launch_pairs_g(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
@@ -2197,7 +2211,7 @@ cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream
     return cudaGetLastError();
 }
 
-size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4) + sizeof(float)); }
+size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4)); }
 
 cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
                             cudaStream_t st) {
