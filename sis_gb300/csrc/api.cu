@@ -424,9 +424,9 @@ int bp_test_blocks(const sis_ctx *ctx) { return ctx->g.bp_model > 0 ? ctx->bpt :
 // The fork event ev_fork is recorded on ctx->st by the caller.
 cudaError_t enqueue_pre(sis_ctx *ctx, int cur) {
     cudaError_t e;
-    if (ctx->g.bp_model == 0) return launch_bonded(ctx->D, ctx->g, cur, ctx->st);
+    if (ctx->g.bp_model == 0) return launch_bonded_step(ctx->D, ctx->g, cur, ctx->st);
     if ((e = cudaStreamWaitEvent(ctx->st4, ctx->ev_fork, 0)) != cudaSuccess) return e;
-    if ((e = launch_bonded(ctx->D, ctx->g, cur, ctx->st4)) != cudaSuccess) return e;
+    if ((e = launch_bonded_step(ctx->D, ctx->g, cur, ctx->st4)) != cudaSuccess) return e;
     if ((e = cudaEventRecord(ctx->ev_bond, ctx->st4)) != cudaSuccess) return e;
     if ((e = launch_bp(ctx->D, ctx->g, cur, bp_test_blocks(ctx), bp_blocks(ctx), ctx->st)) != cudaSuccess) return e;
     if ((e = launch_bp_mc(ctx->D, ctx->g, ctx->st)) != cudaSuccess) return e;
@@ -579,11 +579,11 @@ int autotune(sis_ctx *ctx) {
         }
         if (with_bp) {
             if ((e = cudaStreamWaitEvent(ctx->st4, ctx->ev_fork, 0)) != cudaSuccess) return e;
-            if ((e = launch_bonded(D, ctx->g, ctx->cur, ctx->st4)) != cudaSuccess) return e;
+            if ((e = launch_bonded_step(D, ctx->g, ctx->cur, ctx->st4)) != cudaSuccess) return e;
             if ((e = cudaEventRecord(ctx->ev_bond, ctx->st4)) != cudaSuccess) return e;
             if ((e = launch_bp(D, ctx->g, ctx->cur, bp_test_blocks(ctx), bp_blocks(ctx), ctx->st)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(ctx->st, ctx->ev_bond, 0)) != cudaSuccess) return e;
-        } else if ((e = launch_bonded(D, ctx->g, ctx->cur, ctx->st)) != cudaSuccess) {
+        } else if ((e = launch_bonded_step(D, ctx->g, ctx->cur, ctx->st)) != cudaSuccess) {
             return e;
         }
         if (ov && (e = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0)) != cudaSuccess) return e;
@@ -1078,6 +1078,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
         rc |= dalloc(ctx, &fp, n);
         D.fpair = fp;
     }
+    rc |= dalloc(ctx, &D.fbond, n);
     if (cudaStreamCreateWithFlags(&ctx->st3, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->st4, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||

@@ -210,6 +210,7 @@ struct Dev {
     const BPPf *bppf;       // [7]
     void *slot;             // [8][n] bonded forces per term start (float4 or double4)
     void *fpair;            // [n] pair forces of the current step (float4 or double4)
+    float4 *fbond;          // [n] mixed path: bonded force of the current step per bead (k_bonded_bead)
     const short *bp3_hash;  // [4097]
     const double *bp3_dH, *bp3_dS; // [469]
     const float *bp_dgf;    // [n_inst][469] FP32 dH - T dS at each instance's

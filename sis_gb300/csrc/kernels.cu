@@ -196,9 +196,9 @@ __device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int c
 
 // FP64 re-evaluation of a flagged angle (kind 0) or dihedral (kind 1) term
 // starting at bead s; overwrites its FP32 slot forces.
-__device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, int s, int kind) {
-    float4 *S = (float4 *)D.slot + s;
-    const size_t pl = (size_t)g.n;
+// FP64 forces of the angle (kind 0: F[0..2]) or dihedral (kind 1: F[0..3])
+// term starting at bead s, rounded to FP32
+__device__ __noinline__ void bonded_fp64_f(const Dev &D, const GlobP &g, int cur, int s, int kind, float4 *F4) {
     const int4 bi = D.binfo[s];
     const InstP &ip = D.ip[bi.x];
     const double4 *__restrict__ x64 = x_at(D, cur);
@@ -208,13 +208,113 @@ __device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, 
         V3<double> F[3];
         double c;
         angle_forces<double>(dvec64(x64[q1], x64[s], ip), dvec64(x64[q2], x64[q1], ip), g, F, &c);
-        for (int k = 0; k < 3; ++k) S[(1 + k) * pl] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
+        for (int k = 0; k < 3; ++k) F4[k] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
     } else {
         V3<double> F[4];
         bool nr;
         dih_forces<double>(dvec64(x64[s], x64[q1], ip), dvec64(x64[q2], x64[q1], ip), dvec64(x64[q2], x64[q3], ip), g, F, &nr);
-        for (int k = 0; k < 4; ++k) S[(4 + k) * pl] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
+        for (int k = 0; k < 4; ++k) F4[k] = make_float4((float)F[k].x, (float)F[k].y, (float)F[k].z, 0.f);
     }
+}
+// FP64 re-evaluation of a flagged angle (kind 0) or dihedral (kind 1) term
+// starting at bead s; overwrites its FP32 slot forces.
+__device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, int s, int kind) {
+    float4 *S = (float4 *)D.slot + s;
+    const size_t pl = (size_t)g.n;
+    float4 F[4];
+    bonded_fp64_f(D, g, cur, s, kind, F);
+    for (int k = 0; k < (kind == 0 ? 3 : 4); ++k) S[(kind == 0 ? 1 + k : 4 + k) * pl] = F[k];
+}
+
+// The bonded force on bead i of the mixed path, formed by the bead's own
+// thread: the nine terms that act on it (bonds starting at l-1 and l,
+// angles starting at l-2..l, dihedrals starting at l-3..l, l its chain
+// index), each evaluated as bonded_terms evaluates it (the same FP32
+// operations, the exact cross products near straight angles, FP64 below a
+// sine of 1e-6), its force on bead i summed in the order the slot gather
+// (bonded_gather) adds the slot planes.  E supplies the positions (the
+// global mirror, or a shared-memory copy), D the FP64 state.  mask: 1 bond,
+// 2 angle, 4 dihedral.
+__device__ __forceinline__ V3<float> bonded_bead(const Dev &E, const Dev &D, const GlobP &g, int cur, int i, int mask) {
+    using L = PosLd<float>;
+    const int4 bi = E.binfo[i];
+    const InstP &ip = E.ip[bi.x];
+    const int l = bi_lidx(bi), n = bi_clen(bi);
+    const bool circ = bi_circ(bi);
+    // chain beads l-3 .. l+3 (-1: none) and their mirrors
+    int q[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) q[d] = d == 3 ? i : chain_bead(bi, l - 3 + d);
+    uint4 p[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) p[d] = L::ld(E, cur, q[d] >= 0 ? q[d] : i);
+    const V3<float> z = mk<float>(0.f, 0.f, 0.f);
+    V3<float> ab = z;
+    // bonds (s, s+1) for s = l-1 (force +fb on bead i) and s = l (-fb)
+    if (mask & 1) {
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            const int a = 2 + t; // index of the bond's first bead in q
+            if (q[a] < 0 || q[a + 1] < 0 || !(!circ || n >= 2)) continue;
+            const V3<float> fb = bond_f<float>(L::sep(p[a], p[a + 1], ip), g);
+            ab = ab + (t == 0 ? fb : -fb);
+        }
+    }
+    // angles (s, s+1, s+2) for s = l-2, l-1, l: bead i is their k = 2, 1, 0
+    if (mask & 2) {
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const int a = 1 + t, k = 2 - t;
+            if (q[a] < 0 || q[a + 1] < 0 || q[a + 2] < 0 || !(!circ || n >= 3)) continue;
+            const V3<float> v01 = L::sep(p[a], p[a + 1], ip), v21 = L::sep(p[a + 2], p[a + 1], ip);
+            V3<float> Fa[3];
+            float c;
+            angle_forces<float>(-v01, v21, g, Fa, &c);
+            bool near = fabsf(c) > NEAR_ONE_STRICT;
+            if (near) {
+                const uint4 *mr = mir_at(E, cur);
+                const float4 *rr = res_at(E, cur);
+                const FxV a01 = fxv(mr, rr, q[a], q[a + 1]), a21 = fxv(mr, rr, q[a + 2], q[a + 1]);
+                float s2;
+                angle_forces_cr(-v01, v21, cross_fx(a21, a01, ip), g, Fa, &s2);
+                near = s2 < 1e-12f;
+            }
+            if (near) {
+                float4 F[4];
+                bonded_fp64_f(D, g, cur, q[a], 0, F);
+                Fa[k] = mk<float>(F[k].x, F[k].y, F[k].z);
+            }
+            ab = ab + Fa[k];
+        }
+    }
+    // dihedrals (s .. s+3) for s = l-3 .. l: bead i is their k = 3 .. 0
+    if ((mask & 4) && g.dih_type != 0) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int a = t, k = 3 - t;
+            if (q[a] < 0 || q[a + 1] < 0 || q[a + 2] < 0 || q[a + 3] < 0 || !(!circ || n >= 4)) continue;
+            const V3<float> v01 = L::sep(p[a], p[a + 1], ip), v21 = L::sep(p[a + 2], p[a + 1], ip),
+                            v23 = L::sep(p[a + 2], p[a + 3], ip);
+            V3<float> Fd[4];
+            bool near;
+            dih_forces<float>(v01, v21, v23, g, Fd, &near);
+            if (near) {
+                const uint4 *mr = mir_at(E, cur);
+                const float4 *rr = res_at(E, cur);
+                const FxV a01 = fxv(mr, rr, q[a], q[a + 1]), a21 = fxv(mr, rr, q[a + 2], q[a + 1]);
+                float s2;
+                dih_forces_mn(v01, v21, v23, cross_fx(a01, a21, ip), cross_fx(a21, fxv(mr, rr, q[a + 2], q[a + 3]), ip), g, Fd, &s2);
+                near = s2 < 1e-12f;
+            }
+            if (near) {
+                float4 F[4];
+                bonded_fp64_f(D, g, cur, q[a], 1, F);
+                Fd[k] = mk<float>(F[k].x, F[k].y, F[k].z);
+            }
+            ab = ab + Fd[k];
+        }
+    }
+    return ab;
 }
 
 // window and free-energy test of one record (force mode); returns true when
@@ -472,6 +572,15 @@ template <typename R> __global__ void __launch_bounds__(256) k_bonded(Dev D, Glo
         for (int k = threadIdx.x; k < na; k += blockDim.x) bonded_fp64(D, g, cur, qa[k], 0);
         for (int k = threadIdx.x; k < nd; k += blockDim.x) bonded_fp64(D, g, cur, qd[k], 1);
     }
+}
+
+// The mixed path's bonded pass of a step: each bead's bonded force by its
+// own thread (bonded_bead) into fbond, which k_step_mixed reads as one load.
+__global__ void __launch_bounds__(256) k_bonded_bead(Dev D, GlobP g, int cur) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n) return;
+    const V3<float> f = bonded_bead(D, D, g, cur, i, 7);
+    D.fbond[i] = make_float4(f.x, f.y, f.z, 0.f);
 }
 
 // Base-pair records in two passes.  k_bp_test gives every record one thread
@@ -969,8 +1078,18 @@ template <typename R, int G> __global__ void __launch_bounds__(256, 5) k_pairs(D
 // list and inside sigma, Debye-Hueckel (force_ele_DH.F90:39-82) when it is on
 // the electrostatic list and inside the cutoff
 struct PairCoef {
-    float sig2, wcoef, ecoef, rc, cut2;
+    float sig2, wcoef, ecoef, rc, rcl2, cut2; // rcl2: rc log2(e)
 };
+__device__ __forceinline__ PairCoef pair_coef_of(const GlobP &g, const InstP &ip) {
+    PairCoef P;
+    P.sig2 = g.f_wca_sig2;
+    P.wcoef = g.f_wca_coef;
+    P.ecoef = ip.ele_coef_f;
+    P.rc = ip.rcdist_f;
+    P.rcl2 = ip.rcdist_f * 1.44269504f;
+    P.cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+    return P;
+}
 // 1/d2: the hardware approximation refined by one Newton-Raphson step
 // (r1 = r0 + r0 (1 - d2 r0)), within an ulp or so of the rounded quotient
 __device__ __forceinline__ float rcp_nr(float d2) {
@@ -984,26 +1103,41 @@ __device__ __forceinline__ float2 rcp_nr2(float2 d2) {
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0.y) : "f"(d2.y));
     return __ffma2_rn(r0, __ffma2_rn(make_float2(-d2.x, -d2.y), r0, make_float2(1.f, 1.f)), r0);
 }
-// WCA (force_wca.F90): wcoef ((s/d)^14 - (s/d)^8) with (s/d)^2 = sig2 / d2;
-// Debye-Hueckel (force_ele_DH.F90): ecoef ri^2 (ri + rc) exp(-r rc), ri one
-// Newton step past rsqrt.  Each term is formed for every pair and selected by
-// its list bit and distance, so a warp never branches on them.
-__device__ __forceinline__ float pair_c(bool wca, bool ele, float d2, const PairCoef &P) {
+// 2^t by the hardware approximation (exp(-r rc) = 2^(-r rc log2 e))
+__device__ __forceinline__ float ex2a(float t) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(t));
+    return y;
+}
+// WCA (force_wca.F90): wcoef ((s/d)^14 - (s/d)^8) with (s/d)^2 = sig2 / d2
+__device__ __forceinline__ float wca_c(float d2, const PairCoef &P) {
     const float sq = __fmul_rn(P.sig2, rcp_nr(d2));
     const float s2 = __fmul_rn(sq, sq), s4 = __fmul_rn(s2, s2);
-    const float cw = __fmul_rn(P.wcoef, __fmaf_rn(__fmul_rn(s4, s2), sq, -s4));
+    return __fmul_rn(P.wcoef, __fmaf_rn(__fmul_rn(s4, s2), sq, -s4));
+}
+__device__ __forceinline__ float2 wca_c2(float2 d2, const PairCoef &P) {
+    const float2 sq = __fmul2_rn(make_float2(P.sig2, P.sig2), rcp_nr2(d2));
+    const float2 s2 = __fmul2_rn(sq, sq), s4 = __fmul2_rn(s2, s2);
+    return __fmul2_rn(make_float2(P.wcoef, P.wcoef), __ffma2_rn(__fmul2_rn(s4, s2), sq, make_float2(-s4.x, -s4.y)));
+}
+// Debye-Hueckel (force_ele_DH.F90): ecoef ri^2 (ri + rc) exp(-r rc), ri one
+// Newton step past rsqrt, the exponential as 2^(-r rc log2 e).  Each term is
+// selected by its list bit and distance (pair2: the electrostatic term is
+// formed for every pair, the WCA term only when some lane of the warp has a
+// pair inside sigma, a warp-uniform branch).
+__device__ __forceinline__ float pair_c(bool wca, bool ele, float d2, const PairCoef &P) {
     float ri = rsqrtf(d2);
     ri = __fmul_rn(ri, __fmaf_rn(__fmul_rn(__fmul_rn(-0.5f, d2), ri), ri, 1.5f));
     const float rr = __fmul_rn(d2, ri);
-    const float ce = __fmul_rn(__fmul_rn(__fmul_rn(P.ecoef, __fmul_rn(ri, ri)), __fadd_rn(ri, P.rc)), __expf(-rr * P.rc));
+    const float ce = __fmul_rn(__fmul_rn(__fmul_rn(P.ecoef, __fmul_rn(ri, ri)), __fadd_rn(ri, P.rc)), ex2a(-rr * P.rcl2));
     const float e = (ele && d2 <= P.cut2) ? ce : 0.f;
-    return (wca && d2 < P.sig2) ? __fadd_rn(cw, e) : e;
+    return (wca && d2 < P.sig2) ? __fadd_rn(wca_c(d2, P), e) : e;
 }
 
 // Two pairs at once with paired FP32 instructions (FFMA2 and relatives of
 // sm_100 and later): the separations v of (i, j) and (i, j') from the mirror
 // differences, and the force coefficients c of pair_c, lane by lane the same
-// IEEE operations as pair_c.
+// IEEE operations as pair_c.  Called by all 32 lanes of a warp.
 struct Pair2 {
     float2 vx, vy, vz, c;
 };
@@ -1014,21 +1148,23 @@ __device__ __forceinline__ Pair2 pair2(const uint4 &mi, const uint4 &ma, const u
     r.vy = __fmul2_rn(make_float2((float)(int)(mi.y - ma.y), (float)(int)(mi.y - mb.y)), f1);
     r.vz = __fmul2_rn(make_float2((float)(int)(mi.z - ma.z), (float)(int)(mi.z - mb.z)), f2);
     const float2 d2 = __ffma2_rn(r.vx, r.vx, __ffma2_rn(r.vy, r.vy, __fmul2_rn(r.vz, r.vz)));
-    const float2 sq = __fmul2_rn(make_float2(P.sig2, P.sig2), rcp_nr2(d2));
-    const float2 s2 = __fmul2_rn(sq, sq), s4 = __fmul2_rn(s2, s2);
-    const float2 cw = __fmul2_rn(make_float2(P.wcoef, P.wcoef), __ffma2_rn(__fmul2_rn(s4, s2), sq, make_float2(-s4.x, -s4.y)));
     float2 ri = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
     const float2 h = __fmul2_rn(__fmul2_rn(make_float2(-0.5f, -0.5f), d2), ri);
     ri = __fmul2_rn(ri, __ffma2_rn(h, ri, make_float2(1.5f, 1.5f)));
-    const float2 rr = __fmul2_rn(d2, ri);
-    const float2 ex = make_float2(__expf(-rr.x * P.rc), __expf(-rr.y * P.rc));
+    const float2 t = __fmul2_rn(__fmul2_rn(d2, ri), make_float2(-P.rcl2, -P.rcl2));
+    const float2 ex = make_float2(ex2a(t.x), ex2a(t.y));
     const float2 ce = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(P.ecoef, P.ecoef), __fmul2_rn(ri, ri)),
                                             __fadd2_rn(ri, make_float2(P.rc, P.rc))),
                                  ex);
-    const float ex_ = (ea && d2.x <= P.cut2) ? ce.x : 0.f, ey_ = (eb && d2.y <= P.cut2) ? ce.y : 0.f;
-    const float2 cs = __fadd2_rn(cw, make_float2(ex_, ey_));
-    r.c.x = (wa && d2.x < P.sig2) ? cs.x : ex_;
-    r.c.y = (wb && d2.y < P.sig2) ? cs.y : ey_;
+    r.c.x = (ea && d2.x <= P.cut2) ? ce.x : 0.f;
+    r.c.y = (eb && d2.y <= P.cut2) ? ce.y : 0.f;
+    const bool w0 = wa && d2.x < P.sig2, w1 = wb && d2.y < P.sig2;
+    if (__any_sync(0xffffffffu, w0 || w1)) {
+        const float2 cw = wca_c2(d2, P);
+        const float2 cs = __fadd2_rn(cw, r.c);
+        r.c.x = w0 ? cs.x : r.c.x;
+        r.c.y = w1 ? cs.y : r.c.y;
+    }
     return r;
 }
 
@@ -1069,12 +1205,7 @@ __global__ void __launch_bounds__(256, 5) k_pairs_cl(Dev D, GlobP g, int cur, in
     const uint4 mi = mir[first + (a < cnt ? a : 0)];
     const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
                  f2 = make_float2(ip.finv[2], ip.finv[2]);
-    PairCoef P;
-    P.sig2 = g.f_wca_sig2;
-    P.wcoef = g.f_wca_coef;
-    P.ecoef = ip.ele_coef_f;
-    P.rc = ip.rcdist_f;
-    P.cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+    const PairCoef P = pair_coef_of(g, ip);
     const unsigned wsel = (mask & 16) ? 0xffu : 0u, esel = (mask & 32) ? 0xffu : 0u;
     float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
     const int nc = D.ncl[ic];
@@ -1094,8 +1225,11 @@ __global__ void __launch_bounds__(256, 5) k_pairs_cl(Dev D, GlobP g, int cur, in
             }
             cp_async_wait_all();
             __syncwarp();
-            for (int k = q; k < nk; k += 4) {
-                const ulonglong2 m = s_cm[w][k];
+            for (int k0 = 0; k0 < nk; k0 += 4) {
+                // every lane runs every round; a lane past the chunk's end
+                // takes cluster 0 with empty masks (exact zeros)
+                const int k = k0 + q < nk ? k0 + q : 0;
+                const ulonglong2 m = k0 + q < nk ? s_cm[w][k] : make_ulonglong2(0ull, 0ull);
                 const unsigned wb = (unsigned)(m.x >> (a * kCl)) & wsel, eb = (unsigned)(m.y >> (a * kCl)) & esel;
                 const uint4 *mj = s_mj[w] + k * kCl;
 #pragma unroll
@@ -1271,7 +1405,8 @@ __global__ void __launch_bounds__(256) k_step_mixed(Dev D, GlobP g, int cur, con
     const double4 x = x_at(D, cur)[i], m = D.mdc[i], v = D.v[i], b = D.beta[i];
     const uint4 m0 = D.mir0[i];
     const unsigned long long step = *D.step_ctr;
-    const V3<float> ab = (mask & 7) ? bonded_gather<float>(D, g, bi, 0, 1, mask) : mk<float>(0.f, 0.f, 0.f);
+    const float4 fbd = D.fbond[i];
+    const V3<float> ab = (mask & 7) ? mk<float>(fbd.x, fbd.y, fbd.z) : mk<float>(0.f, 0.f, 0.f);
     float xi[3];
     mixed_noise(g, i, jp, noise, noise_step, step, xi);
     float F[3] = {fp.x + ab.x, fp.y + ab.y, fp.z + ab.z};
@@ -1532,6 +1667,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     float4 *s_res = (float4 *)(s_mir + cap);
     double4 *s_fbp = (double4 *)(s_res + cap);
     float4 *s_F = (float4 *)(s_fbp + cap);   // pair force of the step (xyz)
+    float4 *s_B = s_F + cap;                 // bonded force of the step (xyz)
     __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst];
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
@@ -1635,10 +1771,10 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     if (s_any) rebuild(cur, true);
     const unsigned long long step0 = *D.step_ctr;
     for (int st = 0; st < nsteps; ++st) {
-        // Forces.  Base pairs, bonded terms and pair forces need no barrier
-        // between them: the base-pair forces add into s_fbp (exact fixed-point
-        // atomics), the bonded terms write their slot planes, the pair sums
-        // go to s_F, and the update reads all three after one barrier.
+        // Forces.  Base pairs, bonded and pair forces need no barrier between
+        // them: the base-pair forces add into s_fbp (exact fixed-point
+        // atomics), each bead's bonded force (bonded_bead) goes to s_B and its
+        // pair sum to s_F; the update reads all three after one barrier.
         // ------------------------------------------------ base pairs
         if (g.bp_model > 0) {
             // every warp tests 32 records at a time and queues the ones in the
@@ -1677,15 +1813,12 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
             }
         }
-        // ------------------------------------------------ bonded terms
+        // ------------------------------------------------ bonded forces
         for (int s = tid; s < nb; s += nt) {
             const int q = small_inst(s_sb, ni, s);
             const int gi = s_off[q] + (s - s_sb[q]);
-            const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
-            bool an, dn;
-            bonded_terms<float>(E, g, cur, gi, &an, &dn);
-            if (an) bonded_fp64(D, g, cur, gi, 0);
-            if (dn) bonded_fp64(D, g, cur, gi, 1);
+            const V3<float> f = bonded_bead(small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]), D, g, cur, gi, 7);
+            s_B[s] = make_float4(f.x, f.y, f.z, 0.f);
         }
         // ------------------------------------------------ pair forces
         {
@@ -1701,12 +1834,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const int4 bi = D.binfo[gi];
                 const InstP &ip = D.ip[bi.x];
                 const uint4 mi = s_mir[s];
-                PairCoef P;
-                P.sig2 = g.f_wca_sig2;
-                P.wcoef = g.f_wca_coef;
-                P.ecoef = ip.ele_coef_f;
-                P.rc = ip.rcdist_f;
-                P.cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
+                const PairCoef P = pair_coef_of(g, ip);
                 const int m = min(D.nnbr[gi], g.cap);
                 const int *__restrict__ nbl = D.nbr + (size_t)gi * g.cap;
                 const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
@@ -1718,7 +1846,9 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 // term bit (an exact zero)
                 float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
                 constexpr int L = kSmallLanes;
-                for (int k0 = sub; k0 < m; k0 += 8 * L) {
+                // every lane runs the batches of the warp's longest list
+                const int mmax = __reduce_max_sync(0xffffffffu, m);
+                for (int k0 = sub; k0 - sub < mmax; k0 += 8 * L) {
                     int e[8];
 #pragma unroll
                     for (int u = 0; u < 8; ++u) e[u] = k0 + u * L < m ? __ldg(nbl + k0 + u * L) : gi;
@@ -1757,7 +1887,8 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const int4 bi = D.binfo[gi];
             const double4 x = x_at(D, cur)[gi], mc = D.mdc[gi], v = D.v[gi], b = D.beta[gi];
             const InstP &jp = D.ip[s_iid[q]];
-            const V3<float> ab = bonded_gather<float>(D, g, bi, 0, 1, 7);
+            const float4 B4 = s_B[s];
+            const V3<float> ab = mk<float>(B4.x, B4.y, B4.z);
             float xi[3];
             mixed_noise(g, gi, jp, noise, st, step, xi);
             const float4 F4 = s_F[s];
@@ -1978,6 +2109,11 @@ int force_kernels(const GlobP &g, int mask) { return 1 + (g.prec != 0 && (mask &
 cudaError_t launch_bonded(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
     if (g.prec == 0) k_bonded<double><<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur);
     else k_bonded<float><<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur);
+    return cudaGetLastError();
+}
+cudaError_t launch_bonded_step(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
+    if (g.prec == 0) return launch_bonded(D, g, cur, st);
+    k_bonded_bead<<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur);
     return cudaGetLastError();
 }
 
@@ -2211,7 +2347,7 @@ cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream
     return cudaGetLastError();
 }
 
-size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4)); }
+size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + 2 * sizeof(float4)); }
 
 cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
                             cudaStream_t st) {

@@ -52,6 +52,8 @@ cudaError_t launch_pre(const Dev &D, const GlobP &g, int cur, int do_bonded, int
                        cudaStream_t st);
 int pre_kernels(const GlobP &g, int do_bonded, int do_bp);
 cudaError_t launch_bonded(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
+// the bonded pass of a step: slot planes (FP64 path) or per-bead forces (fbond, mixed path)
+cudaError_t launch_bonded_step(const Dev &D, const GlobP &g, int cur, cudaStream_t st);
 // k_bp_test and k_bp_eval
 cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int test_blocks, int eval_blocks, cudaStream_t st);
 int bp_kernels(const GlobP &g);
