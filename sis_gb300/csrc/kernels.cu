@@ -134,11 +134,9 @@ template <> struct PosLd<double> {
 // from the fixed-point mirror and its residuals (cross_fx); only a sine below
 // 1e-6 leaves it flagged for the caller's FP64 evaluation.
 template <typename R>
-__device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int cur, int s, bool *angle_near, bool *dih_near) {
-    using V4 = typename Vec4<R>::type;
+__device__ __forceinline__ void bonded_terms_to(const Dev &D, const GlobP &g, int cur, int s, typename Vec4<R>::type *S, size_t pl,
+                                                bool *angle_near, bool *dih_near) {
     using L = PosLd<R>;
-    V4 *S = (V4 *)D.slot + s;
-    const size_t pl = (size_t)g.n;
     const int4 bi = D.binfo[s];
     const InstP &ip = D.ip[bi.x];
     const int l = bi_lidx(bi), n = bi_clen(bi);
@@ -196,6 +194,13 @@ __device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int c
 
 // FP64 re-evaluation of a flagged angle (kind 0) or dihedral (kind 1) term
 // starting at bead s; overwrites its FP32 slot forces.
+// the terms starting at bead s into the context's slot planes slot[k][s]
+template <typename R>
+__device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int cur, int s, bool *angle_near, bool *dih_near) {
+    using V4 = typename Vec4<R>::type;
+    bonded_terms_to<R>(D, g, cur, s, (V4 *)D.slot + s, (size_t)g.n, angle_near, dih_near);
+}
+
 // FP64 forces of the angle (kind 0: F[0..2]) or dihedral (kind 1: F[0..3])
 // term starting at bead s, rounded to FP32
 __device__ __noinline__ void bonded_fp64_f(const Dev &D, const GlobP &g, int cur, int s, int kind, float4 *F4) {
@@ -217,13 +222,15 @@ __device__ __noinline__ void bonded_fp64_f(const Dev &D, const GlobP &g, int cur
     }
 }
 // FP64 re-evaluation of a flagged angle (kind 0) or dihedral (kind 1) term
-// starting at bead s; overwrites its FP32 slot forces.
-__device__ __noinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, int s, int kind) {
-    float4 *S = (float4 *)D.slot + s;
-    const size_t pl = (size_t)g.n;
+// starting at bead s; overwrites its FP32 slot forces (planes S[k * pl], by
+// default the context's slot planes at s).
+__device__ __noinline__ void bonded_fp64_to(const Dev &D, const GlobP &g, int cur, int s, int kind, float4 *S, size_t pl) {
     float4 F[4];
     bonded_fp64_f(D, g, cur, s, kind, F);
     for (int k = 0; k < (kind == 0 ? 3 : 4); ++k) S[(kind == 0 ? 1 + k : 4 + k) * pl] = F[k];
+}
+__device__ __forceinline__ void bonded_fp64(const Dev &D, const GlobP &g, int cur, int s, int kind) {
+    bonded_fp64_to(D, g, cur, s, kind, (float4 *)D.slot + s, (size_t)g.n);
 }
 
 // The bonded force on bead i of the mixed path, formed by the bead's own
@@ -574,13 +581,57 @@ template <typename R> __global__ void __launch_bounds__(256) k_bonded(Dev D, Glo
     }
 }
 
-// The mixed path's bonded pass of a step: each bead's bonded force by its
-// own thread (bonded_bead) into fbond, which k_step_mixed reads as one load.
-__global__ void __launch_bounds__(256) k_bonded_bead(Dev D, GlobP g, int cur) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= g.n) return;
+// The mixed path's bonded pass of a step: the terms starting at the block's
+// 256 beads and at the 3 beads before them (k_bonded's evaluation) into
+// shared-memory slot planes, then each bead's sum in slot order (the order
+// of bonded_gather) into fbond, which k_step_mixed reads as one load.  A
+// bead whose terms start outside that range (the wrap of a circular chain)
+// forms its sum itself (bonded_bead, the same values).
+constexpr int kBondHalo = 3;
+__device__ __noinline__ float4 bonded_bead_global(const Dev &D, const GlobP &g, int cur, int i) {
     const V3<float> f = bonded_bead(D, D, g, cur, i, 7);
-    D.fbond[i] = make_float4(f.x, f.y, f.z, 0.f);
+    return make_float4(f.x, f.y, f.z, 0.f);
+}
+__global__ void __launch_bounds__(256, 3) k_bonded_fb(const __grid_constant__ Dev D, const __grid_constant__ GlobP g, int cur) {
+    __shared__ float4 sS[8][256 + kBondHalo];
+    constexpr int pl = 256 + kBondHalo;
+    const int b0 = blockIdx.x * 256;
+    for (int t = threadIdx.x; t < pl; t += 256) {
+        const int s = b0 - kBondHalo + t;
+        if (s < 0 || s >= g.n) continue;
+        bool an, dn;
+        bonded_terms_to<float>(D, g, cur, s, &sS[0][t], pl, &an, &dn);
+        if (an) bonded_fp64_to(D, g, cur, s, 0, &sS[0][t], pl);
+        if (dn) bonded_fp64_to(D, g, cur, s, 1, &sS[0][t], pl);
+    }
+    __syncthreads();
+    const int i = b0 + threadIdx.x;
+    if (i >= g.n) return;
+    const int4 bi = D.binfo[i];
+    const int l = bi_lidx(bi);
+    int qs[9], ks[9];
+    bool inside = true;
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        const int start = t < 2 ? l - 1 + t : t < 5 ? l - 2 + (t - 2) : l - 3 + (t - 5);
+        ks[t] = t < 2 ? 0 : t < 5 ? 1 + (2 - (t - 2)) : 4 + (3 - (t - 5));
+        qs[t] = chain_bead(bi, start);
+        const int loc = qs[t] - (b0 - kBondHalo);
+        inside &= qs[t] < 0 || (loc >= 0 && loc < pl);
+    }
+    if (!inside) {
+        D.fbond[i] = bonded_bead_global(D, g, cur, i);
+        return;
+    }
+    V3<float> ab = mk<float>(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+        if (qs[t] < 0) continue;
+        const float4 v = sS[ks[t]][qs[t] - (b0 - kBondHalo)];
+        const V3<float> f = mk<float>(v.x, v.y, v.z);
+        ab = ab + (t == 1 ? -f : f);
+    }
+    D.fbond[i] = make_float4(ab.x, ab.y, ab.z, 0.f);
 }
 
 // Base-pair records in two passes.  k_bp_test gives every record one thread
@@ -1667,7 +1718,6 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     float4 *s_res = (float4 *)(s_mir + cap);
     double4 *s_fbp = (double4 *)(s_res + cap);
     float4 *s_F = (float4 *)(s_fbp + cap);   // pair force of the step (xyz)
-    float4 *s_B = s_F + cap;                 // bonded force of the step (xyz)
     __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst];
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
@@ -1771,10 +1821,11 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     if (s_any) rebuild(cur, true);
     const unsigned long long step0 = *D.step_ctr;
     for (int st = 0; st < nsteps; ++st) {
-        // Forces.  Base pairs, bonded and pair forces need no barrier between
-        // them: the base-pair forces add into s_fbp (exact fixed-point
-        // atomics), each bead's bonded force (bonded_bead) goes to s_B and its
-        // pair sum to s_F; the update reads all three after one barrier.
+        // Forces.  Base pairs, bonded terms and pair forces need no barrier
+        // between them: the base-pair forces add into s_fbp (exact
+        // fixed-point atomics), the bonded terms write their slot planes, the
+        // pair sums go to s_F, and the update reads all three after one
+        // barrier.
         // ------------------------------------------------ base pairs
         if (g.bp_model > 0) {
             // every warp tests 32 records at a time and queues the ones in the
@@ -1813,12 +1864,15 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
             }
         }
-        // ------------------------------------------------ bonded forces
+        // ------------------------------------------------ bonded terms
         for (int s = tid; s < nb; s += nt) {
             const int q = small_inst(s_sb, ni, s);
             const int gi = s_off[q] + (s - s_sb[q]);
-            const V3<float> f = bonded_bead(small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]), D, g, cur, gi, 7);
-            s_B[s] = make_float4(f.x, f.y, f.z, 0.f);
+            const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+            bool an, dn;
+            bonded_terms<float>(E, g, cur, gi, &an, &dn);
+            if (an) bonded_fp64(D, g, cur, gi, 0);
+            if (dn) bonded_fp64(D, g, cur, gi, 1);
         }
         // ------------------------------------------------ pair forces
         {
@@ -1887,8 +1941,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const int4 bi = D.binfo[gi];
             const double4 x = x_at(D, cur)[gi], mc = D.mdc[gi], v = D.v[gi], b = D.beta[gi];
             const InstP &jp = D.ip[s_iid[q]];
-            const float4 B4 = s_B[s];
-            const V3<float> ab = mk<float>(B4.x, B4.y, B4.z);
+            const V3<float> ab = bonded_gather<float>(D, g, bi, 0, 1, 7);
             float xi[3];
             mixed_noise(g, gi, jp, noise, st, step, xi);
             const float4 F4 = s_F[s];
@@ -2113,16 +2166,18 @@ cudaError_t launch_bonded(const Dev &D, const GlobP &g, int cur, cudaStream_t st
 }
 cudaError_t launch_bonded_step(const Dev &D, const GlobP &g, int cur, cudaStream_t st) {
     if (g.prec == 0) return launch_bonded(D, g, cur, st);
-    k_bonded_bead<<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur);
+    k_bonded_fb<<<(g.n + 255) / 256, 256, 0, st>>>(D, g, cur);
     return cudaGetLastError();
 }
 
 // test_blocks covers the staging capacity (grid stride beyond it), eval_blocks
 // the windowed records of an ordinary step
+// (one wave of k_bp, two blocks per SM, each taking a grid-stride share of
+// the records: the evaluations of every block then run at once)
 cudaError_t launch_bp(const Dev &D, const GlobP &g, int cur, int test_blocks, int eval_blocks, cudaStream_t st) {
-    (void)eval_blocks;
-    if (g.prec == 0) k_bp<double><<<test_blocks, 256, 0, st>>>(D, g, cur);
-    else k_bp<float><<<test_blocks, 256, 0, st>>>(D, g, cur);
+    const int blocks = std::max(1, std::min(test_blocks, eval_blocks));
+    if (g.prec == 0) k_bp<double><<<blocks, 256, 0, st>>>(D, g, cur);
+    else k_bp<float><<<blocks, 256, 0, st>>>(D, g, cur);
     return cudaGetLastError();
 }
 int bp_kernels(const GlobP &g) { return g.bp_model > 0 ? 1 : 0; }
@@ -2347,7 +2402,7 @@ cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream
     return cudaGetLastError();
 }
 
-size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + 2 * sizeof(float4)); }
+size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4)); }
 
 cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
                             cudaStream_t st) {
