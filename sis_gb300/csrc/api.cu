@@ -638,31 +638,53 @@ bool small_active(const sis_ctx *ctx) {
     return ctx->small_ok && ctx->small_mode != 0 && ctx->g.nstep_mc == 0 && !ctx->g.flg_bias && !ctx->mc_pending;
 }
 
-// Buckets of whole instances for k_md_small: longest first into the bucket
-// with the fewest beads (at most kSmallMaxInst instances and kSmallMaxBeads
-// beads each), about `target` buckets; each bucket lists its instances in
-// ascending order.
+// Buckets of whole instances for k_md_small: costliest first into the
+// bucket with the least cost (at most kSmallMaxInst instances and
+// kSmallMaxBeads beads each), about `target` buckets; each bucket lists its
+// instances in ascending order.
 int small_plan(sis_ctx *ctx, int target) {
     const int ni = ctx->n_inst;
+    // cost of an instance: its pair-list entries plus a per-bead share (the
+    // update, bonded and base-pair terms cost about as much as 90 entries);
+    // by capacity when slots are loaded in place (sis_gpu_load_slot)
+    std::vector<double> cost(ni);
+    bool slots = false;
+    for (int k = 0; k < ni; ++k) slots |= ctx->ip[k].n_act != ctx->ip[k].n;
+    std::vector<int> nn;
+    if (!slots && ctx->lists_valid) {
+        nn.resize(ctx->n);
+        CK(cudaMemcpyAsync(nn.data(), ctx->D.nnbr, sizeof(int) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    for (int k = 0; k < ni; ++k) {
+        const InstP &I = ctx->ip[k];
+        double c = 90.0 * I.n;
+        if (!nn.empty())
+            for (int i = I.bead_off; i < I.bead_off + I.n; ++i) c += std::min(nn[i], ctx->g.cap);
+        cost[k] = c;
+    }
     std::vector<int> order(ni);
     for (int k = 0; k < ni; ++k) order[k] = k;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return ctx->ip[a].n > ctx->ip[b].n; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
     const int nbins = std::max(1, std::min(target, ni));
     std::vector<std::vector<int>> bins(nbins);
     std::vector<int> beads(nbins, 0);
+    std::vector<double> load(nbins, 0.0);
     for (int k : order) {
         int best = -1;
         for (int b = 0; b < (int)bins.size(); ++b)
             if ((int)bins[b].size() < kSmallMaxInst && beads[b] + ctx->ip[k].n <= kSmallMaxBeads &&
-                (best < 0 || beads[b] < beads[best]))
+                (best < 0 || load[b] < load[best]))
                 best = b;
         if (best < 0) {
             bins.emplace_back();
             beads.push_back(0);
+            load.push_back(0.0);
             best = (int)bins.size() - 1;
         }
         bins[best].push_back(k);
         beads[best] += ctx->ip[k].n;
+        load[best] += cost[k];
     }
     std::vector<int> off(1, 0), inst;
     int cap = 1;
@@ -730,7 +752,7 @@ int64_t small_autotune(sis_ctx *ctx, int64_t budget, int *rc) {
     for (int t : targets) {
         if ((*rc = small_plan(ctx, t))) return taken;
         for (int w : widths) {
-            if (small_smem_bytes(ctx->sp.cap) > 200 * 1024) continue;
+            if (small_smem_bytes(ctx->sp.cap) > 212 * 1024) continue;
             ctx->small_threads = w;
             cudaEventRecord(ctx->ev[12], ctx->st);
             if ((*rc = run_small(ctx, per, nullptr))) return taken;

@@ -1718,6 +1718,8 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     float4 *s_res = (float4 *)(s_mir + cap);
     double4 *s_fbp = (double4 *)(s_res + cap);
     float4 *s_F = (float4 *)(s_fbp + cap);   // pair force of the step (xyz)
+    double2 *s_cd = (double2 *)(s_F + cap);  // integrator coefficients a, sqrt(b) h (mdc.x, mdc.z)
+    float2 *s_cf = (float2 *)(s_cd + cap);   // FP32 force and noise coefficients of the update
     __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst];
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
@@ -1752,6 +1754,10 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         s_mir[s] = mir_at(D, cur)[gi];
         s_res[s] = res_at(D, cur)[gi];
         s_fbp[s] = make_double4(0.0, 0.0, 0.0, 0.0);
+        // GJF-2GJ: F -> sqrt(b) h / m, noise -> its amplitude; Ermak-McCammon: F -> h / gamma
+        const double4 mc = D.mdc[gi];
+        s_cd[s] = make_double2(mc.x, mc.z);
+        s_cf[s] = make_float2((float)(g.integrator == 1 ? mc.y : mc.x), (float)mc.w);
     }
     __syncthreads();
     // the rebuild of the instances with s_fire set (neighbor_list.F90), from
@@ -1894,24 +1900,24 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
                              f2 = make_float2(ip.finv[2], ip.finv[2]);
                 // lane sub takes entries sub, sub + L, sub + 2L, ... (L =
-                // kSmallLanes), two at a time (pair2), in batches of four
-                // pairs whose list words, then partners' mirrors, load before
-                // any is used; a missing entry is the bead itself with no
-                // term bit (an exact zero)
+                // kSmallLanes), two at a time (pair2), in batches of 16
+                // entries whose list words load before any is used; a
+                // missing entry is the bead itself with no term bit (an
+                // exact zero)
                 float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
                 constexpr int L = kSmallLanes;
                 // every lane runs the batches of the warp's longest list
                 const int mmax = __reduce_max_sync(0xffffffffu, m);
-                for (int k0 = sub; k0 - sub < mmax; k0 += 8 * L) {
-                    int e[8];
+                for (int k0 = sub; k0 - sub < mmax; k0 += 16 * L) {
+                    // the batch's 16 list words in flight at once
+                    int e[16];
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) e[u] = k0 + u * L < m ? __ldg(nbl + k0 + u * L) : gi;
-                    uint4 mj[8];
+                    for (int u = 0; u < 16; ++u) e[u] = k0 + u * L < m ? __ldg(nbl + k0 + u * L) : gi;
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) mj[u] = s_mir[sb + (e[u] & IDX_MASK) - off];
-#pragma unroll
-                    for (int u = 0; u < 8; u += 2) {
-                        const Pair2 pr = pair2(mi, mj[u], mj[u + 1], f0, f1, f2, e[u] & WCA_BIT, e[u + 1] & WCA_BIT, e[u] & ELE_BIT,
+                    for (int u = 0; u < 16; u += 2) {
+                        if (k0 - sub + u * L >= mmax) break; // warp-uniform: past every lane's list
+                        const uint4 ma = s_mir[sb + (e[u] & IDX_MASK) - off], mb = s_mir[sb + (e[u + 1] & IDX_MASK) - off];
+                        const Pair2 pr = pair2(mi, ma, mb, f0, f1, f2, e[u] & WCA_BIT, e[u + 1] & WCA_BIT, e[u] & ELE_BIT,
                                                e[u + 1] & ELE_BIT, P);
                         ax = __ffma2_rn(pr.c, pr.vx, ax);
                         ay = __ffma2_rn(pr.c, pr.vy, ay);
@@ -1939,7 +1945,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             // every global load of the bead's update first
             const uint4 m0 = D.mir0[gi];
             const int4 bi = D.binfo[gi];
-            const double4 x = x_at(D, cur)[gi], mc = D.mdc[gi], v = D.v[gi], b = D.beta[gi];
+            const double4 x = x_at(D, cur)[gi], v = D.v[gi], b = D.beta[gi];
             const InstP &jp = D.ip[s_iid[q]];
             const V3<float> ab = bonded_gather<float>(D, g, bi, 0, 1, 7);
             float xi[3];
@@ -1959,9 +1965,9 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 }
             }
             float4 r4;
-            // GJF-2GJ: F -> sqrt(b) h / m, noise -> its amplitude; Ermak-McCammon: F -> h / gamma
-            const float cf0 = (float)(g.integrator == 1 ? mc.y : mc.x), cf1 = (float)mc.w;
-            const uint4 m1 = mixed_update_core(D, g, cur, gi, jp, F, cf0, cf1, xi, x, mc, v, b, &r4);
+            const double2 cd = s_cd[s];
+            const float2 cf = s_cf[s];
+            const uint4 m1 = mixed_update_core(D, g, cur, gi, jp, F, cf.x, cf.y, xi, x, make_double4(cd.x, 0.0, cd.y, 0.0), v, b, &r4);
             s_mir[s] = m1;
             s_res[s] = r4;
             const float *fi = jp.finv;
@@ -2402,7 +2408,9 @@ cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream
     return cudaGetLastError();
 }
 
-size_t small_smem_bytes(int cap) { return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4)); }
+size_t small_smem_bytes(int cap) {
+    return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4) + sizeof(double2) + sizeof(float2));
+}
 
 cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
                             cudaStream_t st) {
