@@ -244,19 +244,28 @@ def run_gpu(args):
     total_ms = max_over_ranks(sum(times), world)
     value = world * N * S * args.steps / (total_ms * 1e-3)
 
-    # roofline of the dominant kernel (k_step), per-kernel events on the same stream
+    # roofline of the pair and update kernels (k_pairs_cl + k_step_mixed, one
+    # after the other under CUDA events on the stream that launches them).
+    # Algorithmic bytes per bead and MD step: k_pairs_cl reads the bead's
+    # mirror (16), its share of the cluster records (20 per j-cluster per
+    # 8 beads) and writes its pair force (16); k_step_mixed reads the pair
+    # and bonded forces (16 + 16), reads and clears the base-pair sum
+    # (32 + 32), reads and writes FP64 x, v, beta (2 x 72), reads the
+    # coefficients (32), the mirror at the last rebuild (16) and the bead
+    # record (16), and writes the mirror and residual (32).
     prof_steps = min(200, S * args.steps)
     ms3 = eng.step_profiled(prof_steps)
     lst = list_stats(eng)
     L = (lst[0] + lst[1] + lst[2]) / N
-    bytes_per_bead = 144 + 32 + 4 * L
+    C = st1["cluster_pairs"] / max(1, st1["i_clusters"])
+    bytes_per_bead = 16 + 20 * C / 8 + 16 + 336
     step_ms = ms3[1] / prof_steps
     achieved = N * bytes_per_bead / (step_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     rebuilds = st1["rebuilds"] - st0["rebuilds"]
     k_rebuild = (S * args.steps * len(sysm.instances)) / rebuilds if rebuilds else None
     traffic = None
-    tf = ROOT / "profiles" / f"k_step_{args.workload}_traffic.json"
+    tf = ROOT / "profiles" / f"step_kernels_{args.workload}_traffic.json"
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("bytes_per_launch")
 
@@ -312,9 +321,9 @@ def run_gpu(args):
            "gpu_launches": int(launches),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": traffic, "peak_kind": peak_kind,
-                        "kernel": "k_pairs + k_step" if st1["overlap"] else "k_step", "kernel_ms": step_ms,
+                        "kernel": "k_pairs_cl + k_step_mixed", "kernel_ms": step_ms,
                         "bonded_bp_ms": ms3[0] / prof_steps, "trigger_rebuild_ms": ms3[2] / prof_steps,
-                        "bytes_per_bead_step": bytes_per_bead},
+                        "bytes_per_bead_step": bytes_per_bead, "j_clusters_per_i_cluster": C},
            "clocks": clk.summary()}
     eng.close()
     if not args.no_sub and args.workload == "crowded":

@@ -133,6 +133,9 @@ typedef struct sis_stats {
     int32_t overlap;        /* 1: pair forces in their own kernel (sis_gpu_set_overlap) */
     int32_t small_blocks;   /* blocks of the per-block kernel of small instances (0: not used) */
     int32_t small_threads;  /* threads per block of that kernel */
+    int64_t cluster_pairs;  /* mixed path: current cluster-pair list entries (i-cluster x j-cluster) */
+    int32_t i_clusters;     /* mixed path: i-clusters of 8 beads (those whose j-clusters fit) */
+    int32_t reserved;
 } sis_stats;
 
 /* Creates a context and uploads topology and parameters.  Replaces the

@@ -67,6 +67,7 @@ class sis_stats(C.Structure):
         ("ele_pairs", C.c_int64), ("bp_pairs", C.c_int64), ("error_flags", C.c_int32), ("n_beads", C.c_int32),
         ("n_inst", C.c_int32), ("lanes_per_bead", C.c_int32), ("capped", C.c_int64),
         ("bp_blocks", C.c_int32), ("overlap", C.c_int32), ("small_blocks", C.c_int32), ("small_threads", C.c_int32),
+        ("cluster_pairs", C.c_int64), ("i_clusters", C.c_int32), ("reserved", C.c_int32),
     ]
 
 

@@ -1856,6 +1856,16 @@ extern "C" int sis_gpu_get_stats(sis_ctx *ctx, sis_stats *s) {
     s->error_flags = e;
     for (int i = 0; i < ctx->n; ++i) s->pair_entries += std::min(nn[i], ctx->g.cap);
     for (int k = 0; k < ctx->n_inst; ++k) s->bp_pairs += std::min(bc[k], ctx->ip[k].bp_cap);
+    if (ctx->g.prec != 0 && ctx->g.n_cl > 0) {
+        std::vector<int> nc(ctx->g.n_cl);
+        CK(cudaMemcpyAsync(nc.data(), ctx->D.ncl, sizeof(int) * nc.size(), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int c : nc)
+            if (c >= 0) {
+                s->cluster_pairs += c;
+                ++s->i_clusters;
+            }
+    }
     return SIS_OK;
 }
 
