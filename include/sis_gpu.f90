@@ -48,12 +48,26 @@ module sis_gpu_mod
     type(c_ptr) :: tempK, ionic_strength, box, stream
   end type
 
+  type, bind(C) :: sis_stats
+    integer(c_int64_t) :: steps, rebuilds, pair_entries, wca_pairs, ele_pairs, bp_pairs
+    integer(c_int32_t) :: error_flags, n_beads, n_inst, lanes_per_bead
+    integer(c_int64_t) :: capped
+    integer(c_int32_t) :: bp_blocks, overlap, small_blocks, small_threads
+    integer(c_int64_t) :: cluster_pairs
+    integer(c_int32_t) :: i_clusters, reserved
+  end type
+
   interface
     integer(c_int) function sis_gpu_create(top, par, ctx) bind(C, name="sis_gpu_create")
       import :: c_int, c_ptr, sis_topology, sis_params
       type(sis_topology), intent(in) :: top
       type(sis_params), intent(in) :: par
       type(c_ptr), intent(out) :: ctx
+    end function
+    integer(c_int) function sis_gpu_get_stats(ctx, st) bind(C, name="sis_gpu_get_stats")
+      import :: c_int, c_ptr, sis_stats
+      type(c_ptr), value :: ctx
+      type(sis_stats), intent(out) :: st
     end function
     subroutine sis_gpu_destroy(ctx) bind(C, name="sis_gpu_destroy")
       import :: c_ptr

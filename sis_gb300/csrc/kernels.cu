@@ -675,113 +675,11 @@ template <typename R> __global__ void __launch_bounds__(256) k_bp_test(Dev D, Gl
 // evaluated in FP64 by the same thread.  Each record writes its own energy
 // and status, and forces add exactly (fixed point) in the mixed path, so
 // the order of evaluation does not matter.
-// bp_eval_f with four lanes per record: lanes 4k .. 4k+3 of a warp take the
-// record `slot` (valid: there is one; the same for the four lanes), each
-// forming part of its terms (bp_force_part_f), summed over the four lanes
-// in a fixed order; the energy, status and the six beads' forces follow as
-// in bp_eval_f (each lane scatters one or two beads).  A record near a
-// straight bond angle is evaluated by the group's first lane the
-// single-lane way (bp_eval_f, then FP64 if needed: bp_eval_d on D's state).
-// E supplies the mirrors and the force target.  Called by all 32 lanes of a
-// warp.
-__device__ __forceinline__ void bp_eval_f4(const Dev &E, const Dev &D, const GlobP &g, int cur, int slot, bool valid) {
-    const int part = threadIdx.x & 3;
-    const uint4 *__restrict__ m = mir_at(E, cur);
-    int4 rec = make_int4(0, 0, 0, 0), nb = rec;
-    V3<float> f[6];
-    float u = 0.f;
-    bool ok = false, nr = false;
-    if (valid) {
-        rec = E.bps[slot];
-        nb = E.bps_n[slot];
-        const InstP &ip = E.ip[rec.w];
-        const BPPf &bf = E.bppf[rec.z & 0xff];
-        const V3<float> v12 = dvec32(m[rec.x], m[rec.y], ip), v13 = dvec32(m[rec.x], m[nb.x], ip),
-                        v15 = dvec32(m[rec.x], m[nb.z], ip), v42 = dvec32(m[nb.y], m[rec.y], ip),
-                        v62 = dvec32(m[nb.w], m[rec.y], ip);
-        ok = bp_force_part_f(part, v12, v13, v15, v42, v62, bf, f, &u, &nr);
-    } else {
-#pragma unroll
-        for (int q = 0; q < 6; ++q) f[q] = mk<float>(0.f, 0.f, 0.f);
-    }
-#pragma unroll
-    for (int o = 1; o <= 2; o <<= 1) {
-        u += __shfl_xor_sync(0xffffffffu, u, o);
-#pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            f[q].x += __shfl_xor_sync(0xffffffffu, f[q].x, o);
-            f[q].y += __shfl_xor_sync(0xffffffffu, f[q].y, o);
-            f[q].z += __shfl_xor_sync(0xffffffffu, f[q].z, o);
-        }
-    }
-    if (!valid) return;
-    if (nr) {
-        if (part == 0 && bp_eval_f(E, g, cur, slot)) bp_eval_d(D, g, cur, slot, E.fbp);
-        return;
-    }
-    const BPPf &bf = E.bppf[rec.z & 0xff];
-    float e = 0.f;
-    unsigned char st = 0;
-    if (ok) {
-        const bool triplet = g.bp_model == 4 || g.bp_model == 5;
-        const float ex = expf(-u);
-        e = triplet ? bf.U0 * E.bp_dgf[rec.w * 469 + (rec.z >> 8)] * ex : bf.U0 * ex;
-        st = e <= g.f_bp_cutoff_energy;
-        if (!st) {
-            e = 0.f;
-        } else if (g.nstep_mc > 0 && E.mc_due[rec.w]) {
-            // Monte Carlo pass: keep the record's forces until k_bp_mc decides
-            if (part == 0) {
-                long long *fr = E.bp_frec + (size_t)slot * 18;
-                for (int q = 0; q < 6; ++q) {
-                    const float c[3] = {e * f[q].x, e * f[q].y, e * f[q].z};
-                    for (int k = 0; k < 3; ++k) {
-                        long long w = 0;
-                        if (u <= 20.f) {
-                            if (fabsf(c[k]) < FX_LIMIT) w = fx_of(c[k]);
-                            else atomicOr(E.err, ERR_NONFINITE);
-                        }
-                        fr[3 * q + k] = w;
-                    }
-                }
-            }
-        } else if (u <= 20.f) {
-            const int ids[6] = {rec.x, rec.y, nb.x, nb.y, nb.z, nb.w};
-#pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                if ((q & 3) != part) continue;
-                const float cx = e * f[q].x, cy = e * f[q].y, cz = e * f[q].z;
-                if (!(fabsf(cx) < FX_LIMIT && fabsf(cy) < FX_LIMIT && fabsf(cz) < FX_LIMIT)) {
-                    atomicOr(E.err, ERR_NONFINITE);
-                    continue;
-                }
-                fx_scatter(E.fbp, ids[q], fx_of(cx), fx_of(cy), fx_of(cz));
-            }
-        }
-    }
-    if (part == 0) {
-        E.ene_bp[slot] = (double)e;
-        E.bp_status[slot] = st;
-    }
-}
-
 template <typename R> __device__ __forceinline__ void bp_eval_now(const Dev &D, const GlobP &g, int cur, int slot) {
     if constexpr (sizeof(R) == 4) {
         if (bp_eval_f(D, g, cur, slot)) bp_eval_d(D, g, cur, slot, D.fbp);
     } else {
         bp_eval_d(D, g, cur, slot, D.fbp);
-    }
-}
-// The first n records of a block's queue q: FP32, four lanes per record
-// (64 records per pass of the block); FP64, one thread per record.
-template <typename R> __device__ __forceinline__ void bp_eval_queue(const Dev &D, const GlobP &g, int cur, const int *q, int n) {
-    if constexpr (sizeof(R) == 4) {
-        for (int r0 = 0; r0 < n; r0 += (int)blockDim.x / 4) {
-            const int r = r0 + (int)threadIdx.x / 4;
-            bp_eval_f4(D, D, g, cur, r < n ? q[r] : 0, r < n);
-        }
-    } else {
-        if ((int)threadIdx.x < n) bp_eval_d(D, g, cur, q[threadIdx.x], D.fbp);
     }
 }
 template <typename R> __global__ void __launch_bounds__(256, 2) k_bp(Dev D, GlobP g, int cur) {
@@ -803,14 +701,14 @@ template <typename R> __global__ void __launch_bounds__(256, 2) k_bp(Dev D, Glob
         __syncthreads();
         const int n = s_n; // at most 511
         if (n >= 256) {
-            bp_eval_queue<R>(D, g, cur, s_q, 256);
+            bp_eval_now<R>(D, g, cur, s_q[threadIdx.x]);
             __syncthreads();
             if ((int)threadIdx.x < n - 256) s_q[threadIdx.x] = s_q[256 + threadIdx.x];
             if (threadIdx.x == 0) s_n = n - 256;
         }
         __syncthreads();
     }
-    bp_eval_queue<R>(D, g, cur, s_q, s_n);
+    if ((int)threadIdx.x < s_n) bp_eval_now<R>(D, g, cur, s_q[threadIdx.x]);
 }
 
 template <typename R> __global__ void __launch_bounds__(256) k_bp_eval(Dev D, GlobP g, int cur) {
@@ -1957,20 +1855,19 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 wn += __popc(bal);
                 __syncwarp();
                 if (wn >= 32) {
-                    for (int k0 = 0; k0 < 32; k0 += 8) {
-                        const int2 w = wq[k0 + (lane >> 2)];
-                        bp_eval_f4(small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]), D, g, cur, w.y, true);
-                    }
+                    const int2 w = wq[lane];
+                    const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
+                    if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
                     __syncwarp();
                     if (lane < wn - 32) wq[lane] = wq[32 + lane];
                     wn -= 32;
                     __syncwarp();
                 }
             }
-            for (int k0 = 0; k0 < wn; k0 += 8) {
-                const int k = k0 + (lane >> 2);
-                const int2 w = wq[k < wn ? k : 0];
-                bp_eval_f4(small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]), D, g, cur, w.y, k < wn);
+            if (lane < wn) {
+                const int2 w = wq[lane];
+                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
+                if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
             }
         }
         // ------------------------------------------------ bonded terms

@@ -645,118 +645,6 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     return true;
 }
 
-// bp_force_core_f split over four lanes (part 0..3): every lane forms the
-// shared separations and checks; part 0 takes the bond and the angle
-// 3-1=2, part 1 the angles 1=2-4 and 5-1=2, part 2 the angle 1=2-6 and the
-// dihedral 4-2=1=3, part 3 the dihedral 6-2=1=5.  Each term is formed by the
-// same FP32 operations as in bp_force_core_f; the lane's forces f (zeroed
-// here) and energy u are its terms' only, summed over the four lanes by the
-// caller.  Returns false outside the distance window, or with *near set (the
-// caller then takes the single-lane path with exact cross products).
-__device__ __forceinline__ bool bp_force_part_f(int part, const V3<float> &v12, const V3<float> &v13, const V3<float> &v15,
-                                                const V3<float> &v42, const V3<float> &v62, const BPPf &b, V3<float> f[6],
-                                                float *u_out, bool *near) {
-    const V3<float> z = mk<float>(0.f, 0.f, 0.f);
-#pragma unroll
-    for (int q = 0; q < 6; ++q) f[q] = z;
-    *u_out = 0.f;
-    *near = false;
-    const float d1212 = dot3(v12, v12);
-    const float a12 = sqrtf(d1212);
-    float d = a12 - b.bond_r;
-    if (fabsf(d) > b.cutoff_ddist) return false;
-    const float d1313 = dot3(v13, v13), d4242 = dot3(v42, v42), d1515 = dot3(v15, v15), d6262 = dot3(v62, v62);
-    const V3<float> c13 = cross_acc(v12, v13), c15 = cross_acc(v12, v15);
-    const V3<float> m42 = cross_acc(v42, v12), m62 = cross_acc(v62, v12);
-    const float s13 = dot3(c13, c13), s15 = dot3(c15, c15), s42 = dot3(m42, m42), s62 = dot3(m62, m62);
-    const float kSin2 = 9e-4f;
-    *near = s13 < kSin2 * d1212 * d1313 || s15 < kSin2 * d1212 * d1515 || s42 < kSin2 * d1212 * d4242 ||
-            s62 < kSin2 * d1212 * d6262;
-    if (*near) return false;
-    const float d1213 = dot3(v12, v13), d1242 = dot3(v12, v42), d1215 = dot3(v12, v15), d1262 = dot3(v12, v62);
-    float u = 0.f, r, pre;
-    V3<float> f0 = z, f1 = z, fi, fk, fl;
-    if (part == 0) {
-        u = b.bond_k * (d * d);
-        const V3<float> fb = (2.f * b.bond_k * d / a12) * v12;
-        f0 = fb;
-        f1 = -fb;
-        // 3-1=2 (imp-1 -- imp -- jmp)
-        r = sqrtf(s13);
-        d = atan2f(r, d1213) - b.angl_theta[1];
-        u += b.angl_k[1] * (d * d);
-        pre = 2.f * b.angl_k[1] * d / r;
-        fi = (pre / d1313) * cross3(v13, c13);
-        fk = (pre / d1212) * cross3(c13, v12);
-        f0 = f0 - fi - fk;
-        f1 = f1 + fk;
-        f[2] = fi;
-    } else if (part == 1) {
-        // 1=2-4 (imp -- jmp -- jmp-1)
-        r = sqrtf(s42);
-        d = atan2f(r, d1242) - b.angl_theta[0];
-        u = b.angl_k[0] * (d * d);
-        pre = 2.f * b.angl_k[0] * d / r;
-        fi = (-pre / d1212) * cross3(v12, m42);
-        fk = (-pre / d4242) * cross3(m42, v42);
-        f0 = fi;
-        f1 = -fi - fk;
-        f[3] = fk;
-        // 5-1=2 (imp+1 -- imp -- jmp)
-        r = sqrtf(s15);
-        d = atan2f(r, d1215) - b.angl_theta[3];
-        u += b.angl_k[3] * (d * d);
-        pre = 2.f * b.angl_k[3] * d / r;
-        fi = (pre / d1515) * cross3(v15, c15);
-        fk = (pre / d1212) * cross3(c15, v12);
-        f0 = f0 - fi - fk;
-        f1 = f1 + fk;
-        f[4] = fi;
-    } else if (part == 2) {
-        // 1=2-6 (imp -- jmp -- jmp+1)
-        r = sqrtf(s62);
-        d = atan2f(r, d1262) - b.angl_theta[2];
-        u = b.angl_k[2] * (d * d);
-        pre = 2.f * b.angl_k[2] * d / r;
-        fi = (-pre / d1212) * cross3(v12, m62);
-        fk = (-pre / d6262) * cross3(m62, v62);
-        f0 = fi;
-        f1 = -fi - fk;
-        f[5] = fk;
-        // dihedral 4-2=1=3: m = v42 x v12, n = v12 x v13
-        const float o13 = d1213 / d1212, o42 = d1242 / d1212;
-        float sn, cs;
-        d = atan2f(dot3(v42, c13) * a12, dot3(m42, c13)) + b.dihd_phi[0];
-        sincosf(d, &sn, &cs);
-        u += b.dihd_k[0] * (1.f + cs);
-        pre = -b.dihd_k[0] * sn * a12;
-        fi = (pre / s42) * m42;
-        fl = (-pre / s13) * c13;
-        f[3] = fi;
-        f1 = f1 + (o42 - 1.f) * fi - o13 * fl;
-        f0 = f0 + (o13 - 1.f) * fl - o42 * fi;
-        f[2] = fl;
-    } else {
-        // dihedral 6-2=1=5: m = v62 x v12, n = v12 x v15
-        const float o15 = d1215 / d1212, o62 = d1262 / d1212;
-        float sn, cs;
-        d = atan2f(dot3(v62, c15) * a12, dot3(m62, c15)) + b.dihd_phi[1];
-        sincosf(d, &sn, &cs);
-        u = b.dihd_k[1] * (1.f + cs);
-        pre = -b.dihd_k[1] * sn * a12;
-        fi = (pre / s62) * m62;
-        fl = (-pre / s15) * c15;
-        f[5] = fi;
-        f1 = (o62 - 1.f) * fi - o15 * fl;
-        f0 = (o15 - 1.f) * fl - o62 * fi;
-        f[4] = fl;
-    }
-    f[0] = f0;
-    f[1] = f1;
-    *u_out = u;
-    return true;
-}
-
 // energy_bp.F90 mp_angle (clamped) and mp_dihedral
 template <typename T> __device__ __forceinline__ T mp_angle(const V3<T> &v12, const V3<T> &v32) {
     T co = dot3(v32, v12) / fm::sqrt(dot3(v12, v12) * dot3(v32, v32));

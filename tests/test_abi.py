@@ -169,7 +169,7 @@ def _fortran_type_fields(doc, name):
     return out
 
 
-@pytest.mark.parametrize("name", ["sis_params", "sis_topology"])
+@pytest.mark.parametrize("name", ["sis_params", "sis_topology", "sis_stats"])
 def test_fortran_struct_types_match_the_header(name):
     """The bind(C) derived types of include/sis_gpu.f90 list the C structs'
     fields in order, with matching kinds and array sizes."""
