@@ -1832,21 +1832,15 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         // fixed-point atomics), the bonded terms write their slot planes, the
         // pair sums go to s_F, and the update reads all three after one
         // barrier.
-        // The first nbw warps take the base-pair records, the others the
-        // bonded terms and the pair forces, so that the base-pair latency
-        // chains run beside the pair work (about 400 records per base-pair
-        // warp, at most a quarter of the warps).
-        const int nrec = g.bp_model > 0 ? s_bp[ni] : 0;
-        const int nbw = nrec > 0 && nwarps > 1 ? min((nrec + 399) / 400, max(1, nwarps / 4)) : 0;
-        const int wf = warp - nbw, nwf = nwarps - nbw; // force warps
         // ------------------------------------------------ base pairs
-        if (warp < nbw) {
-            // every base-pair warp tests 32 records at a time and queues the
-            // ones in the distance window (bucket-local instance | slot); a
-            // full queue is evaluated by the whole warp, the rest at the end
+        if (g.bp_model > 0) {
+            // every warp tests 32 records at a time and queues the ones in the
+            // distance window (bucket-local instance | slot); a full queue is
+            // evaluated by the whole warp, the rest at the end
             int2 *wq = s_qi + warp * 64;
             int wn = 0;
-            for (int r0 = warp * 32; r0 < nrec; r0 += nbw * 32) {
+            const int nrec = s_bp[ni];
+            for (int r0 = warp * 32; r0 < nrec; r0 += nt) {
                 const int r = r0 + lane;
                 bool pass = false;
                 int q = 0, slot = 0;
@@ -1877,21 +1871,20 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             }
         }
         // ------------------------------------------------ bonded terms
-        if (warp >= nbw)
-            for (int s = wf * 32 + lane; s < nb; s += nwf * 32) {
-                const int q = small_inst(s_sb, ni, s);
-                const int gi = s_off[q] + (s - s_sb[q]);
-                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
-                bool an, dn;
-                bonded_terms<float>(E, g, cur, gi, &an, &dn);
-                if (an) bonded_fp64(D, g, cur, gi, 0);
-                if (dn) bonded_fp64(D, g, cur, gi, 1);
-            }
+        for (int s = tid; s < nb; s += nt) {
+            const int q = small_inst(s_sb, ni, s);
+            const int gi = s_off[q] + (s - s_sb[q]);
+            const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+            bool an, dn;
+            bonded_terms<float>(E, g, cur, gi, &an, &dn);
+            if (an) bonded_fp64(D, g, cur, gi, 0);
+            if (dn) bonded_fp64(D, g, cur, gi, 1);
+        }
         // ------------------------------------------------ pair forces
-        if (warp >= nbw) {
+        {
             constexpr int BPW = 32 / kSmallLanes; // beads per warp and pass
             const int sub = lane & (kSmallLanes - 1);
-            for (int base = wf * BPW; base < nb; base += nwf * BPW) {
+            for (int base = warp * BPW; base < nb; base += nwarps * BPW) {
                 // every lane of a warp runs the same passes (shuffles below)
                 const int s0 = base + lane / kSmallLanes;
                 const int s = min(s0, nb - 1);
