@@ -303,15 +303,15 @@ template <> struct Pos<float> {
 };
 
 // Mirror component q = round(x*S) mod 2^32 and the residual x*S - q (units of
-// 1/S, |r| <= 1/2) that the mirror drops, with two FP64 operations: adding
-// M = 1.5 * 2^40 to t = x*S leaves round(t * 2^12) + 2^51 in the low 52
-// mantissa bits of the sum (valid for |t| < 2^39), so the integer part and
-// the residual (to 2^-12 units) follow from integer arithmetic.  q rounds t
-// half up after t has been rounded to 2^-12 units; every mirror of the
-// library comes from this function, so all agree.  Returns false when t is
-// out of range or not finite (then q and r are meaningless).
+// 1/S, |r| <= 1/2) that the mirror drops, with one FP64 operation: the
+// fused x*S + M, M = 1.5 * 2^40, leaves round(x*S * 2^12) + 2^51 in the low
+// 52 mantissa bits of the sum (valid for |x*S| < 2^39), so the integer part
+// and the residual (to 2^-12 units) follow from integer arithmetic.  q
+// rounds x*S half up after it has been rounded to 2^-12 units; every mirror
+// of the library comes from this function, so all agree.  Returns false
+// when x*S is out of range or not finite (then q and r are meaningless).
 __device__ __forceinline__ bool fixed_mirror(double x, double s, unsigned int &q, float &r) {
-    const double u = __dadd_rn(__dmul_rn(x, s), 1649267441664.0); // 1.5 * 2^40
+    const double u = __fma_rn(x, s, 1649267441664.0); // 1.5 * 2^40
     const long long b = __double_as_longlong(u);
     const long long w = (b & 0xFFFFFFFFFFFFFLL) - (1LL << 51);  // round(t * 2^12)
     const long long qq = (w + 2048) >> 12;

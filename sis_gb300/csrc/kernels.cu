@@ -1387,17 +1387,15 @@ __device__ __forceinline__ uint4 mixed_update_core(const Dev &D, const GlobP &g,
     bool ok = true;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        double dx;
         if (g.integrator == 1) {
             const float bn = cf1 * xi[c];
             const double vn = fma(m.x, vc[c], bc[c]) + (double)fmaf(cf0, F[c], bn);
             bc[c] = (double)bn;
             vc[c] = vn;
-            dx = m.z * vn;
+            xc[c] = fma(m.z, vn, xc[c]); // x + sqrt(b) h v, one rounding
         } else {
-            dx = (double)fmaf(cf0, F[c], cf1 * xi[c]);
+            xc[c] = xc[c] + (double)fmaf(cf0, F[c], cf1 * xi[c]);
         }
-        xc[c] = xc[c] + dx;
         ok &= fixed_mirror(xc[c], jp.fsc[c], q[c], r[c]);
     }
     if (!ok) atomicOr(D.err, ERR_NONFINITE);
