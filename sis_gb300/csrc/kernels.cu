@@ -1718,7 +1718,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     float4 *s_F = (float4 *)(s_fbp + cap);   // pair force of the step (xyz)
     double2 *s_cd = (double2 *)(s_F + cap);  // integrator coefficients a, sqrt(b) h (mdc.x, mdc.z)
     float2 *s_cf = (float2 *)(s_cd + cap);   // FP32 force and noise coefficients of the update
-    __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst];
+    __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst], s_bpo[kSmallMaxInst];
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
     __shared__ int s_fire[kSmallMaxInst];
@@ -1734,6 +1734,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             s_iid[q] = id;
             s_off[q] = ip.bead_off;
             s_n[q] = ip.n_act;
+            s_bpo[q] = ip.bp_off;
             s_sb[q] = sb;
             s_bp[q] = nbp;
             sb += ip.n_act;
@@ -1844,7 +1845,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 int q = 0, slot = 0;
                 if (r < nrec) {
                     q = small_inst(s_bp, ni, r);
-                    slot = D.ip[s_iid[q]].bp_off + (r - s_bp[q]);
+                    slot = s_bpo[q] + (r - s_bp[q]);
                     const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
                     pass = bp_test<float>(E, g, cur, slot);
                 }
@@ -1893,24 +1894,31 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const InstP &ip = D.ip[bi.x];
                 const uint4 mi = s_mir[s];
                 const PairCoef P = pair_coef_of(g, ip);
-                const int m = min(D.nnbr[gi], g.cap);
                 const int *__restrict__ nbl = D.nbr + (size_t)gi * g.cap;
                 const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
                              f2 = make_float2(ip.finv[2], ip.finv[2]);
                 // lane sub takes entries sub, sub + L, sub + 2L, ... (L =
                 // kSmallLanes), two at a time (pair2), in batches of 16
-                // entries whose list words load before any is used; a
-                // missing entry is the bead itself with no term bit (an
-                // exact zero)
+                // entries whose list words load before any is used (the
+                // first batch beside the list length: words past it, inside
+                // the bead's capacity, are read and dropped); a missing
+                // entry is the bead itself with no term bit (an exact zero)
                 float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
                 constexpr int L = kSmallLanes;
+                int w0[16];
+#pragma unroll
+                for (int u = 0; u < 16; ++u) w0[u] = sub + u * L < g.cap ? __ldg(nbl + sub + u * L) : 0;
+                const int m = min(D.nnbr[gi], g.cap);
                 // every lane runs the batches of the warp's longest list
                 const int mmax = __reduce_max_sync(0xffffffffu, m);
                 for (int k0 = sub; k0 - sub < mmax; k0 += 16 * L) {
                     // the batch's 16 list words in flight at once
                     int e[16];
 #pragma unroll
-                    for (int u = 0; u < 16; ++u) e[u] = k0 + u * L < m ? __ldg(nbl + k0 + u * L) : gi;
+                    for (int u = 0; u < 16; ++u) {
+                        const int k = k0 + u * L;
+                        e[u] = k < m ? (k0 == sub ? w0[u] : __ldg(nbl + k)) : gi;
+                    }
 #pragma unroll
                     for (int u = 0; u < 16; u += 2) {
                         if (k0 - sub + u * L >= mmax) break; // warp-uniform: past every lane's list
