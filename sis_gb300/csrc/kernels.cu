@@ -1894,31 +1894,24 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const InstP &ip = D.ip[bi.x];
                 const uint4 mi = s_mir[s];
                 const PairCoef P = pair_coef_of(g, ip);
+                const int m = min(D.nnbr[gi], g.cap);
                 const int *__restrict__ nbl = D.nbr + (size_t)gi * g.cap;
                 const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
                              f2 = make_float2(ip.finv[2], ip.finv[2]);
                 // lane sub takes entries sub, sub + L, sub + 2L, ... (L =
                 // kSmallLanes), two at a time (pair2), in batches of 16
-                // entries whose list words load before any is used (the
-                // first batch beside the list length: words past it, inside
-                // the bead's capacity, are read and dropped); a missing
-                // entry is the bead itself with no term bit (an exact zero)
+                // entries whose list words load before any is used; a
+                // missing entry is the bead itself with no term bit (an
+                // exact zero)
                 float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
                 constexpr int L = kSmallLanes;
-                int w0[16];
-#pragma unroll
-                for (int u = 0; u < 16; ++u) w0[u] = sub + u * L < g.cap ? __ldg(nbl + sub + u * L) : 0;
-                const int m = min(D.nnbr[gi], g.cap);
                 // every lane runs the batches of the warp's longest list
                 const int mmax = __reduce_max_sync(0xffffffffu, m);
                 for (int k0 = sub; k0 - sub < mmax; k0 += 16 * L) {
                     // the batch's 16 list words in flight at once
                     int e[16];
 #pragma unroll
-                    for (int u = 0; u < 16; ++u) {
-                        const int k = k0 + u * L;
-                        e[u] = k < m ? (k0 == sub ? w0[u] : __ldg(nbl + k)) : gi;
-                    }
+                    for (int u = 0; u < 16; ++u) e[u] = k0 + u * L < m ? __ldg(nbl + k0 + u * L) : gi;
 #pragma unroll
                     for (int u = 0; u < 16; u += 2) {
                         if (k0 - sub + u * L >= mmax) break; // warp-uniform: past every lane's list
