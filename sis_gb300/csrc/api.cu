@@ -136,6 +136,8 @@ struct sis_ctx {
     bool small_ok = false;
     int small_mode = -1;
     bool small_tuned = false;
+    int small_target = 0;            // bucket count the autotuner chose
+    int64_t small_planned = 0;       // steps at the last bucket plan
     int small_threads = 256;
     int *sp_off_d = nullptr, *sp_inst_d = nullptr;
     SmallPlan sp{};
@@ -644,23 +646,28 @@ bool small_active(const sis_ctx *ctx) {
 // instances in ascending order.
 int small_plan(sis_ctx *ctx, int target) {
     const int ni = ctx->n_inst;
-    // cost of an instance: its pair-list entries plus a per-bead share (the
-    // update, bonded and base-pair terms cost about as much as 90 entries);
-    // by capacity when slots are loaded in place (sis_gpu_load_slot)
+    // cost of an instance: its pair-list entries, a per-bead share (the
+    // update and bonded terms cost about as much as 90 entries) and its
+    // base-pair records; by capacity when slots are loaded in place
+    // (sis_gpu_load_slot)
     std::vector<double> cost(ni);
     bool slots = false;
     for (int k = 0; k < ni; ++k) slots |= ctx->ip[k].n_act != ctx->ip[k].n;
-    std::vector<int> nn;
+    std::vector<int> nn, nbp;
     if (!slots && ctx->lists_valid) {
         nn.resize(ctx->n);
+        nbp.resize(ni);
         CK(cudaMemcpyAsync(nn.data(), ctx->D.nnbr, sizeof(int) * ctx->n, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaMemcpyAsync(nbp.data(), ctx->D.bp_cnt, sizeof(int) * ni, cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
     }
     for (int k = 0; k < ni; ++k) {
         const InstP &I = ctx->ip[k];
         double c = 90.0 * I.n;
-        if (!nn.empty())
+        if (!nn.empty()) {
             for (int i = I.bead_off; i < I.bead_off + I.n; ++i) c += std::min(nn[i], ctx->g.cap);
+            c += 8.0 * std::min(nbp[k], I.bp_cap); // base-pair records: a test each
+        }
         cost[k] = c;
     }
     std::vector<int> order(ni);
@@ -708,6 +715,7 @@ int small_plan(sis_ctx *ctx, int target) {
 // nsteps steps through k_md_small, at most kSmallChunk per launch; noise: the
 // device copy of fed noise (nsteps x n x 3) or NULL
 constexpr int kSmallChunk = 1000;
+constexpr int64_t kSmallReplan = 2000; // MD steps between bucket plans
 int run_small(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     for (int64_t s = 0; s < nsteps;) {
         const int chunk = (int)std::min<int64_t>(kSmallChunk, nsteps - s);
@@ -769,6 +777,8 @@ int64_t small_autotune(sis_ctx *ctx, int64_t budget, int *rc) {
         }
     }
     if ((*rc = small_plan(ctx, best_t))) return taken;
+    ctx->small_target = best_t;
+    ctx->small_planned = ctx->steps + taken;
     ctx->small_threads = best_w;
     ctx->small_tuned = true;
     return taken;
@@ -1500,6 +1510,12 @@ extern "C" int sis_gpu_step(sis_ctx *ctx, int64_t nsteps, const double *noise) {
             if (rc) return rc;
         } else if (!ctx->sp.n_cta && (rc = small_plan(ctx, std::min(ctx->n_inst, 2 * ctx->sms)))) {
             return rc;
+        } else if (ctx->small_tuned && ctx->steps - ctx->small_planned >= kSmallReplan) {
+            // the instances' list lengths drift as they fold or unfold: the
+            // buckets are balanced again on the current lists (the trajectory
+            // does not depend on them)
+            if ((rc = small_plan(ctx, ctx->small_target))) return rc;
+            ctx->small_planned = ctx->steps;
         }
         if ((rc = run_small(ctx, nsteps - done, noise ? ctx->noise_d + (size_t)done * ctx->n * 3 : nullptr))) return rc;
         ctx->steps += nsteps;
