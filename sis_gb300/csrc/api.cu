@@ -962,7 +962,7 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
     g.n_inst = ctx->n_inst;
     g.cap = cap;
     g.n_cl = n_cl;
-    g.ccap = std::min(kClCapMax, std::max(64, 2 * cap));
+    g.ccap = std::min(kClCapMax, std::max(32, cap / 2));
     g.prec = p.precision;
     g.integrator = p.integrator;
     g.angl_reb = p.angl_reb;

@@ -57,7 +57,7 @@ constexpr int kMaxCoopBlocks = 4096;
 // conversion from per-bead lists, and the largest j-cluster count per i-cluster
 constexpr int kCl = 8;
 constexpr int kClHash = 512;
-constexpr int kClCapMax = 512;
+constexpr int kClCapMax = 256;
 
 // Fixed-point base-pair force accumulation of the mixed path: one unit is
 // 2^-32 kcal/mol/A; contributions of magnitude 2^30 or more are reported as
@@ -125,7 +125,7 @@ struct InstP {
 
 struct GlobP {
     int n, n_inst, cap, prec, integrator;
-    int n_cl, ccap; // i-clusters of all instances; partner slots per i-cluster
+    int n_cl, ccap; // i-clusters of all instances; j-cluster slots per i-cluster
     int angl_reb, dih_type, bp_model, flg_ele, temp_indep;
     int bp_min_loop, bp_jnext_compat, ele_excl_bond, ele_excl_angle;
     double bond_k, bond_r0, angl_k, angl_t0, cos_t0, dih_k, dih_w, dih_p0;
@@ -189,12 +189,12 @@ struct Dev {
     double *rgv;
     double *mass;
     int *nbr, *nnbr;
-    // cluster partner lists (mixed path): per i-cluster its first bead, its
-    // partner count (-1: more than ccap, the pair kernel then walks the
-    // per-bead lists of its beads), and ccap slots of (partner bead, masks:
-    // bit a WCA, bit 8 + a electrostatics for the cluster's bead a)
+    // cluster-pair lists (mixed path): per i-cluster its first bead, its
+    // j-cluster count (-1: more than ccap, the pair kernel then walks the
+    // per-bead lists of its beads), and ccap slots of (j-cluster first bead,
+    // WCA mask, electrostatic mask)
     int *cl_first, *ncl, *cl_j;
-    unsigned int *cl_m;
+    ulonglong2 *cl_m;
     uint4 *mir0;            // [n] mirror at the last rebuild (mixed path)
     // base-pair lists
     int4 *bps, *bps_n;      // per-instance staging segments (records, neighbour beads)

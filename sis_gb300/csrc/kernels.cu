@@ -1227,23 +1227,24 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// Pair forces of the mixed path over the cluster partner lists (lists.cu
-// cluster_lists) into fpair: one warp per i-cluster of 8 beads, whose list
-// is the union of its beads' partners, each with a mask of the beads that
-// pair with it.  The warp stages the partners, up to kClChunk at a time, in
-// shared memory: lane k loads the records of partners k, k + 32, ... and
-// copies their mirrors with cp.async, so the whole chunk is in flight at
-// once.  Lane (a = lane & 7, q = lane >> 3) then takes i-bead a against
-// partners k0 + q and k0 + q + 4 of every round of 8 (pair2, masked by bit a
-// of each partner's masks).  Sums: the two partners of a round apart, then
-// added, in list order per lane, then over q (xor 8, then 16): a fixed
-// order, and a partner beyond every cutoff adds an exact zero.  mask bit 16:
-// WCA, bit 32: electrostatics.  An i-cluster whose partners did not fit
-// (count -1) walks its beads' per-bead lists, 4 lanes per bead.
-constexpr int kClChunk = 128;
+// Pair forces of the mixed path over the cluster-pair lists (lists.cu
+// cluster_lists) into fpair: one warp per i-cluster of 8 beads.  The warp
+// stages the j-clusters of its list, up to kClChunk at a time, in shared
+// memory: lane k loads the k-th cluster record (first bead, WCA and
+// electrostatic masks), then the 8 lanes of each group copy the 8 mirrors of
+// every 4th cluster (128 contiguous bytes) with cp.async, so the whole
+// chunk's mirrors are in flight at once.  Lane (a = lane & 7, q = lane >> 3)
+// then takes i-bead a against all 8 j-beads of every 4th j-cluster of the
+// list, starting at the q-th, two pairs at a time (pair2).  Sums: even and
+// odd partners apart, then added, in list order per lane, then over q (xor
+// 8, then 16): a fixed order, and a partner beyond every cutoff adds an
+// exact zero.  mask bit 16: WCA, bit 32: electrostatics.  An i-cluster whose
+// j-clusters did not fit (count -1) walks its beads' per-bead lists, 4 lanes
+// per bead.
+constexpr int kClChunk = 32;
 __global__ void __launch_bounds__(256, 5) k_pairs_cl(Dev D, GlobP g, int cur, int mask) {
-    __shared__ __align__(16) uint4 s_mj[8][kClChunk];
-    __shared__ unsigned s_cm[8][kClChunk];
+    __shared__ __align__(16) uint4 s_mj[8][kClChunk * kCl];
+    __shared__ ulonglong2 s_cm[8][kClChunk];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int ic = blockIdx.x * 8 + w;
     if (ic >= g.n_cl) return;
@@ -1256,29 +1257,40 @@ __global__ void __launch_bounds__(256, 5) k_pairs_cl(Dev D, GlobP g, int cur, in
     const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
                  f2 = make_float2(ip.finv[2], ip.finv[2]);
     const PairCoef P = pair_coef_of(g, ip);
-    const unsigned wsel = (mask & 16) ? 1u : 0u, esel = (mask & 32) ? 1u : 0u;
+    const unsigned wsel = (mask & 16) ? 0xffu : 0u, esel = (mask & 32) ? 0xffu : 0u;
     float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
     const int nc = D.ncl[ic];
     if (nc >= 0) {
         const size_t base = (size_t)ic * g.ccap;
         for (int c0 = 0; c0 < nc; c0 += kClChunk) {
             const int nk = min(kClChunk, nc - c0);
-            for (int k = lane; k < nk; k += 32) {
-                s_cm[w][k] = __ldg(D.cl_m + base + c0 + k);
-                cp_async16(&s_mj[w][k], mir + __ldg(D.cl_j + base + c0 + k));
+            int j0 = 0;
+            if (lane < nk) {
+                j0 = __ldg(D.cl_j + base + c0 + lane);
+                s_cm[w][lane] = __ldg(D.cl_m + base + c0 + lane);
+            }
+            for (int t = 0; 4 * t < nk; ++t) {
+                const int k = q + 4 * t;
+                const int jk = __shfl_sync(0xffffffffu, j0, k & 31);
+                if (k < nk) cp_async16(&s_mj[w][k * kCl + a], mir + jk + a);
             }
             cp_async_wait_all();
             __syncwarp();
-            for (int k0 = 0; k0 < nk; k0 += 8) {
-                // every lane runs every round; a partner past the chunk's
-                // end is partner 0 with an empty mask (exact zeros)
-                const int ka = k0 + q, kb = k0 + q + 4;
-                const unsigned ma = ka < nk ? s_cm[w][ka] : 0u, mb = kb < nk ? s_cm[w][kb] : 0u;
-                const Pair2 pr = pair2(mi, s_mj[w][ka < nk ? ka : 0], s_mj[w][kb < nk ? kb : 0], f0, f1, f2,
-                                       (ma >> a) & wsel, (mb >> a) & wsel, (ma >> (8 + a)) & esel, (mb >> (8 + a)) & esel, P);
-                ax = __ffma2_rn(pr.c, pr.vx, ax);
-                ay = __ffma2_rn(pr.c, pr.vy, ay);
-                az = __ffma2_rn(pr.c, pr.vz, az);
+            for (int k0 = 0; k0 < nk; k0 += 4) {
+                // every lane runs every round; a lane past the chunk's end
+                // takes cluster 0 with empty masks (exact zeros)
+                const int k = k0 + q < nk ? k0 + q : 0;
+                const ulonglong2 m = k0 + q < nk ? s_cm[w][k] : make_ulonglong2(0ull, 0ull);
+                const unsigned wb = (unsigned)(m.x >> (a * kCl)) & wsel, eb = (unsigned)(m.y >> (a * kCl)) & esel;
+                const uint4 *mj = s_mj[w] + k * kCl;
+#pragma unroll
+                for (int b = 0; b < kCl; b += 2) {
+                    const Pair2 pr = pair2(mi, mj[b], mj[b + 1], f0, f1, f2, (wb >> b) & 1u, (wb >> (b + 1)) & 1u, (eb >> b) & 1u,
+                                           (eb >> (b + 1)) & 1u, P);
+                    ax = __ffma2_rn(pr.c, pr.vx, ax);
+                    ay = __ffma2_rn(pr.c, pr.vy, ay);
+                    az = __ffma2_rn(pr.c, pr.vz, az);
+                }
             }
             __syncwarp();
         }

@@ -249,43 +249,39 @@ __device__ __forceinline__ void bead_end(const Dev &D, const GlobP &g, int gi, i
 }
 
 __device__ __forceinline__ unsigned cl_hash(int J) { return ((unsigned)J * 2654435761u) >> 23; } // 9 bits: kClHash
-// The partner list of i-cluster ic (one warp; key and msk: the warp's
-// 2 * kClHash words of shared memory): the distinct partners j of its beads
-// (the union of their per-bead lists), in ascending local index, each with
-// bit a (WCA) and bit 8 + a (electrostatics) for every bead a of the cluster
-// that has j in its list with that term.  More than ccap distinct partners
-// (or a full table) gives the count -1: the pair kernel then walks the
-// beads' per-bead lists.
-static __device__ void cluster_one(const Dev &D, const GlobP &g, int ic, int *key, unsigned *msk) {
+__device__ __forceinline__ int cl_find(const int *key, int J) {
+    unsigned h = cl_hash(J);
+    for (int p = 0; p < kClHash; ++p) {
+        if (key[h] == J) return (int)h;
+        h = (h + 1) & (kClHash - 1);
+    }
+    return -1;
+}
+// The cluster-pair list of i-cluster ic (one warp; key and rank: the warp's
+// 2 * kClHash ints of shared memory).
+static __device__ void cluster_one(const Dev &D, const GlobP &g, int ic, int *key, int *rank) {
     const int lane = threadIdx.x & 31;
     const int first = D.cl_first[ic];
     const InstP &ip = D.ip[D.binfo[first].x];
     const int cnt = min(kCl, ip.bead_off + ip.n - first);
-    for (int h = lane; h < kClHash; h += 32) {
-        key[h] = -1;
-        msk[h] = 0u;
-    }
+    for (int h = lane; h < kClHash; h += 32) key[h] = -1;
     __syncwarp();
+    // distinct clusters of the entries (the table holds at most kClHash)
     int full = 0;
     for (int a = 0; a < cnt; ++a) {
         const int gi = first + a;
         const int m = min(__ldcg(D.nnbr + gi), g.cap);
         const int *nb = D.nbr + (size_t)gi * g.cap;
         for (int k = lane; k < m; k += 32) {
-            const int e = __ldcg(nb + k);
-            const int jl = (e & IDX_MASK) - ip.bead_off;
-            unsigned h = cl_hash(jl);
+            const int J = ((__ldcg(nb + k) & IDX_MASK) - ip.bead_off) / kCl;
+            unsigned h = cl_hash(J);
             int p = 0;
             for (; p < kClHash; ++p) {
-                const int old = atomicCAS(&key[h], -1, jl);
-                if (old == -1 || old == jl) break;
+                const int old = atomicCAS(&key[h], -1, J);
+                if (old == -1 || old == J) break;
                 h = (h + 1) & (kClHash - 1);
             }
-            if (p == kClHash) {
-                full = 1;
-                continue;
-            }
-            atomicOr(&msk[h], ((e & WCA_BIT) ? 1u << a : 0u) | ((e & ELE_BIT) ? 1u << (8 + a) : 0u));
+            full |= p == kClHash;
         }
     }
     __syncwarp();
@@ -298,7 +294,7 @@ static __device__ void cluster_one(const Dev &D, const GlobP &g, int ic, int *ke
         __syncwarp();
         return;
     }
-    // each partner at its rank: the number of smaller ones
+    // rank of every distinct cluster: the number of smaller ones
     for (int h = lane; h < kClHash; h += 32) {
         const int v = key[h];
         if (v < 0) continue;
@@ -307,8 +303,25 @@ static __device__ void cluster_one(const Dev &D, const GlobP &g, int ic, int *ke
             const int w = key[q];
             r += w >= 0 && w < v;
         }
-        D.cl_j[base + r] = ip.bead_off + v;
-        D.cl_m[base + r] = msk[h];
+        rank[h] = r;
+        D.cl_j[base + r] = ip.bead_off + v * kCl;
+        D.cl_m[base + r] = make_ulonglong2(0ull, 0ull);
+    }
+    __syncwarp();
+    for (int a = 0; a < cnt; ++a) {
+        const int gi = first + a;
+        const int m = min(__ldcg(D.nnbr + gi), g.cap);
+        const int *nb = D.nbr + (size_t)gi * g.cap;
+        for (int k = lane; k < m; k += 32) {
+            const int e = __ldcg(nb + k);
+            const int jl = (e & IDX_MASK) - ip.bead_off;
+            const int h = cl_find(key, jl / kCl);
+            if (h < 0) continue; // not reached: every cluster was inserted
+            const unsigned long long bit = 1ull << (a * kCl + jl % kCl);
+            ulonglong2 *dst = D.cl_m + base + rank[h];
+            if (e & WCA_BIT) atomicOr(&dst->x, bit);
+            if (e & ELE_BIT) atomicOr(&dst->y, bit);
+        }
     }
     if (lane == 0) D.ncl[ic] = nu;
     __syncwarp();

@@ -311,23 +311,23 @@ __device__ void cell_search(const Dev &D, const GlobP &g, int cur, const int2 *l
     }
 }
 
-// ------------------------------------------------------ cluster partners
-// The mixed path's pair kernel walks, per i-cluster of 8 beads, the union of
-// its beads' per-bead lists instead of each list (kernels.cu k_pairs_cl).
-// For every i-cluster of a rebuilt instance one warp gathers the partners of
-// its beads' list entries into a hash table in shared memory, ORs each
-// entry's bit a (WCA) or 8 + a (electrostatics; a: the bead's place in the
-// cluster) into its partner's mask, and writes the distinct partners in
-// ascending local index (listcore.cuh cluster_one), so an instance gives the
-// same lists alone and in any batch.  An i-cluster with more than ccap
-// distinct partners gets the count -1, and the pair kernel walks its beads'
+// ------------------------------------------------------ cluster pairs
+// The mixed path's pair kernel walks cluster pairs instead of per-bead lists
+// (kernels.cu k_pairs_cl).  For every i-cluster of a rebuilt instance one
+// warp gathers the clusters J (local index of the partner / 8) of its beads'
+// list entries into a hash table in shared memory, ranks the distinct J in
+// ascending order, and ORs each entry's bit 8a+b (a, b: the beads' places in
+// their clusters) into the WCA or electrostatic mask of its J (listcore.cuh
+// cluster_one).  The order is that of the local indices, so an instance
+// gives the same lists alone and in any batch.  An i-cluster with more than
+// ccap distinct J gets the count -1, and the pair kernel walks its beads'
 // per-bead lists instead.
 __device__ void cluster_lists(const Dev &D, const GlobP &g, int *sh) {
     const int warp = threadIdx.x >> 5;
     int *key = sh + warp * 2 * kClHash;
     for (int ic = blockIdx.x * 8 + warp; ic < g.n_cl; ic += gridDim.x * 8) {
         if (__ldcg(D.flag + D.binfo[D.cl_first[ic]].x) == 0) continue;
-        cluster_one(D, g, ic, key, (unsigned *)(key + kClHash));
+        cluster_one(D, g, ic, key, key + kClHash);
     }
 }
 
