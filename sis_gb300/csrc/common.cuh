@@ -325,6 +325,14 @@ __device__ __forceinline__ unsigned int fixed_res(double x, double s, float &r) 
     return q;
 }
 
+// 1/d: the hardware approximation refined by one Newton-Raphson step
+// (r1 = r0 + r0 (1 - d r0)), within an ulp or so of the rounded quotient
+__device__ __forceinline__ float rcp_nr(float d) {
+    float r0;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(d));
+    return __fmaf_rn(r0, __fmaf_rn(-d, r0, 1.f), r0);
+}
+
 // The displacement trigger of instance k (job_md.F90:376-395): the two
 // largest squared displacements since the last rebuild (FP64 bit patterns,
 // merged with integer atomics) move the instance by more than the list margin.

@@ -1141,13 +1141,6 @@ __device__ __forceinline__ PairCoef pair_coef_of(const GlobP &g, const InstP &ip
     P.cut2 = g.flg_ele ? ip.ele_cut2_f : -1.f;
     return P;
 }
-// 1/d2: the hardware approximation refined by one Newton-Raphson step
-// (r1 = r0 + r0 (1 - d2 r0)), within an ulp or so of the rounded quotient
-__device__ __forceinline__ float rcp_nr(float d2) {
-    float r0;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(d2));
-    return __fmaf_rn(r0, __fmaf_rn(-d2, r0, 1.f), r0);
-}
 __device__ __forceinline__ float2 rcp_nr2(float2 d2) {
     float2 r0;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0.x) : "f"(d2.x));
@@ -1171,14 +1164,14 @@ __device__ __forceinline__ float2 wca_c2(float2 d2, const PairCoef &P) {
     const float2 s2 = __fmul2_rn(sq, sq), s4 = __fmul2_rn(s2, s2);
     return __fmul2_rn(make_float2(P.wcoef, P.wcoef), __ffma2_rn(__fmul2_rn(s4, s2), sq, make_float2(-s4.x, -s4.y)));
 }
-// Debye-Hueckel (force_ele_DH.F90): ecoef ri^2 (ri + rc) exp(-r rc), ri one
-// Newton step past rsqrt, the exponential as 2^(-r rc log2 e).  Each term is
+// Debye-Hueckel (force_ele_DH.F90): ecoef ri^2 (ri + rc) exp(-r rc), ri the
+// hardware reciprocal square root (relative error below 2^-22), the
+// exponential as 2^(-r rc log2 e).  Each term is
 // selected by its list bit and distance (pair2: the electrostatic term is
 // formed for every pair, the WCA term only when some lane of the warp has a
 // pair inside sigma, a warp-uniform branch).
 __device__ __forceinline__ float pair_c(bool wca, bool ele, float d2, const PairCoef &P) {
-    float ri = rsqrtf(d2);
-    ri = __fmul_rn(ri, __fmaf_rn(__fmul_rn(__fmul_rn(-0.5f, d2), ri), ri, 1.5f));
+    const float ri = rsqrtf(d2);
     const float rr = __fmul_rn(d2, ri);
     const float ce = __fmul_rn(__fmul_rn(__fmul_rn(P.ecoef, __fmul_rn(ri, ri)), __fadd_rn(ri, P.rc)), ex2a(-rr * P.rcl2));
     const float e = (ele && d2 <= P.cut2) ? ce : 0.f;
@@ -1199,9 +1192,7 @@ __device__ __forceinline__ Pair2 pair2(const uint4 &mi, const uint4 &ma, const u
     r.vy = __fmul2_rn(make_float2((float)(int)(mi.y - ma.y), (float)(int)(mi.y - mb.y)), f1);
     r.vz = __fmul2_rn(make_float2((float)(int)(mi.z - ma.z), (float)(int)(mi.z - mb.z)), f2);
     const float2 d2 = __ffma2_rn(r.vx, r.vx, __ffma2_rn(r.vy, r.vy, __fmul2_rn(r.vz, r.vz)));
-    float2 ri = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
-    const float2 h = __fmul2_rn(__fmul2_rn(make_float2(-0.5f, -0.5f), d2), ri);
-    ri = __fmul2_rn(ri, __ffma2_rn(h, ri, make_float2(1.5f, 1.5f)));
+    const float2 ri = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
     const float2 t = __fmul2_rn(__fmul2_rn(d2, ri), make_float2(-P.rcl2, -P.rcl2));
     const float2 ex = make_float2(ex2a(t.x), ex2a(t.y));
     const float2 ce = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(P.ecoef, P.ecoef), __fmul2_rn(ri, ri)),

@@ -571,18 +571,20 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
             s62 < kSin2 * d1212 * d6262;
     if (*near) return true;
     const float d1213 = dot3(v12, v13), d1242 = dot3(v12, v42), d1215 = dot3(v12, v15), d1262 = dot3(v12, v62);
-    const float o13 = d1213 / d1212, o42 = d1242 / d1212, o15 = d1215 / d1212, o62 = d1262 / d1212;
+    // quotients as products with reciprocals (rcp_nr, within an ulp or so)
+    const float i1212 = rcp_nr(d1212);
+    const float o13 = d1213 * i1212, o42 = d1242 * i1212, o15 = d1215 * i1212, o62 = d1262 * i1212;
     float u = b.bond_k * (d * d);
-    const V3<float> fb = (2.f * b.bond_k * d / a12) * v12;
+    const V3<float> fb = (2.f * b.bond_k * d * rcp_nr(a12)) * v12;
     V3<float> f0 = fb, f1 = -fb, fi, fk, fl;
     float r, pre;
     // 3-1=2 (imp-1 -- imp -- jmp)
     r = sqrtf(s13);
     d = atan2f(r, d1213) - b.angl_theta[1];
     u += b.angl_k[1] * (d * d);
-    pre = 2.f * b.angl_k[1] * d / r;
-    fi = (pre / d1313) * cross3(v13, c13);
-    fk = (pre / d1212) * cross3(c13, v12);
+    pre = 2.f * b.angl_k[1] * d * rcp_nr(r);
+    fi = (pre * rcp_nr(d1313)) * cross3(v13, c13);
+    fk = (pre * i1212) * cross3(c13, v12);
     f0 = f0 - fi - fk;
     f1 = f1 + fk;
     f[2] = fi;
@@ -590,9 +592,9 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     r = sqrtf(s42);
     d = atan2f(r, d1242) - b.angl_theta[0];
     u += b.angl_k[0] * (d * d);
-    pre = 2.f * b.angl_k[0] * d / r;
-    fi = (-pre / d1212) * cross3(v12, m42);
-    fk = (-pre / d4242) * cross3(m42, v42);
+    pre = 2.f * b.angl_k[0] * d * rcp_nr(r);
+    fi = (-pre * i1212) * cross3(v12, m42);
+    fk = (-pre * rcp_nr(d4242)) * cross3(m42, v42);
     f0 = f0 + fi;
     f1 = f1 - fi - fk;
     f[3] = fk;
@@ -600,9 +602,9 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     r = sqrtf(s15);
     d = atan2f(r, d1215) - b.angl_theta[3];
     u += b.angl_k[3] * (d * d);
-    pre = 2.f * b.angl_k[3] * d / r;
-    fi = (pre / d1515) * cross3(v15, c15);
-    fk = (pre / d1212) * cross3(c15, v12);
+    pre = 2.f * b.angl_k[3] * d * rcp_nr(r);
+    fi = (pre * rcp_nr(d1515)) * cross3(v15, c15);
+    fk = (pre * i1212) * cross3(c15, v12);
     f0 = f0 - fi - fk;
     f1 = f1 + fk;
     f[4] = fi;
@@ -610,9 +612,9 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     r = sqrtf(s62);
     d = atan2f(r, d1262) - b.angl_theta[2];
     u += b.angl_k[2] * (d * d);
-    pre = 2.f * b.angl_k[2] * d / r;
-    fi = (-pre / d1212) * cross3(v12, m62);
-    fk = (-pre / d6262) * cross3(m62, v62);
+    pre = 2.f * b.angl_k[2] * d * rcp_nr(r);
+    fi = (-pre * i1212) * cross3(v12, m62);
+    fk = (-pre * rcp_nr(d6262)) * cross3(m62, v62);
     f0 = f0 + fi;
     f1 = f1 - fi - fk;
     f[5] = fk;
@@ -622,8 +624,8 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     sincosf(d, &sn, &cs);
     u += b.dihd_k[0] * (1.f + cs);
     pre = -b.dihd_k[0] * sn * a12;
-    fi = (pre / s42) * m42;
-    fl = (-pre / s13) * c13;
+    fi = (pre * rcp_nr(s42)) * m42;
+    fl = (-pre * rcp_nr(s13)) * c13;
     f[3] = f[3] + fi;
     f1 = f1 + (o42 - 1.f) * fi - o13 * fl;
     f0 = f0 + (o13 - 1.f) * fl - o42 * fi;
@@ -633,8 +635,8 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     sincosf(d, &sn, &cs);
     u += b.dihd_k[1] * (1.f + cs);
     pre = -b.dihd_k[1] * sn * a12;
-    fi = (pre / s62) * m62;
-    fl = (-pre / s15) * c15;
+    fi = (pre * rcp_nr(s62)) * m62;
+    fl = (-pre * rcp_nr(s15)) * c15;
     f[5] = f[5] + fi;
     f1 = f1 + (o62 - 1.f) * fi - o15 * fl;
     f0 = f0 + (o15 - 1.f) * fl - o62 * fi;
