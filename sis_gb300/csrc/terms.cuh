@@ -28,6 +28,10 @@ __device__ __forceinline__ double exp(double x) { return ::exp(x); }
 __device__ __forceinline__ float fabs(float x) { return fabsf(x); }
 __device__ __forceinline__ double fabs(double x) { return ::fabs(x); }
 __device__ __forceinline__ float copysign(float a, float b) { return copysignf(a, b); }
+// a / b: FP32 as a product with the Newton-refined reciprocal (within an ulp
+// or so), FP64 as the rounded quotient
+__device__ __forceinline__ float div(float a, float b) { return a * rcp_nr(b); }
+__device__ __forceinline__ double div(double a, double b) { return a / b; }
 __device__ __forceinline__ double copysign(double a, double b) { return ::copysign(a, b); }
 } // namespace fm
 
@@ -151,9 +155,9 @@ __device__ __forceinline__ void angle_forces<float>(const V3<float> &x21, const 
     if (!g.angl_reb) {
         const float delta = atan2f(sqrtf(t), -d2132) - g.f_angl_t0;
         if (t <= 1.f) t = 1.f;
-        const float f = g.f_angl_k * delta / sqrtf(t);
-        const V3<float> f21 = f * ((d2132 / d21) * x21 - x32);
-        const V3<float> f32 = f * ((d2132 / d32) * x32 - x21);
+        const float f = g.f_angl_k * delta * rsqrtf(t);
+        const V3<float> f21 = f * ((d2132 * rcp_nr(d21)) * x21 - x32);
+        const V3<float> f32 = f * ((d2132 * rcp_nr(d32)) * x32 - x21);
         F[0] = -f21;
         F[1] = f21 - f32;
         F[2] = f32;
@@ -161,12 +165,12 @@ __device__ __forceinline__ void angle_forces<float>(const V3<float> &x21, const 
         // v12 = -x21; cos = v12.x32/|v12||x32|; 1 - cos^2 = t/(d12 d32)
         const V3<float> v12 = -x21;
         const float k = g.f_angl_k, co0 = g.f_cos_t0;
-        const float a1232 = sqrtf(d21 * d32);
-        const float cs = -d2132 / a1232;
-        const float omc = t / (d21 * d32);
-        const float f = -k * (cs - co0) * (1.f - cs * co0) / (omc * omc);
-        const V3<float> f1 = f * ((1.f / a1232) * x32 - (cs / d21) * v12);
-        const V3<float> f3 = f * ((1.f / a1232) * v12 - (cs / d32) * x32);
+        const float ia = rsqrtf(d21 * d32), i21 = rcp_nr(d21), i32 = rcp_nr(d32);
+        const float cs = -d2132 * ia;
+        const float omc = t * (i21 * i32);
+        const float f = -k * (cs - co0) * (1.f - cs * co0) * rcp_nr(omc * omc);
+        const V3<float> f1 = f * (ia * x32 - (cs * i21) * v12);
+        const V3<float> f3 = f * (ia * v12 - (cs * i32) * x32);
         F[0] = f1;
         F[1] = -(f1 + f3);
         F[2] = f3;
@@ -307,9 +311,9 @@ __device__ __forceinline__ void dih_forces(const V3<T> &vij, const V3<T> &vkj, c
         const T dd = dih - p0;
         pre = (k * w) * dd * fm::exp((T(-0.5) * w) * (dd * dd)) * akj;
     }
-    const V3<T> fi = (-pre / dot3(m, m)) * m;
-    const V3<T> fl = (pre / dot3(n, n)) * n;
-    const T a = dot3(vij, vkj) / akj2, b = dot3(vkl, vkj) / akj2;
+    const V3<T> fi = fm::div(-pre, dot3(m, m)) * m;
+    const V3<T> fl = fm::div(pre, dot3(n, n)) * n;
+    const T a = fm::div(dot3(vij, vkj), akj2), b = fm::div(dot3(vkl, vkj), akj2);
     F[0] = fi;
     F[1] = (T(-1) + a) * fi + (-b) * fl;
     F[2] = (-a) * fi + (T(-1) + b) * fl;
@@ -621,7 +625,7 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     // dihedral 4-2=1=3: m = v42 x v12, n = v12 x v13
     float sn, cs;
     d = atan2f(dot3(v42, c13) * a12, dot3(m42, c13)) + b.dihd_phi[0];
-    sincosf(d, &sn, &cs);
+    __sincosf(d, &sn, &cs); // the fast intrinsic: absolute error of order 1e-6 on this range
     u += b.dihd_k[0] * (1.f + cs);
     pre = -b.dihd_k[0] * sn * a12;
     fi = (pre * rcp_nr(s42)) * m42;
@@ -632,7 +636,7 @@ __device__ __forceinline__ bool bp_force_core_f(const V3<float> &v12, const V3<f
     f[2] = f[2] + fl;
     // dihedral 6-2=1=5: m = v62 x v12, n = v12 x v15
     d = atan2f(dot3(v62, c15) * a12, dot3(m62, c15)) + b.dihd_phi[1];
-    sincosf(d, &sn, &cs);
+    __sincosf(d, &sn, &cs); // the fast intrinsic: absolute error of order 1e-6 on this range
     u += b.dihd_k[1] * (1.f + cs);
     pre = -b.dihd_k[1] * sn * a12;
     fi = (pre * rcp_nr(s62)) * m62;
