@@ -1823,50 +1823,43 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         // pair sums go to s_F, and the update reads all three after one
         // barrier.
         // ------------------------------------------------ base pairs
-        // (even warps before their bonded terms and pair forces, odd warps
-        // after them, so that the warps' base-pair latency chains overlap
-        // other warps' pair work)
-        auto base_pairs = [&]() {
-            if (g.bp_model > 0) {
-                // every warp tests 32 records at a time and queues the ones in the
-                // distance window (bucket-local instance | slot); a full queue is
-                // evaluated by the whole warp, the rest at the end
-                int2 *wq = s_qi + warp * 64;
-                int wn = 0;
-                const int nrec = s_bp[ni];
-                for (int r0 = warp * 32; r0 < nrec; r0 += nt) {
-                    const int r = r0 + lane;
-                    bool pass = false;
-                    int q = 0, slot = 0;
-                    if (r < nrec) {
-                        q = small_inst(s_bp, ni, r);
-                        slot = s_bpo[q] + (r - s_bp[q]);
-                        const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
-                        pass = bp_test<float>(E, g, cur, slot);
-                    }
-                    const unsigned bal = __ballot_sync(0xffffffffu, pass);
-                    if (pass) wq[wn + __popc(bal & ((1u << lane) - 1u))] = make_int2(q, slot);
-                    wn += __popc(bal);
-                    __syncwarp();
-                    if (wn >= 32) {
-                        const int2 w = wq[lane];
-                        const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
-                        if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
-                        __syncwarp();
-                        if (lane < wn - 32) wq[lane] = wq[32 + lane];
-                        wn -= 32;
-                        __syncwarp();
-                    }
+        if (g.bp_model > 0) {
+            // every warp tests 32 records at a time and queues the ones in the
+            // distance window (bucket-local instance | slot); a full queue is
+            // evaluated by the whole warp, the rest at the end
+            int2 *wq = s_qi + warp * 64;
+            int wn = 0;
+            const int nrec = s_bp[ni];
+            for (int r0 = warp * 32; r0 < nrec; r0 += nt) {
+                const int r = r0 + lane;
+                bool pass = false;
+                int q = 0, slot = 0;
+                if (r < nrec) {
+                    q = small_inst(s_bp, ni, r);
+                    slot = s_bpo[q] + (r - s_bp[q]);
+                    const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+                    pass = bp_test<float>(E, g, cur, slot);
                 }
-                if (lane < wn) {
+                const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                if (pass) wq[wn + __popc(bal & ((1u << lane) - 1u))] = make_int2(q, slot);
+                wn += __popc(bal);
+                __syncwarp();
+                if (wn >= 32) {
                     const int2 w = wq[lane];
                     const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
                     if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
+                    __syncwarp();
+                    if (lane < wn - 32) wq[lane] = wq[32 + lane];
+                    wn -= 32;
+                    __syncwarp();
                 }
             }
-        };
-        const bool bp_first = (warp & 1) == 0;
-        if (bp_first) base_pairs();
+            if (lane < wn) {
+                const int2 w = wq[lane];
+                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
+                if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
+            }
+        }
         // ------------------------------------------------ bonded terms
         for (int s = tid; s < nb; s += nt) {
             const int q = small_inst(s_sb, ni, s);
@@ -1931,7 +1924,6 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 if (sub == 0 && s0 < nb) s_F[s] = make_float4(fx, fy, fz, 0.f);
             }
         }
-        if (!bp_first) base_pairs();
         __syncthreads();
         // ------------------------------------------------ update and trigger (job_md.F90:376-395)
         // the step's force: pair + bonded (its slot planes, in slot order) +
