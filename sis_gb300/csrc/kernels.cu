@@ -1680,14 +1680,22 @@ constexpr int kSmallLanes = 8;
 // the context as seen by one instance of a bucket: its beads' mirrors,
 // residuals and base-pair force sums at their shared-memory slots, addressed
 // by global bead index (sb: the instance's first slot, off: its first bead)
-// (both buffers name the shared copy: the block keeps one mirror)
-__device__ __forceinline__ Dev small_view(const Dev &D, uint4 *s_mir, float4 *s_res, double4 *s_fbp, int sb, int off) {
+// (both buffers name the shared copy: the block keeps one mirror); with
+// ipc, the instance record as the shared copy ipc, addressed by the
+// instance's global index id, and the base-pair parameters as bpf
+__device__ __forceinline__ Dev small_view(const Dev &D, uint4 *s_mir, float4 *s_res, double4 *s_fbp, int sb, int off,
+                                          const InstP *ipc, int id, const BPPf *bpf) {
     Dev E = D;
     E.mir[0] = E.mir[1] = s_mir + (sb - off);
     E.res[0] = E.res[1] = s_res + (sb - off);
     E.fbp = s_fbp + (sb - off);
+    if (ipc) E.ip = ipc - id;
+    E.bppf = bpf;
     return E;
 }
+// instance records a block keeps in shared memory (blocks of more instances
+// read them from global memory)
+constexpr int kSmallIpCache = 8;
 
 // bucket-local instance of slot s (s_sb: the instances' first slots, ascending)
 __device__ __forceinline__ int small_inst(const int *s_sb, int ni, int s) {
@@ -1715,6 +1723,8 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     __shared__ int s_fire[kSmallMaxInst];
     __shared__ int s_any;
     __shared__ int2 s_qi[16 * 64]; // per warp: queued base-pair records (2 warp widths)
+    __shared__ InstP s_ipc[kSmallIpCache];
+    __shared__ BPPf s_bpf[MAX_BP_TYPES];
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const int k0 = sp.cta_off[blockIdx.x], ni = sp.cta_off[blockIdx.x + 1] - k0;
     if (tid == 0) {
@@ -1738,6 +1748,18 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     if (tid < ni) s_m1[tid] = s_m2[tid] = 0u;
     __syncthreads();
     const int nb = s_sb[ni];
+    // the instance records (when they fit) and the base-pair parameters, as
+    // 32-bit words; the view of instance q is view(q)
+    const bool ipc_on = ni <= kSmallIpCache;
+    if (ipc_on) {
+        constexpr int w = (int)(sizeof(InstP) / 4);
+        for (int t = tid; t < ni * w; t += nt)
+            ((int *)s_ipc)[t] = ((const int *)(D.ip + s_iid[t / w]))[t % w];
+    }
+    for (int t = tid; t < MAX_BP_TYPES * (int)(sizeof(BPPf) / 4); t += nt) ((int *)s_bpf)[t] = ((const int *)D.bppf)[t];
+    auto view = [&](int q) {
+        return small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q], ipc_on ? s_ipc + q : nullptr, s_iid[q], s_bpf);
+    };
     for (int s = tid; s < nb; s += nt) {
         const int q = small_inst(s_sb, ni, s);
         const int gi = s_off[q] + (s - s_sb[q]);
@@ -1760,7 +1782,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             if (!s_fire[q]) continue;
             const int id = s_iid[q], off = s_off[q], na = s_n[q];
             const InstP &ip = D.ip[id];
-            const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], off);
+            const Dev E = view(q);
             const float maxcut2f = scan_cut2f(ip, 1.001f);
             for (int li = warp; li < na; li += nwarps) {
                 const int gi = off + li;
@@ -1837,7 +1859,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 if (r < nrec) {
                     q = small_inst(s_bp, ni, r);
                     slot = s_bpo[q] + (r - s_bp[q]);
-                    const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+                    const Dev E = view(q);
                     pass = bp_test<float>(E, g, cur, slot);
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, pass);
@@ -1846,7 +1868,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 __syncwarp();
                 if (wn >= 32) {
                     const int2 w = wq[lane];
-                    const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
+                    const Dev E = view(w.x);
                     if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
                     __syncwarp();
                     if (lane < wn - 32) wq[lane] = wq[32 + lane];
@@ -1856,7 +1878,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             }
             if (lane < wn) {
                 const int2 w = wq[lane];
-                const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[w.x], s_off[w.x]);
+                const Dev E = view(w.x);
                 if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
             }
         }
@@ -1864,7 +1886,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         for (int s = tid; s < nb; s += nt) {
             const int q = small_inst(s_sb, ni, s);
             const int gi = s_off[q] + (s - s_sb[q]);
-            const Dev E = small_view(D, s_mir, s_res, s_fbp, s_sb[q], s_off[q]);
+            const Dev E = view(q);
             bool an, dn;
             bonded_terms<float>(E, g, cur, gi, &an, &dn);
             if (an) bonded_fp64(D, g, cur, gi, 0);
@@ -1881,8 +1903,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const int q = small_inst(s_sb, ni, s);
                 const int off = s_off[q], sb = s_sb[q];
                 const int gi = off + (s - sb);
-                const int4 bi = D.binfo[gi];
-                const InstP &ip = D.ip[bi.x];
+                const InstP &ip = ipc_on ? s_ipc[q] : D.ip[s_iid[q]];
                 const uint4 mi = s_mir[s];
                 const PairCoef P = pair_coef_of(g, ip);
                 const int m = min(D.nnbr[gi], g.cap);
@@ -1936,7 +1957,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const uint4 m0 = D.mir0[gi];
             const int4 bi = D.binfo[gi];
             const double4 x = x_at(D, cur)[gi], v = D.v[gi], b = D.beta[gi];
-            const InstP &jp = D.ip[s_iid[q]];
+            const InstP &jp = ipc_on ? s_ipc[q] : D.ip[s_iid[q]];
             const V3<float> ab = bonded_gather<float>(D, g, bi, 0, 1, 7);
             float xi[3];
             mixed_noise(g, gi, jp, noise, st, step, xi);
