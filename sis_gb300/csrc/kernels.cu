@@ -206,7 +206,7 @@ __device__ __forceinline__ void bonded_terms(const Dev &D, const GlobP &g, int c
 __device__ __noinline__ void bonded_fp64_f(const Dev &D, const GlobP &g, int cur, int s, int kind, float4 *F4) {
     const int4 bi = D.binfo[s];
     const InstP &ip = D.ip[bi.x];
-    const double4 *__restrict__ x64 = x_at(D, cur);
+    const double4 *x64 = x_at(D, cur); // coherent: the per-block kernel writes x in the same launch
     const int l = bi_lidx(bi);
     const int q1 = chain_bead(bi, l + 1), q2 = chain_bead(bi, l + 2), q3 = chain_bead(bi, l + 3);
     if (kind == 0) {
@@ -326,8 +326,9 @@ __device__ __forceinline__ V3<float> bonded_bead(const Dev &E, const Dev &D, con
 
 // window and free-energy test of one record (force mode); returns true when
 // the 6-bead term has to be evaluated.  Records that fail are given zero
-// energy and status, as force_bp*.F90 zero ene_bp/bp_status before the loop.
-template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, const GlobP &g, int cur, int slot) {
+// energy and status, as force_bp*.F90 zero ene_bp/bp_status before the loop
+// (with rec_out; a caller that runs several steps writes them on the last).
+template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, const GlobP &g, int cur, int slot, bool rec_out = true) {
     const int4 rec = D.bps[slot];
     const int type = rec.z & 0xff;
     const InstP &ip = D.ip[rec.w];
@@ -381,7 +382,7 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
                 pass = false;
             }
         }
-        if (!pass) {
+        if (!pass && rec_out) {
             D.ene_bp[slot] = 0.0;
             D.bp_status[slot] = 0;
         }
@@ -402,7 +403,7 @@ template <typename R> __device__ __forceinline__ bool bp_test(const Dev &D, cons
         if constexpr (sizeof(R) == 4) pass = D.bp_dgf[rec.w * 469 + h] < 0.f;
         else pass = __dsub_rn(D.bp3_dH[h], __dmul_rn(ip.tempK, D.bp3_dS[h])) < 0.0;
     }
-    if (!pass) {
+    if (!pass && rec_out) {
         D.ene_bp[slot] = 0.0;
         D.bp_status[slot] = 0;
     }
@@ -479,7 +480,7 @@ __device__ __forceinline__ double bp_dG(const Dev &D, const GlobP &g, const int4
 // FP64 evaluation (FP64 path, and records flagged near +-1 by the FP32 path)
 // fbp: the scatter target (the context's fbp, or a block's shared copy)
 __device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, int slot, double4 *fbp) {
-    const double4 *__restrict__ x64 = x_at(D, cur);
+    const double4 *x64 = x_at(D, cur); // coherent: the per-block kernel writes x in the same launch
     const int4 rec = D.bps[slot];
     const int4 nb = D.bps_n[slot];
     const InstP &ip = D.ip[rec.w];
@@ -496,8 +497,8 @@ __device__ __noinline__ void bp_eval_d(const Dev &D, const GlobP &g, int cur, in
 // degrees is evaluated again with its four cross products from the exact
 // mirror differences and residuals (cross_fx); only if an angle is within
 // 1e-6 rad does it return true (writing nothing), so that the caller redoes
-// the record in FP64.
-__device__ __forceinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, int slot) {
+// the record in FP64.  rec_out: write the record's energy and status.
+__device__ __forceinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur, int slot, bool rec_out = true) {
     const uint4 *__restrict__ m = mir_at(D, cur);
     const int4 rec = D.bps[slot];
     const int4 nb = D.bps_n[slot];
@@ -554,8 +555,10 @@ __device__ __forceinline__ bool bp_eval_f(const Dev &D, const GlobP &g, int cur,
             }
         }
     }
-    D.ene_bp[slot] = (double)e;
-    D.bp_status[slot] = st;
+    if (rec_out) {
+        D.ene_bp[slot] = (double)e;
+        D.bp_status[slot] = st;
+    }
     return false;
 }
 
@@ -1075,9 +1078,8 @@ __device__ __forceinline__ V3<R> pair_sum_b(const Dev &D, const GlobP &g, int cu
 // contributions (bond l-1|l, l|l+1; angles starting at l-2, l-1, l;
 // dihedrals starting at l-3 .. l), lane `lane` of G taking every G-th
 template <typename R>
-__device__ __forceinline__ V3<R> bonded_gather(const Dev &D, const GlobP &g, const int4 &bi, int lane, int G, int mask) {
-    using V4 = typename Vec4<R>::type;
-    const V4 *__restrict__ S = (const V4 *)D.slot;
+__device__ __forceinline__ V3<R> bonded_gather_at(const typename Vec4<R>::type *S, size_t pl, int shift, const int4 &bi, int lane,
+                                                 int G, int mask) {
     const int l = bi_lidx(bi);
     V3<R> ab = mk<R>(0, 0, 0);
     for (int t = lane; t < 9; t += G) {
@@ -1098,9 +1100,14 @@ __device__ __forceinline__ V3<R> bonded_gather(const Dev &D, const GlobP &g, con
             k = 4 + (3 - (t - 5));
         }
         const int q = chain_bead(bi, start);
-        if ((mask & cls) && q >= 0) ab = ab + sgn * v3(S[(size_t)k * g.n + q]);
+        if ((mask & cls) && q >= 0) ab = ab + sgn * v3(S[(size_t)k * pl + (q + shift)]);
     }
     return ab;
+}
+// the same from the context's slot planes (plane pitch n, bead index q)
+template <typename R>
+__device__ __forceinline__ V3<R> bonded_gather(const Dev &D, const GlobP &g, const int4 &bi, int lane, int G, int mask) {
+    return bonded_gather_at<R>((const typename Vec4<R>::type *)D.slot, (size_t)g.n, 0, bi, lane, G, mask);
 }
 
 // Pair forces of every bead into fpair (float4 / double4), the step kernel's
@@ -1716,7 +1723,11 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     double4 *s_fbp = (double4 *)(s_res + cap);
     float4 *s_F = (float4 *)(s_fbp + cap);   // pair force of the step (xyz)
     double2 *s_cd = (double2 *)(s_F + cap);  // integrator coefficients a, sqrt(b) h (mdc.x, mdc.z)
-    float2 *s_cf = (float2 *)(s_cd + cap);   // FP32 force and noise coefficients of the update
+    // with sp.sslot, the bonded terms' slot planes (8 planes of cap, by the
+    // slot of the term's first bead); else the context's slot planes
+    const bool sslot = sp.sslot != 0;
+    float4 *s_slot = (float4 *)(s_cd + cap);
+    float2 *s_cf = (float2 *)(s_slot + (sslot ? 8 * cap : 0)); // FP32 force and noise coefficients of the update
     __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst], s_bpo[kSmallMaxInst];
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
@@ -1839,6 +1850,9 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     if (s_any) rebuild(cur, true);
     const unsigned long long step0 = *D.step_ctr;
     for (int st = 0; st < nsteps; ++st) {
+        // the base-pair records' energies and statuses are read only after
+        // the launch: written on its last step
+        const bool rec_out = st == nsteps - 1;
         // Forces.  Base pairs, bonded terms and pair forces need no barrier
         // between them: the base-pair forces add into s_fbp (exact
         // fixed-point atomics), the bonded terms write their slot planes, the
@@ -1860,7 +1874,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                     q = small_inst(s_bp, ni, r);
                     slot = s_bpo[q] + (r - s_bp[q]);
                     const Dev E = view(q);
-                    pass = bp_test<float>(E, g, cur, slot);
+                    pass = bp_test<float>(E, g, cur, slot, rec_out);
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, pass);
                 if (pass) wq[wn + __popc(bal & ((1u << lane) - 1u))] = make_int2(q, slot);
@@ -1869,7 +1883,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 if (wn >= 32) {
                     const int2 w = wq[lane];
                     const Dev E = view(w.x);
-                    if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
+                    if (bp_eval_f(E, g, cur, w.y, rec_out)) bp_eval_d(D, g, cur, w.y, E.fbp);
                     __syncwarp();
                     if (lane < wn - 32) wq[lane] = wq[32 + lane];
                     wn -= 32;
@@ -1879,7 +1893,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             if (lane < wn) {
                 const int2 w = wq[lane];
                 const Dev E = view(w.x);
-                if (bp_eval_f(E, g, cur, w.y)) bp_eval_d(D, g, cur, w.y, E.fbp);
+                if (bp_eval_f(E, g, cur, w.y, rec_out)) bp_eval_d(D, g, cur, w.y, E.fbp);
             }
         }
         // ------------------------------------------------ bonded terms
@@ -1888,9 +1902,11 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const int gi = s_off[q] + (s - s_sb[q]);
             const Dev E = view(q);
             bool an, dn;
-            bonded_terms<float>(E, g, cur, gi, &an, &dn);
-            if (an) bonded_fp64(D, g, cur, gi, 0);
-            if (dn) bonded_fp64(D, g, cur, gi, 1);
+            float4 *S = sslot ? s_slot + s : (float4 *)D.slot + gi;
+            const size_t pl = sslot ? (size_t)cap : (size_t)g.n;
+            bonded_terms_to<float>(E, g, cur, gi, S, pl, &an, &dn);
+            if (an) bonded_fp64_to(D, g, cur, gi, 0, S, pl);
+            if (dn) bonded_fp64_to(D, g, cur, gi, 1, S, pl);
         }
         // ------------------------------------------------ pair forces
         {
@@ -1907,7 +1923,8 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const uint4 mi = s_mir[s];
                 const PairCoef P = pair_coef_of(g, ip);
                 const int m = min(D.nnbr[gi], g.cap);
-                const int *__restrict__ nbl = D.nbr + (size_t)gi * g.cap;
+                // coherent loads: the launch's own rebuilds rewrite the lists
+                const int *nbl = D.nbr + (size_t)gi * g.cap;
                 const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
                              f2 = make_float2(ip.finv[2], ip.finv[2]);
                 // lane sub takes entries sub, sub + L, sub + 2L, ... (L =
@@ -1923,7 +1940,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                     // the batch's 16 list words in flight at once
                     int e[16];
 #pragma unroll
-                    for (int u = 0; u < 16; ++u) e[u] = k0 + u * L < m ? __ldg(nbl + k0 + u * L) : gi;
+                    for (int u = 0; u < 16; ++u) e[u] = k0 + u * L < m ? nbl[k0 + u * L] : gi;
 #pragma unroll
                     for (int u = 0; u < 16; u += 2) {
                         if (k0 - sub + u * L >= mmax) break; // warp-uniform: past every lane's list
@@ -1958,7 +1975,8 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const int4 bi = D.binfo[gi];
             const double4 x = x_at(D, cur)[gi], v = D.v[gi], b = D.beta[gi];
             const InstP &jp = ipc_on ? s_ipc[q] : D.ip[s_iid[q]];
-            const V3<float> ab = bonded_gather<float>(D, g, bi, 0, 1, 7);
+            const V3<float> ab = sslot ? bonded_gather_at<float>(s_slot, (size_t)cap, s_sb[q] - s_off[q], bi, 0, 1, 7)
+                                       : bonded_gather<float>(D, g, bi, 0, 1, 7);
             float xi[3];
             mixed_noise(g, gi, jp, noise, st, step, xi);
             const float4 F4 = s_F[s];
@@ -2419,16 +2437,20 @@ cudaError_t launch_bias_energy(const Dev &D, const GlobP &g, int cur, cudaStream
     return cudaGetLastError();
 }
 
-size_t small_smem_bytes(int cap) {
-    return (size_t)cap * (sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4) + sizeof(double2) + sizeof(float2));
-}
+// per bead: mirror, residual, base-pair sum, pair force, coefficients (FP64
+// and FP32); then the 8 bonded slot planes when they fit in kSmallDynMax
+constexpr size_t kSmallBeadBytes = sizeof(uint4) + sizeof(float4) + sizeof(double4) + sizeof(float4) + sizeof(double2) + sizeof(float2);
+bool small_slot_planes(int cap) { return (size_t)cap * (kSmallBeadBytes + 8 * sizeof(float4)) <= (size_t)kSmallDynMax; }
+size_t small_smem_bytes(int cap) { return (size_t)cap * (kSmallBeadBytes + (small_slot_planes(cap) ? 8 * sizeof(float4) : 0)); }
 
 cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
                             cudaStream_t st) {
     const size_t smem = small_smem_bytes(sp.cap);
     cudaError_t e = cudaFuncSetAttribute(k_md_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_md_small<<<sp.n_cta, threads, smem, st>>>(D, g, cur, sp, nsteps, noise);
+    SmallPlan p = sp;
+    p.sslot = small_slot_planes(sp.cap) ? 1 : 0;
+    k_md_small<<<p.n_cta, threads, smem, st>>>(D, g, cur, p, nsteps, noise);
     return cudaGetLastError();
 }
 

@@ -6,13 +6,18 @@
 namespace sisg {
 
 // buckets of small instances for k_md_small: bucket b holds the instances
-// inst[cta_off[b] .. cta_off[b+1]); cap: beads of the largest bucket
+// inst[cta_off[b] .. cta_off[b+1]); cap: beads of the largest bucket;
+// sslot: the bonded slot planes in shared memory (set by launch_md_small)
 constexpr int kSmallMaxInst = 128;
 constexpr int kSmallMaxBeads = 2048;
+// dynamic shared memory of a k_md_small block with the slot planes at most
+// (its static shared memory, about 16 KB, comes on top, within the 227 KB
+// of a block)
+constexpr int kSmallDynMax = 204 * 1024;
 struct SmallPlan {
     const int *cta_off;
     const int *inst;
-    int n_cta, cap;
+    int n_cta, cap, sslot;
 };
 
 struct RebuildPlan {
@@ -69,6 +74,7 @@ cudaError_t launch_energy(const Dev &D, const GlobP &g, int cur, cudaStream_t st
 // and launch_small_finish
 cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
                             cudaStream_t st);
+// dynamic shared memory of a k_md_small block for buckets of cap beads
 size_t small_smem_bytes(int cap);
 cudaError_t launch_cluster_flagged(const Dev &D, const GlobP &g, cudaStream_t st);
 cudaError_t launch_small_finish(const Dev &D, const GlobP &g, unsigned long long nsteps, cudaStream_t st);
