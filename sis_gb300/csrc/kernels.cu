@@ -1733,6 +1733,10 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
     __shared__ int s_fire[kSmallMaxInst];
     __shared__ int s_any;
+    // the next base-pair record chunk and the next pair-force group of the
+    // step: warps take them as they become free (a bead's and a record's
+    // arithmetic does not depend on the warp that runs it)
+    __shared__ int s_rnext, s_pnext;
     __shared__ int2 s_qi[16 * 64]; // per warp: queued base-pair records (2 warp widths)
     __shared__ InstP s_ipc[kSmallIpCache];
     __shared__ BPPf s_bpf[MAX_BP_TYPES];
@@ -1755,6 +1759,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         s_sb[ni] = sb;
         s_bp[ni] = nbp;
         s_any = 0;
+        s_rnext = s_pnext = 0;
     }
     if (tid < ni) s_m1[tid] = s_m2[tid] = 0u;
     __syncthreads();
@@ -1866,7 +1871,11 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             int2 *wq = s_qi + warp * 64;
             int wn = 0;
             const int nrec = s_bp[ni];
-            for (int r0 = warp * 32; r0 < nrec; r0 += nt) {
+            for (;;) {
+                int r0 = 0;
+                if (lane == 0) r0 = atomicAdd(&s_rnext, 32);
+                r0 = __shfl_sync(0xffffffffu, r0, 0);
+                if (r0 >= nrec) break;
                 const int r = r0 + lane;
                 bool pass = false;
                 int q = 0, slot = 0;
@@ -1912,7 +1921,11 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         {
             constexpr int BPW = 32 / kSmallLanes; // beads per warp and pass
             const int sub = lane & (kSmallLanes - 1);
-            for (int base = warp * BPW; base < nb; base += nwarps * BPW) {
+            for (;;) {
+                int base = 0;
+                if (lane == 0) base = atomicAdd(&s_pnext, BPW);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base >= nb) break;
                 // every lane of a warp runs the same passes (shuffles below)
                 const int s0 = base + lane / kSmallLanes;
                 const int s = min(s0, nb - 1);
@@ -2008,6 +2021,7 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             atomicMax(&s_m2[q], old < bits ? old : bits);
         }
         __syncthreads();
+        if (tid == 0) s_rnext = s_pnext = 0;
         if (tid < ni) {
             const bool f = sqrtf(__uint_as_float(s_m1[tid])) + sqrtf(__uint_as_float(s_m2[tid])) > (float)g.nl_margin;
             s_fire[tid] = f;
