@@ -709,6 +709,8 @@ int small_plan(sis_ctx *ctx, int target) {
     ctx->sp.inst = ctx->sp_inst_d;
     ctx->sp.n_cta = (int)off.size() - 1;
     ctx->sp.cap = cap;
+    ctx->sp.inner = 0;
+    for (int k = 0; k < ni; ++k) ctx->sp.inner |= ctx->ip[k].n >= kInnerMinBeads ? 1 : 0;
     return SIS_OK;
 }
 
@@ -1027,6 +1029,13 @@ extern "C" int sis_gpu_create(const sis_topology *top, const sis_params *par, si
         if (ctx->small_ok) {
             rc |= dalloc(ctx, &ctx->sp_off_d, (size_t)ni + 1);
             rc |= dalloc(ctx, &ctx->sp_inst_d, ni);
+            // the per-block kernel's inner lists; igen -1: never filtered
+            rc |= dalloc(ctx, &D.nbr_in, (size_t)n * cap);
+            rc |= dalloc(ctx, &D.nnbr_in, n);
+            rc |= dalloc(ctx, &D.mir_in, n);
+            rc |= dalloc(ctx, &D.lgen, ni);
+            rc |= dalloc(ctx, &D.igen, ni);
+            if (!rc && cudaMemset(D.igen, 0xFF, sizeof(int) * ni) != cudaSuccess) rc = SIS_ERR_CUDA;
         }
         rc |= dalloc(ctx, &D.mir0, n);
         rc |= dalloc(ctx, &D.cl_first, n_cl);

@@ -196,6 +196,14 @@ struct Dev {
     int *cl_first, *ncl, *cl_j;
     ulonglong2 *cl_m;
     uint4 *mir0;            // [n] mirror at the last rebuild (mixed path)
+    // inner pair lists of the per-block kernel (contexts of small instances):
+    // each bead's list entries within their cutoff + kInnerMargin at the last
+    // refresh, in list order, and the mirror at that refresh; per instance
+    // the list rebuilds so far (lgen, counted by every rebuild path) and the
+    // rebuild count the inner lists were filtered from (igen)
+    int *nbr_in, *nnbr_in;
+    uint4 *mir_in;
+    int *lgen, *igen;
     // base-pair lists
     int4 *bps, *bps_n;      // per-instance staging segments (records, neighbour beads)
     int *bp_cnt;            // [2*n_inst] staging counts, then their exclusive prefix

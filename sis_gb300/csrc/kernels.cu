@@ -1683,6 +1683,19 @@ __global__ void __launch_bounds__(256, 5) k_step(Dev D, GlobP g, int cur, const 
 // Lane l of a bead takes the entries l, l + 8, l + 16, ... of its list; the
 // lane sums are reduced over the 8 lanes in a fixed order.
 constexpr int kSmallLanes = 8;
+// The pair forces of the per-block kernel walk inner lists: the entries of
+// the bead's list (whose radius is the cutoff + the list margin) within
+// their own cutoff (electrostatic, WCA) + kInnerMargin A.  An instance's
+// inner lists are filtered again from its lists when the two largest bead
+// displacements since their last filtering sum to more than kInnerMargin
+// (no pair can then have come within a cutoff without being listed), when
+// its lists were rebuilt, and at the start of a launch whose state moved
+// since.  Entries beyond every cutoff add exact zeros, so the inner lists
+// leave the forces' terms unchanged.  Instances of fewer than
+// kInnerMinBeads moving beads, whose lists hold few such entries, walk
+// their lists directly; a context with no instance of that capacity runs
+// the kernel without the inner lists (INNER false).
+constexpr float kInnerMargin = 2.5f;
 
 // the context as seen by one instance of a bucket: its beads' mirrors,
 // residuals and base-pair force sums at their shared-memory slots, addressed
@@ -1715,6 +1728,7 @@ __device__ __forceinline__ int small_inst(const int *s_sb, int ni, int s) {
     return lo;
 }
 
+template <bool INNER>
 __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, SmallPlan sp, int nsteps, const double *noise) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     const int cap = sp.cap;
@@ -1731,8 +1745,9 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     __shared__ int s_iid[kSmallMaxInst], s_off[kSmallMaxInst], s_n[kSmallMaxInst], s_bpo[kSmallMaxInst];
     __shared__ int s_sb[kSmallMaxInst + 1], s_bp[kSmallMaxInst + 1];
     __shared__ unsigned int s_m1[kSmallMaxInst], s_m2[kSmallMaxInst];
-    __shared__ int s_fire[kSmallMaxInst];
-    __shared__ int s_any;
+    __shared__ unsigned int s_m3[kSmallMaxInst], s_m4[kSmallMaxInst]; // the same since the inner lists' filtering
+    __shared__ int s_fire[kSmallMaxInst], s_ifire[kSmallMaxInst];
+    __shared__ int s_any, s_anyi;
     // the next base-pair record chunk and the next pair-force group of the
     // step: warps take them as they become free (a bead's and a record's
     // arithmetic does not depend on the warp that runs it)
@@ -1758,10 +1773,10 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         }
         s_sb[ni] = sb;
         s_bp[ni] = nbp;
-        s_any = 0;
+        s_any = s_anyi = 0;
         s_rnext = s_pnext = 0;
     }
-    if (tid < ni) s_m1[tid] = s_m2[tid] = 0u;
+    if (tid < ni) s_m1[tid] = s_m2[tid] = s_m3[tid] = s_m4[tid] = 0u;
     __syncthreads();
     const int nb = s_sb[ni];
     // the instance records (when they fit) and the base-pair parameters, as
@@ -1786,6 +1801,15 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         const double4 mc = D.mdc[gi];
         s_cd[s] = make_double2(mc.x, mc.z);
         s_cf[s] = make_float2((float)(g.integrator == 1 ? mc.y : mc.x), (float)mc.w);
+        // displacement since the inner lists' filtering (state moved between launches)
+        if (!INNER || s_n[q] < kInnerMinBeads) continue;
+        const uint4 mI = D.mir_in[gi], m = s_mir[s];
+        const float *fi = D.ip[s_iid[q]].finv; // (s_ipc is being filled)
+        const float dx = (float)(int)(m.x - mI.x) * fi[0], dy = (float)(int)(m.y - mI.y) * fi[1],
+                    dz = (float)(int)(m.z - mI.z) * fi[2];
+        const unsigned int bits = __float_as_uint(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+        const unsigned int old = atomicMax(&s_m3[q], bits);
+        atomicMax(&s_m4[q], old < bits ? old : bits);
     }
     __syncthreads();
     // the rebuild of the instances with s_fire set (neighbor_list.F90), from
@@ -1841,6 +1865,61 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
         __syncthreads();
         if (tid == 0) s_any = 0;
     };
+    // the inner lists of the instances with s_ifire set, from their lists and
+    // the current mirrors (one warp per bead, kept entries in list order);
+    // ends with s_anyi cleared
+    auto refresh = [&]() {
+        for (int q = 0; q < ni; ++q) {
+            if (!s_ifire[q]) continue;
+            const int id = s_iid[q], off = s_off[q], sb = s_sb[q], na = s_n[q];
+            const InstP &ip = ipc_on ? s_ipc[q] : D.ip[id];
+            const float re = g.flg_ele ? sqrtf(ip.ele_cut2_f) : 0.f, rw = sqrtf(g.f_wca_sig2);
+            for (int li = warp; li < na; li += nwarps) {
+                const int gi = off + li;
+                const uint4 mi = s_mir[sb + li];
+                const int m = min(D.nnbr[gi], g.cap);
+                const int *src = D.nbr + (size_t)gi * g.cap;
+                int *dst = D.nbr_in + (size_t)gi * g.cap;
+                int cnt = 0;
+                for (int k0 = 0; k0 < m; k0 += 32) {
+                    const int k = k0 + lane;
+                    int e = 0;
+                    bool keep = false;
+                    if (k < m) {
+                        e = src[k];
+                        const uint4 mj = s_mir[sb + (e & IDX_MASK) - off];
+                        const float dx = (float)(int)(mi.x - mj.x) * ip.finv[0], dy = (float)(int)(mi.y - mj.y) * ip.finv[1],
+                                    dz = (float)(int)(mi.z - mj.z) * ip.finv[2];
+                        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        const float r = fmaxf((e & ELE_BIT) ? re : 0.f, (e & WCA_BIT) ? rw : 0.f) + kInnerMargin;
+                        keep = d2 <= r * r * 1.0001f;
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                    if (keep) dst[cnt + __popc(bal & ((1u << lane) - 1u))] = e;
+                    cnt += __popc(bal);
+                }
+                if (lane == 0) {
+                    D.nnbr_in[gi] = cnt;
+                    D.mir_in[gi] = mi;
+                }
+            }
+            if (tid == 0) D.igen[id] = __ldcg(D.lgen + id);
+        }
+        __syncthreads();
+        if (tid == 0) s_anyi = 0;
+    };
+    // the inner lists due at a step's end or at the launch's start (first):
+    // the instances whose lists were rebuilt since their filtering (in the
+    // launch: rebuilt; before it: their counts differ), or whose two largest
+    // displacements since it (s_m3, s_m4) sum to more than the margin
+    auto inner_due = [&](int k, bool rebuilt, bool first) {
+        const bool f = INNER && s_n[k] >= kInnerMinBeads &&
+                       (rebuilt || (first && __ldcg(D.igen + s_iid[k]) != __ldcg(D.lgen + s_iid[k])) ||
+                        sqrtf(__uint_as_float(s_m3[k])) + sqrtf(__uint_as_float(s_m4[k])) > kInnerMargin);
+        s_ifire[k] = f;
+        s_m3[k] = s_m4[k] = 0u;
+        if (f) s_anyi = 1;
+    };
     // instances flagged before the launch (slots loaded since the last
     // launch): their lists first
     if (tid < ni) {
@@ -1853,6 +1932,11 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
     }
     __syncthreads();
     if (s_any) rebuild(cur, true);
+    if (INNER) {
+        if (tid < ni) inner_due(tid, false, true);
+        __syncthreads();
+        if (s_anyi) refresh();
+    }
     const unsigned long long step0 = *D.step_ctr;
     for (int st = 0; st < nsteps; ++st) {
         // the base-pair records' energies and statuses are read only after
@@ -1935,9 +2019,10 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 const InstP &ip = ipc_on ? s_ipc[q] : D.ip[s_iid[q]];
                 const uint4 mi = s_mir[s];
                 const PairCoef P = pair_coef_of(g, ip);
-                const int m = min(D.nnbr[gi], g.cap);
-                // coherent loads: the launch's own rebuilds rewrite the lists
-                const int *nbl = D.nbr + (size_t)gi * g.cap;
+                const bool inner = INNER && s_n[q] >= kInnerMinBeads;
+                const int m = min(inner ? D.nnbr_in[gi] : D.nnbr[gi], g.cap);
+                // coherent loads: the launch rewrites the lists
+                const int *nbl = (inner ? D.nbr_in : D.nbr) + (size_t)gi * g.cap;
                 const float2 f0 = make_float2(ip.finv[0], ip.finv[0]), f1 = make_float2(ip.finv[1], ip.finv[1]),
                              f2 = make_float2(ip.finv[2], ip.finv[2]);
                 // lane sub takes entries sub, sub + L, sub + 2L, ... (L =
@@ -1984,7 +2069,8 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const int q = small_inst(s_sb, ni, s);
             const int gi = s_off[q] + (s - s_sb[q]);
             // every global load of the bead's update first
-            const uint4 m0 = D.mir0[gi];
+            const bool inner = INNER && s_n[q] >= kInnerMinBeads;
+            const uint4 m0 = D.mir0[gi], mI = inner ? D.mir_in[gi] : m0;
             const int4 bi = D.binfo[gi];
             const double4 x = x_at(D, cur)[gi], v = D.v[gi], b = D.beta[gi];
             const InstP &jp = ipc_on ? s_ipc[q] : D.ip[s_iid[q]];
@@ -2019,6 +2105,13 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
             const unsigned int bits = __float_as_uint(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
             const unsigned int old = atomicMax(&s_m1[q], bits);
             atomicMax(&s_m2[q], old < bits ? old : bits);
+            if (inner) {
+                const float ix = (float)(int)(m1.x - mI.x) * fi[0], iy = (float)(int)(m1.y - mI.y) * fi[1],
+                            iz = (float)(int)(m1.z - mI.z) * fi[2];
+                const unsigned int ibits = __float_as_uint(fmaf(ix, ix, fmaf(iy, iy, iz * iz)));
+                const unsigned int iold = atomicMax(&s_m3[q], ibits);
+                atomicMax(&s_m4[q], iold < ibits ? iold : ibits);
+            }
         }
         __syncthreads();
         if (tid == 0) s_rnext = s_pnext = 0;
@@ -2030,10 +2123,12 @@ __global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, Small
                 s_any = 1;
                 D.bp_cnt[s_iid[tid]] = 0;
             }
+            if (INNER) inner_due(tid, f, false);
         }
         __syncthreads();
         cur ^= 1;
         if (s_any) rebuild(cur, false);
+        if (INNER && s_anyi) refresh();
     }
 }
 
@@ -2460,11 +2555,17 @@ size_t small_smem_bytes(int cap) { return (size_t)cap * (kSmallBeadBytes + (smal
 cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPlan &sp, int nsteps, const double *noise, int threads,
                             cudaStream_t st) {
     const size_t smem = small_smem_bytes(sp.cap);
-    cudaError_t e = cudaFuncSetAttribute(k_md_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     SmallPlan p = sp;
     p.sslot = small_slot_planes(sp.cap) ? 1 : 0;
-    k_md_small<<<p.n_cta, threads, smem, st>>>(D, g, cur, p, nsteps, noise);
+    if (sp.inner) {
+        cudaError_t e = cudaFuncSetAttribute(k_md_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_md_small<true><<<p.n_cta, threads, smem, st>>>(D, g, cur, p, nsteps, noise);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(k_md_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_md_small<false><<<p.n_cta, threads, smem, st>>>(D, g, cur, p, nsteps, noise);
+    }
     return cudaGetLastError();
 }
 

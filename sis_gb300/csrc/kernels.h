@@ -7,9 +7,12 @@ namespace sisg {
 
 // buckets of small instances for k_md_small: bucket b holds the instances
 // inst[cta_off[b] .. cta_off[b+1]); cap: beads of the largest bucket;
-// sslot: the bonded slot planes in shared memory (set by launch_md_small)
+// sslot: the bonded slot planes in shared memory (set by launch_md_small);
+// inner: some instance has kInnerMinBeads beads or more (pair forces over
+// inner lists, kernels.cu)
 constexpr int kSmallMaxInst = 128;
 constexpr int kSmallMaxBeads = 2048;
+constexpr int kInnerMinBeads = 256;
 // dynamic shared memory of a k_md_small block with the slot planes at most
 // (its static shared memory, about 16 KB, comes on top, within the 227 KB
 // of a block)
@@ -17,7 +20,7 @@ constexpr int kSmallDynMax = 204 * 1024;
 struct SmallPlan {
     const int *cta_off;
     const int *inst;
-    int n_cta, cap, sslot;
+    int n_cta, cap, sslot, inner;
 };
 
 struct RebuildPlan {

@@ -232,6 +232,8 @@ __device__ __forceinline__ void warp_append(const Dev &D, const GlobP &g, int gi
 __device__ __forceinline__ void bead_begin(const Dev &D, int cur, int gi, const InstP &ip, int lane, double4 &xi_w) {
     xi_w = wrap_pos(x_at(D, cur)[gi], ip);
     if (lane == 0) {
+        // one count per rebuild of the instance (its first bead)
+        if (D.lgen && gi == ip.bead_off) atomicAdd(D.lgen + D.binfo[gi].x, 1);
         if (ip.pbc) x_at(D, cur)[gi] = xi_w;
         D.move[gi] = make_double4(0.0, 0.0, 0.0, 0.0);
         // the mirror is the same before and after the wrap (the box is 2^32 units)

@@ -20,14 +20,30 @@ import pytest
 
 from oracle.oracle import Oracle
 from sis_gb300 import MIXED
-from sis_gb300.coil import single_chain, uneven_batch
+from sis_gb300.coil import random_coil, random_sequence, single_chain, sis_options, uneven_batch
 from sis_gb300.engine import Engine
+from sis_gb300.model import Chain, Instance, System
 
 pytestmark = pytest.mark.gpu
 
 
-def _batch(ff, n_inst=12, seed=5):
-    return uneven_batch(ff, n_inst=n_inst, lmin=20, lmax=200, seed=seed)
+def _batch(ff, n_inst=12, seed=5, lmin=20, lmax=200, clean=False):
+    if not clean:
+        return uneven_batch(ff, n_inst=n_inst, lmin=lmin, lmax=lmax, seed=seed)
+    # coils without WCA overlaps (no pair closer than 10 A), so that short
+    # trajectories of two paths whose FP32 sums differ stay comparable
+    rng = np.random.default_rng(seed)
+    insts = []
+    for _ in range(n_inst):
+        n = int(rng.integers(lmin, lmax + 1))
+        insts.append(Instance([Chain(random_sequence(rng, n))], tempK=float(rng.uniform(280.0, 340.0)),
+                              ionic_strength=float(rng.uniform(0.02, 0.5)), xyz=random_coil(rng, n, rmin=10.0)))
+    return System(ff, sis_options(), insts)
+
+
+# chain lengths of the batches: short chains walk their lists; chains of 256
+# moving beads and more walk inner lists (kernels.cu kInnerMinBeads)
+LENGTHS = [pytest.param((20, 200), id="short"), pytest.param((256, 400), id="inner")]
 
 
 def as_set(a):
@@ -86,10 +102,12 @@ def test_fed_noise_mixed_trajectory_matches_oracle(small, sis_ff):
     assert np.abs(v - orc.get_velos(0)).max() <= 1e-4 * np.abs(orc.get_velos(0)).max()
 
 
-def test_small_follows_the_general_kernels(sis_ff):
+@pytest.mark.parametrize("lengths", LENGTHS)
+def test_small_follows_the_general_kernels(lengths, sis_ff):
     """Same state, same Philox noise: the two paths differ in the order of
     FP32 sums only, so over 20 steps they stay within FP32 rounding."""
-    sysm = _batch(sis_ff)
+    long = lengths[1] > 200
+    sysm = _batch(sis_ff, n_inst=6 if long else 12, lmin=lengths[0], lmax=lengths[1], clean=long)
     a = Engine(sysm, precision=MIXED, seed=8)
     b = Engine(sysm, precision=MIXED, seed=8)
     b.set_small(0)
@@ -101,11 +119,13 @@ def test_small_follows_the_general_kernels(sis_ff):
     assert a.stats()["small_blocks"] > 0 and b.stats()["small_blocks"] == 0
 
 
-def test_small_trajectory_independent_of_calls_and_buckets(sis_ff):
+@pytest.mark.parametrize("lengths", LENGTHS)
+def test_small_trajectory_independent_of_calls_and_buckets(lengths, sis_ff):
     """One 400-step call (whose first steps time several bucket plans and
     block widths), 40 calls of 10 steps (the default plan) and 400 calls of
-    one step give the same state bit for bit, with the same rebuilds."""
-    sysm = _batch(sis_ff, n_inst=40, seed=7)
+    one step give the same state bit for bit, with the same rebuilds (and,
+    for long chains, the same inner-list filterings)."""
+    sysm = _batch(sis_ff, n_inst=40 if lengths[1] <= 200 else 12, seed=7, lmin=lengths[0], lmax=lengths[1])
     runs = []
     for calls, per in ((1, 400), (40, 10), (400, 1)):
         e = Engine(sysm, precision=MIXED, seed=11)
