@@ -339,7 +339,9 @@ def uneven_record(args, rank, world):
     """The uneven batch (256 chains of U[20,500] nt, each with its own salt and
     temperature, no PBC), the workload the >= 20x target is stated on: mixed
     path against the plain FP64 path from the same state, L2 flushed between
-    timed blocks, max over ranks."""
+    timed blocks, max over ranks.  The same protocol as the --workload uneven
+    line: 3000 capped + 3000 free relaxation steps from the random coils,
+    --warmup untimed and --steps timed blocks of --md-steps MD steps."""
     from sis_gb300 import FP64, MIXED
     from sis_gb300.engine import Engine
 
@@ -347,14 +349,14 @@ def uneven_record(args, rank, world):
     N, S = sysm.nmp, args.md_steps
     eng = Engine(sysm, precision=MIXED, seed=2024 + rank)
     eng.init_velocities()
-    eng.relax(capped_steps=2000, fmax=1000.0, free_steps=2000)
+    eng.relax(capped_steps=3000, fmax=1000.0, free_steps=3000)
     eng.set_force_cap(args.force_cap)
-    for _ in range(3):
+    for _ in range(max(3, args.warmup)):
         eng.flush_l2()
         eng.step(S)
     st0 = eng.stats()
     t = []
-    for _ in range(5):
+    for _ in range(max(1, args.steps)):
         eng.flush_l2()
         eng.event(0)
         eng.step(S)
@@ -387,7 +389,7 @@ def uneven_record(args, rank, world):
             "target_speedup_vs_fp64": 20.0, "force_rms_rel_err_vs_fp64": err,
             "steps_per_rebuild": S * len(t) * len(sysm.instances) / reb if reb else None,
             "lanes_per_bead": st1["lanes_per_bead"], "timed_blocks": len(t), "md_steps_per_block": S,
-            "relax_steps": {"force_capped": 2000, "free": 2000}, "l2": "flushed between timed blocks (512 MiB write)"}
+            "relax_steps": {"force_capped": 3000, "free": 3000}, "l2": "flushed between timed blocks (512 MiB write)"}
 
 
 def serve_record(args, rank, world, seconds=4.0, scale=0.01):
