@@ -14,6 +14,7 @@ module sis_gpu_mod
                                SIS_ERR_TIMEOUT = -7
   integer(c_int32_t), parameter :: SIS_PREC_FP64 = 0, SIS_PREC_MIXED = 1
   integer(c_int32_t), parameter :: SIS_LIST_WCA = 0, SIS_LIST_ELE = 1, SIS_LIST_BP = 2
+  integer(c_int32_t), parameter :: SIS_LIST_WCA_INNER = 3, SIS_LIST_ELE_INNER = 4
 
   ! include/sis_gpu.h struct sis_params, field by field
   type, bind(C) :: sis_params

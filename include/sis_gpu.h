@@ -62,6 +62,11 @@ extern "C" {
 #define SIS_LIST_WCA 0 /* wca_mp(2,n)  src/var_potential.F90 */
 #define SIS_LIST_ELE 1 /* ele_mp(2,n) */
 #define SIS_LIST_BP 2  /* bp_mp(7,n)  */
+/* the WCA / electrostatic pairs (2,n) of the per-block kernel's inner lists
+ * (contexts of small instances, instances of 256 moving beads or more: the
+ * list entries within their cutoff + 2.5 A, as last filtered by the kernel) */
+#define SIS_LIST_WCA_INNER 3
+#define SIS_LIST_ELE_INNER 4
 
 /* Model parameters: the .ff file (src/read_force_field.F90) and the input
  * TOML sections [Basepair] [Electrostatic] [MD] (src/read_input.F90). */
@@ -166,7 +171,8 @@ int sis_gpu_init_velocities(sis_ctx *ctx);
  * replaces src/neighbor_list.F90:1 and src/pbc.F90:196-226. */
 int sis_gpu_neighbor_list(sis_ctx *ctx, int32_t inst);
 /* Copies a list of instance inst (kind SIS_LIST_*, 1-based local indices,
- * records (2,n) or (7,n) in unspecified order).  *n_out = number of records. */
+ * records (2,n) or (7,n) in unspecified order).  *n_out = number of records.
+ * The inner kinds need a context of small instances (SIS_ERR_ARG otherwise). */
 int sis_gpu_get_list(sis_ctx *ctx, int32_t inst, int32_t kind, int32_t *out, int32_t cap, int32_t *n_out);
 /* bp_coef(2,n) (dH, dS) aligned with the SIS_LIST_BP records of the last get_list call order */
 int sis_gpu_get_bp_coef(sis_ctx *ctx, int32_t inst, double *out, int32_t cap, int32_t *n_out);

@@ -1329,18 +1329,21 @@ extern "C" int sis_gpu_neighbor_list(sis_ctx *ctx, int32_t inst) {
 
 extern "C" int sis_gpu_get_list(sis_ctx *ctx, int32_t inst, int32_t kind, int32_t *out, int32_t cap, int32_t *n_out) {
     DevGuard dg_(ctx);
-    if (!ctx || inst < 0 || inst >= ctx->n_inst || kind < 0 || kind > 2 || !n_out) return SIS_ERR_ARG;
+    if (!ctx || inst < 0 || inst >= ctx->n_inst || kind < 0 || kind > 4 || !n_out) return SIS_ERR_ARG;
+    const bool inner = kind == SIS_LIST_WCA_INNER || kind == SIS_LIST_ELE_INNER;
+    if (inner && !ctx->D.nbr_in) return fail(ctx, SIS_ERR_ARG, "get_list: inner lists exist for contexts of small instances only");
     int rc = ensure_lists(ctx);
     if (rc) return rc;
     const InstP &I = ctx->ip[inst];
     const int off = I.bead_off, cnt = I.n;
     std::vector<int> res;
-    if (kind < 2) {
+    if (kind != SIS_LIST_BP) {
         std::vector<int> nn(cnt), nb((size_t)cnt * ctx->g.cap);
-        CK(cudaMemcpyAsync(nn.data(), ctx->D.nnbr + off, sizeof(int) * cnt, cudaMemcpyDeviceToHost, ctx->st));
-        CK(cudaMemcpyAsync(nb.data(), ctx->D.nbr + (size_t)off * ctx->g.cap, sizeof(int) * nb.size(), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaMemcpyAsync(nn.data(), (inner ? ctx->D.nnbr_in : ctx->D.nnbr) + off, sizeof(int) * cnt, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaMemcpyAsync(nb.data(), (inner ? ctx->D.nbr_in : ctx->D.nbr) + (size_t)off * ctx->g.cap, sizeof(int) * nb.size(),
+                           cudaMemcpyDeviceToHost, ctx->st));
         CK(cudaStreamSynchronize(ctx->st));
-        const int bit = kind == 0 ? WCA_BIT : ELE_BIT;
+        const int bit = (kind == SIS_LIST_WCA || kind == SIS_LIST_WCA_INNER) ? WCA_BIT : ELE_BIT;
         for (int i = 0; i < cnt; ++i) {
             const int c = std::min(nn[i], ctx->g.cap);
             for (int k = 0; k < c; ++k) {

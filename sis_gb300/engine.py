@@ -87,7 +87,8 @@ class Engine:
         self._ck(self.L.sis_gpu_neighbor_list(self.h, inst))
 
     def get_list(self, inst: int, kind: int) -> np.ndarray:
-        """kind 0 wca (n,2), 1 ele (n,2), 2 bp (n,7); 1-based local indices."""
+        """kind 0 wca (n,2), 1 ele (n,2), 2 bp (n,7), 3 / 4 the wca / ele pairs
+        of the per-block kernel's inner lists (n,2); 1-based local indices."""
         w = 7 if kind == 2 else 2
         n = C.c_int32()
         self._ck(self.L.sis_gpu_get_list(self.h, inst, kind, None, 0, C.byref(n)))

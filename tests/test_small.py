@@ -155,3 +155,35 @@ def test_small_rebuild_rate_matches_general_kernels(sis_ff):
         e.step(600)
         out.append(e.stats()["rebuilds"])
     assert abs(out[0] - out[1]) <= max(3, 0.1 * out[1]), out
+
+
+def test_inner_lists_hold_every_pair_within_its_cutoff(sis_ff):
+    """After 400 steps of chains of 256-400 beads from coils with WCA
+    overlaps (fast motion: many inner filterings and list rebuilds), every
+    listed pair within its cutoff at the current positions is in the inner
+    lists, the inner lists are part of the lists, and they leave out the
+    pairs well beyond the cutoffs."""
+    sysm = _batch(sis_ff, n_inst=6, seed=13, lmin=256, lmax=400)
+    eng = Engine(sysm, precision=MIXED, seed=17)
+    eng.set_force_cap(1000.0)
+    eng.init_velocities()
+    eng.step(400)
+    assert eng.stats()["small_blocks"] > 0
+    x = eng.get_state(-1)[0]
+    off, left_out, total = 0, 0, 0
+    for k, inst in enumerate(sysm.instances):
+        n = inst.nmp
+        xk = x[off:off + n]
+        cut = {0: 10.0, 1: eng.get_ele(k)[2]}  # WCA sigma (sis.ff), electrostatic cutoff
+        for kind, kind_in in ((0, 3), (1, 4)):
+            outer = as_set(eng.get_list(k, kind))
+            inner = as_set(eng.get_list(k, kind_in))
+            assert inner <= outer, (k, kind)
+            for i, j in outer:
+                d = np.linalg.norm(xk[i - 1] - xk[j - 1])
+                if d <= cut[kind]:
+                    assert (i, j) in inner, (k, kind, i, j, d)
+            left_out += len(outer) - len(inner)
+            total += len(outer)
+        off += n
+    assert left_out > 0.05 * total, (left_out, total)
