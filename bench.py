@@ -305,6 +305,7 @@ def run_gpu(args):
     cfg = {"workload": args.workload, "description": WORKLOADS[args.workload], "n_beads": N,
            "n_instances": len(sysm.instances), "md_steps_per_step": S, "precision": "FP32 terms / FP64 accumulate+integrate",
            "list_entries_per_bead": round(L, 3), "steps_per_rebuild": k_rebuild, "lanes_per_bead": st1["lanes_per_bead"], "pair_kernel_beside_bonded": bool(st1["overlap"]), "bp_blocks": st1["bp_blocks"],
+           "small_blocks": st1["small_blocks"], "small_threads": st1["small_threads"],
            "l2": "flushed between timed steps (512 MiB write)", "fp64_value": fp64_value,
            "speedup_vs_fp64": value / fp64_value, "force_rms_rel_err_vs_fp64": err,
            "start": "relaxed positions of sis_gb300/data/crowded_relaxed.npz" if relaxed else "random coil",
@@ -388,7 +389,8 @@ def uneven_record(args, rank, world):
             "unit": UNIT, "ms_per_md_step": ms / (len(t) * S), "fp64_value": v64, "speedup_vs_fp64": value / v64,
             "target_speedup_vs_fp64": 20.0, "force_rms_rel_err_vs_fp64": err,
             "steps_per_rebuild": S * len(t) * len(sysm.instances) / reb if reb else None,
-            "lanes_per_bead": st1["lanes_per_bead"], "timed_blocks": len(t), "md_steps_per_block": S,
+            "lanes_per_bead": st1["lanes_per_bead"], "small_blocks": st1["small_blocks"], "small_threads": st1["small_threads"],
+            "timed_blocks": len(t), "md_steps_per_block": S,
             "relax_steps": {"force_capped": 3000, "free": 3000}, "l2": "flushed between timed blocks (512 MiB write)"}
 
 

@@ -733,9 +733,11 @@ int run_small(sis_ctx *ctx, int64_t nsteps, const double *noise) {
     return SIS_OK;
 }
 
-// Picks the bucket count and the block width of k_md_small by timing a few
-// real steps of each candidate; the per-bead arithmetic is the same for all,
-// so the steps are part of the trajectory.  Returns the steps it took.
+// Picks the bucket count and the block width of k_md_small by timing real
+// steps of each candidate, in two rounds, by each candidate's faster round
+// (a list rebuild inside one timed window does not decide the pick); the
+// per-bead arithmetic is the same for all, so the steps are part of the
+// trajectory.  Returns the steps it took.
 int64_t small_autotune(sis_ctx *ctx, int64_t budget, int *rc) {
     *rc = SIS_OK;
     const int sms = ctx->sms;
@@ -744,40 +746,50 @@ int64_t small_autotune(sis_ctx *ctx, int64_t budget, int *rc) {
         const int t = std::min(ctx->n_inst, f * sms);
         if (targets.empty() || targets.back() != t) targets.push_back(t);
     }
-    const std::vector<int> widths = {128, 256, 512};
-    const int per = 8;
-    const int64_t need = (int64_t)(targets.size() * widths.size() + 1) * per;
+    const std::vector<int> widths = {128, 256, 384, 512};
+    const int per = 16, rounds = 2;
+    const int64_t need = (int64_t)(rounds * targets.size() * widths.size() + 1) * per;
     if (budget < need) {
         if (!ctx->sp.n_cta && (*rc = small_plan(ctx, std::min(ctx->n_inst, 2 * sms)))) return 0;
         return 0;
     }
-    float best = 1e30f;
-    int best_t = targets[0], best_w = widths[0];
+    std::vector<float> best_ms(targets.size() * widths.size(), 1e30f);
     int64_t taken = 0;
     // the first pass warms up (list state, first-touch), untimed
     if ((*rc = small_plan(ctx, targets[0]))) return taken;
     ctx->small_threads = widths[0];
     if ((*rc = run_small(ctx, per, nullptr))) return taken;
     taken += per;
-    for (int t : targets) {
-        if ((*rc = small_plan(ctx, t))) return taken;
-        for (int w : widths) {
-            if (small_smem_bytes(ctx->sp.cap) > 212 * 1024) continue;
-            ctx->small_threads = w;
-            cudaEventRecord(ctx->ev[12], ctx->st);
-            if ((*rc = run_small(ctx, per, nullptr))) return taken;
-            cudaEventRecord(ctx->ev[13], ctx->st);
-            cudaEventSynchronize(ctx->ev[13]);
-            float ms = 1e30f;
-            cudaEventElapsedTime(&ms, ctx->ev[12], ctx->ev[13]);
-            taken += per;
-            if (ms < best) {
-                best = ms;
-                best_t = t;
-                best_w = w;
+    for (int r = 0; r < rounds; ++r) {
+        for (size_t ti = 0; ti < targets.size(); ++ti) {
+            if ((*rc = small_plan(ctx, targets[ti]))) return taken;
+            for (size_t wi = 0; wi < widths.size(); ++wi) {
+                const int w = widths[wi];
+                if (small_smem_bytes(ctx->sp.cap) > 212 * 1024) continue;
+                // the 384-thread bound (168 registers, a third of the spills,
+                // 12 warps) against 512 (16 warps), by bucket size as measured
+                // in steady state: buckets of 64 beads ran 7% faster with 384,
+                // of 120 beads as fast, of ~600 beads 13% slower; so 384 only
+                // up to 384 beads, and 512 only above 96
+                if (w == 384 && ctx->sp.cap > 384) continue;
+                if (w == 512 && ctx->sp.cap <= 96) continue;
+                ctx->small_threads = w;
+                cudaEventRecord(ctx->ev[12], ctx->st);
+                if ((*rc = run_small(ctx, per, nullptr))) return taken;
+                cudaEventRecord(ctx->ev[13], ctx->st);
+                cudaEventSynchronize(ctx->ev[13]);
+                float ms = 1e30f;
+                cudaEventElapsedTime(&ms, ctx->ev[12], ctx->ev[13]);
+                taken += per;
+                float &b = best_ms[ti * widths.size() + wi];
+                b = std::min(b, ms);
             }
         }
     }
+    size_t bi = 0;
+    for (size_t k = 1; k < best_ms.size(); ++k)
+        if (best_ms[k] < best_ms[bi]) bi = k;
+    const int best_t = targets[bi / widths.size()], best_w = widths[bi % widths.size()];
     if ((*rc = small_plan(ctx, best_t))) return taken;
     ctx->small_target = best_t;
     ctx->small_planned = ctx->steps + taken;

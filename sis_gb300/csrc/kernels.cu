@@ -1728,8 +1728,10 @@ __device__ __forceinline__ int small_inst(const int *s_sb, int ni, int s) {
     return lo;
 }
 
-template <bool INNER>
-__global__ void __launch_bounds__(512) k_md_small(Dev D, GlobP g, int cur, SmallPlan sp, int nsteps, const double *noise) {
+// MAXT: the block width bound (512: 128 registers a thread; 384: 168, and a
+// third of the register spills, for blocks of up to 384 threads)
+template <bool INNER, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_md_small(Dev D, GlobP g, int cur, SmallPlan sp, int nsteps, const double *noise) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     const int cap = sp.cap;
     uint4 *s_mir = (uint4 *)s_dyn;
@@ -2557,15 +2559,11 @@ cudaError_t launch_md_small(const Dev &D, const GlobP &g, int cur, const SmallPl
     const size_t smem = small_smem_bytes(sp.cap);
     SmallPlan p = sp;
     p.sslot = small_slot_planes(sp.cap) ? 1 : 0;
-    if (sp.inner) {
-        cudaError_t e = cudaFuncSetAttribute(k_md_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_md_small<true><<<p.n_cta, threads, smem, st>>>(D, g, cur, p, nsteps, noise);
-    } else {
-        cudaError_t e = cudaFuncSetAttribute(k_md_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_md_small<false><<<p.n_cta, threads, smem, st>>>(D, g, cur, p, nsteps, noise);
-    }
+    auto kern = sp.inner ? (threads <= 384 ? k_md_small<true, 384> : k_md_small<true, 512>)
+                         : (threads <= 384 ? k_md_small<false, 384> : k_md_small<false, 512>);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<p.n_cta, threads, smem, st>>>(D, g, cur, p, nsteps, noise);
     return cudaGetLastError();
 }
 
